@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""Benchmark of the dense g2 correlator (tensor-core Gram path) on GB300.
+
+Workload: 514 x 1030 uint8 frames, 10,000 frames, 16 equal annular q-bins with
+radii 20-400 px around (257, 515); synthetic AR(1) speckle (rho 0.99, mean 0.1
+photons/pixel), generated on the device with a fixed seed.  One step = one
+full correlation of the stack through the public API
+(``MatMulCorrelator.correlate_device``: pack + bin sums, tensor-core Gram with
+fused lag sums, denominator, g2), inputs resident in HBM.  ``e2e`` repeats it
+with the frames in pinned host memory (``MatMulCorrelator.correlate``: H2D copy,
+pipeline, g2 back to the host).  The stack (5.3 GB) is larger than L2, so no
+flush is needed between steps.
+
+``--impl reference`` times the CPU baseline instead: the float32 restatement
+of the reference's MatMulCorrelator (numpy BLAS on all host cores) on the
+first 2048 frames of the same stack, scaled to 10,000 frames by its O(T^2) cost.
+
+Multi-GPU (torchrun): independent replicas, one stack per GPU ("weak" scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {
+    "workload": "dense_514x1030_u8_T10000_16bins",
+    "frame_shape": [514, 1030], "nframes": 10000, "dtype": "uint8", "n_bins": 16,
+    "qmask": "16 equal annuli r 20-400 px around (257, 515)", "rho": 0.99, "mean_photons": 0.1, "seed": 1,
+    "l2": "inputs (5.3 GB) larger than L2; no flush",
+}
+CPU_SAMPLE_FRAMES = 2048
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparator")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--frames", type=int, default=WORKLOAD["nframes"], help="override T (testing only)")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic(name):
+    """Per-launch DRAM bytes of a kernel from a committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.strip().startswith("traffic_bytes_per_launch"):
+                return float(line.split("=")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons every 200 ms during the timed region."""
+
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, uuid):
+        self.uuid = (uuid or "").lower()
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"]
+            self.proc = subprocess.Popen(cmd, stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.flush()
+        self.out.seek(0)
+        rows = [[x.strip() for x in line.split(",")] for line in self.out.read().splitlines()]
+        os.unlink(self.out.name)
+        rows = [r for r in rows if len(r) >= 8]
+        mine = [r for r in rows if self.uuid and self.uuid in r[0].lower()]
+        rows = mine or rows
+        sm, smax, power, reasons = [], [], [], set()
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                power.append(float(r[3]))
+            except ValueError:
+                continue
+            for n, v in zip(self.REASONS, r[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_workload(dev, T):
+    from dynamix_gb300.speckle import annular_qmask, speckle_torch
+    H, W = WORKLOAD["frame_shape"]
+    qmask = annular_qmask((H, W), WORKLOAD["n_bins"], 20.0, 400.0, center=(257, 515))
+    frames = speckle_torch(T, (H, W), WORKLOAD["rho"], WORKLOAD["mean_photons"], seed=WORKLOAD["seed"],
+                           device=dev)
+    return frames, qmask
+
+
+def cpu_port_time(frames_host, qmask, repeats=1):
+    """Seconds per call of the float32 MatMulCorrelator restatement (all host threads)."""
+    from oracle.g2_oracle import matmul_correlator_port
+    ts = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        matmul_correlator_port(frames_host, qmask)
+        ts.append(time.perf_counter() - t0)
+    return ts
+
+
+def cpu_scale(T_full, t_sample, T_sample):
+    # cost of the MatMul correlator is O(T^2) (Gram and per-lag diagonal loop)
+    return T_full / (t_sample * (T_full / T_sample) ** 2)
+
+
+def run_reference(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    T_full = args.frames
+    Ts = min(CPU_SAMPLE_FRAMES, T_full)
+    dev = torch.device("cuda", local) if torch.cuda.is_available() else torch.device("cpu")
+    frames, qmask = make_workload(dev, Ts)
+    host = frames.cpu().numpy()
+    del frames
+    for _ in range(args.warmup):
+        cpu_port_time(host, qmask)
+    ts = cpu_port_time(host, qmask, repeats=args.steps)
+    t = sum(ts) / len(ts)
+    v = cpu_scale(T_full, t, Ts)
+    ncores = os.cpu_count()
+    line = {
+        "metric": "g2_frames_per_s", "value": v, "unit": "frames/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(WORKLOAD, nframes=T_full),
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": ncores, "kind": "port",
+                         "sample": "first %d of the %d frames, all 16 bins; float32 MatMulCorrelator restatement "
+                                   "(numpy BLAS, %d threads); O(T^2) cost scaled to %d frames"
+                                   % (Ts, T_full, ncores, T_full)},
+        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from dynamix_gb300 import build as b
+    from dynamix_gb300.correlator import MatMulCorrelator
+    from dynamix_gb300.plan import gram_macs
+
+    rank, world, local = dist_info()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    b.build(force=False)
+
+    T = args.frames
+    frames, qmask = make_workload(dev, T)
+    H, W = WORKLOAD["frame_shape"]
+    corr = MatMulCorrelator((H, W), T, qmask=qmask)
+    eng = corr.engine
+    npix = np.bincount(qmask.ravel(), minlength=17)[1:]
+    macs = gram_macs(T, npix)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident steps
+    for _ in range(max(args.warmup, 3)):
+        corr.correlate_device(frames)
+    eng.check_error()
+    stream = torch.cuda.current_stream(dev)
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    sampler = ClockSampler(uuid)
+    eng.profile = True
+    gram_ms, pack_ms = [], []
+    barrier()
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step_events = []
+    for _ in range(args.steps):
+        corr.correlate_device(frames)
+        step_events.append(eng.take_events())
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    eng.profile = False
+    for ev in step_events:
+        st = eng.stage_times(ev)
+        gram_ms.append(st.get("gram_tc", float("nan")))
+        pack_ms.append(st.get("pack", float("nan")))
+    eng.check_error()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    value = world * T / (ms / 1e3)
+    launches_per_step = 4  # pack, gram, denominator, finalize
+    info = dict(eng.last)
+
+    peaks, peak_kind = measured_peaks()
+    gram_avg = sum(gram_ms) / len(gram_ms)
+    achieved = 2.0 * macs / (gram_avg / 1e3) / 1e12
+    peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+    pack_bytes = T * H * W + T * info["packed_cols"] * 2
+    pack_avg = sum(pack_ms) / len(pack_ms)
+    traffic = profile_traffic("gram_tc_dense_514x1030_T10000.md")
+
+    line = {
+        "metric": "g2_frames_per_s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": dict(WORKLOAD, nframes=T, parallelism="replicas" if world > 1 else "single",
+                       mma_kind="tcgen05 kind::f16 (fp16 operands, fp32 accumulate, exact below 2^24)"),
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": "g2_gram_tc",
+                     "peak_source": "%s bf16_tflops_sustained (dense f16 rate)" % peak_kind,
+                     "algorithmic_ops_per_launch": 2 * macs, "launch_ms": gram_avg},
+        "stages_ms": {"pack": pack_avg, "gram_tc": gram_avg},
+        "pack_roofline": {"bound": "hbm", "achieved": pack_bytes / (pack_avg / 1e3) / 1e9,
+                          "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                          "frac": pack_bytes / (pack_avg / 1e3) / 1e9 / peaks.get("hbm_gbs")},
+        "clocks": clocks, "gpu_launches": launches_per_step * args.steps, "plan": info,
+    }
+
+    # ---- end to end through the public API, frames in pinned host memory
+    if not args.no_e2e:
+        host = frames.cpu().pin_memory()
+        corr.correlate(host)
+        barrier()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            corr.correlate(host)
+        e1.record(stream)
+        barrier()
+        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+        d2h = eng.n_bins * T * 4 + 4 + eng.n_bins * T * 8 + info["packed_cols"] // 64 * 4
+        line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
+                       "h2d_bytes_per_step": int(host.numel() * host.element_size()),
+                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+        del host
+
+    # ---- same-GPU plain (CUDA-core) comparator
+    if not args.no_plain:
+        pc = MatMulCorrelator((H, W), T, qmask=qmask, extra_options={"method": "plain"})
+        pc.correlate_device(frames)
+        barrier()
+        e0.record(stream)
+        nplain = 2
+        for _ in range(nplain):
+            pc.correlate_device(frames)
+        e1.record(stream)
+        barrier()
+        pms = max_over_ranks(e0.elapsed_time(e1) / nplain)
+        same = bool(torch.equal(pc.engine.numer, eng.numer) and torch.equal(pc.engine.denom, eng.denom))
+        line["plain"] = {"ms_per_step": pms, "value": world * T / (pms / 1e3), "unit": "frames/s",
+                         "speedup_tc_vs_plain": pms / ms, "bit_identical_N_D": same}
+        del pc
+
+    # ---- CPU baseline (rank 0, bounded sample)
+    if not args.no_cpu and rank == 0:
+        Ts = min(CPU_SAMPLE_FRAMES, T)
+        host = frames[:Ts].cpu().numpy()
+        ts = cpu_port_time(host, qmask)
+        ncores = os.cpu_count()
+        line["cpu_baseline"] = {
+            "value": cpu_scale(T, ts[0], Ts), "unit": "frames/s", "cores": ncores, "kind": "port",
+            "sample": "first %d of the %d frames, all 16 bins; float32 MatMulCorrelator restatement (numpy BLAS, "
+                      "%d threads) took %.2f s; O(T^2) cost scaled to %d frames" % (Ts, T, ncores, ts[0], T)}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

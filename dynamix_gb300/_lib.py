@@ -1,0 +1,108 @@
+"""ctypes binding of the C ABI in ``include/dynamix_g2.h``.
+
+The library is built in-tree (``python -m dynamix_gb300.build``) at
+``dynamix_gb300/_lib/libdynamix_g2.so``.  There is no fallback: if the library
+is missing, every correlator raises at construction.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libdynamix_g2.so")
+
+G2_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "unsupported device or feature",
+          4: "size exceeds a kernel limit"}
+DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE = 1, 2, 4
+
+BK = 64
+TC_BM, TC_BN = 128, 256
+PLAIN_BM, PLAIN_BN = 128, 128
+MAX_JOBS = 32
+
+# numpy mirror of g2_gram_item (40 bytes, 8-byte aligned)
+ITEM_DTYPE = np.dtype([("job", "<i4"), ("i0", "<i4"), ("j0", "<i4"), ("a_k0", "<i4"), ("b_k0", "<i4"),
+                       ("k_len", "<i4"), ("shift", "<i4"), ("nframes", "<i4"), ("out_off", "<i8")])
+assert ITEM_DTYPE.itemsize == 40
+
+
+class Job(C.Structure):
+    _fields_ = [("packed_dev", C.c_void_p), ("nframes", C.c_int64), ("packed_cols", C.c_int64)]
+
+
+_p = C.c_void_p
+_i32 = C.c_int32
+_i64 = C.c_int64
+
+# name -> (restype, argtypes); every symbol declared in include/dynamix_g2.h
+SIGNATURES = {
+    "g2_abi_version": (C.c_int, []),
+    "g2_status_string": (C.c_char_p, [C.c_int]),
+    "g2_device_info": (C.c_int, [C.c_int, _p, _p, _p]),
+    "g2_pack_frames": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _p, _i64, _i32, _p, _i64, _p, _i32, _p, _p, _p]),
+    "g2_binned_max": (C.c_int, [_p, _i32, _i64, _i64, _p, _i64, _p, _p]),
+    "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i32, _p]),
+    "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
+    "g2_denominator": (C.c_int, [_p, _i32, _i64, _p, _p]),
+    "g2_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class G2Error(RuntimeError):
+    pass
+
+
+def load(path=None):
+    """Load (once) and return the ctypes library; raise if it is not built."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise ImportError("dynamix_gb300 CUDA library not built (%s); run `python -m dynamix_gb300.build` "
+                              "or __graft_entry__.build()" % p)
+        lib = C.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def check(status, what):
+    if status != G2_OK:
+        raise G2Error("%s failed: %s (status %d)" % (what, STATUS.get(status, "unknown"), status))
+
+
+def jobs_array(jobs):
+    """[(packed_ptr, nframes, packed_cols), ...] -> ctypes array of Job."""
+    if not 1 <= len(jobs) <= MAX_JOBS:
+        raise ValueError("between 1 and %d jobs per launch" % MAX_JOBS)
+    arr = (Job * len(jobs))()
+    for i, (ptr, T, cols) in enumerate(jobs):
+        arr[i].packed_dev = ptr
+        arr[i].nframes = T
+        arr[i].packed_cols = cols
+    return arr
+
+
+def device_error_message(code):
+    msgs = []
+    if code & DEVERR_TIMEOUT:
+        msgs.append("a bounded device wait timed out")
+    if code & DEVERR_BOUNDS:
+        msgs.append("an out-of-range index was skipped")
+    if code & DEVERR_RANGE:
+        msgs.append("a count does not fit the packing")
+    return "; ".join(msgs) or "device error %d" % code

@@ -1,0 +1,4 @@
+"""Correlator API, mirroring ``dynamix.correlator`` (dense, event, sparse)."""
+from .common import BaseCorrelator  # noqa: F401
+from .dense import (CorrelationResult, CublasMatMulCorrelator, DenseCorrelator,  # noqa: F401
+                    MatMulCorrelator, py_dense_correlator)

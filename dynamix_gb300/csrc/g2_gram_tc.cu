@@ -1,0 +1,286 @@
+// G2: tensor-core Gram of each q-bin's (frames x pixels) matrix with the
+// lag-diagonal sums fused into the epilogue.
+//
+// For one item, the CTA computes the 128 x 256 block G(t, t') = sum_k A(t,k) B(t',k)
+// (t = i0 + r, t' = j0 + c) with tcgen05.mma kind::f16 into TMEM, then adds
+// every element with t' >= t to the lag tau = t' - t:
+//     N(tau) += 2^shift * sum_{c - r = tau - (j0 - i0)} G(r, c).
+// The Gram never reaches HBM.  Counts are exact in fp16 (<= 2048), products
+// exact in fp32, and the caller splits K so that every fp32 partial sum is an
+// integer below 2^24; the epilogue converts each element to uint32 and sums the
+// lag diagonals in uint32 shared-memory counters (<= 128 * 2^24 < 2^32), which
+// are then added to the int64 numerator.
+//
+// Roles (192 threads, one CTA per SM, persistent over a static item schedule):
+//   warp 0 lane 0  TMA producer: A (128 x 64) and B (256 x 64) fp16 tiles per
+//                  stage, 4-stage ring, 128-byte swizzle
+//   warp 1 lane 0  MMA issuer: 4 x (M128 N256 K16) per stage into one of two
+//                  TMEM accumulators (2 x 256 columns)
+//   warps 2..5     epilogue: tcgen05.ld 32 columns at a time, skewed lag sums
+//                  in shared memory, int64 atomics to the numerator
+// Replaces dense.py:54,61-64 (numpy sgemm + diagonal loop), cuda.py:67-116
+// (cuBLAS sgemm + extract_upper_diags) and densecorrelator.cl:6-56.
+#include <cstring>
+#include <mutex>
+#include "g2_ptx.cuh"
+#include "g2_host.h"
+
+namespace g2 {
+namespace tc {
+
+constexpr int BM = G2_TC_BM;      // 128 rows of A per item (TMEM lanes)
+constexpr int BN = G2_TC_BN;      // 256 rows of B per item (TMEM columns)
+constexpr int BK = G2_BK;         // 64 fp16 = 128 bytes per row per stage
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;
+constexpr int B_BYTES = BN * BK * 2;
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int NDIAG = BM + BN - 1;  // lags covered by one item
+constexpr int NDIAG_PAD = 384;
+constexpr int TMEM_COLS = 2 * BN;
+constexpr int NUM_THREADS = 192;
+constexpr int EPI_THREADS = 128;
+constexpr uint32_t IDESC = idesc_f16_f32(BM, BN);
+
+constexpr int SMEM_BAR_OFF = STAGES * STAGE_BYTES;
+constexpr int SMEM_BYTES = 1024 /*alignment slack*/ + SMEM_BAR_OFF + 256 + 2 * NDIAG_PAD * 4;
+
+struct MapsParam {
+  CUtensorMap a[G2_MAX_JOBS];
+  CUtensorMap b[G2_MAX_JOBS];
+};
+
+__device__ __forceinline__ bool named_bar_any(uint32_t id, uint32_t n, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %3, 0;\n\t"
+      "bar.red.or.pred p, %1, %2, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"(id), "r"(n), "r"(static_cast<uint32_t>(v))
+      : "memory");
+  return r != 0;
+}
+
+// Every role applies the same test, so a malformed item is skipped by all of
+// them consistently (the epilogue records G2_DEVERR_BOUNDS).
+__device__ __forceinline__ bool item_ok(const g2_gram_item& w, int n_jobs, int64_t numer_len) {
+  return w.job >= 0 && w.job < n_jobs && w.k_len > 0 && (w.k_len % BK) == 0 && (w.a_k0 % BK) == 0 &&
+         (w.b_k0 % BK) == 0 && w.nframes > 0 && w.shift >= 0 && w.shift <= 32 && w.out_off >= 0 &&
+         w.out_off + w.nframes <= numer_len;
+}
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    gram_tc_kernel(const __grid_constant__ MapsParam maps, int n_jobs, const g2_gram_item* __restrict__ items,
+                   int64_t n_items, unsigned long long* __restrict__ numer, int64_t numer_len,
+                   int32_t* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + STAGES * A_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + SMEM_BAR_OFF);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accf = empty + STAGES;
+  uint64_t* acce = accf + 2;
+  uint64_t* drain = acce + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  uint32_t* diag = reinterpret_cast<uint32_t*>(smem + SMEM_BAR_OFF + 256);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], EPI_THREADS);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  for (int i = threadIdx.x; i < 2 * NDIAG_PAD; i += NUM_THREADS) diag[i] = 0;
+  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int64_t issued = 0;
+      bool ok = true;
+      for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+        const g2_gram_item w = items[it];
+        if (!item_ok(w, n_jobs, numer_len)) continue;
+        const CUtensorMap* ma = &maps.a[w.job];
+        const CUtensorMap* mb = &maps.b[w.job];
+        const int nk = w.k_len / BK;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
+          tma_load_2d(sA + stage * A_BYTES, ma, &full[stage], w.a_k0 + kb * BK, w.i0);
+          tma_load_2d(sB + stage * B_BYTES, mb, &full[stage], w.b_k0 + kb * BK, w.j0);
+          ++issued;
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // Make sure no TMA write into this CTA's shared memory is still in
+      // flight when the CTA exits (returns at once on the normal path).
+      const int64_t last = issued < STAGES ? issued : STAGES;
+      for (int64_t k = 1; k <= last; ++k) {
+        const int64_t idx = issued - k;
+        mbar_wait_drain(&full[idx % STAGES], static_cast<uint32_t>((idx / STAGES) & 1), 200000000ull);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int64_t local = 0;
+      bool ok = true;
+      for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+        const g2_gram_item w = items[it];
+        if (!item_ok(w, n_jobs, numer_len)) continue;
+        const int buf = static_cast<int>(local & 1);
+        const uint32_t ap = static_cast<uint32_t>((local >> 1) & 1);
+        if (!mbar_wait(&acce[buf], ap ^ 1, abort_flag, err)) break;
+        tc_fence_after();
+        const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(buf * BN);
+        const int nk = w.k_len / BK;
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!mbar_wait(&full[stage], phase, abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = smem_addr(sA + stage * A_BYTES);
+          const uint32_t b0 = smem_addr(sB + stage * B_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            tc_mma_f16(d_tmem, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), IDESC,
+                       (kb | kk) != 0 ? 1u : 0u);
+          }
+          tc_commit(&empty[stage]);
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (ok) tc_commit(&accf[buf]);
+        ++local;
+      }
+      // All MMAs issued by this thread complete before TMEM is released.
+      tc_commit(drain);
+      mbar_wait_drain(drain, 0, 200000000ull);
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q = warp & 3;  // TMEM sub-partition this warp may access
+    const int row = q * 32 + lane;
+    const int etid = threadIdx.x - 64;
+    int64_t local = 0;
+    for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x, ++local) {
+      const g2_gram_item w = items[it];
+      if (!item_ok(w, n_jobs, numer_len)) {
+        if (etid == 0) atomicOr(err, G2_DEVERR_BOUNDS);
+        --local;
+        continue;
+      }
+      const int buf = static_cast<int>(local & 1);
+      const uint32_t ap = static_cast<uint32_t>((local >> 1) & 1);
+      uint32_t* dacc = diag + (local & 1) * NDIAG_PAD;
+      const bool ok = mbar_wait(&accf[buf], ap, abort_flag, err);
+      if (named_bar_any(1, EPI_THREADS, !ok)) break;
+      tc_fence_after();
+      const uint32_t tbase = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * BN);
+#pragma unroll 1
+      for (int cc = 0; cc < BN / 32; ++cc) {
+        uint32_t v[32];
+        tmem_ld_32x32b_x32(tbase + static_cast<uint32_t>(cc * 32), v);
+        tmem_wait_ld();
+        const int dbase = cc * 32 - row + (BM - 1);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const uint32_t x = __float2uint_rn(__uint_as_float(v[j]));
+          if (x) atomicAdd(&dacc[dbase + j], x);
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acce[buf]);
+      named_bar_sync(1, EPI_THREADS);
+      const int lag0 = w.j0 - w.i0 - (BM - 1);
+      for (int d = etid; d < NDIAG; d += EPI_THREADS) {
+        const uint32_t s = dacc[d];
+        if (s) {
+          const int tau = lag0 + d;
+          if (tau >= 0 && tau < w.nframes)
+            atomicAdd(&numer[w.out_off + tau], static_cast<unsigned long long>(s) << w.shift);
+          dacc[d] = 0;
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, TMEM_COLS);
+  }
+}
+
+}  // namespace tc
+}  // namespace g2
+
+extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                          uint64_t* numer_dev, int64_t numer_len, int32_t* err_dev, int32_t grid, void* stream) {
+  using namespace g2;
+  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !numer_dev || numer_len <= 0 || !err_dev)
+    return G2_ERR_ARG;
+  if (n_items > 0 && !items_dev) return G2_ERR_ARG;
+  for (int j = 0; j < n_jobs; ++j) {
+    const g2_job& jb = jobs[j];
+    if (!jb.packed_dev || !aligned(jb.packed_dev, 16) || jb.nframes <= 0 || jb.nframes >= (1ll << 31) ||
+        jb.packed_cols <= 0 || jb.packed_cols % G2_BK != 0 || jb.packed_cols >= (1ll << 31))
+      return G2_ERR_ARG;
+  }
+  if (n_items == 0) return G2_OK;
+  static tc::MapsParam maps;  // large; filled under the lock below
+  static std::mutex* mu = new std::mutex;
+  std::lock_guard<std::mutex> lk(*mu);
+  std::memset(&maps, 0, sizeof(maps));
+  for (int j = 0; j < n_jobs; ++j) {
+    int st = encode_tmap_fp16_2d(&maps.a[j], jobs[j].packed_dev, jobs[j].packed_cols, jobs[j].nframes, tc::BK, tc::BM);
+    if (st != G2_OK) return st;
+    st = encode_tmap_fp16_2d(&maps.b[j], jobs[j].packed_dev, jobs[j].packed_cols, jobs[j].nframes, tc::BK, tc::BN);
+    if (st != G2_OK) return st;
+  }
+  if (cudaFuncSetAttribute(tc::gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES) !=
+      cudaSuccess)
+    return G2_ERR_CUDA;
+  int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  int64_t g = grid > 0 ? grid : sms;
+  if (g > n_items) g = n_items;
+  tc::gram_tc_kernel<<<static_cast<unsigned>(g), tc::NUM_THREADS, tc::SMEM_BYTES, as_stream(stream)>>>(
+      maps, n_jobs, items_dev, n_items, reinterpret_cast<unsigned long long*>(numer_dev), numer_len, err_dev);
+  return launch_status();
+}

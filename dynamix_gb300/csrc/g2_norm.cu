@@ -1,0 +1,94 @@
+// G3 (denominator) and G4 (finalize).
+//
+// G3: D[r][tau] = sum_t S[r][t] * S[r][t+tau] in int64 for every row r (one row
+// per (job, bin)).  A block owns 256 consecutive lags of one row and walks t in
+// shared-memory windows of 1024 frames; the shifted window is padded with
+// zeros beyond T, so no per-term bounds test is needed.
+// Replaces correlate_1D (densecorrelator.cl:156-176), the sum loop of
+// normalize_correlation (evtcorrelator.cl:70-73) and the mean outer product
+// of py_dense_correlator (dense.py:55, :63).
+//
+// G4: g2 = scale * N / D in float64 (the only float64 arithmetic on the GPU),
+// written as float32 and/or float64.  0/0 gives NaN as in the reference.
+// Replaces densecorrelator.cl:54, evtcorrelator.cl:75 and dense.py:64.
+#include "g2_ptx.cuh"
+#include "g2_host.h"
+
+namespace g2 {
+namespace norm {
+
+constexpr int LAGS = 256;
+constexpr int WIN = 1024;
+
+__global__ void __launch_bounds__(LAGS)
+    denom_kernel(const long long* __restrict__ S, int64_t T, long long* __restrict__ D) {
+  __shared__ long long s1[WIN];
+  __shared__ long long s2[WIN + LAGS];
+  const int64_t r = blockIdx.y;
+  const int64_t tau0 = static_cast<int64_t>(blockIdx.x) * LAGS;
+  const long long* row = S + r * T;
+  long long acc = 0;
+  for (int64_t t0 = 0; t0 < T - tau0; t0 += WIN) {
+    for (int i = threadIdx.x; i < WIN; i += LAGS) {
+      const int64_t t = t0 + i;
+      s1[i] = t < T ? row[t] : 0;
+    }
+    for (int i = threadIdx.x; i < WIN + LAGS; i += LAGS) {
+      const int64_t t = t0 + tau0 + i;
+      s2[i] = t < T ? row[t] : 0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int i = 0; i < WIN; ++i) acc += s1[i] * s2[i + threadIdx.x];
+    __syncthreads();
+  }
+  const int64_t tau = tau0 + threadIdx.x;
+  if (tau < T) D[r * T + tau] = acc;
+}
+
+__global__ void finalize_kernel(const long long* __restrict__ N, const long long* __restrict__ D,
+                                const double* __restrict__ scale, int64_t rows, int64_t T, float* __restrict__ g32,
+                                double* __restrict__ g64) {
+  const int64_t total = rows * T;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / T;
+    const double g = scale[r] * static_cast<double>(N[i]) / static_cast<double>(D[i]);
+    if (g32) g32[i] = static_cast<float>(g);
+    if (g64) g64[i] = g;
+  }
+}
+
+}  // namespace norm
+}  // namespace g2
+
+extern "C" int g2_denominator(const int64_t* sums_dev, int32_t n_rows, int64_t nframes, int64_t* denom_dev,
+                              void* stream) {
+  using namespace g2;
+  if (!sums_dev || !denom_dev || n_rows < 0 || nframes <= 0) return G2_ERR_ARG;
+  if (n_rows == 0) return G2_OK;
+  if (n_rows > 65535) return G2_ERR_TOO_LARGE;
+  const int64_t gx = (nframes + norm::LAGS - 1) / norm::LAGS;
+  if (gx > 0x7fffffff) return G2_ERR_TOO_LARGE;
+  dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(n_rows));
+  norm::denom_kernel<<<grid, norm::LAGS, 0, as_stream(stream)>>>(reinterpret_cast<const long long*>(sums_dev),
+                                                                 nframes, reinterpret_cast<long long*>(denom_dev));
+  return launch_status();
+}
+
+extern "C" int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, const double* scale_dev,
+                           int32_t n_rows, int64_t nframes, float* g2_f32_dev, double* g2_f64_dev, void* stream) {
+  using namespace g2;
+  if (!numer_dev || !denom_dev || !scale_dev || n_rows < 0 || nframes <= 0 || (!g2_f32_dev && !g2_f64_dev))
+    return G2_ERR_ARG;
+  if (n_rows == 0) return G2_OK;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  const int64_t total = static_cast<int64_t>(n_rows) * nframes;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > sms * 8) blocks = sms * 8;
+  norm::finalize_kernel<<<static_cast<unsigned>(blocks), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const long long*>(numer_dev), reinterpret_cast<const long long*>(denom_dev), scale_dev,
+      n_rows, nframes, g2_f32_dev, g2_f64_dev);
+  return launch_status();
+}

@@ -1,0 +1,266 @@
+"""Device pipelines behind the correlator classes.
+
+PyTorch only owns device memory and the CUDA stream; all arithmetic runs in
+the hand-written sm_103a kernels of ``libdynamix_g2.so`` (C ABI in
+``include/dynamix_g2.h``).  There is no CPU path: constructing an engine
+without a CUDA device or without the built library raises.
+
+Dense pipeline (one job = one frame stack, all its q-bins):
+
+    G1 pack + bin sums   -> packed fp16 operand [T][cols], S (int64), segment energies
+       (host: K split from the segment energies, item list; cached)
+    G2 tensor-core Gram  -> N (int64), or G5 plain direct kernel (comparator)
+    G3 denominator       -> D (int64)
+    G4 finalize          -> g2 (float32 and float64)
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .plan import EXACT_LIMIT, FP16_MAX_EXACT, PackLayout, chunk_grams, gram_items
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def require_cuda(device=None):
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError("dynamix_gb300 needs a CUDA device (sm_103); none is available")
+    dev = torch.device(device if device is not None else "cuda")
+    if dev.type != "cuda":
+        raise ValueError("device must be a CUDA device")
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    return dev
+
+
+def ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def stream_handle(dev):
+    return C.c_void_p(_torch().cuda.current_stream(dev).cuda_stream)
+
+
+class DeviceError(RuntimeError):
+    pass
+
+
+def frames_to_device(frames, dev):
+    """Validate a (T, H, W) stack of non-negative integer counts and return a
+    contiguous uint8 / uint16 device tensor.
+
+    numpy arrays and CPU tensors are copied (asynchronously when pinned);
+    device tensors of a supported dtype are used in place."""
+    torch = _torch()
+    if isinstance(frames, torch.Tensor):
+        t = frames
+        if t.dtype in (torch.uint8, torch.uint16):
+            return t.to(dev, non_blocking=True).contiguous()
+        frames = t.cpu().numpy()
+    a = np.asarray(frames)
+    if a.dtype == np.uint8 or a.dtype == np.uint16:
+        host = torch.from_numpy(np.ascontiguousarray(a))
+        return host.to(dev, non_blocking=False)
+    if a.dtype.kind not in "iuf":
+        raise TypeError("frames must hold integer photon counts")
+    if a.size:
+        if a.dtype.kind == "f" and not np.all(np.isfinite(a) & (a == np.round(a))):
+            raise TypeError("float frames must hold integer counts")
+        lo, hi = a.min(), a.max()
+        if lo < 0:
+            raise ValueError("counts must be non-negative")
+        if hi > 65535:
+            raise ValueError("counts above 65535 are not supported")
+    tgt = np.uint8 if (a.size == 0 or a.max() <= 255) else np.uint16
+    return torch.from_numpy(np.ascontiguousarray(a.astype(tgt))).to(dev)
+
+
+class DenseEngine:
+    """Exact g2 of a dense (T, H, W) stack for the bins of one q-mask."""
+
+    def __init__(self, shape, nframes, qmask, n_bins, scale, device=None, method="tc",
+                 exact_limit=EXACT_LIMIT, grid=0):
+        torch = _torch()
+        self.lib = _lib.load()
+        self.dev = require_cuda(device)
+        self.shape = tuple(int(s) for s in shape)
+        self.T = int(nframes)
+        self.npix = self.shape[0] * self.shape[1]
+        self.qmask = np.ascontiguousarray(qmask, dtype=np.int32)
+        self.n_bins = int(n_bins)
+        if method not in ("tc", "plain"):
+            raise ValueError("method must be 'tc' or 'plain'")
+        self.method = method
+        self.exact_limit = int(exact_limit)
+        self.grid = int(grid)
+        self.scale = torch.as_tensor(np.asarray(scale, dtype=np.float64), device=self.dev)
+        rows = max(self.n_bins, 1)
+        z = lambda dt: torch.zeros((rows, self.T), dtype=dt, device=self.dev)
+        self.sums = z(torch.int64)
+        self.numer = z(torch.int64)
+        self.denom = z(torch.int64)
+        self.g2_f32 = z(torch.float32)
+        self.g2_f64 = z(torch.float64)
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.maxval = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self._layouts = {}
+        self._items_cache = {}
+        self.packed = None
+        self.last = {}
+        self.profile = False      # record CUDA events around every stage
+        self.stage_ms = {}
+        self._events = []
+
+    def _mark(self, name):
+        if self.profile:
+            torch = _torch()
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(torch.cuda.current_stream(self.dev))
+            self._events.append((name, ev))
+
+    def take_events(self):
+        """Hand over the stage events of the last run (no synchronisation)."""
+        ev, self._events = self._events, []
+        return ev
+
+    @staticmethod
+    def stage_times(events):
+        """Milliseconds per stage from a list of (name, event); synchronises."""
+        out = {}
+        if len(events) >= 2:
+            events[-1][1].synchronize()
+            for (n0, e0), (_, e1) in zip(events[:-1], events[1:]):
+                out[n0] = out.get(n0, 0.0) + e0.elapsed_time(e1)
+        return out
+
+    # -- layout / buffers ------------------------------------------------
+    def _layout(self, split):
+        if split not in self._layouts:
+            torch = _torch()
+            L = PackLayout(self.qmask, self.n_bins, split)
+            d = lambda a: torch.as_tensor(a, device=self.dev)
+            L.d_col_src = d(L.col_src)
+            L.d_seg_bin = d(L.seg_bin)
+            L.d_seg_dst0 = d(L.seg_dst0)
+            L.d_seg_dst1 = d(L.seg_dst1)
+            L.d_seg_emax = torch.zeros(L.packed_cols // _lib.BK, dtype=torch.int32, device=self.dev)
+            self._layouts[split] = L
+        return self._layouts[split]
+
+    def _packed_buffer(self, cols):
+        torch = _torch()
+        need = self.T * cols
+        if self.packed is None or self.packed.numel() < need:
+            self.packed = None
+            self.packed = torch.empty(need, dtype=torch.float16, device=self.dev)
+        return self.packed
+
+    # -- stages ----------------------------------------------------------
+    def choose_split(self, frames_dev):
+        if frames_dev.element_size() == 1:
+            return 0
+        L0 = self._layout(0)
+        self.maxval.zero_()
+        _lib.check(self.lib.g2_binned_max(ptr(frames_dev), 2, self.T, self.npix, ptr(L0.d_col_src),
+                                          L0.col_src.size, ptr(self.maxval), stream_handle(self.dev)),
+                   "g2_binned_max")
+        return 0 if int(self.maxval.item()) <= FP16_MAX_EXACT else 1
+
+    def pack(self, frames_dev, split):
+        L = self._layout(split)
+        packed = self._packed_buffer(L.packed_cols)
+        self.sums.zero_()
+        L.d_seg_emax.zero_()
+        self.err.zero_()
+        st = stream_handle(self.dev)
+        _lib.check(self.lib.g2_pack_frames(
+            ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_col_src), ptr(L.d_seg_bin),
+            ptr(L.d_seg_dst0), ptr(L.d_seg_dst1), L.n_segs, split, ptr(packed), L.packed_cols, ptr(self.sums),
+            self.n_bins, ptr(L.d_seg_emax), ptr(self.err), st), "g2_pack_frames")
+        return L
+
+    def items_for(self, L, seg_emax):
+        grams = chunk_grams(L, seg_emax, self.exact_limit)
+        key = (L.split, self.method, tuple(grams))
+        if key not in self._items_cache:
+            torch = _torch()
+            items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method)
+            dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
+            if len(self._items_cache) > 8:
+                self._items_cache.clear()
+            self._items_cache[key] = (items, dev_items, len(grams))
+        return self._items_cache[key]
+
+    def numerator(self, L, items_dev, n_items):
+        self.numer.zero_()
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols)])
+        st = stream_handle(self.dev)
+        if self.method == "tc":
+            _lib.check(self.lib.g2_gram_tc(jobs, 1, ptr(items_dev), n_items, ptr(self.numer), self.numer.numel(),
+                                           ptr(self.err), self.grid, st), "g2_gram_tc")
+        else:
+            _lib.check(self.lib.g2_plain_direct(jobs, 1, ptr(items_dev), n_items, ptr(self.numer),
+                                                self.numer.numel(), ptr(self.err), st), "g2_plain_direct")
+
+    def normalise(self):
+        st = stream_handle(self.dev)
+        if self.n_bins == 0:
+            return
+        _lib.check(self.lib.g2_denominator(ptr(self.sums), self.n_bins, self.T, ptr(self.denom), st),
+                   "g2_denominator")
+        _lib.check(self.lib.g2_finalize(ptr(self.numer), ptr(self.denom), ptr(self.scale), self.n_bins, self.T,
+                                        ptr(self.g2_f32), ptr(self.g2_f64), st), "g2_finalize")
+
+    def check_error(self):
+        code = int(self.err.item())
+        if code:
+            raise DeviceError(_lib.device_error_message(code))
+
+    # -- whole pipeline ----------------------------------------------------
+    def run(self, frames_dev):
+        """Run G1..G4 on a device stack; returns the float32 g2 device tensor.
+
+        Synchronises once after G1 to read the segment energies (K split)."""
+        if tuple(frames_dev.shape) != (self.T,) + self.shape:
+            raise ValueError("frames should have shape %s, got %s" % ((self.T,) + self.shape,
+                                                                    tuple(frames_dev.shape)))
+        if self.n_bins == 0:
+            return self.g2_f32[:0]
+        self._events = []
+        self._mark("split")
+        split = self.choose_split(frames_dev)
+        self._mark("pack")
+        L = self.pack(frames_dev, split)
+        self._mark("plan")
+        seg_emax = L.d_seg_emax.cpu().numpy().view(np.uint32)
+        self.check_error()
+        try:
+            grams = chunk_grams(L, seg_emax, self.exact_limit)
+        except OverflowError:
+            if split == 1:
+                raise
+            L = self.pack(frames_dev, 1)
+            seg_emax = L.d_seg_emax.cpu().numpy().view(np.uint32)
+            self.check_error()
+        items, items_dev, n_chunks = self.items_for(L, seg_emax)
+        self._mark("gram_" + self.method)
+        self.numerator(L, items_dev, items.size)
+        self._mark("normalise")
+        self.normalise()
+        self._mark("end")
+        self.last = {"split": L.split, "n_items": int(items.size), "n_grams": n_chunks,
+                     "packed_cols": L.packed_cols}
+        return self.g2_f32[: self.n_bins]
+
+    def check_denominator_range(self):
+        """Raise if int64 D could have overflowed (checked from S on the host)."""
+        S = self.sums[: self.n_bins].cpu().numpy()
+        if S.size and float(S.max()) ** 2 * self.T >= 2.0 ** 63:
+            raise OverflowError("denominator exceeds int64 for these counts")

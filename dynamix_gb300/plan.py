@@ -1,0 +1,184 @@
+"""Host-side planning of the dense g2 pipeline.
+
+* :class:`PackLayout` -- where each q-bin's pixels go in the packed fp16
+  operand matrix ``[T][packed_cols]`` (bins are contiguous, each padded to a
+  multiple of 64 columns; with ``split=1`` a bin holds a high-byte plane and a
+  low-byte plane side by side).
+* :func:`k_chunks` -- the K split of one Gram so that every fp32 partial sum
+  is an integer below ``limit`` (2^24 by default): by Cauchy-Schwarz,
+  ``|sum_k a(t,k) b(t',k)| <= sqrt(max_t sum a^2 * max_t' sum b^2)``, and the
+  pack kernel reports ``max_t sum`` of squares per 64-column segment.
+* :func:`gram_items` -- the upper-triangle item list (g2_gram_item records) for
+  one job, LPT-ordered (longest K first) for the persistent kernel.
+
+The per-bin arithmetic it plans is that of ``py_dense_correlator``
+(dynamix/correlator/dense.py:48-64) with bins from ``BaseCorrelator._set_qmask``
+(dynamix/correlator/common.py:36-46).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from ._lib import BK, ITEM_DTYPE, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN
+
+EXACT_LIMIT = 1 << 24   # fp32 represents every integer up to 2^24 exactly
+FP16_MAX_EXACT = 2048   # fp16 represents every integer up to 2^11 exactly
+
+
+def _roundup(x, m):
+    return (x + m - 1) // m * m
+
+
+class PackLayout:
+    """Packed-column layout of the bins of one q-mask."""
+
+    def __init__(self, qmask, n_bins, split):
+        qflat = np.ascontiguousarray(qmask, dtype=np.int32).ravel()
+        qflat = np.where(qflat >= 1, qflat, 0)               # bins are 1..n_bins, the rest unused
+        self.npix_total = qflat.size
+        self.n_bins = int(n_bins)
+        self.split = int(split)
+        order = np.argsort(qflat, kind="stable")            # raster order within each bin
+        counts = np.bincount(qflat, minlength=self.n_bins + 1)[: self.n_bins + 1]
+        starts = np.concatenate([[0], np.cumsum(counts)])
+        self.npix = counts[1:].astype(np.int64)               # P_b, b = 1..n_bins
+        self.kpad = _roundup(self.npix, BK)
+        nseg_b = self.kpad // BK
+        self.n_segs = int(nseg_b.sum())
+        col_src = np.full(int(self.kpad.sum()), -1, dtype=np.int32)
+        self.src_off = np.concatenate([[0], np.cumsum(self.kpad)])[:-1]
+        for b in range(self.n_bins):
+            pix = order[starts[b + 1]:starts[b + 2]]
+            col_src[self.src_off[b]:self.src_off[b] + pix.size] = pix
+        self.col_src = col_src
+        self.seg_bin = np.repeat(np.arange(self.n_bins, dtype=np.int32), nseg_b)
+        seg_local = np.arange(self.n_segs, dtype=np.int64) - np.repeat(self.src_off // BK, nseg_b)
+        width = self.kpad * (2 if self.split else 1)
+        self.bin_off = np.concatenate([[0], np.cumsum(width)])[:-1].astype(np.int64)
+        self.packed_cols = int(max(BK, width.sum()))
+        # plane offsets (first packed column) per bin
+        self.plane0 = self.bin_off.copy()                       # counts (split 0) or high bytes
+        self.plane1 = self.bin_off + self.kpad if self.split else None  # low bytes
+        self.seg_dst0 = (np.repeat(self.plane0, nseg_b) + seg_local * BK).astype(np.int32)
+        if self.split:
+            self.seg_dst1 = (np.repeat(self.plane1, nseg_b) + seg_local * BK).astype(np.int32)
+        else:
+            self.seg_dst1 = np.zeros(self.n_segs, dtype=np.int32)
+        if self.packed_cols >= 2 ** 31:
+            raise ValueError("too many binned pixels for one job")
+
+    def grams(self):
+        """The Grams to run per bin: (bin, a_plane_off, b_plane_off, kpad, shift)."""
+        out = []
+        for b in range(self.n_bins):
+            if self.kpad[b] == 0:
+                continue
+            kp = int(self.kpad[b])
+            if not self.split:
+                out.append((b, int(self.plane0[b]), int(self.plane0[b]), kp, 0))
+            else:
+                h, lo = int(self.plane0[b]), int(self.plane1[b])
+                out.append((b, h, h, kp, 16))    # high x high, weight 2^16
+                out.append((b, h, lo, kp, 8))    # high x low,  weight 2^8
+                out.append((b, lo, h, kp, 8))    # low  x high, weight 2^8
+                out.append((b, lo, lo, kp, 0))   # low  x low
+        return out
+
+
+def k_chunks(emax_a, emax_b, limit=EXACT_LIMIT):
+    """Split a Gram's 64-column segments into chunks with exact fp32 sums.
+
+    ``emax_a[s]`` / ``emax_b[s]``: max over frames of the sum of squares of the
+    A / B packed values in segment ``s``.  A chunk ``[s0, s1)`` is valid when
+    ``sum(emax_a) * sum(emax_b) <= limit^2`` (hence every partial sum of the
+    dot products is <= limit).  A single segment always fits (64 * 2048^2 can
+    exceed 2^24, but then the K split cannot help; such a segment is reported
+    as infeasible).  Returns a list of ``(s0, s1)``.
+    """
+    ea = np.asarray(emax_a, dtype=np.float64)
+    eb = np.asarray(emax_b, dtype=np.float64)
+    n = ea.size
+    lim2 = float(limit) * float(limit)
+    if n and np.any(ea * eb > lim2):
+        raise OverflowError("a 64-column segment exceeds the exact fp32 bound")
+    chunks = []
+    s0 = 0
+    sa = sb = 0.0
+    for s in range(n):
+        na, nb = sa + ea[s], sb + eb[s]
+        if na * nb > lim2:
+            chunks.append((s0, s))
+            s0, sa, sb = s, ea[s], eb[s]
+        else:
+            sa, sb = na, nb
+    if n:
+        chunks.append((s0, n))
+    return chunks
+
+
+_TILE_CACHE = {}
+
+
+def _tiles(T, bm, bn):
+    """(i0, j0) of every bm x bn block that holds some t' >= t, t, t' < T."""
+    key = (T, bm, bn)
+    if key not in _TILE_CACHE:
+        ni = -(-T // bm)
+        nj = -(-T // bn)
+        ii, jj = np.meshgrid(np.arange(ni), np.arange(nj), indexing="ij")
+        i0 = (ii * bm).ravel()
+        j0 = (jj * bn).ravel()
+        keep = j0 + bn - 1 >= i0
+        _TILE_CACHE[key] = (i0[keep].astype(np.int32), j0[keep].astype(np.int32))
+    return _TILE_CACHE[key]
+
+
+def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc"):
+    """Build the item list of one job.
+
+    ``chunked_grams``: iterable of ``(bin, a_off, b_off, k0, k_len, shift)`` with
+    columns relative to the job's packed matrix.  ``kind`` selects the block
+    shape (tensor-core 128x256 or plain 128x128).  Items are sorted by k_len
+    (descending, stable) so that the persistent kernel's static round-robin
+    schedule starts with the longest items.
+    """
+    bm, bn = (TC_BM, TC_BN) if kind == "tc" else (PLAIN_BM, PLAIN_BN)
+    i0, j0 = _tiles(int(T), bm, bn)
+    parts = []
+    for (b, a_off, b_off, k0, klen, shift) in chunked_grams:
+        it = np.empty(i0.size, dtype=ITEM_DTYPE)
+        it["job"] = job
+        it["i0"] = i0
+        it["j0"] = j0
+        it["a_k0"] = a_off + k0
+        it["b_k0"] = b_off + k0
+        it["k_len"] = klen
+        it["shift"] = shift
+        it["nframes"] = T
+        it["out_off"] = out_base + b * T
+        parts.append(it)
+    if not parts:
+        return np.empty(0, dtype=ITEM_DTYPE)
+    items = np.concatenate(parts)
+    order = np.argsort(-items["k_len"].astype(np.int64), kind="stable")
+    return items[order]
+
+
+def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT):
+    """Apply :func:`k_chunks` to every Gram of a layout.
+
+    ``seg_emax`` is indexed by packed column // 64.  Returns the list of
+    ``(bin, a_off, b_off, k0, k_len, shift)`` and the number of chunks."""
+    out = []
+    for (b, a_off, b_off, kp, shift) in layout.grams():
+        nseg = kp // BK
+        ea = seg_emax[a_off // BK: a_off // BK + nseg]
+        eb = seg_emax[b_off // BK: b_off // BK + nseg]
+        for (s0, s1) in k_chunks(ea, eb, limit):
+            out.append((b, a_off, b_off, s0 * BK, (s1 - s0) * BK, shift))
+    return out
+
+
+def gram_macs(T, npix):
+    """Algorithmic multiply-accumulates of the upper-triangle Grams (incl. diagonal)."""
+    return int(np.sum(np.asarray(npix, dtype=np.int64))) * T * (T + 1) // 2

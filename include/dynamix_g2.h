@@ -1,0 +1,149 @@
+/*
+ * dynamix_g2.h -- C ABI of the GB300 (sm_103a) g2 correlator kernels.
+ *
+ * All pointers named *_dev are device pointers owned by the caller; the
+ * library allocates no device memory.  Every entry point is asynchronous on
+ * the given CUDA stream (a cudaStream_t passed as void*; NULL = legacy default
+ * stream), returns a status code (G2_OK = 0) and never throws.  Argument
+ * errors are detected on the host before anything is launched.
+ *
+ * Quantities (per q-bin b with P_b pixels, frames I(t,p), t = 0..T-1):
+ *   N_b(tau) = sum_t sum_{p in b} I(t,p) I(t+tau,p)      numerator   (int64)
+ *   S_b(t)   = sum_{p in b} I(t,p)                        bin sums    (int64)
+ *   D_b(tau) = sum_t S_b(t) S_b(t+tau)                    denominator (int64)
+ *   g2_b(tau)= scale_b * N_b(tau) / D_b(tau)              (float64 -> float32)
+ *
+ * Citations are paths inside the dynamix project (silx-kit/dynamix).
+ */
+#ifndef DYNAMIX_G2_H
+#define DYNAMIX_G2_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define G2_OK               0
+#define G2_ERR_ARG          1  /* bad argument (null pointer, size, alignment) */
+#define G2_ERR_CUDA         2  /* a CUDA runtime call failed */
+#define G2_ERR_UNSUPPORTED  3  /* device is not sm_103 or feature missing */
+#define G2_ERR_TOO_LARGE    4  /* a size exceeds a kernel limit */
+
+/* bits a kernel may set in its device error word (int32) */
+#define G2_DEVERR_TIMEOUT   1  /* a bounded wait expired; the kernel bailed out */
+#define G2_DEVERR_BOUNDS    2  /* an index was out of range and was skipped */
+#define G2_DEVERR_RANGE     4  /* a count does not fit the requested packing */
+
+#define G2_ABI_VERSION      1
+
+/* Tile sizes of the tensor-core Gram: an item covers a 128 x 256 block of
+ * the (t, t') Gram, the plain kernel a 128 x 128 block; k_len is a multiple
+ * of 64 packed columns. */
+#define G2_TC_BM      128
+#define G2_TC_BN      256
+#define G2_PLAIN_BM   128
+#define G2_PLAIN_BN   128
+#define G2_BK         64
+#define G2_MAX_JOBS   32
+
+/* One unit of Gram work: rows [i0, i0+BM) of the A operand against rows
+ * [j0, j0+BN) of the B operand over packed columns [a_k0, a_k0+k_len) and
+ * [b_k0, b_k0+k_len).  The lag-diagonal sums of the t' >= t part are added,
+ * multiplied by 2^shift, to numer[out_off + tau] for 0 <= tau < nframes. */
+typedef struct g2_gram_item {
+    int32_t job;       /* index into the jobs array of the launch */
+    int32_t i0;        /* first frame of the A rows */
+    int32_t j0;        /* first frame of the B rows */
+    int32_t a_k0;      /* first packed column of A (multiple of 64) */
+    int32_t b_k0;      /* first packed column of B (multiple of 64) */
+    int32_t k_len;     /* packed columns, multiple of 64, > 0 */
+    int32_t shift;     /* weight 2^shift (0, 8 or 16 for byte-split planes) */
+    int32_t nframes;   /* T of the job */
+    int64_t out_off;   /* element offset of N_b(0) in numer */
+} g2_gram_item;
+
+/* A dense job: its packed operand matrix, row-major [nframes][packed_cols]
+ * of fp16 bit patterns (integer counts <= 2048, exact in fp16). */
+typedef struct g2_job {
+    const void* packed_dev;
+    int64_t nframes;
+    int64_t packed_cols;   /* multiple of 64 */
+} g2_job;
+
+/* ---- host utilities ---------------------------------------------------- */
+int         g2_abi_version(void);
+const char* g2_status_string(int status);
+/* SM count and compute capability of a device. */
+int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+
+/* ---- G1: pack + bin sums ------------------------------------------------
+ * Replaces compute_sums_dense (dynamix/resources/opencl/densecorrelator.cl:65-150)
+ * and the per-bin gather + float32 cast of py_dense_correlator
+ * (dynamix/correlator/dense.py:48-50).
+ *
+ * frames_dev: [nframes][npix] counts, elem_bytes 1 (u8) or 2 (u16).
+ * Source columns come in 64-column segments; segment s belongs to bin
+ * seg_bin[s] (0-based) and col_src[64*s + j] is the flat pixel index of its
+ * column j (or -1 for padding).  split == 0: the count is written as fp16 to
+ * packed column seg_dst0[s] + j.  split == 1: the high byte goes to
+ * seg_dst0[s] + j and the low byte to seg_dst1[s] + j.
+ * Adds S_b(t) into sums_dev[b * nframes + t] (caller zeroes it) and raises
+ * seg_emax_dev[c / 64] (caller zeroes it) to max_t of the sum of squares of
+ * the packed values in output segment c / 64.
+ */
+int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
+                   const int32_t* col_src_dev, const int32_t* seg_bin_dev,
+                   const int32_t* seg_dst0_dev, const int32_t* seg_dst1_dev, int64_t n_segs,
+                   int32_t split, void* packed_dev, int64_t packed_cols,
+                   int64_t* sums_dev, int32_t n_bins, uint32_t* seg_emax_dev, int32_t* err_dev,
+                   void* stream);
+
+/* Largest count over the binned pixels (col_src >= 0): picks split 0/1.
+ * No reference counterpart (the reference never checks its dtype range). */
+int g2_binned_max(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
+                  const int32_t* col_src_dev, int64_t n_cols, uint32_t* max_dev, void* stream);
+
+/* ---- G2: tensor-core Gram with fused lag-diagonal sums ------------------
+ * Replaces the numerator of py_dense_correlator (dynamix/correlator/dense.py:54,
+ * :61-64), CublasMatMulCorrelator._correlate_matmul_cublas + extract_upper_diags
+ * (dynamix/correlator/cuda.py:67-74, :101-116) and correlator_multiQ_dense
+ * (dynamix/resources/opencl/densecorrelator.cl:6-56).
+ * tcgen05.mma kind::f16 (fp16 x fp16 -> fp32 in TMEM) on TMA-staged tiles;
+ * every FP32 partial sum is an integer below 2^24 when the caller's K split
+ * honours the segment energy bound, and is promoted to int64 per item.
+ * numer_dev is accumulated into (uint64 two's complement of int64).
+ * items_dev: n_items g2_gram_item (BM=128, BN=256).  grid <= 0: one CTA per SM.
+ */
+int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+               uint64_t* numer_dev, int64_t numer_len, int32_t* err_dev, int32_t grid, void* stream);
+
+/* ---- G5: plain direct kernel (CUDA cores, integer) ----------------------
+ * The same-GPU non-tensor-core comparator: the direct integer numerator of
+ * correlator_multiQ_dense (dynamix/resources/opencl/densecorrelator.cl:6-56),
+ * register-tiled on CUDA cores (uint32 IMAD) over 128 x 128 items. */
+int g2_plain_direct(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev,
+                    int64_t n_items, uint64_t* numer_dev, int64_t numer_len, int32_t* err_dev,
+                    void* stream);
+
+/* ---- G3: denominator ----------------------------------------------------
+ * Replaces correlate_1D (dynamix/resources/opencl/densecorrelator.cl:156-176),
+ * the denominator loop of normalize_correlation (evtcorrelator.cl:70-73) and
+ * the mean outer product of py_dense_correlator (dense.py:50, :55, :63).
+ * D[r][tau] = sum_t S[r][t] S[r][t+tau] in int64 for n_rows rows. */
+int g2_denominator(const int64_t* sums_dev, int32_t n_rows, int64_t nframes,
+                   int64_t* denom_dev, void* stream);
+
+/* ---- G4: finalize -------------------------------------------------------
+ * Replaces the division of dense.py:64, densecorrelator.cl:54 and
+ * normalize_correlation (evtcorrelator.cl:58-77): g2 = scale[r] * N / D in
+ * float64; written as float32 (g2_f32_dev) and/or float64 (either may be NULL). */
+int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, const double* scale_dev,
+                int32_t n_rows, int64_t nframes, float* g2_f32_dev, double* g2_f64_dev,
+                void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DYNAMIX_G2_H */

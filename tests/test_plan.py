@@ -1,0 +1,121 @@
+"""Host logic of the dense pipeline, checked on the CPU.
+
+A numpy emulation of the pack kernel and of the per-item semantics of the
+Gram kernels (what each g2_gram_item adds to N) must reproduce the oracle's
+numerator exactly; this pins the layout, the K split and the upper-triangle
+item enumeration independently of the GPU.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from dynamix_gb300 import plan
+from dynamix_gb300._lib import BK, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN
+from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+from oracle import g2_oracle as o
+
+
+def emulate_pack(frames, L):
+    T = frames.shape[0]
+    flat = frames.reshape(T, -1).astype(np.int64)
+    packed = np.zeros((T, L.packed_cols), dtype=np.int64)
+    cs = L.col_src.reshape(-1, BK)
+    for s in range(L.n_segs):
+        src = cs[s]
+        v = np.where(src >= 0, flat[:, np.maximum(src, 0)], 0)
+        if L.split:
+            packed[:, L.seg_dst0[s]:L.seg_dst0[s] + BK] = v >> 8
+            packed[:, L.seg_dst1[s]:L.seg_dst1[s] + BK] = v & 255
+        else:
+            packed[:, L.seg_dst0[s]:L.seg_dst0[s] + BK] = v
+    emax = (packed.reshape(T, -1, BK) ** 2).sum(axis=2).max(axis=0)
+    return packed, emax
+
+
+def run_items(packed, items, n_rows, T, bm, bn):
+    N = np.zeros(n_rows * T, dtype=np.int64)
+    P = np.concatenate([packed, np.zeros((bn, packed.shape[1]), dtype=np.int64)])
+    for it in items:
+        i0, j0, a0, b0, kl = int(it["i0"]), int(it["j0"]), int(it["a_k0"]), int(it["b_k0"]), int(it["k_len"])
+        G = P[i0:i0 + bm, a0:a0 + kl] @ P[j0:j0 + bn, b0:b0 + kl].T
+        assert G.max(initial=0) <= plan.EXACT_LIMIT
+        r, c = np.meshgrid(np.arange(bm), np.arange(bn), indexing="ij")
+        tau = (j0 + c) - (i0 + r)
+        ok = (tau >= 0) & (tau < T)
+        np.add.at(N, int(it["out_off"]) + tau[ok], G[ok] << int(it["shift"]))
+    return N.reshape(n_rows, T)
+
+
+@pytest.mark.parametrize("split", [0, 1])
+@pytest.mark.parametrize("kind", ["tc", "plain"])
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_u16"])
+def test_item_semantics_reproduce_oracle(name, kind, split):
+    z = golden(name)
+    fr, qm = z["frames"], z["qmask"]
+    T = fr.shape[0]
+    nb = int(qm.max())
+    L = plan.PackLayout(qm, nb, split)
+    if not split and fr.max() > plan.FP16_MAX_EXACT:
+        pytest.skip("counts do not fit fp16")
+    packed, emax = emulate_pack(fr, L)
+    grams = plan.chunk_grams(L, emax)
+    items = plan.gram_items(T, grams, kind=kind)
+    bm, bn = (TC_BM, TC_BN) if kind == "tc" else (PLAIN_BM, PLAIN_BN)
+    N = run_items(packed, items, nb, T, bm, bn)
+    ref = o.g2_exact(fr, qm)
+    assert np.array_equal(N, ref["numerator"])
+
+
+def test_k_split_honours_bound_with_bright_counts():
+    # all counts 255: a 64-column segment has energy 64*255^2 = 4.16e6, so a
+    # Gram over 1000 columns must be split to keep sums <= 2^24
+    T, shape = 40, (20, 50)
+    fr = np.full((T,) + shape, 255, dtype=np.uint8)
+    qm = np.ones(shape, dtype=np.int32)
+    L = plan.PackLayout(qm, 1, 0)
+    packed, emax = emulate_pack(fr, L)
+    grams = plan.chunk_grams(L, emax)
+    assert len(grams) > 1
+    for (_, a, b, k0, kl, _) in grams:
+        assert (packed[:, a + k0:a + k0 + kl] ** 2).sum(axis=1).max() <= plan.EXACT_LIMIT
+    items = plan.gram_items(T, grams, kind="tc")
+    N = run_items(packed, items, 1, T, TC_BM, TC_BN)
+    assert np.array_equal(N, o.g2_exact(fr, qm)["numerator"])
+
+
+def test_tiles_cover_upper_triangle_once():
+    for T in (1, 5, 127, 128, 129, 255, 256, 257, 300, 1000):
+        for bm, bn in ((TC_BM, TC_BN), (PLAIN_BM, PLAIN_BN)):
+            i0, j0 = plan._tiles(T, bm, bn)
+            cover = np.zeros((T + bn, T + bn), dtype=np.int32)
+            for a, b in zip(i0, j0):
+                cover[a:a + bm, b:b + bn] += 1
+            up = np.triu(np.ones((T, T), dtype=bool))
+            assert np.all(cover[:T, :T][up] == 1)
+
+
+def test_layout_groups_bins_in_raster_order():
+    qm = annular_qmask((30, 34), 3, 2.0, 15.0)
+    L = plan.PackLayout(qm, 3, 0)
+    for b in range(3):
+        pix = L.col_src[L.src_off[b]:L.src_off[b] + L.npix[b]]
+        assert np.array_equal(pix, np.flatnonzero(qm.ravel() == b + 1))
+        assert np.all(L.col_src[L.src_off[b] + L.npix[b]:L.src_off[b] + L.kpad[b]] == -1)
+    assert L.packed_cols % BK == 0
+
+
+def test_gram_macs_matches_config():
+    # 514 x 1030, 16 annuli r in [20, 400) around (257, 515): 1.898e13 MACs at T = 10000
+    qm = annular_qmask((514, 1030), 16, 20.0, 400.0, center=(257, 515))
+    npix = np.bincount(qm.ravel(), minlength=17)[1:]
+    assert npix.sum() == 379563
+    assert abs(plan.gram_macs(10000, npix) - 1.898e13) / 1.898e13 < 1e-3
+
+
+def test_speckle_generator_statistics():
+    fr = speckle_numpy(200, (32, 32), 0.9, 2.0, seed=3)
+    m = fr.mean()
+    assert 1.7 < m < 2.3
+    # speckle contrast: var/mean^2 ~ 1 + 1/mean for Poisson-exponential counts
+    c = fr.var() / m ** 2
+    assert 1.0 < c < 2.2
