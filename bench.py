@@ -43,7 +43,7 @@ CPU_SAMPLE_FRAMES = 2048
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparator")
@@ -95,7 +95,7 @@ class ClockSampler:
 
     def start(self):
         try:
-            cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"]
+            cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "100"]
             self.proc = subprocess.Popen(cmd, stdout=self.out, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
