@@ -20,10 +20,12 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "unsupport
           4: "size exceeds a kernel limit"}
 DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE = 1, 2, 4
 
-BK = 64
+BK = 64          # source segment width (pixels)
+PAD = 128        # packed bins and packed_cols are multiples of this
 TC_BM, TC_BN = 128, 256
 PLAIN_BM, PLAIN_BN = 128, 128
 MAX_JOBS = 32
+KIND_FP16, KIND_E4M3 = 0, 1
 
 # numpy mirror of g2_gram_item (40 bytes, 8-byte aligned)
 ITEM_DTYPE = np.dtype([("job", "<i4"), ("i0", "<i4"), ("j0", "<i4"), ("a_k0", "<i4"), ("b_k0", "<i4"),
@@ -32,7 +34,8 @@ assert ITEM_DTYPE.itemsize == 40
 
 
 class Job(C.Structure):
-    _fields_ = [("packed_dev", C.c_void_p), ("nframes", C.c_int64), ("packed_cols", C.c_int64)]
+    _fields_ = [("packed_dev", C.c_void_p), ("nframes", C.c_int64), ("packed_cols", C.c_int64),
+                ("elem_kind", C.c_int32), ("reserved", C.c_int32)]
 
 
 _p = C.c_void_p
@@ -86,14 +89,15 @@ def check(status, what):
 
 
 def jobs_array(jobs):
-    """[(packed_ptr, nframes, packed_cols), ...] -> ctypes array of Job."""
+    """[(packed_ptr, nframes, packed_cols, elem_kind), ...] -> ctypes array of Job."""
     if not 1 <= len(jobs) <= MAX_JOBS:
         raise ValueError("between 1 and %d jobs per launch" % MAX_JOBS)
     arr = (Job * len(jobs))()
-    for i, (ptr, T, cols) in enumerate(jobs):
+    for i, (ptr, T, cols, kind) in enumerate(jobs):
         arr[i].packed_dev = ptr
         arr[i].nframes = T
         arr[i].packed_cols = cols
+        arr[i].elem_kind = kind
     return arr
 
 

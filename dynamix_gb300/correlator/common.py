@@ -15,6 +15,8 @@ Extra options understood here:
   ``device``       CUDA device (default: the current one)
   ``method``       ``"tc"`` (tensor-core Gram, default) or ``"plain"`` (CUDA-core comparator)
   ``exact_limit``  bound on every fp32 partial sum of the Gram (default 2^24)
+  ``operand``      packed element type of the Gram: ``"auto"`` (default),
+                   ``"e4m3"`` (counts <= 16), ``"fp16"`` (<= 2048) or ``"bytes"``
 """
 from __future__ import annotations
 

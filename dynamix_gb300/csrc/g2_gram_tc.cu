@@ -2,7 +2,9 @@
 // lag-diagonal sums fused into the epilogue.
 //
 // For one item, the CTA computes the 128 x 256 block G(t, t') = sum_k A(t,k) B(t',k)
-// (t = i0 + r, t' = j0 + c) with tcgen05.mma kind::f16 into TMEM, then adds
+// (t = i0 + r, t' = j0 + c) with tcgen05.mma into TMEM -- kind::f16 on fp16
+// counts (exact to 2048) or kind::f8f6f4 on e4m3 counts (exact to 16, half the
+// bytes and twice the MMA rate), chosen per job -- then adds
 // every element with t' >= t to the lag tau = t' - t:
 //     N(tau) += 2^shift * sum_{c - r = tau - (j0 - i0)} G(r, c).
 // The Gram never reaches HBM.  Counts are exact in fp16 (<= 2048), products
@@ -30,17 +32,17 @@ namespace tc {
 
 constexpr int BM = G2_TC_BM;      // 128 rows of A per item (TMEM lanes)
 constexpr int BN = G2_TC_BN;      // 256 rows of B per item (TMEM columns)
-constexpr int BK = G2_BK;         // 64 fp16 = 128 bytes per row per stage
+constexpr int ROW_BYTES = 128;   // bytes per operand row per stage (64 fp16 or 128 e4m3)
 constexpr int STAGES = 4;
-constexpr int A_BYTES = BM * BK * 2;
-constexpr int B_BYTES = BN * BK * 2;
+constexpr int A_BYTES = BM * ROW_BYTES;
+constexpr int B_BYTES = BN * ROW_BYTES;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int NDIAG = BM + BN - 1;  // lags covered by one item
 constexpr int NDIAG_PAD = 384;
 constexpr int TMEM_COLS = 2 * BN;
 constexpr int NUM_THREADS = 192;
 constexpr int EPI_THREADS = 128;
-constexpr uint32_t IDESC = idesc_f16_f32(BM, BN);
+constexpr uint32_t IDESC = idesc_f32acc(BM, BN);  // same bits for fp16 and e4m3 operands
 
 constexpr int SMEM_BAR_OFF = STAGES * STAGE_BYTES;
 constexpr int SMEM_BYTES = 1024 /*alignment slack*/ + SMEM_BAR_OFF + 256 + 2 * NDIAG_PAD * 4;
@@ -48,7 +50,11 @@ constexpr int SMEM_BYTES = 1024 /*alignment slack*/ + SMEM_BAR_OFF + 256 + 2 * N
 struct MapsParam {
   CUtensorMap a[G2_MAX_JOBS];
   CUtensorMap b[G2_MAX_JOBS];
+  int32_t kind[G2_MAX_JOBS];  // G2_KIND_FP16 or G2_KIND_E4M3
 };
+
+// packed elements per 128-byte stage row
+__device__ __forceinline__ int stage_elems(int kind) { return kind == G2_KIND_E4M3 ? 128 : 64; }
 
 __device__ __forceinline__ bool named_bar_any(uint32_t id, uint32_t n, bool v) {
   uint32_t r;
@@ -65,10 +71,12 @@ __device__ __forceinline__ bool named_bar_any(uint32_t id, uint32_t n, bool v) {
 
 // Every role applies the same test, so a malformed item is skipped by all of
 // them consistently (the epilogue records G2_DEVERR_BOUNDS).
-__device__ __forceinline__ bool item_ok(const g2_gram_item& w, int n_jobs, int64_t numer_len) {
-  return w.job >= 0 && w.job < n_jobs && w.k_len > 0 && (w.k_len % BK) == 0 && (w.a_k0 % BK) == 0 &&
-         (w.b_k0 % BK) == 0 && w.nframes > 0 && w.shift >= 0 && w.shift <= 32 && w.out_off >= 0 &&
-         w.out_off + w.nframes <= numer_len;
+__device__ __forceinline__ bool item_ok(const g2_gram_item& w, const MapsParam& maps, int n_jobs,
+                                        int64_t numer_len) {
+  if (w.job < 0 || w.job >= n_jobs) return false;
+  const int bk = stage_elems(maps.kind[w.job]);
+  return w.k_len > 0 && (w.k_len % bk) == 0 && (w.a_k0 % bk) == 0 && (w.b_k0 % bk) == 0 && w.nframes > 0 &&
+         w.shift >= 0 && w.shift <= 32 && w.out_off >= 0 && w.out_off + w.nframes <= numer_len;
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
@@ -120,18 +128,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok(w, n_jobs, numer_len)) continue;
+        if (!item_ok(w, maps, n_jobs, numer_len)) continue;
         const CUtensorMap* ma = &maps.a[w.job];
         const CUtensorMap* mb = &maps.b[w.job];
-        const int nk = w.k_len / BK;
+        const int bk = stage_elems(maps.kind[w.job]);
+        const int nk = w.k_len / bk;
         for (int kb = 0; kb < nk; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err)) {
             ok = false;
             break;
           }
           mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
-          tma_load_2d(sA + stage * A_BYTES, ma, &full[stage], w.a_k0 + kb * BK, w.i0);
-          tma_load_2d(sB + stage * B_BYTES, mb, &full[stage], w.b_k0 + kb * BK, w.j0);
+          tma_load_2d(sA + stage * A_BYTES, ma, &full[stage], w.a_k0 + kb * bk, w.i0);
+          tma_load_2d(sB + stage * B_BYTES, mb, &full[stage], w.b_k0 + kb * bk, w.j0);
           ++issued;
           if (++stage == STAGES) {
             stage = 0;
@@ -157,13 +166,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok(w, n_jobs, numer_len)) continue;
+        if (!item_ok(w, maps, n_jobs, numer_len)) continue;
+        const bool fp8 = maps.kind[w.job] == G2_KIND_E4M3;
         const int buf = static_cast<int>(local & 1);
         const uint32_t ap = static_cast<uint32_t>((local >> 1) & 1);
         if (!mbar_wait(&acce[buf], ap ^ 1, abort_flag, err)) break;
         tc_fence_after();
         const uint32_t d_tmem = tmem_base + static_cast<uint32_t>(buf * BN);
-        const int nk = w.k_len / BK;
+        const int nk = w.k_len / stage_elems(maps.kind[w.job]);
         for (int kb = 0; kb < nk; ++kb) {
           if (!mbar_wait(&full[stage], phase, abort_flag, err)) {
             ok = false;
@@ -172,10 +182,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           tc_fence_after();
           const uint32_t a0 = smem_addr(sA + stage * A_BYTES);
           const uint32_t b0 = smem_addr(sB + stage * B_BYTES);
+          // four MMAs of 32 bytes of K each (K = 16 fp16 or 32 e4m3)
+          if (fp8) {
 #pragma unroll
-          for (int kk = 0; kk < BK / 16; ++kk) {
-            tc_mma_f16(d_tmem, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), IDESC,
-                       (kb | kk) != 0 ? 1u : 0u);
+            for (int kk = 0; kk < 4; ++kk)
+              tc_mma_f8f6f4(d_tmem, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), IDESC,
+                            (kb | kk) != 0 ? 1u : 0u);
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+              tc_mma_f16(d_tmem, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), IDESC,
+                         (kb | kk) != 0 ? 1u : 0u);
           }
           tc_commit(&empty[stage]);
           if (++stage == STAGES) {
@@ -199,7 +216,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     int64_t local = 0;
     for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x, ++local) {
       const g2_gram_item w = items[it];
-      if (!item_ok(w, n_jobs, numer_len)) {
+      if (!item_ok(w, maps, n_jobs, numer_len)) {
         if (etid == 0) atomicOr(err, G2_DEVERR_BOUNDS);
         --local;
         continue;
@@ -259,7 +276,8 @@ extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item
   for (int j = 0; j < n_jobs; ++j) {
     const g2_job& jb = jobs[j];
     if (!jb.packed_dev || !aligned(jb.packed_dev, 16) || jb.nframes <= 0 || jb.nframes >= (1ll << 31) ||
-        jb.packed_cols <= 0 || jb.packed_cols % G2_BK != 0 || jb.packed_cols >= (1ll << 31))
+        jb.packed_cols <= 0 || jb.packed_cols % G2_PAD != 0 || jb.packed_cols >= (1ll << 31) ||
+        (jb.elem_kind != G2_KIND_FP16 && jb.elem_kind != G2_KIND_E4M3))
       return G2_ERR_ARG;
   }
   if (n_items == 0) return G2_OK;
@@ -268,10 +286,15 @@ extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item
   std::lock_guard<std::mutex> lk(*mu);
   std::memset(&maps, 0, sizeof(maps));
   for (int j = 0; j < n_jobs; ++j) {
-    int st = encode_tmap_fp16_2d(&maps.a[j], jobs[j].packed_dev, jobs[j].packed_cols, jobs[j].nframes, tc::BK, tc::BM);
+    const int eb = jobs[j].elem_kind == G2_KIND_E4M3 ? 1 : 2;
+    const uint32_t box_cols = tc::ROW_BYTES / eb;
+    int st = encode_tmap_2d(&maps.a[j], jobs[j].packed_dev, eb, jobs[j].packed_cols, jobs[j].nframes, box_cols,
+                            tc::BM);
     if (st != G2_OK) return st;
-    st = encode_tmap_fp16_2d(&maps.b[j], jobs[j].packed_dev, jobs[j].packed_cols, jobs[j].nframes, tc::BK, tc::BN);
+    st = encode_tmap_2d(&maps.b[j], jobs[j].packed_dev, eb, jobs[j].packed_cols, jobs[j].nframes, box_cols,
+                        tc::BN);
     if (st != G2_OK) return st;
+    maps.kind[j] = jobs[j].elem_kind;
   }
   if (cudaFuncSetAttribute(tc::gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES) !=
       cudaSuccess)

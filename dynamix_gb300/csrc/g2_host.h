@@ -20,9 +20,10 @@ inline int launch_status() {
 // Current device's SM count (cached per device).
 int sm_count_current();
 
-// Encode a 2-D fp16 tiled tensor map over a row-major [rows][cols] matrix
-// with a (box_cols x box_rows) box, 128-byte swizzle, zero fill outside.
-int encode_tmap_fp16_2d(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint32_t box_cols,
-                        uint32_t box_rows);
+// Encode a 2-D tiled tensor map over a row-major [rows][cols] matrix of
+// 2-byte (fp16) or 1-byte (e4m3, as uint8) elements with a (box_cols x
+// box_rows) box, 128-byte swizzle, zero fill outside.
+int encode_tmap_2d(CUtensorMap* map, const void* base, int elem_bytes, uint64_t cols, uint64_t rows,
+                   uint32_t box_cols, uint32_t box_rows);
 
 }  // namespace g2

@@ -12,6 +12,7 @@
 // Replaces compute_sums_dense (densecorrelator.cl:65-150) and the gather /
 // float32 cast of py_dense_correlator (dense.py:48-50).
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include "g2_ptx.cuh"
 #include "g2_host.h"
 
@@ -25,12 +26,16 @@ constexpr int FR = 4;                         // frames per step (loads in fligh
 __device__ __forceinline__ uint32_t half_bits(uint32_t v) {
   return static_cast<uint32_t>(__half_as_ushort(__uint2half_rn(v)));
 }
+// e4m3 byte of an integer count 0..16 (exact in e4m3)
+__device__ __forceinline__ uint32_t e4m3_bits(uint32_t v) {
+  return static_cast<uint32_t>(__nv_cvt_float_to_fp8(static_cast<float>(v), __NV_SATFINITE, __NV_E4M3));
+}
 
 template <typename Tin>
 __global__ void __launch_bounds__(THREADS)
     pack_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix, const int32_t* __restrict__ col_src,
                 const int32_t* __restrict__ seg_bin, const int32_t* __restrict__ seg_dst0,
-                const int32_t* __restrict__ seg_dst1, int64_t n_segs, int split, uint16_t* __restrict__ packed,
+                const int32_t* __restrict__ seg_dst1, int64_t n_segs, int mode, uint8_t* __restrict__ packed,
                 int64_t packed_cols, unsigned long long* __restrict__ sums, int n_bins,
                 uint32_t* __restrict__ seg_emax, int32_t* __restrict__ err) {
   __shared__ unsigned long long s_sum[FR][SEGS_PER_BLOCK];
@@ -52,9 +57,9 @@ __global__ void __launch_bounds__(THREADS)
     src[3] = s4.w;
     bin = seg_bin[seg];
     dst0 = static_cast<int64_t>(seg_dst0[seg]) + qd * 4;
-    dst1 = split ? static_cast<int64_t>(seg_dst1[seg]) + qd * 4 : 0;
+    dst1 = mode == 1 ? static_cast<int64_t>(seg_dst1[seg]) + qd * 4 : 0;
     bool bad = bin < 0 || bin >= n_bins || dst0 < 0 || dst0 + 4 > packed_cols ||
-               (split && (dst1 < 0 || dst1 + 4 > packed_cols));
+               (mode == 1 && (dst1 < 0 || dst1 + 4 > packed_cols));
     for (int k = 0; k < 4; ++k) bad |= src[k] >= npix;
     if (bad) {
       if (qd == 0) atomicOr(err, G2_DEVERR_BOUNDS);
@@ -81,14 +86,22 @@ __global__ void __launch_bounds__(THREADS)
       const int64_t t = t0 + f;
       uint32_t ssum = v[f][0] + v[f][1] + v[f][2] + v[f][3];
       uint32_t e0, e1 = 0;
-      if (!split) {
+      if (mode == 2) {
+        e0 = v[f][0] * v[f][0] + v[f][1] * v[f][1] + v[f][2] * v[f][2] + v[f][3] * v[f][3];
+        range_bad |= (v[f][0] | v[f][1] | v[f][2] | v[f][3]) > 16u ? 1u : 0u;
+        if (writes && t < T) {
+          const uint32_t o = e4m3_bits(v[f][0]) | (e4m3_bits(v[f][1]) << 8) | (e4m3_bits(v[f][2]) << 16) |
+                             (e4m3_bits(v[f][3]) << 24);
+          *reinterpret_cast<uint32_t*>(packed + t * packed_cols + dst0) = o;
+        }
+      } else if (mode == 0) {
         e0 = v[f][0] * v[f][0] + v[f][1] * v[f][1] + v[f][2] * v[f][2] + v[f][3] * v[f][3];
         range_bad |= (v[f][0] | v[f][1] | v[f][2] | v[f][3]) > 2048u ? 1u : 0u;
         if (writes && t < T) {
           uint2 o;
           o.x = half_bits(v[f][0]) | (half_bits(v[f][1]) << 16);
           o.y = half_bits(v[f][2]) | (half_bits(v[f][3]) << 16);
-          *reinterpret_cast<uint2*>(packed + t * packed_cols + dst0) = o;
+          *reinterpret_cast<uint2*>(packed + 2 * (t * packed_cols + dst0)) = o;
         }
       } else {
         uint32_t h[4], l[4];
@@ -107,8 +120,8 @@ __global__ void __launch_bounds__(THREADS)
           oh.y = half_bits(h[2]) | (half_bits(h[3]) << 16);
           ol.x = half_bits(l[0]) | (half_bits(l[1]) << 16);
           ol.y = half_bits(l[2]) | (half_bits(l[3]) << 16);
-          *reinterpret_cast<uint2*>(packed + t * packed_cols + dst0) = oh;
-          *reinterpret_cast<uint2*>(packed + t * packed_cols + dst1) = ol;
+          *reinterpret_cast<uint2*>(packed + 2 * (t * packed_cols + dst0)) = oh;
+          *reinterpret_cast<uint2*>(packed + 2 * (t * packed_cols + dst1)) = ol;
         }
       }
 #pragma unroll
@@ -148,7 +161,7 @@ __global__ void __launch_bounds__(THREADS)
   }
   if (writes && qd == 0) {
     if (emax0) atomicMax(&seg_emax[dst0 >> 6], emax0);
-    if (split && emax1) atomicMax(&seg_emax[dst1 >> 6], emax1);
+    if (mode == 1 && emax1) atomicMax(&seg_emax[dst1 >> 6], emax1);
   }
   if (range_bad) atomicOr(err, G2_DEVERR_RANGE);
 }
@@ -174,7 +187,7 @@ __global__ void binned_max_kernel(const Tin* __restrict__ frames, int64_t T, int
 
 extern "C" int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
                               const int32_t* col_src_dev, const int32_t* seg_bin_dev, const int32_t* seg_dst0_dev,
-                              const int32_t* seg_dst1_dev, int64_t n_segs, int32_t split, void* packed_dev,
+                              const int32_t* seg_dst1_dev, int64_t n_segs, int32_t mode, void* packed_dev,
                               int64_t packed_cols, int64_t* sums_dev, int32_t n_bins, uint32_t* seg_emax_dev,
                               int32_t* err_dev, void* stream) {
   using namespace g2;
@@ -182,7 +195,7 @@ extern "C" int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_
       !seg_emax_dev || !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || nframes <= 0 || npix <= 0 || npix >= (1ll << 31) || n_segs < 0 ||
-      (split != 0 && split != 1) || (split == 1 && !seg_dst1_dev) || packed_cols <= 0 || packed_cols % 64 != 0 ||
+      mode < 0 || mode > 2 || (mode == 1 && !seg_dst1_dev) || packed_cols <= 0 || packed_cols % G2_PAD != 0 ||
       n_bins <= 0)
     return G2_ERR_ARG;
   if (!aligned(col_src_dev, 16) || !aligned(packed_dev, 16)) return G2_ERR_ARG;
@@ -199,15 +212,15 @@ extern "C" int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_
   if (gy < 1) gy = 1;
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
   auto* sums = reinterpret_cast<unsigned long long*>(sums_dev);
-  auto* out = reinterpret_cast<uint16_t*>(packed_dev);
+  auto* out = reinterpret_cast<uint8_t*>(packed_dev);
   if (elem_bytes == 1)
     pack::pack_kernel<uint8_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
         reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, col_src_dev, seg_bin_dev, seg_dst0_dev,
-        seg_dst1_dev, n_segs, split, out, packed_cols, sums, n_bins, seg_emax_dev, err_dev);
+        seg_dst1_dev, n_segs, mode, out, packed_cols, sums, n_bins, seg_emax_dev, err_dev);
   else
     pack::pack_kernel<uint16_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
         reinterpret_cast<const uint16_t*>(frames_dev), nframes, npix, col_src_dev, seg_bin_dev, seg_dst0_dev,
-        seg_dst1_dev, n_segs, split, out, packed_cols, sums, n_bins, seg_emax_dev, err_dev);
+        seg_dst1_dev, n_segs, mode, out, packed_cols, sums, n_bins, seg_emax_dev, err_dev);
   return launch_status();
 }
 

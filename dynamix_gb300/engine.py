@@ -20,7 +20,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .plan import EXACT_LIMIT, FP16_MAX_EXACT, PackLayout, chunk_grams, gram_items
+from .plan import (E4M3_MAX_EXACT, EXACT_LIMIT, FP16_MAX_EXACT, MODE_BYTES, MODE_E4M3, MODE_FP16, PackLayout,
+                   chunk_grams, gram_items)
 
 
 def _torch():
@@ -83,10 +84,17 @@ def frames_to_device(frames, dev):
 
 
 class DenseEngine:
-    """Exact g2 of a dense (T, H, W) stack for the bins of one q-mask."""
+    """Exact g2 of a dense (T, H, W) stack for the bins of one q-mask.
+
+    ``operand`` selects the packed element type of the tensor-core Gram:
+    ``"auto"`` (e4m3 when every binned count is <= 16, else fp16 counts when
+    <= 2048, else fp16 byte planes), or one of ``"e4m3"``, ``"fp16"``,
+    ``"bytes"``.  The plain comparator always uses fp16."""
+
+    MODES = {"fp16": MODE_FP16, "bytes": MODE_BYTES, "e4m3": MODE_E4M3}
 
     def __init__(self, shape, nframes, qmask, n_bins, scale, device=None, method="tc",
-                 exact_limit=EXACT_LIMIT, grid=0):
+                 exact_limit=EXACT_LIMIT, grid=0, operand="auto"):
         torch = _torch()
         self.lib = _lib.load()
         self.dev = require_cuda(device)
@@ -97,7 +105,12 @@ class DenseEngine:
         self.n_bins = int(n_bins)
         if method not in ("tc", "plain"):
             raise ValueError("method must be 'tc' or 'plain'")
+        if operand != "auto" and operand not in self.MODES:
+            raise ValueError("operand must be 'auto', 'e4m3', 'fp16' or 'bytes'")
+        if method == "plain" and operand == "e4m3":
+            raise ValueError("the plain kernel reads fp16 operands")
         self.method = method
+        self.operand = operand
         self.exact_limit = int(exact_limit)
         self.grid = int(grid)
         self.scale = torch.as_tensor(np.asarray(scale, dtype=np.float64), device=self.dev)
@@ -114,6 +127,7 @@ class DenseEngine:
         self._items_cache = {}
         self.packed = None
         self.last = {}
+        self._u8_hint = MODE_E4M3 if method == "tc" else MODE_FP16
         self.profile = False      # record CUDA events around every stage
         self.stage_ms = {}
         self._events = []
@@ -141,54 +155,60 @@ class DenseEngine:
         return out
 
     # -- layout / buffers ------------------------------------------------
-    def _layout(self, split):
-        if split not in self._layouts:
+    def _layout(self, mode):
+        if mode not in self._layouts:
             torch = _torch()
-            L = PackLayout(self.qmask, self.n_bins, split)
+            L = PackLayout(self.qmask, self.n_bins, mode)
             d = lambda a: torch.as_tensor(a, device=self.dev)
             L.d_col_src = d(L.col_src)
             L.d_seg_bin = d(L.seg_bin)
             L.d_seg_dst0 = d(L.seg_dst0)
             L.d_seg_dst1 = d(L.seg_dst1)
             L.d_seg_emax = torch.zeros(L.packed_cols // _lib.BK, dtype=torch.int32, device=self.dev)
-            self._layouts[split] = L
-        return self._layouts[split]
+            self._layouts[mode] = L
+        return self._layouts[mode]
 
-    def _packed_buffer(self, cols):
+    def _packed_buffer(self, nbytes):
         torch = _torch()
-        need = self.T * cols
-        if self.packed is None or self.packed.numel() < need:
+        if self.packed is None or self.packed.numel() < nbytes:
             self.packed = None
-            self.packed = torch.empty(need, dtype=torch.float16, device=self.dev)
+            self.packed = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
         return self.packed
 
     # -- stages ----------------------------------------------------------
-    def choose_split(self, frames_dev):
-        if frames_dev.element_size() == 1:
-            return 0
-        L0 = self._layout(0)
+    def _binned_max(self, frames_dev):
+        L0 = self._layout(MODE_FP16)
         self.maxval.zero_()
-        _lib.check(self.lib.g2_binned_max(ptr(frames_dev), 2, self.T, self.npix, ptr(L0.d_col_src),
-                                          L0.col_src.size, ptr(self.maxval), stream_handle(self.dev)),
-                   "g2_binned_max")
-        return 0 if int(self.maxval.item()) <= FP16_MAX_EXACT else 1
+        _lib.check(self.lib.g2_binned_max(ptr(frames_dev), frames_dev.element_size(), self.T, self.npix,
+                                          ptr(L0.d_col_src), L0.col_src.size, ptr(self.maxval),
+                                          stream_handle(self.dev)), "g2_binned_max")
+        return int(self.maxval.item())
 
-    def pack(self, frames_dev, split):
-        L = self._layout(split)
-        packed = self._packed_buffer(L.packed_cols)
+    def choose_mode(self, frames_dev):
+        if self.operand != "auto":
+            return self.MODES[self.operand]
+        if frames_dev.element_size() == 1:
+            return self._u8_hint
+        m = self._binned_max(frames_dev)
+        if m <= E4M3_MAX_EXACT and self.method == "tc":
+            return MODE_E4M3
+        return MODE_FP16 if m <= FP16_MAX_EXACT else MODE_BYTES
+
+    def pack(self, frames_dev, mode):
+        L = self._layout(mode)
+        packed = self._packed_buffer(self.T * L.packed_bytes_per_frame)
         self.sums.zero_()
         L.d_seg_emax.zero_()
         self.err.zero_()
         st = stream_handle(self.dev)
         _lib.check(self.lib.g2_pack_frames(
             ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_col_src), ptr(L.d_seg_bin),
-            ptr(L.d_seg_dst0), ptr(L.d_seg_dst1), L.n_segs, split, ptr(packed), L.packed_cols, ptr(self.sums),
+            ptr(L.d_seg_dst0), ptr(L.d_seg_dst1), L.n_segs, mode, ptr(packed), L.packed_cols, ptr(self.sums),
             self.n_bins, ptr(L.d_seg_emax), ptr(self.err), st), "g2_pack_frames")
         return L
 
-    def items_for(self, L, seg_emax):
-        grams = chunk_grams(L, seg_emax, self.exact_limit)
-        key = (L.split, self.method, tuple(grams))
+    def items_for(self, L, grams):
+        key = (L.mode, self.method, tuple(grams))
         if key not in self._items_cache:
             torch = _torch()
             items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method)
@@ -200,7 +220,7 @@ class DenseEngine:
 
     def numerator(self, L, items_dev, n_items):
         self.numer.zero_()
-        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols)])
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind)])
         st = stream_handle(self.dev)
         if self.method == "tc":
             _lib.check(self.lib.g2_gram_tc(jobs, 1, ptr(items_dev), n_items, ptr(self.numer), self.numer.numel(),
@@ -223,6 +243,34 @@ class DenseEngine:
         if code:
             raise DeviceError(_lib.device_error_message(code))
 
+    def _pack_and_plan(self, frames_dev, mode):
+        """Pack, read the segment energies and the error word (one sync), plan
+        the K split; fall back to a wider packing when the counts do not fit."""
+        while True:
+            L = self.pack(frames_dev, mode)
+            seg_emax = L.d_seg_emax.cpu().numpy().view(np.uint32)
+            code = int(self.err.item())
+            if code & _lib.DEVERR_RANGE and mode == MODE_E4M3 and self.operand == "auto":
+                mode = MODE_FP16
+                self._u8_hint = MODE_FP16
+                continue
+            if code & _lib.DEVERR_RANGE and mode == MODE_FP16 and self.operand == "auto":
+                mode = MODE_BYTES
+                continue
+            if code:
+                raise DeviceError(_lib.device_error_message(code))
+            try:
+                grams = chunk_grams(L, seg_emax, self.exact_limit)
+            except OverflowError:
+                if mode != MODE_BYTES and self.operand == "auto":
+                    mode = MODE_BYTES
+                    continue
+                raise
+            if (mode == MODE_FP16 and frames_dev.element_size() == 1 and self.method == "tc"
+                    and self.operand == "auto" and seg_emax.size and int(seg_emax.max()) < 17 * 17):
+                self._u8_hint = MODE_E4M3        # every count <= 16: the next call can use e4m3
+            return L, grams
+
     # -- whole pipeline ----------------------------------------------------
     def run(self, frames_dev):
         """Run G1..G4 on a device stack; returns the float32 g2 device tensor.
@@ -235,28 +283,17 @@ class DenseEngine:
             return self.g2_f32[:0]
         self._events = []
         self._mark("split")
-        split = self.choose_split(frames_dev)
+        mode = self.choose_mode(frames_dev)
         self._mark("pack")
-        L = self.pack(frames_dev, split)
-        self._mark("plan")
-        seg_emax = L.d_seg_emax.cpu().numpy().view(np.uint32)
-        self.check_error()
-        try:
-            grams = chunk_grams(L, seg_emax, self.exact_limit)
-        except OverflowError:
-            if split == 1:
-                raise
-            L = self.pack(frames_dev, 1)
-            seg_emax = L.d_seg_emax.cpu().numpy().view(np.uint32)
-            self.check_error()
-        items, items_dev, n_chunks = self.items_for(L, seg_emax)
+        L, grams = self._pack_and_plan(frames_dev, mode)
+        items, items_dev, n_chunks = self.items_for(L, grams)
         self._mark("gram_" + self.method)
         self.numerator(L, items_dev, items.size)
         self._mark("normalise")
         self.normalise()
         self._mark("end")
-        self.last = {"split": L.split, "n_items": int(items.size), "n_grams": n_chunks,
-                     "packed_cols": L.packed_cols}
+        self.last = {"mode": ["fp16", "bytes", "e4m3"][L.mode], "split": int(L.split), "n_items": int(items.size),
+                     "n_grams": n_chunks, "packed_cols": L.packed_cols}
         return self.g2_f32[: self.n_bins]
 
     def check_denominator_range(self):

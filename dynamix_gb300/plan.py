@@ -1,15 +1,17 @@
 """Host-side planning of the dense g2 pipeline.
 
-* :class:`PackLayout` -- where each q-bin's pixels go in the packed fp16
-  operand matrix ``[T][packed_cols]`` (bins are contiguous, each padded to a
-  multiple of 64 columns; with ``split=1`` a bin holds a high-byte plane and a
-  low-byte plane side by side).
+* :class:`PackLayout` -- where each q-bin's pixels go in the packed operand
+  matrix ``[T][packed_cols]``.  Bins are contiguous and padded to a multiple
+  of 128 columns.  Packing modes: 0 = fp16 counts (<= 2048), 1 = fp16 high-byte
+  and low-byte planes side by side (any uint16), 2 = e4m3 counts (<= 16, one
+  byte per element).
 * :func:`k_chunks` -- the K split of one Gram so that every fp32 partial sum
   is an integer below ``limit`` (2^24 by default): by Cauchy-Schwarz,
   ``|sum_k a(t,k) b(t',k)| <= sqrt(max_t sum a^2 * max_t' sum b^2)``, and the
   pack kernel reports ``max_t sum`` of squares per 64-column segment.
 * :func:`gram_items` -- the upper-triangle item list (g2_gram_item records) for
-  one job, LPT-ordered (longest K first) for the persistent kernel.
+  one job, LPT-ordered (longest K first) and, within a Gram, grouped in square
+  super-tiles so that the CTAs running at the same time share operand rows in L2.
 
 The per-bin arithmetic it plans is that of ``py_dense_correlator``
 (dynamix/correlator/dense.py:48-64) with bins from ``BaseCorrelator._set_qmask``
@@ -19,10 +21,14 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._lib import BK, ITEM_DTYPE, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN
+from ._lib import BK, ITEM_DTYPE, KIND_E4M3, KIND_FP16, PAD, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN
 
 EXACT_LIMIT = 1 << 24   # fp32 represents every integer up to 2^24 exactly
 FP16_MAX_EXACT = 2048   # fp16 represents every integer up to 2^11 exactly
+E4M3_MAX_EXACT = 16     # e4m3 represents every integer up to 2^4 exactly
+SUPER_ROWS = 2048       # frames per side of a super-tile
+
+MODE_FP16, MODE_BYTES, MODE_E4M3 = 0, 1, 2
 
 
 def _roundup(x, m):
@@ -30,19 +36,22 @@ def _roundup(x, m):
 
 
 class PackLayout:
-    """Packed-column layout of the bins of one q-mask."""
+    """Packed-column layout of the bins of one q-mask for one packing mode."""
 
-    def __init__(self, qmask, n_bins, split):
+    def __init__(self, qmask, n_bins, mode):
         qflat = np.ascontiguousarray(qmask, dtype=np.int32).ravel()
         qflat = np.where(qflat >= 1, qflat, 0)               # bins are 1..n_bins, the rest unused
         self.npix_total = qflat.size
         self.n_bins = int(n_bins)
-        self.split = int(split)
+        self.mode = int(mode)
+        self.split = self.mode == MODE_BYTES
+        self.kind = KIND_E4M3 if self.mode == MODE_E4M3 else KIND_FP16
+        self.elem_bytes = 1 if self.mode == MODE_E4M3 else 2
         order = np.argsort(qflat, kind="stable")            # raster order within each bin
         counts = np.bincount(qflat, minlength=self.n_bins + 1)[: self.n_bins + 1]
         starts = np.concatenate([[0], np.cumsum(counts)])
         self.npix = counts[1:].astype(np.int64)               # P_b, b = 1..n_bins
-        self.kpad = _roundup(self.npix, BK)
+        self.kpad = _roundup(self.npix, PAD)
         nseg_b = self.kpad // BK
         self.n_segs = int(nseg_b.sum())
         col_src = np.full(int(self.kpad.sum()), -1, dtype=np.int32)
@@ -55,9 +64,9 @@ class PackLayout:
         seg_local = np.arange(self.n_segs, dtype=np.int64) - np.repeat(self.src_off // BK, nseg_b)
         width = self.kpad * (2 if self.split else 1)
         self.bin_off = np.concatenate([[0], np.cumsum(width)])[:-1].astype(np.int64)
-        self.packed_cols = int(max(BK, width.sum()))
+        self.packed_cols = int(max(PAD, width.sum()))
         # plane offsets (first packed column) per bin
-        self.plane0 = self.bin_off.copy()                       # counts (split 0) or high bytes
+        self.plane0 = self.bin_off.copy()                       # counts, or high bytes
         self.plane1 = self.bin_off + self.kpad if self.split else None  # low bytes
         self.seg_dst0 = (np.repeat(self.plane0, nseg_b) + seg_local * BK).astype(np.int32)
         if self.split:
@@ -66,6 +75,10 @@ class PackLayout:
             self.seg_dst1 = np.zeros(self.n_segs, dtype=np.int32)
         if self.packed_cols >= 2 ** 31:
             raise ValueError("too many binned pixels for one job")
+
+    @property
+    def packed_bytes_per_frame(self):
+        return self.packed_cols * self.elem_bytes
 
     def grams(self):
         """The Grams to run per bin: (bin, a_plane_off, b_plane_off, kpad, shift)."""
@@ -86,42 +99,46 @@ class PackLayout:
 
 
 def k_chunks(emax_a, emax_b, limit=EXACT_LIMIT):
-    """Split a Gram's 64-column segments into chunks with exact fp32 sums.
+    """Split a Gram's units into chunks with exact fp32 sums.
 
-    ``emax_a[s]`` / ``emax_b[s]``: max over frames of the sum of squares of the
-    A / B packed values in segment ``s``.  A chunk ``[s0, s1)`` is valid when
-    ``sum(emax_a) * sum(emax_b) <= limit^2`` (hence every partial sum of the
-    dot products is <= limit).  A single segment always fits (64 * 2048^2 can
-    exceed 2^24, but then the K split cannot help; such a segment is reported
-    as infeasible).  Returns a list of ``(s0, s1)``.
+    ``emax_a[u]`` / ``emax_b[u]``: bound on the sum of squares of the A / B
+    packed values of unit ``u`` over every frame.  A chunk ``[u0, u1)`` is valid
+    when ``sum(emax_a) * sum(emax_b) <= limit^2`` (hence every partial sum of
+    the dot products is <= limit).  A unit that alone exceeds the bound is
+    infeasible (OverflowError).  Returns a list of ``(u0, u1)``.
     """
     ea = np.asarray(emax_a, dtype=np.float64)
     eb = np.asarray(emax_b, dtype=np.float64)
     n = ea.size
     lim2 = float(limit) * float(limit)
     if n and np.any(ea * eb > lim2):
-        raise OverflowError("a 64-column segment exceeds the exact fp32 bound")
+        raise OverflowError("a packed unit exceeds the exact fp32 bound")
+    if n and ea.sum() * eb.sum() <= lim2:
+        return [(0, n)]
     chunks = []
-    s0 = 0
+    u0 = 0
     sa = sb = 0.0
-    for s in range(n):
-        na, nb = sa + ea[s], sb + eb[s]
+    for u in range(n):
+        na, nb = sa + ea[u], sb + eb[u]
         if na * nb > lim2:
-            chunks.append((s0, s))
-            s0, sa, sb = s, ea[s], eb[s]
+            chunks.append((u0, u))
+            u0, sa, sb = u, ea[u], eb[u]
         else:
             sa, sb = na, nb
     if n:
-        chunks.append((s0, n))
+        chunks.append((u0, n))
     return chunks
 
 
 _TILE_CACHE = {}
 
 
-def _tiles(T, bm, bn):
-    """(i0, j0) of every bm x bn block that holds some t' >= t, t, t' < T."""
-    key = (T, bm, bn)
+def _tiles(T, bm, bn, super_rows=SUPER_ROWS):
+    """(i0, j0) of every bm x bn block holding some t' >= t (t, t' < T).
+
+    Ordered by square super-tiles of ``super_rows`` frames per side (upper
+    triangle, row-major), then row-major inside a super-tile."""
+    key = (T, bm, bn, super_rows)
     if key not in _TILE_CACHE:
         ni = -(-T // bm)
         nj = -(-T // bn)
@@ -129,7 +146,9 @@ def _tiles(T, bm, bn):
         i0 = (ii * bm).ravel()
         j0 = (jj * bn).ravel()
         keep = j0 + bn - 1 >= i0
-        _TILE_CACHE[key] = (i0[keep].astype(np.int32), j0[keep].astype(np.int32))
+        i0, j0 = i0[keep], j0[keep]
+        order = np.lexsort((j0, i0, j0 // super_rows, i0 // super_rows))
+        _TILE_CACHE[key] = (i0[order].astype(np.int32), j0[order].astype(np.int32))
     return _TILE_CACHE[key]
 
 
@@ -165,17 +184,18 @@ def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc"):
 
 
 def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT):
-    """Apply :func:`k_chunks` to every Gram of a layout.
+    """Apply :func:`k_chunks` to every Gram of a layout, in units of PAD columns.
 
     ``seg_emax`` is indexed by packed column // 64.  Returns the list of
-    ``(bin, a_off, b_off, k0, k_len, shift)`` and the number of chunks."""
+    ``(bin, a_off, b_off, k0, k_len, shift)``."""
+    per = PAD // BK
     out = []
     for (b, a_off, b_off, kp, shift) in layout.grams():
         nseg = kp // BK
-        ea = seg_emax[a_off // BK: a_off // BK + nseg]
-        eb = seg_emax[b_off // BK: b_off // BK + nseg]
-        for (s0, s1) in k_chunks(ea, eb, limit):
-            out.append((b, a_off, b_off, s0 * BK, (s1 - s0) * BK, shift))
+        ea = np.asarray(seg_emax[a_off // BK: a_off // BK + nseg], dtype=np.float64).reshape(-1, per).sum(1)
+        eb = np.asarray(seg_emax[b_off // BK: b_off // BK + nseg], dtype=np.float64).reshape(-1, per).sum(1)
+        for (u0, u1) in k_chunks(ea, eb, limit):
+            out.append((b, a_off, b_off, u0 * PAD, (u1 - u0) * PAD, shift))
     return out
 
 

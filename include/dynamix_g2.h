@@ -39,14 +39,19 @@ extern "C" {
 #define G2_ABI_VERSION      1
 
 /* Tile sizes of the tensor-core Gram: an item covers a 128 x 256 block of
- * the (t, t') Gram, the plain kernel a 128 x 128 block; k_len is a multiple
- * of 64 packed columns. */
+ * the (t, t') Gram, the plain kernel a 128 x 128 block.  A pipeline stage
+ * holds 128 bytes of K per row: 64 fp16 or 128 e4m3 elements; an item's k
+ * offsets and k_len are multiples of that. */
 #define G2_TC_BM      128
 #define G2_TC_BN      256
 #define G2_PLAIN_BM   128
 #define G2_PLAIN_BN   128
-#define G2_BK         64
+#define G2_PAD        128  /* packed_cols and bin segments are multiples of this */
 #define G2_MAX_JOBS   32
+
+/* element kinds of a packed operand matrix */
+#define G2_KIND_FP16  0    /* fp16 bit patterns of integer counts <= 2048 */
+#define G2_KIND_E4M3  1    /* e4m3 bytes of integer counts <= 16 */
 
 /* One unit of Gram work: rows [i0, i0+BM) of the A operand against rows
  * [j0, j0+BN) of the B operand over packed columns [a_k0, a_k0+k_len) and
@@ -56,20 +61,23 @@ typedef struct g2_gram_item {
     int32_t job;       /* index into the jobs array of the launch */
     int32_t i0;        /* first frame of the A rows */
     int32_t j0;        /* first frame of the B rows */
-    int32_t a_k0;      /* first packed column of A (multiple of 64) */
-    int32_t b_k0;      /* first packed column of B (multiple of 64) */
-    int32_t k_len;     /* packed columns, multiple of 64, > 0 */
+    int32_t a_k0;      /* first packed column of A (multiple of the stage width) */
+    int32_t b_k0;      /* first packed column of B (multiple of the stage width) */
+    int32_t k_len;     /* packed columns, multiple of the stage width, > 0 */
     int32_t shift;     /* weight 2^shift (0, 8 or 16 for byte-split planes) */
     int32_t nframes;   /* T of the job */
     int64_t out_off;   /* element offset of N_b(0) in numer */
 } g2_gram_item;
 
 /* A dense job: its packed operand matrix, row-major [nframes][packed_cols]
- * of fp16 bit patterns (integer counts <= 2048, exact in fp16). */
+ * of fp16 bit patterns (G2_KIND_FP16, counts <= 2048) or e4m3 bytes
+ * (G2_KIND_E4M3, counts <= 16); both represent the integer counts exactly. */
 typedef struct g2_job {
     const void* packed_dev;
     int64_t nframes;
-    int64_t packed_cols;   /* multiple of 64 */
+    int64_t packed_cols;   /* multiple of G2_PAD */
+    int32_t elem_kind;     /* G2_KIND_FP16 or G2_KIND_E4M3 */
+    int32_t reserved;
 } g2_job;
 
 /* ---- host utilities ---------------------------------------------------- */
@@ -86,9 +94,11 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
  * frames_dev: [nframes][npix] counts, elem_bytes 1 (u8) or 2 (u16).
  * Source columns come in 64-column segments; segment s belongs to bin
  * seg_bin[s] (0-based) and col_src[64*s + j] is the flat pixel index of its
- * column j (or -1 for padding).  split == 0: the count is written as fp16 to
- * packed column seg_dst0[s] + j.  split == 1: the high byte goes to
- * seg_dst0[s] + j and the low byte to seg_dst1[s] + j.
+ * column j (or -1 for padding).  mode 0: the count is written as fp16 to
+ * packed column seg_dst0[s] + j.  mode 1: the high byte (fp16) goes to
+ * seg_dst0[s] + j and the low byte to seg_dst1[s] + j.  mode 2: the count is
+ * written as an e4m3 byte (counts <= 16) to seg_dst0[s] + j.  A count that
+ * does not fit the mode sets G2_DEVERR_RANGE in err_dev.
  * Adds S_b(t) into sums_dev[b * nframes + t] (caller zeroes it) and raises
  * seg_emax_dev[c / 64] (caller zeroes it) to max_t of the sum of squares of
  * the packed values in output segment c / 64.
@@ -96,7 +106,7 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
 int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
                    const int32_t* col_src_dev, const int32_t* seg_bin_dev,
                    const int32_t* seg_dst0_dev, const int32_t* seg_dst1_dev, int64_t n_segs,
-                   int32_t split, void* packed_dev, int64_t packed_cols,
+                   int32_t mode, void* packed_dev, int64_t packed_cols,
                    int64_t* sums_dev, int32_t n_bins, uint32_t* seg_emax_dev, int32_t* err_dev,
                    void* stream);
 

@@ -50,7 +50,7 @@ def test_argument_errors_are_caught_on_host(built_lib):
 def test_item_layout_matches_c_struct():
     from dynamix_gb300 import _lib
     assert _lib.ITEM_DTYPE.itemsize == 40
-    assert ctypes.sizeof(_lib.Job) == 24
+    assert ctypes.sizeof(_lib.Job) == 32
     assert list(_lib.ITEM_DTYPE.names) == ["job", "i0", "j0", "a_k0", "b_k0", "k_len", "shift", "nframes",
                                            "out_off"]
     assert np.dtype(_lib.ITEM_DTYPE).fields["out_off"][1] == 32

@@ -10,7 +10,7 @@ import pytest
 
 from conftest import golden
 from dynamix_gb300 import plan
-from dynamix_gb300._lib import BK, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN
+from dynamix_gb300._lib import BK, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN  # noqa: F401
 from dynamix_gb300.speckle import annular_qmask, speckle_numpy
 from oracle import g2_oracle as o
 
@@ -46,17 +46,19 @@ def run_items(packed, items, n_rows, T, bm, bn):
     return N.reshape(n_rows, T)
 
 
-@pytest.mark.parametrize("split", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 @pytest.mark.parametrize("kind", ["tc", "plain"])
 @pytest.mark.parametrize("name", ["dense_small_u8", "dense_u16"])
-def test_item_semantics_reproduce_oracle(name, kind, split):
+def test_item_semantics_reproduce_oracle(name, kind, mode):
     z = golden(name)
     fr, qm = z["frames"], z["qmask"]
     T = fr.shape[0]
     nb = int(qm.max())
-    L = plan.PackLayout(qm, nb, split)
-    if not split and fr.max() > plan.FP16_MAX_EXACT:
+    L = plan.PackLayout(qm, nb, mode)
+    if mode == 0 and fr.max() > plan.FP16_MAX_EXACT:
         pytest.skip("counts do not fit fp16")
+    if mode == 2 and fr.max() > plan.E4M3_MAX_EXACT:
+        pytest.skip("counts do not fit e4m3")
     packed, emax = emulate_pack(fr, L)
     grams = plan.chunk_grams(L, emax)
     items = plan.gram_items(T, grams, kind=kind)
@@ -83,6 +85,19 @@ def test_k_split_honours_bound_with_bright_counts():
     assert np.array_equal(N, o.g2_exact(fr, qm)["numerator"])
 
 
+def test_supertile_order_keeps_rows_local():
+    # consecutive windows of 152 items touch far fewer rows than the whole stack
+    i0, j0 = plan._tiles(10000, TC_BM, TC_BN)
+    rows = []
+    for w in range(0, i0.size - 152, 152):
+        r = set()
+        for a, b in zip(i0[w:w + 152], j0[w:w + 152]):
+            r.update(range(a, a + TC_BM))
+            r.update(range(b, b + TC_BN))
+        rows.append(len(r))
+    assert np.mean(rows) < 6000
+
+
 def test_tiles_cover_upper_triangle_once():
     for T in (1, 5, 127, 128, 129, 255, 256, 257, 300, 1000):
         for bm, bn in ((TC_BM, TC_BN), (PLAIN_BM, PLAIN_BN)):
@@ -101,7 +116,7 @@ def test_layout_groups_bins_in_raster_order():
         pix = L.col_src[L.src_off[b]:L.src_off[b] + L.npix[b]]
         assert np.array_equal(pix, np.flatnonzero(qm.ravel() == b + 1))
         assert np.all(L.col_src[L.src_off[b] + L.npix[b]:L.src_off[b] + L.kpad[b]] == -1)
-    assert L.packed_cols % BK == 0
+    assert L.packed_cols % plan.PAD == 0 and np.all(L.kpad % plan.PAD == 0)
 
 
 def test_gram_macs_matches_config():
