@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(THREADS)
       uint32_t e0, e1 = 0;
       if (mode == 2) {
         e0 = v[f][0] * v[f][0] + v[f][1] * v[f][1] + v[f][2] * v[f][2] + v[f][3] * v[f][3];
-        range_bad |= (v[f][0] | v[f][1] | v[f][2] | v[f][3]) > 16u ? 1u : 0u;
+        range_bad |= max(max(v[f][0], v[f][1]), max(v[f][2], v[f][3])) > 16u ? 1u : 0u;
         if (writes && t < T) {
           const uint32_t o = e4m3_bits(v[f][0]) | (e4m3_bits(v[f][1]) << 8) | (e4m3_bits(v[f][2]) << 16) |
                              (e4m3_bits(v[f][3]) << 24);
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(THREADS)
         }
       } else if (mode == 0) {
         e0 = v[f][0] * v[f][0] + v[f][1] * v[f][1] + v[f][2] * v[f][2] + v[f][3] * v[f][3];
-        range_bad |= (v[f][0] | v[f][1] | v[f][2] | v[f][3]) > 2048u ? 1u : 0u;
+        range_bad |= max(max(v[f][0], v[f][1]), max(v[f][2], v[f][3])) > 2048u ? 1u : 0u;
         if (writes && t < T) {
           uint2 o;
           o.x = half_bits(v[f][0]) | (half_bits(v[f][1]) << 16);
