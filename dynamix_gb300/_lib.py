@@ -53,7 +53,9 @@ SIGNATURES = {
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
     "g2_denominator": (C.c_int, [_p, _i32, _i64, _p, _p]),
     "g2_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
+    "g2_normalize_static": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
 }
+STATIC_DENOM_MAX = 1 << 19
 
 _lock = threading.Lock()
 _lib = None

@@ -11,6 +11,7 @@
 // G4: g2 = scale * N / D in float64 (the only float64 arithmetic on the GPU),
 // written as float32 and/or float64.  0/0 gives NaN as in the reference.
 // Replaces densecorrelator.cl:54, evtcorrelator.cl:75 and dense.py:64.
+#include <mutex>
 #include "g2_ptx.cuh"
 #include "g2_host.h"
 
@@ -90,5 +91,54 @@ extern "C" int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, c
   norm::finalize_kernel<<<static_cast<unsigned>(blocks), 256, 0, as_stream(stream)>>>(
       reinterpret_cast<const long long*>(numer_dev), reinterpret_cast<const long long*>(denom_dev), scale_dev,
       n_rows, nframes, g2_f32_dev, g2_f64_dev);
+  return launch_status();
+}
+
+// ---- G3+G4 for callers that cannot allocate ---------------------------------
+// The denominator is kept in this file-scope device array instead of a
+// caller-allocated buffer.  Host code must not pass the symbol itself to a
+// kernel (on the host it names a stand-in, not device memory): the device
+// address is looked up once per device with cudaGetSymbolAddress.
+static __device__ __align__(256) long long g2_static_denom[G2_STATIC_DENOM_MAX];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+long long* g_static_denom_addr[kMaxDevices] = {};
+}  // namespace
+
+extern "C" int g2_normalize_static(const int64_t* numer_dev, const int64_t* sums_dev, const double* scale_dev,
+                                   int32_t n_rows, int64_t nframes, float* g2_f32_dev, double* g2_f64_dev,
+                                   void* stream) {
+  using namespace g2;
+  if (!numer_dev || !sums_dev || !scale_dev || n_rows < 0 || nframes <= 0 || (!g2_f32_dev && !g2_f64_dev))
+    return G2_ERR_ARG;
+  if (n_rows == 0) return G2_OK;
+  if (static_cast<int64_t>(n_rows) * nframes > G2_STATIC_DENOM_MAX) return G2_ERR_TOO_LARGE;
+  if (n_rows > 65535) return G2_ERR_TOO_LARGE;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return G2_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return G2_ERR_UNSUPPORTED;
+  long long* denom = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_denom_addr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g2_static_denom) != cudaSuccess || p == nullptr) return G2_ERR_CUDA;
+      g_static_denom_addr[dev] = static_cast<long long*>(p);
+    }
+    denom = g_static_denom_addr[dev];
+  }
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  const int64_t gx = (nframes + norm::LAGS - 1) / norm::LAGS;
+  dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(n_rows));
+  norm::denom_kernel<<<grid, norm::LAGS, 0, as_stream(stream)>>>(reinterpret_cast<const long long*>(sums_dev),
+                                                                 nframes, denom);
+  const int64_t total = static_cast<int64_t>(n_rows) * nframes;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > sms * 8) blocks = sms * 8;
+  norm::finalize_kernel<<<static_cast<unsigned>(blocks), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const long long*>(numer_dev), denom, scale_dev, n_rows, nframes, g2_f32_dev, g2_f64_dev);
   return launch_status();
 }

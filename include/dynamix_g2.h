@@ -153,6 +153,27 @@ int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, const double
                 int32_t n_rows, int64_t nframes, float* g2_f32_dev, double* g2_f64_dev,
                 void* stream);
 
+/* ---- G3+G4 without allocation -------------------------------------------
+ * No counterpart in the reference.  Same result as g2_denominator followed by
+ * g2_finalize, for callers that cannot allocate device memory: hosts that hand
+ * this library a device-memory budget that is already fully reserved (the
+ * frame buffers of a detector acquisition pipeline, for instance), and loops
+ * that must not call cudaMalloc/cudaFree because cudaFree waits for the whole
+ * device.  The denominator lives in a file-scope device array of
+ * G2_STATIC_DENOM_MAX elements (int64, 4 MiB) that every GPU which loads this
+ * library holds until the process exits; n_rows * nframes above that maximum
+ * returns G2_ERR_TOO_LARGE.  The caller passes N, S, scale and the outputs.
+ * The first call on a device looks up that array's device address (with the
+ * device current) -- make that first call before any stream capture.  All
+ * calls share the one array and it keeps the last call's contents (every
+ * element a call reads is written by the same call first, so nothing needs
+ * clearing); calls whose work overlaps on the GPU race on it.  This entry
+ * point allocates nothing: no cudaMalloc, no cudaFree. */
+#define G2_STATIC_DENOM_MAX (1 << 19)
+int g2_normalize_static(const int64_t* numer_dev, const int64_t* sums_dev, const double* scale_dev,
+                        int32_t n_rows, int64_t nframes, float* g2_f32_dev, double* g2_f64_dev,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif
