@@ -1,14 +1,19 @@
-// G1: gather each q-bin's pixels of every frame into the packed fp16 operand
-// matrix of the Gram, and compute the per-frame bin sums S_b(t) on the way.
+// G1: gather each q-bin's pixels of every frame into the packed operand matrix
+// of the Gram, and compute the per-frame bin sums S_b(t) on the way.
 //
-// The frames are read once; the packed matrix [T][packed_cols] is written
-// once (bins are contiguous 64-column-padded segments).  Each thread owns
-// four consecutive source columns of one 64-column segment (their pixel
-// indices stay in registers for all frames) and handles FR frames per step.
-// A half-warp covers one segment: its lanes reduce the segment's count sum
-// (for S) and sum of squared packed values (for the exactness bound of the
-// Gram's K split) with shuffles; one thread per block merges the segments of
-// the same bin before the int64 atomic into S.
+// Input-oriented: a block owns a chunk of G2_PACK_CHUNK consecutive pixels of
+// the frame and walks a group of frames.  Per step it loads F frames' chunks
+// with aligned 16-byte loads into shared memory (the frames are read exactly
+// once, coalesced), then every thread moves its binned pixels -- up to 8 per
+// thread, their destinations kept in registers for the whole kernel -- to the
+// packed matrix.  Within a chunk the pixels of one bin are consecutive packed
+// columns, so the stores of a warp are contiguous.  Bin sums and the
+// squared-count energies used for the Gram's exact K split are reduced per warp
+// (match_any + reduce_add), then per block in shared memory; S gets one int64
+// atomic per (chunk, bin, frame).  Energies are kept per "piece" = (64-column
+// output segment) x (chunk): piece_emax[p] = max over frames of the piece's
+// sum of squares; the host sums the pieces of a segment, which bounds the
+// segment's energy in every frame.
 // Replaces compute_sums_dense (densecorrelator.cl:65-150) and the gather /
 // float32 cast of py_dense_correlator (dense.py:48-50).
 #include <cuda_fp16.h>
@@ -20,8 +25,11 @@ namespace g2 {
 namespace pack {
 
 constexpr int THREADS = 256;
-constexpr int SEGS_PER_BLOCK = THREADS / 16;  // 16 threads x 4 columns = one 64-column segment
-constexpr int FR = 4;                         // frames per step (loads in flight)
+constexpr int CH = G2_PACK_CHUNK;        // pixels per chunk
+constexpr int EPT = CH / THREADS;        // binned pixels per thread (max)
+constexpr int MAX_SLOTS = G2_PACK_MAX_SLOTS;
+constexpr int MAX_PIECES = G2_PACK_MAX_PIECES;
+constexpr int PPT = MAX_PIECES / THREADS;  // pieces per thread for the running maxima
 
 __device__ __forceinline__ uint32_t half_bits(uint32_t v) {
   return static_cast<uint32_t>(__half_as_ushort(__uint2half_rn(v)));
@@ -31,139 +39,206 @@ __device__ __forceinline__ uint32_t e4m3_bits(uint32_t v) {
   return static_cast<uint32_t>(__nv_cvt_float_to_fp8(static_cast<float>(v), __NV_SATFINITE, __NV_E4M3));
 }
 
+// Frames per step and bytes of one frame's chunk in shared memory (+16 B for
+// the unaligned start).
 template <typename Tin>
-__global__ void __launch_bounds__(THREADS)
-    pack_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix, const int32_t* __restrict__ col_src,
-                const int32_t* __restrict__ seg_bin, const int32_t* __restrict__ seg_dst0,
-                const int32_t* __restrict__ seg_dst1, int64_t n_segs, int mode, uint8_t* __restrict__ packed,
-                int64_t packed_cols, unsigned long long* __restrict__ sums, int n_bins,
-                uint32_t* __restrict__ seg_emax, int32_t* __restrict__ err) {
-  __shared__ unsigned long long s_sum[FR][SEGS_PER_BLOCK];
-  __shared__ int s_bin[SEGS_PER_BLOCK];
-  const int tid = threadIdx.x;
-  const int lseg = tid >> 4;
-  const int qd = tid & 15;
-  const int64_t seg = static_cast<int64_t>(blockIdx.x) * SEGS_PER_BLOCK + lseg;
-  const bool active = seg < n_segs;
+struct Cfg {
+  static constexpr int F = sizeof(Tin) == 1 ? 4 : 2;
+  static constexpr int CHUNK_BYTES = CH * static_cast<int>(sizeof(Tin));
+  static constexpr int BUF = CHUNK_BYTES + 16;
+  static constexpr int WORDS = CHUNK_BYTES / 16 + 1;  // 16-byte words covering one unaligned chunk
+};
 
-  int32_t src[4] = {-1, -1, -1, -1};
-  int bin = -1;
-  int64_t dst0 = 0, dst1 = 0;
-  if (active) {
-    const int4 s4 = *reinterpret_cast<const int4*>(col_src + seg * 64 + qd * 4);
-    src[0] = s4.x;
-    src[1] = s4.y;
-    src[2] = s4.z;
-    src[3] = s4.w;
-    bin = seg_bin[seg];
-    dst0 = static_cast<int64_t>(seg_dst0[seg]) + qd * 4;
-    dst1 = mode == 1 ? static_cast<int64_t>(seg_dst1[seg]) + qd * 4 : 0;
-    bool bad = bin < 0 || bin >= n_bins || dst0 < 0 || dst0 + 4 > packed_cols ||
-               (mode == 1 && (dst1 < 0 || dst1 + 4 > packed_cols));
-    for (int k = 0; k < 4; ++k) bad |= src[k] >= npix;
-    if (bad) {
-      if (qd == 0) atomicOr(err, G2_DEVERR_BOUNDS);
-      src[0] = src[1] = src[2] = src[3] = -1;
-      bin = -1;
+template <typename Tin, int MODE>
+__global__ void __launch_bounds__(THREADS, 4)
+    pack_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix, const int32_t* __restrict__ chunk_entry_off,
+                const int32_t* __restrict__ entry_dst, const uint32_t* __restrict__ entry_meta,
+                const int32_t* __restrict__ chunk_slot_bin, const int32_t* __restrict__ chunk_piece_off,
+                const int32_t* __restrict__ bin_kpad, uint8_t* __restrict__ packed, int64_t packed_cols,
+                unsigned long long* __restrict__ sums, int n_bins, uint32_t* __restrict__ piece_emax,
+                int64_t n_pieces, int32_t* __restrict__ err) {
+  using C = Cfg<Tin>;
+  constexpr int F = C::F;
+  constexpr int PL = MODE == 1 ? 2 : 1;  // energy planes
+  __shared__ __align__(16) uint8_t s_buf[F][C::BUF];
+  __shared__ uint32_t s_sum[F][MAX_SLOTS];
+  __shared__ uint32_t s_e[PL][F][MAX_PIECES];
+  __shared__ int s_bin[MAX_SLOTS];
+  __shared__ int s_kpad[MAX_SLOTS];
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int64_t c = blockIdx.x;
+  const int64_t p0 = c * CH;
+  const int e0 = chunk_entry_off[c];
+  const int ne = min(chunk_entry_off[c + 1] - e0, CH);
+  const int64_t g0 = chunk_piece_off[c];
+  const int64_t np64 = chunk_piece_off[c + 1] - g0;
+  const int np = static_cast<int>(np64 < MAX_PIECES ? np64 : MAX_PIECES);
+
+  int32_t dst[EPT];
+  uint32_t meta[EPT];
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < EPT; ++k) {
+    const int e = tid + k * THREADS;
+    dst[k] = -1;
+    meta[k] = 0;
+    if (e < ne) {
+      const int32_t d = entry_dst[e0 + e];
+      const uint32_t m = entry_meta[e0 + e];
+      const int so = static_cast<int>(m & 2047u);
+      const int pc = static_cast<int>(m >> 16);
+      if (d < 0 || d >= packed_cols || p0 + so >= npix || pc >= np) {
+        bad = true;
+      } else {
+        dst[k] = d;
+        meta[k] = m;
+      }
     }
   }
-  const bool writes = active && bin >= 0;
-  if (qd == 0) s_bin[lseg] = writes ? bin : -1;
-  uint32_t emax0 = 0, emax1 = 0;
-  uint32_t range_bad = 0;
-
-  for (int64_t t0 = static_cast<int64_t>(blockIdx.y) * FR; t0 < T; t0 += static_cast<int64_t>(gridDim.y) * FR) {
-    uint32_t v[FR][4];
-#pragma unroll
-    for (int f = 0; f < FR; ++f) {
-      const int64_t t = t0 + f;
-      const Tin* fr = frames + t * npix;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) v[f][k] = (t < T && src[k] >= 0) ? static_cast<uint32_t>(fr[src[k]]) : 0u;
+  if (tid < MAX_SLOTS) {
+    int b = chunk_slot_bin[c * MAX_SLOTS + tid];
+    if (b >= n_bins) {
+      bad = true;
+      b = -1;
     }
+    s_bin[tid] = b;
+    s_kpad[tid] = (b >= 0 && MODE == 1) ? bin_kpad[b] : 0;
+  }
+  for (int i = tid; i < F * MAX_SLOTS; i += THREADS) (&s_sum[0][0])[i] = 0;
+  for (int i = tid; i < PL * F * MAX_PIECES; i += THREADS) (&s_e[0][0][0])[i] = 0;
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+  uint32_t run_max[PL][PPT];
 #pragma unroll
-    for (int f = 0; f < FR; ++f) {
+  for (int q = 0; q < PL; ++q)
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) run_max[q][j] = 0;
+  uint32_t range_bad = 0;
+  const int64_t total_bytes = T * npix * static_cast<int64_t>(sizeof(Tin));
+  const uint8_t* fbytes = reinterpret_cast<const uint8_t*>(frames);
+  const int64_t row_bytes = packed_cols * (MODE == 2 ? 1 : 2);
+  __syncthreads();
+
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.y) * F; t0 < T; t0 += static_cast<int64_t>(gridDim.y) * F) {
+    // ---- stage F frames' chunks in shared memory with aligned 16-byte loads
+    int delta[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      const int64_t start = ((t0 + f) * npix + p0) * static_cast<int64_t>(sizeof(Tin));
+      delta[f] = static_cast<int>(start & 15);
+    }
+    for (int w = tid; w < F * C::WORDS; w += THREADS) {
+      const int f = w / C::WORDS;
+      const int wi = w - f * C::WORDS;
       const int64_t t = t0 + f;
-      uint32_t ssum = v[f][0] + v[f][1] + v[f][2] + v[f][3];
-      uint32_t e0, e1 = 0;
-      if (mode == 2) {
-        e0 = v[f][0] * v[f][0] + v[f][1] * v[f][1] + v[f][2] * v[f][2] + v[f][3] * v[f][3];
-        range_bad |= max(max(v[f][0], v[f][1]), max(v[f][2], v[f][3])) > 16u ? 1u : 0u;
-        if (writes && t < T) {
-          const uint32_t o = e4m3_bits(v[f][0]) | (e4m3_bits(v[f][1]) << 8) | (e4m3_bits(v[f][2]) << 16) |
-                             (e4m3_bits(v[f][3]) << 24);
-          *reinterpret_cast<uint32_t*>(packed + t * packed_cols + dst0) = o;
-        }
-      } else if (mode == 0) {
-        e0 = v[f][0] * v[f][0] + v[f][1] * v[f][1] + v[f][2] * v[f][2] + v[f][3] * v[f][3];
-        range_bad |= max(max(v[f][0], v[f][1]), max(v[f][2], v[f][3])) > 2048u ? 1u : 0u;
-        if (writes && t < T) {
-          uint2 o;
-          o.x = half_bits(v[f][0]) | (half_bits(v[f][1]) << 16);
-          o.y = half_bits(v[f][2]) | (half_bits(v[f][3]) << 16);
-          *reinterpret_cast<uint2*>(packed + 2 * (t * packed_cols + dst0)) = o;
-        }
-      } else {
-        uint32_t h[4], l[4];
-        e0 = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          h[k] = v[f][k] >> 8;
-          l[k] = v[f][k] & 255u;
-          e0 += h[k] * h[k];
-          e1 += l[k] * l[k];
-          range_bad |= v[f][k] > 65535u ? 1u : 0u;
-        }
-        if (writes && t < T) {
-          uint2 oh, ol;
-          oh.x = half_bits(h[0]) | (half_bits(h[1]) << 16);
-          oh.y = half_bits(h[2]) | (half_bits(h[3]) << 16);
-          ol.x = half_bits(l[0]) | (half_bits(l[1]) << 16);
-          ol.y = half_bits(l[2]) | (half_bits(l[3]) << 16);
-          *reinterpret_cast<uint2*>(packed + 2 * (t * packed_cols + dst0)) = oh;
-          *reinterpret_cast<uint2*>(packed + 2 * (t * packed_cols + dst1)) = ol;
-        }
+      if (t >= T) continue;
+      const int64_t start = (t * npix + p0) * static_cast<int64_t>(sizeof(Tin));
+      const int64_t a = (start & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (a + 16 <= total_bytes) {
+        v = __ldg(reinterpret_cast<const uint4*>(fbytes + a));
+      } else if (a < total_bytes) {
+        uint32_t wv[4] = {0, 0, 0, 0};
+        for (int i = 0; i < 16 && a + i < total_bytes; ++i) wv[i >> 2] |= static_cast<uint32_t>(fbytes[a + i]) << (8 * (i & 3));
+        v = make_uint4(wv[0], wv[1], wv[2], wv[3]);
       }
-#pragma unroll
-      for (int o = 8; o > 0; o >>= 1) {
-        ssum += __shfl_xor_sync(0xffffffffu, ssum, o);
-        e0 += __shfl_xor_sync(0xffffffffu, e0, o);
-        e1 += __shfl_xor_sync(0xffffffffu, e1, o);
-      }
-      if (qd == 0) {
-        emax0 = max(emax0, e0);
-        emax1 = max(emax1, e1);
-        s_sum[f][lseg] = ssum;
-      }
+      *reinterpret_cast<uint4*>(&s_buf[f][wi * 16]) = v;
     }
     __syncthreads();
-    if (tid < FR) {
-      // merge consecutive segments of the same bin, one atomic per run
-      const int f = tid;
-      const int64_t t = t0 + f;
-      if (t < T) {
-        int cur = s_bin[0];
-        unsigned long long acc = s_sum[f][0];
-        for (int k = 1; k < SEGS_PER_BLOCK; ++k) {
-          const int b = s_bin[k];
-          if (b == cur) {
-            acc += s_sum[f][k];
+
+    // ---- move binned pixels to the packed matrix, reduce sums and energies
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+      const bool valid = dst[k] >= 0;
+      const unsigned amask = __ballot_sync(0xffffffffu, valid);
+      if (!valid) continue;
+      const int so = static_cast<int>(meta[k] & 2047u);
+      const int sl = static_cast<int>((meta[k] >> 11) & 31u);
+      const int pc = static_cast<int>(meta[k] >> 16);
+      const unsigned gslot = __match_any_sync(amask, sl);
+      const unsigned gpiece = __match_any_sync(amask, pc);
+      const bool lead_s = (__ffs(gslot) - 1) == lane;
+      const bool lead_p = (__ffs(gpiece) - 1) == lane;
+#pragma unroll
+      for (int f = 0; f < F; ++f) {
+        const int64_t t = t0 + f;
+        uint32_t v = 0;
+        if (t < T) {
+          const int off = delta[f] + so * static_cast<int>(sizeof(Tin));
+          v = sizeof(Tin) == 1 ? static_cast<uint32_t>(s_buf[f][off])
+                               : static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(&s_buf[f][off]));
+          uint8_t* row = packed + t * row_bytes;
+          if (MODE == 2) {
+            range_bad |= v > 16u ? 1u : 0u;
+            row[dst[k]] = static_cast<uint8_t>(e4m3_bits(v));
+          } else if (MODE == 0) {
+            range_bad |= v > 2048u ? 1u : 0u;
+            reinterpret_cast<uint16_t*>(row)[dst[k]] = static_cast<uint16_t>(half_bits(v));
           } else {
-            if (cur >= 0 && acc) atomicAdd(&sums[static_cast<int64_t>(cur) * T + t], acc);
-            cur = b;
-            acc = s_sum[f][k];
+            reinterpret_cast<uint16_t*>(row)[dst[k]] = static_cast<uint16_t>(half_bits(v >> 8));
+            const int64_t d1 = static_cast<int64_t>(dst[k]) + s_kpad[sl];
+            if (d1 < packed_cols)
+              reinterpret_cast<uint16_t*>(row)[d1] = static_cast<uint16_t>(half_bits(v & 255u));
+            else
+              range_bad |= 2u;
           }
         }
-        if (cur >= 0 && acc) atomicAdd(&sums[static_cast<int64_t>(cur) * T + t], acc);
+        const uint32_t vs = __reduce_add_sync(gslot, v);
+        if (lead_s && vs) atomicAdd(&s_sum[f][sl], vs);
+        if (MODE == 1) {
+          const uint32_t h = v >> 8, l = v & 255u;
+          const uint32_t eh = __reduce_add_sync(gpiece, h * h);
+          const uint32_t el = __reduce_add_sync(gpiece, l * l);
+          if (lead_p && eh) atomicAdd(&s_e[0][f][pc], eh);
+          if (lead_p && el) atomicAdd(&s_e[PL - 1][f][pc], el);
+        } else {
+          // counts above the mode's range are flagged; keep the energy finite
+          const uint32_t vv = v <= 2048u ? v * v : 4194304u;
+          const uint32_t e = __reduce_add_sync(gpiece, vv);
+          if (lead_p && e) atomicAdd(&s_e[0][f][pc], e);
+        }
       }
     }
     __syncthreads();
+
+    // ---- flush bin sums, fold piece energies into running maxima
+    for (int i = tid; i < F * MAX_SLOTS; i += THREADS) {
+      const int f = i / MAX_SLOTS, sl = i - f * MAX_SLOTS;
+      const uint32_t s = s_sum[f][sl];
+      if (s) {
+        const int b = s_bin[sl];
+        if (b >= 0 && t0 + f < T)
+          atomicAdd(&sums[static_cast<int64_t>(b) * T + t0 + f], static_cast<unsigned long long>(s));
+        s_sum[f][sl] = 0;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < PL; ++q)
+#pragma unroll
+      for (int j = 0; j < PPT; ++j) {
+        const int pc = tid + j * THREADS;
+        if (pc < np) {
+#pragma unroll
+          for (int f = 0; f < F; ++f) {
+            run_max[q][j] = max(run_max[q][j], s_e[q][f][pc]);
+            s_e[q][f][pc] = 0;
+          }
+        }
+      }
+    // s_buf is rewritten at the top of the next step: wait for every reader
+    __syncthreads();
   }
-  if (writes && qd == 0) {
-    if (emax0) atomicMax(&seg_emax[dst0 >> 6], emax0);
-    if (mode == 1 && emax1) atomicMax(&seg_emax[dst1 >> 6], emax1);
-  }
-  if (range_bad) atomicOr(err, G2_DEVERR_RANGE);
+#pragma unroll
+  for (int q = 0; q < PL; ++q)
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+      const int pc = tid + j * THREADS;
+      if (pc < np && g0 + pc < n_pieces && run_max[q][j])
+        atomicMax(&piece_emax[q * n_pieces + g0 + pc], run_max[q][j]);
+    }
+  if (range_bad & 1u) atomicOr(err, G2_DEVERR_RANGE);
+  if (range_bad & 2u) atomicOr(err, G2_DEVERR_BOUNDS);
 }
 
 template <typename Tin>
@@ -182,45 +257,59 @@ __global__ void binned_max_kernel(const Tin* __restrict__ frames, int64_t T, int
   if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
 }
 
+template <typename Tin, int MODE>
+void launch(dim3 grid, cudaStream_t st, const void* frames, int64_t T, int64_t npix, const int32_t* ceo,
+            const int32_t* ed, const uint32_t* em, const int32_t* csb, const int32_t* cpo, const int32_t* bk,
+            void* packed, int64_t cols, int64_t* sums, int n_bins, uint32_t* pe, int64_t n_pieces, int32_t* err) {
+  pack_kernel<Tin, MODE><<<grid, THREADS, 0, st>>>(reinterpret_cast<const Tin*>(frames), T, npix, ceo, ed, em, csb,
+                                                   cpo, bk, reinterpret_cast<uint8_t*>(packed), cols,
+                                                   reinterpret_cast<unsigned long long*>(sums), n_bins, pe, n_pieces,
+                                                   err);
+}
+
 }  // namespace pack
 }  // namespace g2
 
 extern "C" int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
-                              const int32_t* col_src_dev, const int32_t* seg_bin_dev, const int32_t* seg_dst0_dev,
-                              const int32_t* seg_dst1_dev, int64_t n_segs, int32_t mode, void* packed_dev,
-                              int64_t packed_cols, int64_t* sums_dev, int32_t n_bins, uint32_t* seg_emax_dev,
-                              int32_t* err_dev, void* stream) {
+                              const int32_t* chunk_entry_off_dev, const int32_t* entry_dst_dev,
+                              const uint32_t* entry_meta_dev, const int32_t* chunk_slot_bin_dev,
+                              const int32_t* chunk_piece_off_dev, const int32_t* bin_kpad_dev, int64_t n_chunks,
+                              int32_t mode, void* packed_dev, int64_t packed_cols, int64_t* sums_dev, int32_t n_bins,
+                              uint32_t* piece_emax_dev, int64_t n_pieces, int32_t* err_dev, void* stream) {
   using namespace g2;
-  if (!frames_dev || !col_src_dev || !seg_bin_dev || !seg_dst0_dev || !packed_dev || !sums_dev ||
-      !seg_emax_dev || !err_dev)
+  if (!frames_dev || !chunk_entry_off_dev || !entry_dst_dev || !entry_meta_dev || !chunk_slot_bin_dev ||
+      !chunk_piece_off_dev || !packed_dev || !sums_dev || !piece_emax_dev || !err_dev)
     return G2_ERR_ARG;
-  if ((elem_bytes != 1 && elem_bytes != 2) || nframes <= 0 || npix <= 0 || npix >= (1ll << 31) || n_segs < 0 ||
-      mode < 0 || mode > 2 || (mode == 1 && !seg_dst1_dev) || packed_cols <= 0 || packed_cols % G2_PAD != 0 ||
-      n_bins <= 0)
+  if ((elem_bytes != 1 && elem_bytes != 2) || nframes <= 0 || npix <= 0 || n_chunks < 0 ||
+      n_chunks != (npix + G2_PACK_CHUNK - 1) / G2_PACK_CHUNK || mode < 0 || mode > 2 ||
+      (mode == 1 && (!bin_kpad_dev || elem_bytes != 2)) || packed_cols <= 0 || packed_cols % G2_PAD != 0 ||
+      n_bins <= 0 || n_pieces < 0)
     return G2_ERR_ARG;
-  if (!aligned(col_src_dev, 16) || !aligned(packed_dev, 16)) return G2_ERR_ARG;
-  if (n_segs == 0) return G2_OK;
-  const int64_t gx = (n_segs + pack::SEGS_PER_BLOCK - 1) / pack::SEGS_PER_BLOCK;
-  if (gx > 0x7fffffff) return G2_ERR_TOO_LARGE;
+  if (!aligned(packed_dev, 16) || !aligned(frames_dev, 16)) return G2_ERR_ARG;
+  if (n_chunks == 0) return G2_OK;
+  if (n_chunks > 0x7fffffff) return G2_ERR_TOO_LARGE;
   const int sms = sm_count_current();
   if (sms <= 0) return G2_ERR_CUDA;
-  // enough blocks for ~8 resident per SM; each y-block walks frames with stride gy*FR
-  int64_t gy = (static_cast<int64_t>(sms) * 8 + gx - 1) / gx;
-  const int64_t max_gy = (nframes + pack::FR - 1) / pack::FR;
+  const int F = elem_bytes == 1 ? pack::Cfg<uint8_t>::F : pack::Cfg<uint16_t>::F;
+  int64_t gy = (static_cast<int64_t>(sms) * 16 + n_chunks - 1) / n_chunks;
+  const int64_t max_gy = (nframes + F - 1) / F;
   if (gy > max_gy) gy = max_gy;
   if (gy > 65535) gy = 65535;
   if (gy < 1) gy = 1;
-  dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
-  auto* sums = reinterpret_cast<unsigned long long*>(sums_dev);
-  auto* out = reinterpret_cast<uint8_t*>(packed_dev);
-  if (elem_bytes == 1)
-    pack::pack_kernel<uint8_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
-        reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, col_src_dev, seg_bin_dev, seg_dst0_dev,
-        seg_dst1_dev, n_segs, mode, out, packed_cols, sums, n_bins, seg_emax_dev, err_dev);
-  else
-    pack::pack_kernel<uint16_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
-        reinterpret_cast<const uint16_t*>(frames_dev), nframes, npix, col_src_dev, seg_bin_dev, seg_dst0_dev,
-        seg_dst1_dev, n_segs, mode, out, packed_cols, sums, n_bins, seg_emax_dev, err_dev);
+  dim3 grid(static_cast<unsigned>(n_chunks), static_cast<unsigned>(gy));
+  cudaStream_t st = as_stream(stream);
+#define G2_PACK_ARGS                                                                                                 \
+  grid, st, frames_dev, nframes, npix, chunk_entry_off_dev, entry_dst_dev, entry_meta_dev, chunk_slot_bin_dev,       \
+      chunk_piece_off_dev, bin_kpad_dev, packed_dev, packed_cols, sums_dev, n_bins, piece_emax_dev, n_pieces, err_dev
+  if (elem_bytes == 1) {
+    if (mode == 0) pack::launch<uint8_t, 0>(G2_PACK_ARGS);
+    else pack::launch<uint8_t, 2>(G2_PACK_ARGS);
+  } else {
+    if (mode == 0) pack::launch<uint16_t, 0>(G2_PACK_ARGS);
+    else if (mode == 1) pack::launch<uint16_t, 1>(G2_PACK_ARGS);
+    else pack::launch<uint16_t, 2>(G2_PACK_ARGS);
+  }
+#undef G2_PACK_ARGS
   return launch_status();
 }
 

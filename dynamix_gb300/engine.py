@@ -63,7 +63,10 @@ def frames_to_device(frames, dev):
     if isinstance(frames, torch.Tensor):
         t = frames
         if t.dtype in (torch.uint8, torch.uint16):
-            return t.to(dev, non_blocking=True).contiguous()
+            t = t.to(dev, non_blocking=True).contiguous()
+            if t.data_ptr() % 16:
+                t = t.clone()          # the pack kernel reads 16-byte aligned words
+            return t
         frames = t.cpu().numpy()
     a = np.asarray(frames)
     if a.dtype == np.uint8 or a.dtype == np.uint16:
@@ -128,6 +131,7 @@ class DenseEngine:
         self.packed = None
         self.last = {}
         self._u8_hint = MODE_E4M3 if method == "tc" else MODE_FP16
+        self._packed_mode = None
         self.profile = False      # record CUDA events around every stage
         self.stage_ms = {}
         self._events = []
@@ -161,18 +165,27 @@ class DenseEngine:
             L = PackLayout(self.qmask, self.n_bins, mode)
             d = lambda a: torch.as_tensor(a, device=self.dev)
             L.d_col_src = d(L.col_src)
-            L.d_seg_bin = d(L.seg_bin)
-            L.d_seg_dst0 = d(L.seg_dst0)
-            L.d_seg_dst1 = d(L.seg_dst1)
-            L.d_seg_emax = torch.zeros(L.packed_cols // _lib.BK, dtype=torch.int32, device=self.dev)
+            L.d_chunk_entry_off = d(L.chunk_entry_off)
+            L.d_entry_dst = d(L.entry_dst)
+            L.d_entry_meta = d(L.entry_meta.view(np.int32))
+            L.d_chunk_slot_bin = d(L.chunk_slot_bin)
+            L.d_chunk_piece_off = d(L.chunk_piece_off)
+            L.d_bin_kpad = d(L.bin_kpad)
+            L.d_piece_emax = torch.zeros(max(1, L.n_pieces * L.n_planes), dtype=torch.int32, device=self.dev)
             self._layouts[mode] = L
         return self._layouts[mode]
 
-    def _packed_buffer(self, nbytes):
+    def _packed_buffer(self, nbytes, mode):
+        """The packed operand buffer; zeroed whenever its layout changes, since
+        the pack kernel writes only the binned columns (padding stays 0)."""
         torch = _torch()
         if self.packed is None or self.packed.numel() < nbytes:
             self.packed = None
-            self.packed = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
+            self.packed = torch.zeros(nbytes, dtype=torch.uint8, device=self.dev)
+            self._packed_mode = mode
+        elif self._packed_mode != mode:
+            self.packed.zero_()
+            self._packed_mode = mode
         return self.packed
 
     # -- stages ----------------------------------------------------------
@@ -196,15 +209,16 @@ class DenseEngine:
 
     def pack(self, frames_dev, mode):
         L = self._layout(mode)
-        packed = self._packed_buffer(self.T * L.packed_bytes_per_frame)
+        packed = self._packed_buffer(self.T * L.packed_bytes_per_frame, mode)
         self.sums.zero_()
-        L.d_seg_emax.zero_()
+        L.d_piece_emax.zero_()
         self.err.zero_()
         st = stream_handle(self.dev)
         _lib.check(self.lib.g2_pack_frames(
-            ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_col_src), ptr(L.d_seg_bin),
-            ptr(L.d_seg_dst0), ptr(L.d_seg_dst1), L.n_segs, mode, ptr(packed), L.packed_cols, ptr(self.sums),
-            self.n_bins, ptr(L.d_seg_emax), ptr(self.err), st), "g2_pack_frames")
+            ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_entry_off),
+            ptr(L.d_entry_dst), ptr(L.d_entry_meta), ptr(L.d_chunk_slot_bin), ptr(L.d_chunk_piece_off),
+            ptr(L.d_bin_kpad), L.n_chunks, mode, ptr(packed), L.packed_cols, ptr(self.sums), self.n_bins,
+            ptr(L.d_piece_emax), L.n_pieces, ptr(self.err), st), "g2_pack_frames")
         return L
 
     def items_for(self, L, grams):
@@ -248,7 +262,7 @@ class DenseEngine:
         the K split; fall back to a wider packing when the counts do not fit."""
         while True:
             L = self.pack(frames_dev, mode)
-            seg_emax = L.d_seg_emax.cpu().numpy().view(np.uint32)
+            seg_emax = L.segment_emax(L.d_piece_emax.cpu().numpy().view(np.uint32))
             code = int(self.err.item())
             if code & _lib.DEVERR_RANGE and mode == MODE_E4M3 and self.operand == "auto":
                 mode = MODE_FP16

@@ -21,7 +21,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._lib import BK, ITEM_DTYPE, KIND_E4M3, KIND_FP16, PAD, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN
+from ._lib import (BK, ITEM_DTYPE, KIND_E4M3, KIND_FP16, PACK_CHUNK, PACK_MAX_PIECES, PACK_MAX_SLOTS, PAD, PLAIN_BM,
+                   PLAIN_BN, TC_BM, TC_BN)
 
 EXACT_LIMIT = 1 << 24   # fp32 represents every integer up to 2^24 exactly
 FP16_MAX_EXACT = 2048   # fp16 represents every integer up to 2^11 exactly
@@ -75,6 +76,66 @@ class PackLayout:
             self.seg_dst1 = np.zeros(self.n_segs, dtype=np.int32)
         if self.packed_cols >= 2 ** 31:
             raise ValueError("too many binned pixels for one job")
+        self._build_chunks(qflat, order, starts)
+
+    def _build_chunks(self, qflat, order, starts):
+        """Tables of the pack kernel: binned pixels per 2048-pixel chunk, their
+        packed column, local bin slot and local piece (64-column output
+        segment within the chunk)."""
+        n = self.npix_total
+        self.n_chunks = -(-n // PACK_CHUNK)
+        pix = np.flatnonzero(qflat > 0).astype(np.int64)            # pixel order
+        b = qflat[pix].astype(np.int64) - 1
+        rank = np.empty(n, dtype=np.int64)                             # rank of a pixel inside its bin
+        for bb in range(self.n_bins):
+            seg = order[starts[bb + 1]:starts[bb + 2]]
+            rank[seg] = np.arange(seg.size)
+        dst = self.plane0[b] + rank[pix]
+        chunk = pix // PACK_CHUNK
+        self.chunk_entry_off = np.searchsorted(chunk, np.arange(self.n_chunks + 1)).astype(np.int32)
+        # bin slots within a chunk
+        key = chunk * (self.n_bins + 1) + b
+        ukey = np.unique(key)
+        ukey_chunk = ukey // (self.n_bins + 1)
+        first_of_chunk = np.searchsorted(ukey_chunk, ukey_chunk)
+        slot_of_key = np.arange(ukey.size) - first_of_chunk
+        if slot_of_key.size and slot_of_key.max() >= PACK_MAX_SLOTS:
+            raise ValueError("more than %d bins in one %d-pixel chunk" % (PACK_MAX_SLOTS, PACK_CHUNK))
+        slot = slot_of_key[np.searchsorted(ukey, key)]
+        self.chunk_slot_bin = np.full(self.n_chunks * PACK_MAX_SLOTS, -1, dtype=np.int32)
+        self.chunk_slot_bin[ukey_chunk * PACK_MAX_SLOTS + slot_of_key] = (ukey % (self.n_bins + 1)).astype(np.int32)
+        # pieces: (output segment, chunk)
+        seg = dst // BK
+        nseg = self.packed_cols // BK
+        pkey = chunk * nseg + seg
+        upkey = np.unique(pkey)
+        up_chunk = upkey // nseg
+        self.chunk_piece_off = np.searchsorted(up_chunk, np.arange(self.n_chunks + 1)).astype(np.int32)
+        piece = np.searchsorted(upkey, pkey) - self.chunk_piece_off[chunk]
+        if piece.size and piece.max() >= PACK_MAX_PIECES:
+            raise ValueError("more than %d pieces in one chunk" % PACK_MAX_PIECES)
+        self.n_pieces = int(upkey.size)
+        self.piece_seg = (upkey % nseg).astype(np.int64)
+        if self.split:
+            piece_bin = np.empty(self.n_pieces, dtype=np.int64)          # bin of each piece
+            piece_bin[np.searchsorted(upkey, pkey)] = b
+            self.piece_seg1 = self.piece_seg + self.kpad[piece_bin] // BK
+        self.entry_dst = dst.astype(np.int32)
+        src_off = pix - chunk * PACK_CHUNK
+        self.entry_meta = (src_off | (slot << 11) | (piece << 16)).astype(np.uint32)
+        self.bin_kpad = self.kpad.astype(np.int32)
+        self.n_planes = 2 if self.split else 1
+
+    def segment_emax(self, piece_emax):
+        """Per 64-column output segment, the sum over its pieces of the pieces'
+        max-over-frames energies: an upper bound of the segment's energy in
+        every frame (indexed by packed column // 64)."""
+        pe = np.asarray(piece_emax, dtype=np.float64)
+        nseg = self.packed_cols // BK
+        out = np.bincount(self.piece_seg, weights=pe[: self.n_pieces], minlength=nseg)
+        if self.split:
+            out += np.bincount(self.piece_seg1, weights=pe[self.n_pieces: 2 * self.n_pieces], minlength=nseg)
+        return out
 
     @property
     def packed_bytes_per_frame(self):

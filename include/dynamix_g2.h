@@ -47,6 +47,9 @@ extern "C" {
 #define G2_PLAIN_BM   128
 #define G2_PLAIN_BN   128
 #define G2_PAD        128  /* packed_cols and bin segments are multiples of this */
+#define G2_PACK_CHUNK 2048 /* source pixels per pack chunk */
+#define G2_PACK_MAX_SLOTS  32   /* distinct bins per chunk */
+#define G2_PACK_MAX_PIECES 512  /* (64-column segment x chunk) pieces per chunk */
 #define G2_MAX_JOBS   32
 
 /* element kinds of a packed operand matrix */
@@ -91,23 +94,31 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
  * and the per-bin gather + float32 cast of py_dense_correlator
  * (dynamix/correlator/dense.py:48-50).
  *
- * frames_dev: [nframes][npix] counts, elem_bytes 1 (u8) or 2 (u16).
- * Source columns come in 64-column segments; segment s belongs to bin
- * seg_bin[s] (0-based) and col_src[64*s + j] is the flat pixel index of its
- * column j (or -1 for padding).  mode 0: the count is written as fp16 to
- * packed column seg_dst0[s] + j.  mode 1: the high byte (fp16) goes to
- * seg_dst0[s] + j and the low byte to seg_dst1[s] + j.  mode 2: the count is
- * written as an e4m3 byte (counts <= 16) to seg_dst0[s] + j.  A count that
- * does not fit the mode sets G2_DEVERR_RANGE in err_dev.
+ * frames_dev: [nframes][npix] counts, elem_bytes 1 (u8) or 2 (u16), 16-byte
+ * aligned (the chunks are read with aligned 16-byte loads).  The
+ * pixels are cut into n_chunks = ceil(npix / G2_PACK_CHUNK) chunks.  The
+ * binned pixels of chunk c are entries [chunk_entry_off[c], chunk_entry_off[c+1])
+ * (in pixel order); entry e goes to packed column entry_dst[e] (plane 0) and
+ * entry_meta[e] = offset in the chunk | local bin slot << 11 | local piece << 16.
+ * chunk_slot_bin[c * G2_PACK_MAX_SLOTS + slot] is the 0-based bin of a slot (-1
+ * unused).  A piece is one 64-column output segment within one chunk; chunk c
+ * owns pieces [chunk_piece_off[c], chunk_piece_off[c+1]).
+ * mode 0: the count is written as fp16 to entry_dst (counts <= 2048).
+ * mode 1 (u16 only): high byte (fp16) to entry_dst, low byte to entry_dst +
+ *   bin_kpad[bin] (the low-byte plane of the bin).
+ * mode 2: the count is written as an e4m3 byte (counts <= 16).
+ * A count that does not fit the mode sets G2_DEVERR_RANGE in err_dev.
  * Adds S_b(t) into sums_dev[b * nframes + t] (caller zeroes it) and raises
- * seg_emax_dev[c / 64] (caller zeroes it) to max_t of the sum of squares of
- * the packed values in output segment c / 64.
+ * piece_emax_dev[plane * n_pieces + piece] (caller zeroes it) to the max over
+ * frames of the sum of squared packed values of the piece (plane 1 = low bytes).
+ * Packed columns that no entry maps to (bin padding) are not written.
  */
 int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
-                   const int32_t* col_src_dev, const int32_t* seg_bin_dev,
-                   const int32_t* seg_dst0_dev, const int32_t* seg_dst1_dev, int64_t n_segs,
-                   int32_t mode, void* packed_dev, int64_t packed_cols,
-                   int64_t* sums_dev, int32_t n_bins, uint32_t* seg_emax_dev, int32_t* err_dev,
+                   const int32_t* chunk_entry_off_dev, const int32_t* entry_dst_dev,
+                   const uint32_t* entry_meta_dev, const int32_t* chunk_slot_bin_dev,
+                   const int32_t* chunk_piece_off_dev, const int32_t* bin_kpad_dev, int64_t n_chunks,
+                   int32_t mode, void* packed_dev, int64_t packed_cols, int64_t* sums_dev,
+                   int32_t n_bins, uint32_t* piece_emax_dev, int64_t n_pieces, int32_t* err_dev,
                    void* stream);
 
 /* Largest count over the binned pixels (col_src >= 0): picks split 0/1.

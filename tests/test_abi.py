@@ -43,8 +43,9 @@ def test_argument_errors_are_caught_on_host(built_lib):
     assert built_lib.g2_denominator(None, 1, 10, None, None) == 1
     assert built_lib.g2_finalize(None, None, None, 1, 10, None, None, None) == 1
     assert built_lib.g2_gram_tc(None, 0, None, 0, None, 0, None, 0, None) == 1
-    assert built_lib.g2_pack_frames(None, 1, 1, 1, None, None, None, None, 0, 0, None, 64, None, 1, None, None,
-                                    None) == 1
+    assert built_lib.g2_pack_frames(None, 1, 1, 1, None, None, None, None, None, None, 1, 0, None, 128, None, 1,
+                                    None, 0, None, None) == 1
+    assert built_lib.g2_normalize_static(None, None, None, 1, 10, None, None, None) == 1
 
 
 def test_item_layout_matches_c_struct():

@@ -192,3 +192,19 @@ def test_tc_equals_plain_at_medium_size(built_lib, cuda_device):
         assert int((x * x).sum()) == int(a.numerator[bi, 0])
         assert np.array_equal(x.sum(dim=1).cpu().numpy(), a.sums[bi])
         assert int((x[1:] * x[:-1]).sum()) == int(a.numerator[bi, 1])
+
+
+def test_unaligned_device_view(built_lib, cuda_device):
+    """A device view that starts off a 16-byte boundary is handled (copied)."""
+    import torch
+    from dynamix_gb300.correlator import MatMulCorrelator
+    z = golden("dense_small_u8")
+    fr, qm = z["frames"], z["qmask"]
+    T = fr.shape[0]
+    big = torch.zeros((T + 1,) + fr.shape[1:], dtype=torch.uint8, device=cuda_device)
+    big[1:] = torch.from_numpy(fr).to(cuda_device)
+    view = big[1:]
+    assert view.data_ptr() % 16 != 0
+    c = MatMulCorrelator(fr.shape[1:], T, qmask=qm)
+    g = c.correlate(view)
+    assert_exact(c, o.g2_exact(fr, qm), g)

@@ -10,25 +10,52 @@ import pytest
 
 from conftest import golden
 from dynamix_gb300 import plan
-from dynamix_gb300._lib import BK, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN  # noqa: F401
+from dynamix_gb300._lib import BK, PACK_CHUNK, PACK_MAX_SLOTS, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN  # noqa: F401
 from dynamix_gb300.speckle import annular_qmask, speckle_numpy
 from oracle import g2_oracle as o
 
 
 def emulate_pack(frames, L):
+    """What g2_pack_frames writes, from the layout's chunk tables; the packed
+    matrix is cross-checked against the per-bin column map, and the segment
+    energy bound is built from per-piece maxima exactly as the kernel does."""
     T = frames.shape[0]
     flat = frames.reshape(T, -1).astype(np.int64)
     packed = np.zeros((T, L.packed_cols), dtype=np.int64)
+    chunk = np.repeat(np.arange(L.n_chunks), np.diff(L.chunk_entry_off))
+    meta = L.entry_meta.astype(np.int64)
+    pix = chunk * PACK_CHUNK + (meta & 2047)
+    slot = (meta >> 11) & 31
+    piece = L.chunk_piece_off[chunk] + (meta >> 16)
+    b = L.chunk_slot_bin[chunk * PACK_MAX_SLOTS + slot]
+    # the slot's bin is the bin whose columns hold the entry
+    assert np.all((b >= 0) & (L.plane0[b] <= L.entry_dst) & (L.entry_dst < L.plane0[b] + L.kpad[b]))
+    v = flat[:, pix]
+    energy = np.zeros((L.n_planes, T, max(L.n_pieces, 1)), dtype=np.int64)
+    if L.split:
+        packed[:, L.entry_dst] = v >> 8
+        packed[:, L.entry_dst + L.bin_kpad[b]] = v & 255
+        np.add.at(energy[0].T, piece, ((v >> 8) ** 2).T)
+        np.add.at(energy[1].T, piece, ((v & 255) ** 2).T)
+    else:
+        packed[:, L.entry_dst] = v
+        np.add.at(energy[0].T, piece, (v ** 2).T)
+    # the same matrix from the column map (bins contiguous, raster order)
+    ref = np.zeros_like(packed)
     cs = L.col_src.reshape(-1, BK)
     for s in range(L.n_segs):
         src = cs[s]
-        v = np.where(src >= 0, flat[:, np.maximum(src, 0)], 0)
+        vv = np.where(src >= 0, flat[:, np.maximum(src, 0)], 0)
         if L.split:
-            packed[:, L.seg_dst0[s]:L.seg_dst0[s] + BK] = v >> 8
-            packed[:, L.seg_dst1[s]:L.seg_dst1[s] + BK] = v & 255
+            ref[:, L.seg_dst0[s]:L.seg_dst0[s] + BK] = vv >> 8
+            ref[:, L.seg_dst1[s]:L.seg_dst1[s] + BK] = vv & 255
         else:
-            packed[:, L.seg_dst0[s]:L.seg_dst0[s] + BK] = v
-    emax = (packed.reshape(T, -1, BK) ** 2).sum(axis=2).max(axis=0)
+            ref[:, L.seg_dst0[s]:L.seg_dst0[s] + BK] = vv
+    assert np.array_equal(packed, ref)
+    piece_max = energy.max(axis=1)[:, : L.n_pieces].ravel()
+    emax = L.segment_emax(piece_max)
+    true = (packed.reshape(T, -1, BK) ** 2).sum(axis=2).max(axis=0)
+    assert np.all(emax >= true)
     return packed, emax
 
 
