@@ -201,9 +201,9 @@ def test_unaligned_device_view(built_lib, cuda_device):
     z = golden("dense_small_u8")
     fr, qm = z["frames"], z["qmask"]
     T = fr.shape[0]
-    big = torch.zeros((T + 1,) + fr.shape[1:], dtype=torch.uint8, device=cuda_device)
-    big[1:] = torch.from_numpy(fr).to(cuda_device)
-    view = big[1:]
+    big = torch.zeros(fr.size + 1, dtype=torch.uint8, device=cuda_device)
+    big[1:] = torch.from_numpy(fr.ravel()).to(cuda_device)
+    view = big[1:].view(fr.shape)
     assert view.data_ptr() % 16 != 0
     c = MatMulCorrelator(fr.shape[1:], T, qmask=qm)
     g = c.correlate(view)
