@@ -50,7 +50,7 @@ struct Cfg {
 };
 
 template <typename Tin, int MODE>
-__global__ void __launch_bounds__(THREADS, 4)
+__global__ void __launch_bounds__(THREADS, 3)
     pack_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix, const int32_t* __restrict__ chunk_entry_off,
                 const int32_t* __restrict__ entry_dst, const uint32_t* __restrict__ entry_meta,
                 const int32_t* __restrict__ chunk_slot_bin, const int32_t* __restrict__ chunk_piece_off,
@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(THREADS, 4)
   using C = Cfg<Tin>;
   constexpr int F = C::F;
   constexpr int PL = MODE == 1 ? 2 : 1;  // energy planes
-  __shared__ __align__(16) uint8_t s_buf[F][C::BUF];
+  __shared__ __align__(16) uint8_t s_buf[2][F][C::BUF];  // double buffer: cp.async fills one while
+                                                          // the other is consumed
   __shared__ uint32_t s_sum[F][MAX_SLOTS];
   __shared__ uint32_t s_e[PL][F][MAX_PIECES];
   __shared__ int s_bin[MAX_SLOTS];
@@ -120,54 +121,77 @@ __global__ void __launch_bounds__(THREADS, 4)
   const int64_t row_bytes = packed_cols * (MODE == 2 ? 1 : 2);
   __syncthreads();
 
-  for (int64_t t0 = static_cast<int64_t>(blockIdx.y) * F; t0 < T; t0 += static_cast<int64_t>(gridDim.y) * F) {
-    // ---- stage F frames' chunks in shared memory with aligned 16-byte loads
+  // Warp groups of equal bin slot / piece among the valid entries: fixed for
+  // the whole kernel, so computed once.
+  unsigned gslot[EPT], gpiece[EPT];
+#pragma unroll
+  for (int k = 0; k < EPT; ++k) {
+    const bool valid = dst[k] >= 0;
+    const unsigned amask = __ballot_sync(0xffffffffu, valid);
+    gslot[k] = gpiece[k] = 0;
+    if (valid) {
+      gslot[k] = __match_any_sync(amask, static_cast<int>((meta[k] >> 11) & 31u));
+      gpiece[k] = __match_any_sync(amask, static_cast<int>(meta[k] >> 16));
+    }
+  }
+
+  // Issue the asynchronous copies of one step's F chunks into buffer `buf`:
+  // aligned 16-byte words, zero-filled past the end of the frames.
+  auto issue = [&](int64_t t0, int buf) {
+    for (int w = tid; w < F * C::WORDS; w += THREADS) {
+      const int f = w / C::WORDS;
+      const int wi = w - f * C::WORDS;
+      const int64_t t = t0 + f;
+      const int64_t start = (t * npix + p0) * static_cast<int64_t>(sizeof(Tin));
+      const int64_t a = (start & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
+      int64_t avail = t < T ? total_bytes - a : 0;
+      const int nbytes = avail <= 0 ? 0 : (avail >= 16 ? 16 : static_cast<int>(avail));
+      const uint8_t* src = nbytes ? fbytes + a : fbytes;
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(&s_buf[buf][f][wi * 16])),
+                   "l"(src), "r"(nbytes)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  const int64_t stride = static_cast<int64_t>(gridDim.y) * F;
+  int64_t t0 = static_cast<int64_t>(blockIdx.y) * F;
+  if (t0 < T) issue(t0, 0);
+  for (int step = 0; t0 < T; ++step, t0 += stride) {
+    const int buf = step & 1;
+    // prefetch the next step into the other buffer (always commit a group so
+    // that "wait for all but the newest group" means this step's data)
+    if (t0 + stride < T) {
+      issue(t0 + stride, buf ^ 1);
+    } else {
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncthreads();
     int delta[F];
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       const int64_t start = ((t0 + f) * npix + p0) * static_cast<int64_t>(sizeof(Tin));
       delta[f] = static_cast<int>(start & 15);
     }
-    for (int w = tid; w < F * C::WORDS; w += THREADS) {
-      const int f = w / C::WORDS;
-      const int wi = w - f * C::WORDS;
-      const int64_t t = t0 + f;
-      if (t >= T) continue;
-      const int64_t start = (t * npix + p0) * static_cast<int64_t>(sizeof(Tin));
-      const int64_t a = (start & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (a + 16 <= total_bytes) {
-        v = __ldg(reinterpret_cast<const uint4*>(fbytes + a));
-      } else if (a < total_bytes) {
-        uint32_t wv[4] = {0, 0, 0, 0};
-        for (int i = 0; i < 16 && a + i < total_bytes; ++i) wv[i >> 2] |= static_cast<uint32_t>(fbytes[a + i]) << (8 * (i & 3));
-        v = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-      }
-      *reinterpret_cast<uint4*>(&s_buf[f][wi * 16]) = v;
-    }
-    __syncthreads();
 
     // ---- move binned pixels to the packed matrix, reduce sums and energies
 #pragma unroll
     for (int k = 0; k < EPT; ++k) {
-      const bool valid = dst[k] >= 0;
-      const unsigned amask = __ballot_sync(0xffffffffu, valid);
-      if (!valid) continue;
+      if (dst[k] < 0) continue;
       const int so = static_cast<int>(meta[k] & 2047u);
       const int sl = static_cast<int>((meta[k] >> 11) & 31u);
       const int pc = static_cast<int>(meta[k] >> 16);
-      const unsigned gslot = __match_any_sync(amask, sl);
-      const unsigned gpiece = __match_any_sync(amask, pc);
-      const bool lead_s = (__ffs(gslot) - 1) == lane;
-      const bool lead_p = (__ffs(gpiece) - 1) == lane;
+      const bool lead_s = (__ffs(gslot[k]) - 1) == lane;
+      const bool lead_p = (__ffs(gpiece[k]) - 1) == lane;
 #pragma unroll
       for (int f = 0; f < F; ++f) {
         const int64_t t = t0 + f;
         uint32_t v = 0;
         if (t < T) {
           const int off = delta[f] + so * static_cast<int>(sizeof(Tin));
-          v = sizeof(Tin) == 1 ? static_cast<uint32_t>(s_buf[f][off])
-                               : static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(&s_buf[f][off]));
+          v = sizeof(Tin) == 1 ? static_cast<uint32_t>(s_buf[buf][f][off])
+                               : static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(&s_buf[buf][f][off]));
           uint8_t* row = packed + t * row_bytes;
           if (MODE == 2) {
             range_bad |= v > 16u ? 1u : 0u;
@@ -184,18 +208,18 @@ __global__ void __launch_bounds__(THREADS, 4)
               range_bad |= 2u;
           }
         }
-        const uint32_t vs = __reduce_add_sync(gslot, v);
+        const uint32_t vs = __reduce_add_sync(gslot[k], v);
         if (lead_s && vs) atomicAdd(&s_sum[f][sl], vs);
         if (MODE == 1) {
           const uint32_t h = v >> 8, l = v & 255u;
-          const uint32_t eh = __reduce_add_sync(gpiece, h * h);
-          const uint32_t el = __reduce_add_sync(gpiece, l * l);
+          const uint32_t eh = __reduce_add_sync(gpiece[k], h * h);
+          const uint32_t el = __reduce_add_sync(gpiece[k], l * l);
           if (lead_p && eh) atomicAdd(&s_e[0][f][pc], eh);
           if (lead_p && el) atomicAdd(&s_e[PL - 1][f][pc], el);
         } else {
           // counts above the mode's range are flagged; keep the energy finite
           const uint32_t vv = v <= 2048u ? v * v : 4194304u;
-          const uint32_t e = __reduce_add_sync(gpiece, vv);
+          const uint32_t e = __reduce_add_sync(gpiece[k], vv);
           if (lead_p && e) atomicAdd(&s_e[0][f][pc], e);
         }
       }
@@ -226,9 +250,11 @@ __global__ void __launch_bounds__(THREADS, 4)
           }
         }
       }
-    // s_buf is rewritten at the top of the next step: wait for every reader
+    // the accumulators are reused and the buffer just read is refilled by the
+    // copies issued at the top of the next step: wait for every thread here
     __syncthreads();
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
 #pragma unroll
   for (int q = 0; q < PL; ++q)
 #pragma unroll
