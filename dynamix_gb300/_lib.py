@@ -22,7 +22,7 @@ DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE = 1, 2, 4
 
 BK = 64          # source segment width (pixels)
 PAD = 128        # packed bins and packed_cols are multiples of this
-PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES = 2048, 32, 512
+PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 32, 512, 768
 TC_BM, TC_BN = 128, 256
 PLAIN_BM, PLAIN_BN = 128, 128
 MAX_JOBS = 32
@@ -50,6 +50,7 @@ SIGNATURES = {
     "g2_device_info": (C.c_int, [C.c_int, _p, _p, _p]),
     "g2_pack_frames": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _p, _p, _p, _i64, _i32, _p, _i64, _p, _i32, _p,
                                  _i64, _p, _p]),
+    "g2_pack_e4m3": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _p, _i64, _p, _i64, _p, _i32, _p, _p]),
     "g2_binned_max": (C.c_int, [_p, _i32, _i64, _i64, _p, _i64, _p, _p]),
     "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),

@@ -2,14 +2,17 @@
 // lag-diagonal sums fused into the epilogue.
 //
 // For one item, the CTA computes the 128 x 256 block G(t, t') = sum_k A(t,k) B(t',k)
-// (t = i0 + r, t' = j0 + c) with tcgen05.mma into TMEM -- kind::f16 on fp16
-// counts (exact to 2048) or kind::f8f6f4 on e4m3 counts (exact to 16, half the
-// bytes and twice the MMA rate), chosen per job -- then adds
+// (t = i0 + r, t' = j0 + c) with tcgen05.mma into TMEM -- kind::f16 on 16-bit
+// counts <= 2048 or kind::f8f6f4 on 8-bit counts <= 16 (half the bytes and
+// twice the MMA rate), chosen per job -- then adds
 // every element with t' >= t to the lag tau = t' - t:
 //     N(tau) += 2^shift * sum_{c - r = tau - (j0 - i0)} G(r, c).
-// The Gram never reaches HBM.  Counts are exact in fp16 (<= 2048), products
-// exact in fp32, and the caller splits K so that every fp32 partial sum is an
-// integer below 2^24; the epilogue converts each element to uint32 and sums the
+// The Gram never reaches HBM.  The packed operands are the raw integer counts:
+// read as e4m3, the bytes 0..16 are exactly count * 2^-9 (subnormals and the
+// first binades); read as fp16, the 16-bit values 0..2048 are exactly
+// count * 2^-24.  Products are exact in fp32 and the caller splits K so that
+// every partial sum is an integer below 2^24 times that power of two; the
+// epilogue rescales (exact), converts each element to uint32 and sums the
 // lag diagonals in uint32 shared-memory counters (<= 128 * 2^24 < 2^32), which
 // are then added to the int64 numerator.
 //
@@ -227,6 +230,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const bool ok = mbar_wait(&accf[buf], ap, abort_flag, err);
       if (named_bar_any(1, EPI_THREADS, !ok)) break;
       tc_fence_after();
+      // packed counts are raw integers read as e4m3 (count * 2^-9) or fp16
+      // (count * 2^-24): each accumulator holds sum * 2^-18 or sum * 2^-48
+      const float unscale = maps.kind[w.job] == G2_KIND_E4M3 ? 262144.0f : 281474976710656.0f;
       const uint32_t tbase = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * BN);
 #pragma unroll 1
       for (int cc = 0; cc < BN / 32; ++cc) {
@@ -236,7 +242,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const int dbase = cc * 32 - row + (BM - 1);
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          const uint32_t x = __float2uint_rn(__uint_as_float(v[j]));
+          const uint32_t x = __float2uint_rn(__uint_as_float(v[j]) * unscale);
           if (x) atomicAdd(&dacc[dbase + j], x);
         }
       }

@@ -16,8 +16,6 @@
 // segment's energy in every frame.
 // Replaces compute_sums_dense (densecorrelator.cl:65-150) and the gather /
 // float32 cast of py_dense_correlator (dense.py:48-50).
-#include <cuda_fp16.h>
-#include <cuda_fp8.h>
 #include "g2_ptx.cuh"
 #include "g2_host.h"
 
@@ -31,13 +29,6 @@ constexpr int MAX_SLOTS = G2_PACK_MAX_SLOTS;
 constexpr int MAX_PIECES = G2_PACK_MAX_PIECES;
 constexpr int PPT = MAX_PIECES / THREADS;  // pieces per thread for the running maxima
 
-__device__ __forceinline__ uint32_t half_bits(uint32_t v) {
-  return static_cast<uint32_t>(__half_as_ushort(__uint2half_rn(v)));
-}
-// e4m3 byte of an integer count 0..16 (exact in e4m3)
-__device__ __forceinline__ uint32_t e4m3_bits(uint32_t v) {
-  return static_cast<uint32_t>(__nv_cvt_float_to_fp8(static_cast<float>(v), __NV_SATFINITE, __NV_E4M3));
-}
 
 // Frames per step and bytes of one frame's chunk in shared memory (+16 B for
 // the unaligned start).
@@ -195,15 +186,15 @@ __global__ void __launch_bounds__(THREADS, 3)
           uint8_t* row = packed + t * row_bytes;
           if (MODE == 2) {
             range_bad |= v > 16u ? 1u : 0u;
-            row[dst[k]] = static_cast<uint8_t>(e4m3_bits(v));
+            row[dst[k]] = static_cast<uint8_t>(v);
           } else if (MODE == 0) {
             range_bad |= v > 2048u ? 1u : 0u;
-            reinterpret_cast<uint16_t*>(row)[dst[k]] = static_cast<uint16_t>(half_bits(v));
+            reinterpret_cast<uint16_t*>(row)[dst[k]] = static_cast<uint16_t>(v);
           } else {
-            reinterpret_cast<uint16_t*>(row)[dst[k]] = static_cast<uint16_t>(half_bits(v >> 8));
+            reinterpret_cast<uint16_t*>(row)[dst[k]] = static_cast<uint16_t>(v >> 8);
             const int64_t d1 = static_cast<int64_t>(dst[k]) + s_kpad[sl];
             if (d1 < packed_cols)
-              reinterpret_cast<uint16_t*>(row)[d1] = static_cast<uint16_t>(half_bits(v & 255u));
+              reinterpret_cast<uint16_t*>(row)[d1] = static_cast<uint16_t>(v & 255u);
             else
               range_bad |= 2u;
           }
@@ -265,6 +256,179 @@ __global__ void __launch_bounds__(THREADS, 3)
     }
   if (range_bad & 1u) atomicOr(err, G2_DEVERR_RANGE);
   if (range_bad & 2u) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// ---- e4m3 (counts <= 16): a pure byte permutation --------------------------
+// The raw count bytes are the e4m3 operand (bytes 0..16 read as e4m3 are
+// count * 2^-9), so no conversion is needed, and counts <= 16 bound every
+// Gram sum by themselves, so no energies are needed either.  A thread owns up
+// to WPT "words" = 4 consecutive packed columns of one bin; per frame it reads
+// the 4 source bytes from the staged chunk, stores one 32-bit word (byte
+// stores only for the two partial words at the ends of a bin's run in the
+// chunk, whose other bytes belong to the neighbouring chunk), and adds the
+// word's byte sum (dp4a) to the bin sum through one warp reduction.
+constexpr int WPT = 3;
+constexpr uint32_t NO_SRC = 0xFFFu;
+
+template <typename Tin>
+__global__ void __launch_bounds__(THREADS, 4)
+    pack_e4m3_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix,
+                     const int32_t* __restrict__ chunk_word_off, const int32_t* __restrict__ word_dst,
+                     const uint2* __restrict__ word_src, const int32_t* __restrict__ chunk_slot_bin,
+                     uint8_t* __restrict__ packed, int64_t packed_cols, unsigned long long* __restrict__ sums,
+                     int n_bins, int32_t* __restrict__ err) {
+  using C = Cfg<Tin>;
+  constexpr int F = C::F;
+  __shared__ __align__(16) uint8_t s_buf[2][F][C::BUF];
+  __shared__ uint32_t s_sum[F][MAX_SLOTS];
+  __shared__ int s_bin[MAX_SLOTS];
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int64_t c = blockIdx.x;
+  const int64_t p0 = c * CH;
+  const int w0 = chunk_word_off[c];
+  const int nw = min(chunk_word_off[c + 1] - w0, WPT * THREADS);
+
+  int32_t dst[WPT];
+  uint32_t src[WPT][4];
+  int slot[WPT];
+  bool full[WPT];
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < WPT; ++k) {
+    const int w = tid + k * THREADS;
+    dst[k] = -1;
+    slot[k] = 0;
+    full[k] = false;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) src[k][i] = NO_SRC;
+    if (w < nw) {
+      const int32_t d = word_dst[w0 + w];
+      const uint2 m = word_src[w0 + w];
+      uint32_t sv[4] = {m.x & 0xFFFu, (m.x >> 12) & 0xFFFu, (m.x >> 24) | ((m.y & 0xFu) << 8), (m.y >> 4) & 0xFFFu};
+      bool ok = d >= 0 && (d & 3) == 0 && d + 4 <= packed_cols;
+      bool all = true;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (sv[i] == NO_SRC) {
+          all = false;
+        } else if (sv[i] >= static_cast<uint32_t>(CH) || p0 + sv[i] >= npix) {
+          ok = false;
+        }
+      }
+      if (!ok) {
+        bad = true;
+      } else {
+        dst[k] = d;
+        slot[k] = static_cast<int>((m.y >> 16) & 31u);
+        full[k] = all;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) src[k][i] = sv[i];
+      }
+    }
+  }
+  if (tid < MAX_SLOTS) {
+    int b = chunk_slot_bin[c * MAX_SLOTS + tid];
+    if (b >= n_bins) {
+      bad = true;
+      b = -1;
+    }
+    s_bin[tid] = b;
+  }
+  for (int i = tid; i < F * MAX_SLOTS; i += THREADS) (&s_sum[0][0])[i] = 0;
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+  unsigned gslot[WPT];
+#pragma unroll
+  for (int k = 0; k < WPT; ++k) {
+    const bool valid = dst[k] >= 0;
+    const unsigned amask = __ballot_sync(0xffffffffu, valid);
+    gslot[k] = valid ? __match_any_sync(amask, slot[k]) : 0u;
+  }
+  uint32_t range_bad = 0;
+  const int64_t total_bytes = T * npix * static_cast<int64_t>(sizeof(Tin));
+  const uint8_t* fbytes = reinterpret_cast<const uint8_t*>(frames);
+  __syncthreads();
+
+  auto issue = [&](int64_t t0, int buf) {
+    for (int w = tid; w < F * C::WORDS; w += THREADS) {
+      const int f = w / C::WORDS;
+      const int wi = w - f * C::WORDS;
+      const int64_t t = t0 + f;
+      const int64_t start = (t * npix + p0) * static_cast<int64_t>(sizeof(Tin));
+      const int64_t a = (start & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
+      const int64_t avail = t < T ? total_bytes - a : 0;
+      const int nbytes = avail <= 0 ? 0 : (avail >= 16 ? 16 : static_cast<int>(avail));
+      const uint8_t* srcp = nbytes ? fbytes + a : fbytes;
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(&s_buf[buf][f][wi * 16])),
+                   "l"(srcp), "r"(nbytes)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  const int64_t stride = static_cast<int64_t>(gridDim.y) * F;
+  int64_t t0 = static_cast<int64_t>(blockIdx.y) * F;
+  if (t0 < T) issue(t0, 0);
+  for (int step = 0; t0 < T; ++step, t0 += stride) {
+    const int buf = step & 1;
+    if (t0 + stride < T) {
+      issue(t0 + stride, buf ^ 1);
+    } else {
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncthreads();
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      const int64_t t = t0 + f;
+      const bool live = t < T;
+      const int delta = static_cast<int>(((t * npix + p0) * static_cast<int64_t>(sizeof(Tin))) & 15);
+      const uint8_t* sb = &s_buf[buf][f][delta];
+      uint8_t* row = packed + t * packed_cols;
+#pragma unroll
+      for (int k = 0; k < WPT; ++k) {
+        if (dst[k] < 0) continue;
+        uint32_t word = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          if (src[k][i] != NO_SRC) {
+            const uint32_t v = sizeof(Tin) == 1
+                                   ? static_cast<uint32_t>(sb[src[k][i]])
+                                   : static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(sb + 2 * src[k][i]));
+            range_bad |= v > 16u ? 1u : 0u;
+            word |= (v & 0xFFu) << (8 * i);
+          }
+        }
+        if (live) {
+          if (full[k]) {
+            *reinterpret_cast<uint32_t*>(row + dst[k]) = word;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (src[k][i] != NO_SRC) row[dst[k] + i] = static_cast<uint8_t>(word >> (8 * i));
+          }
+        }
+        const uint32_t bs = live ? __dp4a(word, 0x01010101u, 0u) : 0u;
+        const uint32_t vs = __reduce_add_sync(gslot[k], bs);
+        if ((__ffs(gslot[k]) - 1) == lane && vs) atomicAdd(&s_sum[f][slot[k]], vs);
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < F * MAX_SLOTS; i += THREADS) {
+      const int f = i / MAX_SLOTS, sl = i - f * MAX_SLOTS;
+      const uint32_t sv = s_sum[f][sl];
+      if (sv) {
+        const int b = s_bin[sl];
+        if (b >= 0 && t0 + f < T)
+          atomicAdd(&sums[static_cast<int64_t>(b) * T + t0 + f], static_cast<unsigned long long>(sv));
+        s_sum[f][sl] = 0;
+      }
+    }
+    __syncthreads();
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (range_bad) atomicOr(err, G2_DEVERR_RANGE);
 }
 
 template <typename Tin>
@@ -336,6 +500,45 @@ extern "C" int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_
     else pack::launch<uint16_t, 2>(G2_PACK_ARGS);
   }
 #undef G2_PACK_ARGS
+  return launch_status();
+}
+
+extern "C" int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
+                            const int32_t* chunk_word_off_dev, const int32_t* word_dst_dev,
+                            const uint32_t* word_src_dev, const int32_t* chunk_slot_bin_dev, int64_t n_chunks,
+                            void* packed_dev, int64_t packed_cols, int64_t* sums_dev, int32_t n_bins,
+                            int32_t* err_dev, void* stream) {
+  using namespace g2;
+  if (!frames_dev || !chunk_word_off_dev || !word_dst_dev || !word_src_dev || !chunk_slot_bin_dev || !packed_dev ||
+      !sums_dev || !err_dev)
+    return G2_ERR_ARG;
+  if ((elem_bytes != 1 && elem_bytes != 2) || nframes <= 0 || npix <= 0 ||
+      n_chunks != (npix + G2_PACK_CHUNK - 1) / G2_PACK_CHUNK || packed_cols <= 0 || packed_cols % G2_PAD != 0 ||
+      n_bins <= 0)
+    return G2_ERR_ARG;
+  if (!aligned(packed_dev, 16) || !aligned(frames_dev, 16) || !aligned(word_src_dev, 8)) return G2_ERR_ARG;
+  if (n_chunks == 0) return G2_OK;
+  if (n_chunks > 0x7fffffff) return G2_ERR_TOO_LARGE;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  const int F = elem_bytes == 1 ? pack::Cfg<uint8_t>::F : pack::Cfg<uint16_t>::F;
+  int64_t gy = (static_cast<int64_t>(sms) * 16 + n_chunks - 1) / n_chunks;
+  const int64_t max_gy = (nframes + F - 1) / F;
+  if (gy > max_gy) gy = max_gy;
+  if (gy > 65535) gy = 65535;
+  if (gy < 1) gy = 1;
+  dim3 grid(static_cast<unsigned>(n_chunks), static_cast<unsigned>(gy));
+  auto* ws = reinterpret_cast<const uint2*>(word_src_dev);
+  auto* out = reinterpret_cast<uint8_t*>(packed_dev);
+  auto* sm = reinterpret_cast<unsigned long long*>(sums_dev);
+  if (elem_bytes == 1)
+    pack::pack_e4m3_kernel<uint8_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
+        reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, chunk_word_off_dev, word_dst_dev, ws,
+        chunk_slot_bin_dev, out, packed_cols, sm, n_bins, err_dev);
+  else
+    pack::pack_e4m3_kernel<uint16_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
+        reinterpret_cast<const uint16_t*>(frames_dev), nframes, npix, chunk_word_off_dev, word_dst_dev, ws,
+        chunk_slot_bin_dev, out, packed_cols, sm, n_bins, err_dev);
   return launch_status();
 }
 

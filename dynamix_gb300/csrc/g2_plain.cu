@@ -6,9 +6,8 @@
 // 32-bit unsigned integer multiply-adds -- but register-tiled: a 256-thread
 // block owns a 128 x 128 block of (t, t') pairs, each thread an 8 x 8 set of
 // uint32 accumulators fed from shared memory, and the lag diagonals are summed
-// in shared memory before the int64 atomics.  Operands are the packed fp16
-// counts of G1, converted back to integers when they are staged.
-#include <cuda_fp16.h>
+// in shared memory before the int64 atomics.  Operands are the packed 16-bit
+// counts of G1 (raw integers), widened to 32 bits when they are staged.
 #include "g2_ptx.cuh"
 #include "g2_host.h"
 
@@ -53,9 +52,8 @@ __device__ __forceinline__ void load_tile(const uint16_t* __restrict__ base, int
   }
 }
 
-__device__ __forceinline__ uint32_t h2u(uint32_t bits16) {
-  return __half2uint_rn(__ushort_as_half(static_cast<unsigned short>(bits16)));
-}
+// packed fp16 operands hold the raw integer counts (0..2048) as 16-bit values
+__device__ __forceinline__ uint32_t h2u(uint32_t bits16) { return bits16; }
 
 __device__ __forceinline__ void store_tile(uint32_t* __restrict__ s, const uint4 (&reg)[2]) {
 #pragma unroll

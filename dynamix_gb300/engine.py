@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _lib
 from .plan import (E4M3_MAX_EXACT, EXACT_LIMIT, FP16_MAX_EXACT, MODE_BYTES, MODE_E4M3, MODE_FP16, PackLayout,
-                   chunk_grams, gram_items)
+                   chunk_grams, e4m3_segment_bound, gram_items)
 
 
 def _torch():
@@ -172,6 +172,10 @@ class DenseEngine:
             L.d_chunk_piece_off = d(L.chunk_piece_off)
             L.d_bin_kpad = d(L.bin_kpad)
             L.d_piece_emax = torch.zeros(max(1, L.n_pieces * L.n_planes), dtype=torch.int32, device=self.dev)
+            if mode == MODE_E4M3:
+                L.d_chunk_word_off = d(L.chunk_word_off)
+                L.d_word_dst = d(L.word_dst)
+                L.d_word_src = d(L.word_src.view(np.int32))
             self._layouts[mode] = L
         return self._layouts[mode]
 
@@ -214,6 +218,12 @@ class DenseEngine:
         L.d_piece_emax.zero_()
         self.err.zero_()
         st = stream_handle(self.dev)
+        if mode == MODE_E4M3:
+            _lib.check(self.lib.g2_pack_e4m3(
+                ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_word_off),
+                ptr(L.d_word_dst), ptr(L.d_word_src), ptr(L.d_chunk_slot_bin), L.n_chunks, ptr(packed),
+                L.packed_cols, ptr(self.sums), self.n_bins, ptr(self.err), st), "g2_pack_e4m3")
+            return L
         _lib.check(self.lib.g2_pack_frames(
             ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_entry_off),
             ptr(L.d_entry_dst), ptr(L.d_entry_meta), ptr(L.d_chunk_slot_bin), ptr(L.d_chunk_piece_off),
@@ -262,7 +272,10 @@ class DenseEngine:
         the K split; fall back to a wider packing when the counts do not fit."""
         while True:
             L = self.pack(frames_dev, mode)
-            seg_emax = L.segment_emax(L.d_piece_emax.cpu().numpy().view(np.uint32))
+            if mode == MODE_E4M3:
+                seg_emax = e4m3_segment_bound(L)          # counts <= 16 bound every sum
+            else:
+                seg_emax = L.segment_emax(L.d_piece_emax.cpu().numpy().view(np.uint32))
             code = int(self.err.item())
             if code & _lib.DEVERR_RANGE and mode == MODE_E4M3 and self.operand == "auto":
                 mode = MODE_FP16

@@ -21,8 +21,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._lib import (BK, ITEM_DTYPE, KIND_E4M3, KIND_FP16, PACK_CHUNK, PACK_MAX_PIECES, PACK_MAX_SLOTS, PAD, PLAIN_BM,
-                   PLAIN_BN, TC_BM, TC_BN)
+from ._lib import (BK, ITEM_DTYPE, KIND_E4M3, KIND_FP16, PACK_CHUNK, PACK_MAX_PIECES, PACK_MAX_SLOTS,
+                   PACK_WORDS_PER_CHUNK, PAD, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN)
 
 EXACT_LIMIT = 1 << 24   # fp32 represents every integer up to 2^24 exactly
 FP16_MAX_EXACT = 2048   # fp16 represents every integer up to 2^11 exactly
@@ -125,6 +125,25 @@ class PackLayout:
         self.entry_meta = (src_off | (slot << 11) | (piece << 16)).astype(np.uint32)
         self.bin_kpad = self.kpad.astype(np.int32)
         self.n_planes = 2 if self.split else 1
+        # words of the byte-permutation pack (e4m3): 4 aligned packed columns of
+        # one bin (bins are 128-column aligned) with their 4 chunk-local sources
+        if self.mode == MODE_E4M3:
+            nq = self.packed_cols // 4
+            wkey = chunk * nq + dst // 4
+            uw, widx = np.unique(wkey, return_inverse=True)
+            srcs = np.full((uw.size, 4), 0xFFF, dtype=np.int64)
+            srcs[widx, dst % 4] = src_off
+            wslot = np.zeros(uw.size, dtype=np.int64)
+            wslot[widx] = slot
+            wchunk = uw // nq
+            self.chunk_word_off = np.searchsorted(wchunk, np.arange(self.n_chunks + 1)).astype(np.int32)
+            if uw.size and np.diff(self.chunk_word_off).max() > PACK_WORDS_PER_CHUNK:
+                raise ValueError("more than %d packed words in one chunk" % PACK_WORDS_PER_CHUNK)
+            self.word_dst = ((uw % nq) * 4).astype(np.int32)
+            ws = np.empty((uw.size, 2), dtype=np.uint32)
+            ws[:, 0] = (srcs[:, 0] | (srcs[:, 1] << 12) | ((srcs[:, 2] & 0xFF) << 24)).astype(np.uint32)
+            ws[:, 1] = ((srcs[:, 2] >> 8) | (srcs[:, 3] << 4) | (wslot << 16)).astype(np.uint32)
+            self.word_src = ws
 
     def segment_emax(self, piece_emax):
         """Per 64-column output segment, the sum over its pieces of the pieces'
@@ -258,6 +277,13 @@ def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT):
         for (u0, u1) in k_chunks(ea, eb, limit):
             out.append((b, a_off, b_off, u0 * PAD, (u1 - u0) * PAD, shift))
     return out
+
+
+def e4m3_segment_bound(layout):
+    """Energy bound per 64-column segment for e4m3 operands without looking at
+    the data: every count is <= 16, so a segment's sum of squares is <= 64 * 256
+    (a Gram chunk of up to 65,536 columns stays below 2^24)."""
+    return np.full(layout.packed_cols // BK, BK * E4M3_MAX_EXACT ** 2, dtype=np.float64)
 
 
 def gram_macs(T, npix):

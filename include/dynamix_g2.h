@@ -50,11 +50,12 @@ extern "C" {
 #define G2_PACK_CHUNK 2048 /* source pixels per pack chunk */
 #define G2_PACK_MAX_SLOTS  32   /* distinct bins per chunk */
 #define G2_PACK_MAX_PIECES 512  /* (64-column segment x chunk) pieces per chunk */
+#define G2_PACK_WORDS_PER_CHUNK 768 /* 4-column words per chunk (g2_pack_e4m3) */
 #define G2_MAX_JOBS   32
 
 /* element kinds of a packed operand matrix */
-#define G2_KIND_FP16  0    /* fp16 bit patterns of integer counts <= 2048 */
-#define G2_KIND_E4M3  1    /* e4m3 bytes of integer counts <= 16 */
+#define G2_KIND_FP16  0    /* 16-bit raw counts <= 2048, MMA kind::f16 */
+#define G2_KIND_E4M3  1    /* 8-bit raw counts <= 16, MMA kind::f8f6f4 (e4m3) */
 
 /* One unit of Gram work: rows [i0, i0+BM) of the A operand against rows
  * [j0, j0+BN) of the B operand over packed columns [a_k0, a_k0+k_len) and
@@ -73,8 +74,9 @@ typedef struct g2_gram_item {
 } g2_gram_item;
 
 /* A dense job: its packed operand matrix, row-major [nframes][packed_cols]
- * of fp16 bit patterns (G2_KIND_FP16, counts <= 2048) or e4m3 bytes
- * (G2_KIND_E4M3, counts <= 16); both represent the integer counts exactly. */
+ * of raw integer counts, 16-bit (G2_KIND_FP16, counts <= 2048, read as fp16 =
+ * count * 2^-24) or 8-bit (G2_KIND_E4M3, counts <= 16, read as e4m3 =
+ * count * 2^-9); both represent the counts exactly. */
 typedef struct g2_job {
     const void* packed_dev;
     int64_t nframes;
@@ -103,10 +105,13 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
  * chunk_slot_bin[c * G2_PACK_MAX_SLOTS + slot] is the 0-based bin of a slot (-1
  * unused).  A piece is one 64-column output segment within one chunk; chunk c
  * owns pieces [chunk_piece_off[c], chunk_piece_off[c+1]).
- * mode 0: the count is written as fp16 to entry_dst (counts <= 2048).
- * mode 1 (u16 only): high byte (fp16) to entry_dst, low byte to entry_dst +
+ * The packed values are the raw integers: read as fp16, the 16-bit values
+ * 0..2048 are exactly count * 2^-24; read as e4m3, the bytes 0..16 are exactly
+ * count * 2^-9 (g2_gram_tc rescales by the power of two).
+ * mode 0: the count as a 16-bit value at entry_dst (counts <= 2048).
+ * mode 1 (u16 only): high byte (16-bit) at entry_dst, low byte at entry_dst +
  *   bin_kpad[bin] (the low-byte plane of the bin).
- * mode 2: the count is written as an e4m3 byte (counts <= 16).
+ * mode 2: the count as a byte at entry_dst (counts <= 16).
  * A count that does not fit the mode sets G2_DEVERR_RANGE in err_dev.
  * Adds S_b(t) into sums_dev[b * nframes + t] (caller zeroes it) and raises
  * piece_emax_dev[plane * n_pieces + piece] (caller zeroes it) to the max over
@@ -120,6 +125,21 @@ int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, 
                    int32_t mode, void* packed_dev, int64_t packed_cols, int64_t* sums_dev,
                    int32_t n_bins, uint32_t* piece_emax_dev, int64_t n_pieces, int32_t* err_dev,
                    void* stream);
+
+/* G1 for e4m3 operands (every count <= 16): a pure byte permutation.  The
+ * raw count bytes are the operand (bytes 0..16 read as e4m3 are exactly
+ * count * 2^-9; g2_gram_tc rescales).  Chunks as for g2_pack_frames; chunk c
+ * owns words [chunk_word_off[c], chunk_word_off[c+1]) of at most
+ * G2_PACK_WORDS_PER_CHUNK; word w covers packed columns word_dst[w] ..
+ * word_dst[w]+3 of one bin, word_src[2w], word_src[2w+1] hold the 4 chunk-local
+ * source offsets (12 bits each, 0xFFF = column owned by another chunk) and the
+ * bin slot (bits 16-20 of word_src[2w+1]).  Adds S_b(t) into sums_dev; a count
+ * above 16 sets G2_DEVERR_RANGE.  Same role as g2_pack_frames mode 2. */
+int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
+                 const int32_t* chunk_word_off_dev, const int32_t* word_dst_dev,
+                 const uint32_t* word_src_dev, const int32_t* chunk_slot_bin_dev, int64_t n_chunks,
+                 void* packed_dev, int64_t packed_cols, int64_t* sums_dev, int32_t n_bins,
+                 int32_t* err_dev, void* stream);
 
 /* Largest count over the binned pixels (col_src >= 0): picks split 0/1.
  * No reference counterpart (the reference never checks its dtype range). */

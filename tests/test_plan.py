@@ -161,3 +161,25 @@ def test_speckle_generator_statistics():
     # speckle contrast: var/mean^2 ~ 1 + 1/mean for Poisson-exponential counts
     c = fr.var() / m ** 2
     assert 1.0 < c < 2.2
+
+
+def test_e4m3_word_tables_decode_to_entries():
+    qm = annular_qmask((70, 90), 5, 3.0, 40.0)
+    L = plan.PackLayout(qm, 5, plan.MODE_E4M3)
+    chunk_e = np.repeat(np.arange(L.n_chunks), np.diff(L.chunk_entry_off))
+    want = set(zip((chunk_e * PACK_CHUNK + (L.entry_meta.astype(np.int64) & 2047)).tolist(),
+                   L.entry_dst.tolist()))
+    got = set()
+    chunk_w = np.repeat(np.arange(L.n_chunks), np.diff(L.chunk_word_off))
+    x = L.word_src[:, 0].astype(np.int64)
+    y = L.word_src[:, 1].astype(np.int64)
+    srcs = np.stack([x & 0xFFF, (x >> 12) & 0xFFF, (x >> 24) | ((y & 0xF) << 8), (y >> 4) & 0xFFF], axis=1)
+    assert np.all(L.word_dst % 4 == 0)
+    for w in range(L.word_dst.size):
+        for i in range(4):
+            if srcs[w, i] != 0xFFF:
+                got.add((int(chunk_w[w] * PACK_CHUNK + srcs[w, i]), int(L.word_dst[w] + i)))
+        # the slot names the bin whose columns hold the word
+        b = L.chunk_slot_bin[chunk_w[w] * PACK_MAX_SLOTS + ((y[w] >> 16) & 31)]
+        assert L.plane0[b] <= L.word_dst[w] < L.plane0[b] + L.kpad[b]
+    assert got == want
