@@ -264,10 +264,12 @@ __global__ void __launch_bounds__(THREADS, 3)
 // Gram sum by themselves, so no energies are needed either.  A thread owns up
 // to WPT "words" = 4 consecutive packed columns of one bin; per frame it reads
 // the 4 source bytes from the staged chunk, stores one 32-bit word (byte
-// stores only for the two partial words at the ends of a bin's run in the
-// chunk, whose other bytes belong to the neighbouring chunk), and adds the
-// word's byte sum (dp4a) to the bin sum through one warp reduction.
-constexpr int WPT = 3;
+// stores only for the partial words at the ends of a bin's run in the chunk,
+// whose other bytes belong to the neighbouring chunk), and adds the word's
+// byte sum (dp4a) to the bin sum.  The host lays the words out in warp tiles
+// of 32 words of one bin (padded with empty words), so the loop is free of
+// divergence and each warp reduces its sums with one full-warp reduction.
+constexpr int WPT = G2_PACK_WORDS_PER_CHUNK / THREADS;
 constexpr uint32_t NO_SRC = 0xFFFu;
 
 template <typename Tin>
@@ -306,25 +308,28 @@ __global__ void __launch_bounds__(THREADS, 4)
     if (w < nw) {
       const int32_t d = word_dst[w0 + w];
       const uint2 m = word_src[w0 + w];
-      uint32_t sv[4] = {m.x & 0xFFFu, (m.x >> 12) & 0xFFFu, (m.x >> 24) | ((m.y & 0xFu) << 8), (m.y >> 4) & 0xFFFu};
-      bool ok = d >= 0 && (d & 3) == 0 && d + 4 <= packed_cols;
-      bool all = true;
+      slot[k] = static_cast<int>((m.y >> 16) & 31u);
+      if (d >= 0) {
+        uint32_t sv[4] = {m.x & 0xFFFu, (m.x >> 12) & 0xFFFu, (m.x >> 24) | ((m.y & 0xFu) << 8),
+                          (m.y >> 4) & 0xFFFu};
+        bool ok = (d & 3) == 0 && d + 4 <= packed_cols;
+        bool all = true;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        if (sv[i] == NO_SRC) {
-          all = false;
-        } else if (sv[i] >= static_cast<uint32_t>(CH) || p0 + sv[i] >= npix) {
-          ok = false;
+        for (int i = 0; i < 4; ++i) {
+          if (sv[i] == NO_SRC) {
+            all = false;
+          } else if (sv[i] >= static_cast<uint32_t>(CH) || p0 + sv[i] >= npix) {
+            ok = false;
+          }
         }
-      }
-      if (!ok) {
-        bad = true;
-      } else {
-        dst[k] = d;
-        slot[k] = static_cast<int>((m.y >> 16) & 31u);
-        full[k] = all;
+        if (!ok) {
+          bad = true;
+        } else {
+          dst[k] = d;
+          full[k] = all;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) src[k][i] = sv[i];
+          for (int i = 0; i < 4; ++i) src[k][i] = sv[i];
+        }
       }
     }
   }
@@ -338,13 +343,6 @@ __global__ void __launch_bounds__(THREADS, 4)
   }
   for (int i = tid; i < F * MAX_SLOTS; i += THREADS) (&s_sum[0][0])[i] = 0;
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
-  unsigned gslot[WPT];
-#pragma unroll
-  for (int k = 0; k < WPT; ++k) {
-    const bool valid = dst[k] >= 0;
-    const unsigned amask = __ballot_sync(0xffffffffu, valid);
-    gslot[k] = valid ? __match_any_sync(amask, slot[k]) : 0u;
-  }
   uint32_t range_bad = 0;
   const int64_t total_bytes = T * npix * static_cast<int64_t>(sizeof(Tin));
   const uint8_t* fbytes = reinterpret_cast<const uint8_t*>(frames);
@@ -388,19 +386,18 @@ __global__ void __launch_bounds__(THREADS, 4)
       uint8_t* row = packed + t * packed_cols;
 #pragma unroll
       for (int k = 0; k < WPT; ++k) {
-        if (dst[k] < 0) continue;
         uint32_t word = 0;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          if (src[k][i] != NO_SRC) {
-            const uint32_t v = sizeof(Tin) == 1
-                                   ? static_cast<uint32_t>(sb[src[k][i]])
-                                   : static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(sb + 2 * src[k][i]));
-            range_bad |= v > 16u ? 1u : 0u;
-            word |= (v & 0xFFu) << (8 * i);
-          }
+          const bool has = src[k][i] != NO_SRC;
+          const uint32_t so = has ? src[k][i] : 0u;
+          uint32_t v = sizeof(Tin) == 1 ? static_cast<uint32_t>(sb[so])
+                                        : static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(sb + 2 * so));
+          v = has ? v : 0u;
+          range_bad |= v > 16u ? 1u : 0u;
+          word |= (v & 0xFFu) << (8 * i);
         }
-        if (live) {
+        if (live && dst[k] >= 0) {
           if (full[k]) {
             *reinterpret_cast<uint32_t*>(row + dst[k]) = word;
           } else {
@@ -410,8 +407,8 @@ __global__ void __launch_bounds__(THREADS, 4)
           }
         }
         const uint32_t bs = live ? __dp4a(word, 0x01010101u, 0u) : 0u;
-        const uint32_t vs = __reduce_add_sync(gslot[k], bs);
-        if ((__ffs(gslot[k]) - 1) == lane && vs) atomicAdd(&s_sum[f][slot[k]], vs);
+        const uint32_t vs = __reduce_add_sync(0xffffffffu, bs);  // the warp's words share one bin
+        if (lane == 0 && vs) atomicAdd(&s_sum[f][slot[k]], vs);
       }
     }
     __syncthreads();

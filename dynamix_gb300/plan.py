@@ -136,14 +136,29 @@ class PackLayout:
             wslot = np.zeros(uw.size, dtype=np.int64)
             wslot[widx] = slot
             wchunk = uw // nq
-            self.chunk_word_off = np.searchsorted(wchunk, np.arange(self.n_chunks + 1)).astype(np.int32)
-            if uw.size and np.diff(self.chunk_word_off).max() > PACK_WORDS_PER_CHUNK:
-                raise ValueError("more than %d packed words in one chunk" % PACK_WORDS_PER_CHUNK)
-            self.word_dst = ((uw % nq) * 4).astype(np.int32)
-            ws = np.empty((uw.size, 2), dtype=np.uint32)
-            ws[:, 0] = (srcs[:, 0] | (srcs[:, 1] << 12) | ((srcs[:, 2] & 0xFF) << 24)).astype(np.uint32)
-            ws[:, 1] = ((srcs[:, 2] >> 8) | (srcs[:, 3] << 4) | (wslot << 16)).astype(np.uint32)
+            wdst = (uw % nq) * 4
+            # slot-uniform warp tiles: the words of one (chunk, slot) run are
+            # padded to a multiple of 32 with empty words (no sources, dst -1),
+            # so every warp of the kernel reduces one bin
+            run = wchunk * PACK_MAX_SLOTS + wslot
+            urun, run_start, run_len = np.unique(run, return_index=True, return_counts=True)
+            padded = (run_len + 31) // 32 * 32
+            out_start = np.concatenate([[0], np.cumsum(padded)])[:-1]
+            pos = np.repeat(out_start - run_start, run_len) + np.arange(uw.size)
+            total = int(padded.sum())
+            self.word_dst = np.full(total, -1, dtype=np.int32)
+            self.word_dst[pos] = wdst
+            ws = np.empty((total, 2), dtype=np.uint32)
+            ws[:, 0] = 0xFFF | (0xFFF << 12) | (0xFF << 24)
+            empty_slot = np.repeat(urun % PACK_MAX_SLOTS, padded)
+            ws[:, 1] = (0xF | (0xFFF << 4) | (empty_slot << 16)).astype(np.uint32)
+            ws[pos, 0] = (srcs[:, 0] | (srcs[:, 1] << 12) | ((srcs[:, 2] & 0xFF) << 24)).astype(np.uint32)
+            ws[pos, 1] = ((srcs[:, 2] >> 8) | (srcs[:, 3] << 4) | (wslot << 16)).astype(np.uint32)
             self.word_src = ws
+            pchunk = np.repeat(urun // PACK_MAX_SLOTS, padded)
+            self.chunk_word_off = np.searchsorted(pchunk, np.arange(self.n_chunks + 1)).astype(np.int32)
+            if total and np.diff(self.chunk_word_off).max() > PACK_WORDS_PER_CHUNK:
+                raise ValueError("more than %d packed words in one chunk" % PACK_WORDS_PER_CHUNK)
 
     def segment_emax(self, piece_emax):
         """Per 64-column output segment, the sum over its pieces of the pieces'

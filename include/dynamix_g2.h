@@ -50,7 +50,7 @@ extern "C" {
 #define G2_PACK_CHUNK 2048 /* source pixels per pack chunk */
 #define G2_PACK_MAX_SLOTS  32   /* distinct bins per chunk */
 #define G2_PACK_MAX_PIECES 512  /* (64-column segment x chunk) pieces per chunk */
-#define G2_PACK_WORDS_PER_CHUNK 768 /* 4-column words per chunk (g2_pack_e4m3) */
+#define G2_PACK_WORDS_PER_CHUNK 1024 /* 4-column words per chunk (g2_pack_e4m3) */
 #define G2_MAX_JOBS   32
 
 /* element kinds of a packed operand matrix */
@@ -133,8 +133,10 @@ int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, 
  * G2_PACK_WORDS_PER_CHUNK; word w covers packed columns word_dst[w] ..
  * word_dst[w]+3 of one bin, word_src[2w], word_src[2w+1] hold the 4 chunk-local
  * source offsets (12 bits each, 0xFFF = column owned by another chunk) and the
- * bin slot (bits 16-20 of word_src[2w+1]).  Adds S_b(t) into sums_dev; a count
- * above 16 sets G2_DEVERR_RANGE.  Same role as g2_pack_frames mode 2. */
+ * bin slot (bits 16-20 of word_src[2w+1]); word_dst[w] = -1 marks an empty
+ * word.  Every aligned group of 32 words of a chunk must belong to one bin
+ * slot (the bin sums are reduced per warp).  Adds S_b(t) into sums_dev; a
+ * count above 16 sets G2_DEVERR_RANGE.  Same role as g2_pack_frames mode 2. */
 int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
                  const int32_t* chunk_word_off_dev, const int32_t* word_dst_dev,
                  const uint32_t* word_src_dev, const int32_t* chunk_slot_bin_dev, int64_t n_chunks,

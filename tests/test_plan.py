@@ -174,8 +174,14 @@ def test_e4m3_word_tables_decode_to_entries():
     x = L.word_src[:, 0].astype(np.int64)
     y = L.word_src[:, 1].astype(np.int64)
     srcs = np.stack([x & 0xFFF, (x >> 12) & 0xFFF, (x >> 24) | ((y & 0xF) << 8), (y >> 4) & 0xFFF], axis=1)
-    assert np.all(L.word_dst % 4 == 0)
-    for w in range(L.word_dst.size):
+    live = L.word_dst >= 0
+    assert np.all(L.word_dst[live] % 4 == 0)
+    assert np.all(srcs[~live] == 0xFFF)
+    # every aligned group of 32 words of a chunk names one bin slot
+    assert np.all(np.diff(L.chunk_word_off) % 32 == 0)
+    wslot = (y >> 16) & 31
+    assert np.all(wslot.reshape(-1, 32) == wslot.reshape(-1, 32)[:, :1])
+    for w in np.flatnonzero(live):
         for i in range(4):
             if srcs[w, i] != 0xFFF:
                 got.add((int(chunk_w[w] * PACK_CHUNK + srcs[w, i]), int(L.word_dst[w] + i)))
