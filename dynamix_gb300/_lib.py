@@ -22,21 +22,22 @@ DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE = 1, 2, 4
 
 BK = 64          # source segment width (pixels)
 PAD = 128        # packed bins and packed_cols are multiples of this
-PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 32, 512, 1024
+PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 32, 512, 512
 TC_BM, TC_BN = 128, 256
 PLAIN_BM, PLAIN_BN = 128, 128
 MAX_JOBS = 32
 KIND_FP16, KIND_E4M3 = 0, 1
 
-# numpy mirror of g2_gram_item (40 bytes, 8-byte aligned)
+# numpy mirror of g2_gram_item (48 bytes, 8-byte aligned)
 ITEM_DTYPE = np.dtype([("job", "<i4"), ("i0", "<i4"), ("j0", "<i4"), ("a_k0", "<i4"), ("b_k0", "<i4"),
-                       ("k_len", "<i4"), ("shift", "<i4"), ("nframes", "<i4"), ("out_off", "<i8")])
-assert ITEM_DTYPE.itemsize == 40
+                       ("k_len", "<i4"), ("shift", "<i4"), ("nframes", "<i4"), ("out_off", "<i8"),
+                       ("s_off", "<i8")])
+assert ITEM_DTYPE.itemsize == 48
 
 
 class Job(C.Structure):
     _fields_ = [("packed_dev", C.c_void_p), ("nframes", C.c_int64), ("packed_cols", C.c_int64),
-                ("elem_kind", C.c_int32), ("reserved", C.c_int32)]
+                ("elem_kind", C.c_int32), ("ones_row", C.c_int32)]
 
 
 _p = C.c_void_p
@@ -50,9 +51,9 @@ SIGNATURES = {
     "g2_device_info": (C.c_int, [C.c_int, _p, _p, _p]),
     "g2_pack_frames": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _p, _p, _p, _i64, _i32, _p, _i64, _p, _i32, _p,
                                  _i64, _p, _p]),
-    "g2_pack_e4m3": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _p, _i64, _p, _i64, _p, _i32, _p, _p]),
+    "g2_pack_e4m3": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _p, _p]),
     "g2_binned_max": (C.c_int, [_p, _i32, _i64, _i64, _p, _i64, _p, _p]),
-    "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i32, _p]),
+    "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
     "g2_denominator": (C.c_int, [_p, _i32, _i64, _p, _p]),
     "g2_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
@@ -94,15 +95,16 @@ def check(status, what):
 
 
 def jobs_array(jobs):
-    """[(packed_ptr, nframes, packed_cols, elem_kind), ...] -> ctypes array of Job."""
+    """[(packed_ptr, nframes, packed_cols, elem_kind, ones_row), ...] -> ctypes array of Job."""
     if not 1 <= len(jobs) <= MAX_JOBS:
         raise ValueError("between 1 and %d jobs per launch" % MAX_JOBS)
     arr = (Job * len(jobs))()
-    for i, (ptr, T, cols, kind) in enumerate(jobs):
+    for i, (ptr, T, cols, kind, ones) in enumerate(jobs):
         arr[i].packed_dev = ptr
         arr[i].nframes = T
         arr[i].packed_cols = cols
         arr[i].elem_kind = kind
+        arr[i].ones_row = int(bool(ones))
     return arr
 
 

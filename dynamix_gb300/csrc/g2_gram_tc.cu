@@ -54,6 +54,7 @@ struct MapsParam {
   CUtensorMap a[G2_MAX_JOBS];
   CUtensorMap b[G2_MAX_JOBS];
   int32_t kind[G2_MAX_JOBS];  // G2_KIND_FP16 or G2_KIND_E4M3
+  int32_t ones[G2_MAX_JOBS];  // packed matrix has the row of ones at row nframes
 };
 
 // packed elements per 128-byte stage row
@@ -75,17 +76,18 @@ __device__ __forceinline__ bool named_bar_any(uint32_t id, uint32_t n, bool v) {
 // Every role applies the same test, so a malformed item is skipped by all of
 // them consistently (the epilogue records G2_DEVERR_BOUNDS).
 __device__ __forceinline__ bool item_ok(const g2_gram_item& w, const MapsParam& maps, int n_jobs,
-                                        int64_t numer_len) {
+                                        int64_t numer_len, int64_t sums_len) {
   if (w.job < 0 || w.job >= n_jobs) return false;
   const int bk = stage_elems(maps.kind[w.job]);
   return w.k_len > 0 && (w.k_len % bk) == 0 && (w.a_k0 % bk) == 0 && (w.b_k0 % bk) == 0 && w.nframes > 0 &&
-         w.shift >= 0 && w.shift <= 32 && w.out_off >= 0 && w.out_off + w.nframes <= numer_len;
+         w.shift >= 0 && w.shift <= 32 && w.out_off >= 0 && w.out_off + w.nframes <= numer_len &&
+         (w.s_off < 0 || (maps.ones[w.job] && w.shift == 0 && w.s_off + w.nframes <= sums_len));
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     gram_tc_kernel(const __grid_constant__ MapsParam maps, int n_jobs, const g2_gram_item* __restrict__ items,
                    int64_t n_items, unsigned long long* __restrict__ numer, int64_t numer_len,
-                   int32_t* __restrict__ err) {
+                   unsigned long long* __restrict__ sums, int64_t sums_len, int32_t* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok(w, maps, n_jobs, numer_len)) continue;
+        if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) continue;
         const CUtensorMap* ma = &maps.a[w.job];
         const CUtensorMap* mb = &maps.b[w.job];
         const int bk = stage_elems(maps.kind[w.job]);
@@ -169,7 +171,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok(w, maps, n_jobs, numer_len)) continue;
+        if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) continue;
         const bool fp8 = maps.kind[w.job] == G2_KIND_E4M3;
         const int buf = static_cast<int>(local & 1);
         const uint32_t ap = static_cast<uint32_t>((local >> 1) & 1);
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     int64_t local = 0;
     for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x, ++local) {
       const g2_gram_item w = items[it];
-      if (!item_ok(w, maps, n_jobs, numer_len)) {
+      if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) {
         if (etid == 0) atomicOr(err, G2_DEVERR_BOUNDS);
         --local;
         continue;
@@ -234,16 +236,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       // (count * 2^-24): each accumulator holds sum * 2^-18 or sum * 2^-48
       const float unscale = maps.kind[w.job] == G2_KIND_E4M3 ? 262144.0f : 281474976710656.0f;
       const uint32_t tbase = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(buf * BN);
+      // frames >= nframes (TMA zero fill, or the row of ones) never enter the
+      // lag sums; the column of the row of ones, when this block holds it,
+      // goes to the bin sums instead
+      const bool row_live = w.i0 + row < w.nframes;
+      const int ones_col = w.s_off >= 0 ? w.nframes - w.j0 : -1;  // -1 or >= BN: not in this block
+      const int col_end = min(BN, w.nframes - w.j0);                // columns < col_end are frames
 #pragma unroll 1
       for (int cc = 0; cc < BN / 32; ++cc) {
         uint32_t v[32];
+        __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the previous chunk
         tmem_ld_32x32b_x32(tbase + static_cast<uint32_t>(cc * 32), v);
         tmem_wait_ld();
+        if (!row_live) continue;
         const int dbase = cc * 32 - row + (BM - 1);
+        const int jx = ones_col - cc * 32;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const uint32_t x = __float2uint_rn(__uint_as_float(v[j]) * unscale);
-          if (x) atomicAdd(&dacc[dbase + j], x);
+          if (j == jx) {
+            if (x) atomicAdd(&sums[w.s_off + w.i0 + row], static_cast<unsigned long long>(x));
+          } else if (x && cc * 32 + j < col_end) {
+            atomicAdd(&dacc[dbase + j], x);
+          }
         }
       }
       tc_fence_before();
@@ -274,16 +289,18 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 }  // namespace g2
 
 extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
-                          uint64_t* numer_dev, int64_t numer_len, int32_t* err_dev, int32_t grid, void* stream) {
+                          uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
+                          int32_t* err_dev, int32_t grid, void* stream) {
   using namespace g2;
-  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !numer_dev || numer_len <= 0 || !err_dev)
+  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !numer_dev || numer_len <= 0 || !err_dev ||
+      sums_len < 0 || (sums_len > 0 && !sums_dev))
     return G2_ERR_ARG;
   if (n_items > 0 && !items_dev) return G2_ERR_ARG;
   for (int j = 0; j < n_jobs; ++j) {
     const g2_job& jb = jobs[j];
     if (!jb.packed_dev || !aligned(jb.packed_dev, 16) || jb.nframes <= 0 || jb.nframes >= (1ll << 31) ||
         jb.packed_cols <= 0 || jb.packed_cols % G2_PAD != 0 || jb.packed_cols >= (1ll << 31) ||
-        (jb.elem_kind != G2_KIND_FP16 && jb.elem_kind != G2_KIND_E4M3))
+        (jb.elem_kind != G2_KIND_FP16 && jb.elem_kind != G2_KIND_E4M3) || (jb.ones_row != 0 && jb.ones_row != 1))
       return G2_ERR_ARG;
   }
   if (n_items == 0) return G2_OK;
@@ -294,13 +311,13 @@ extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item
   for (int j = 0; j < n_jobs; ++j) {
     const int eb = jobs[j].elem_kind == G2_KIND_E4M3 ? 1 : 2;
     const uint32_t box_cols = tc::ROW_BYTES / eb;
-    int st = encode_tmap_2d(&maps.a[j], jobs[j].packed_dev, eb, jobs[j].packed_cols, jobs[j].nframes, box_cols,
-                            tc::BM);
+    const uint64_t rows = static_cast<uint64_t>(jobs[j].nframes) + (jobs[j].ones_row ? 1 : 0);
+    int st = encode_tmap_2d(&maps.a[j], jobs[j].packed_dev, eb, jobs[j].packed_cols, rows, box_cols, tc::BM);
     if (st != G2_OK) return st;
-    st = encode_tmap_2d(&maps.b[j], jobs[j].packed_dev, eb, jobs[j].packed_cols, jobs[j].nframes, box_cols,
-                        tc::BN);
+    st = encode_tmap_2d(&maps.b[j], jobs[j].packed_dev, eb, jobs[j].packed_cols, rows, box_cols, tc::BN);
     if (st != G2_OK) return st;
     maps.kind[j] = jobs[j].elem_kind;
+    maps.ones[j] = jobs[j].ones_row;
   }
   if (cudaFuncSetAttribute(tc::gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES) !=
       cudaSuccess)
@@ -310,6 +327,7 @@ extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item
   int64_t g = grid > 0 ? grid : sms;
   if (g > n_items) g = n_items;
   tc::gram_tc_kernel<<<static_cast<unsigned>(g), tc::NUM_THREADS, tc::SMEM_BYTES, as_stream(stream)>>>(
-      maps, n_jobs, items_dev, n_items, reinterpret_cast<unsigned long long*>(numer_dev), numer_len, err_dev);
+      maps, n_jobs, items_dev, n_items, reinterpret_cast<unsigned long long*>(numer_dev), numer_len,
+      reinterpret_cast<unsigned long long*>(sums_dev), sums_len, err_dev);
   return launch_status();
 }

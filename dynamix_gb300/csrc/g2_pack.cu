@@ -260,15 +260,15 @@ __global__ void __launch_bounds__(THREADS, 3)
 
 // ---- e4m3 (counts <= 16): a pure byte permutation --------------------------
 // The raw count bytes are the e4m3 operand (bytes 0..16 read as e4m3 are
-// count * 2^-9), so no conversion is needed, and counts <= 16 bound every
-// Gram sum by themselves, so no energies are needed either.  A thread owns up
-// to WPT "words" = 4 consecutive packed columns of one bin; per frame it reads
-// the 4 source bytes from the staged chunk, stores one 32-bit word (byte
+// count * 2^-9), so no conversion is needed; counts <= 16 bound every Gram sum
+// by themselves, so no energies are needed; and the bin sums come from the
+// Gram (row of ones), so this kernel only moves bytes.  A thread owns up to WPT
+// "words" = 4 consecutive packed columns of one bin; per frame it reads the 4
+// source bytes from the staged chunk -- one funnel shift of two aligned 32-bit
+// shared loads when the sources are consecutive pixels (inside a run of the
+// annulus), four byte loads otherwise -- and stores one 32-bit word (byte
 // stores only for the partial words at the ends of a bin's run in the chunk,
-// whose other bytes belong to the neighbouring chunk), and adds the word's
-// byte sum (dp4a) to the bin sum.  The host lays the words out in warp tiles
-// of 32 words of one bin (padded with empty words), so the loop is free of
-// divergence and each warp reduces its sums with one full-warp reduction.
+// whose other bytes belong to the neighbouring chunk).
 constexpr int WPT = G2_PACK_WORDS_PER_CHUNK / THREADS;
 constexpr uint32_t NO_SRC = 0xFFFu;
 
@@ -276,17 +276,13 @@ template <typename Tin>
 __global__ void __launch_bounds__(THREADS, 4)
     pack_e4m3_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix,
                      const int32_t* __restrict__ chunk_word_off, const int32_t* __restrict__ word_dst,
-                     const uint2* __restrict__ word_src, const int32_t* __restrict__ chunk_slot_bin,
-                     uint8_t* __restrict__ packed, int64_t packed_cols, unsigned long long* __restrict__ sums,
-                     int n_bins, int32_t* __restrict__ err) {
+                     const uint2* __restrict__ word_src, uint8_t* __restrict__ packed, int64_t packed_cols,
+                     int32_t* __restrict__ err) {
   using C = Cfg<Tin>;
   constexpr int F = C::F;
-  __shared__ __align__(16) uint8_t s_buf[2][F][C::BUF];
-  __shared__ uint32_t s_sum[F][MAX_SLOTS];
-  __shared__ int s_bin[MAX_SLOTS];
+  __shared__ __align__(16) uint8_t s_buf[2][F][C::BUF + 4];
 
   const int tid = threadIdx.x;
-  const int lane = tid & 31;
   const int64_t c = blockIdx.x;
   const int64_t p0 = c * CH;
   const int w0 = chunk_word_off[c];
@@ -294,21 +290,18 @@ __global__ void __launch_bounds__(THREADS, 4)
 
   int32_t dst[WPT];
   uint32_t src[WPT][4];
-  int slot[WPT];
-  bool full[WPT];
+  bool full[WPT], run4[WPT];
   bool bad = false;
 #pragma unroll
   for (int k = 0; k < WPT; ++k) {
     const int w = tid + k * THREADS;
     dst[k] = -1;
-    slot[k] = 0;
-    full[k] = false;
+    full[k] = run4[k] = false;
 #pragma unroll
     for (int i = 0; i < 4; ++i) src[k][i] = NO_SRC;
     if (w < nw) {
       const int32_t d = word_dst[w0 + w];
       const uint2 m = word_src[w0 + w];
-      slot[k] = static_cast<int>((m.y >> 16) & 31u);
       if (d >= 0) {
         uint32_t sv[4] = {m.x & 0xFFFu, (m.x >> 12) & 0xFFFu, (m.x >> 24) | ((m.y & 0xFu) << 8),
                           (m.y >> 4) & 0xFFFu};
@@ -322,31 +315,23 @@ __global__ void __launch_bounds__(THREADS, 4)
             ok = false;
           }
         }
+        const bool consec = all && sv[1] == sv[0] + 1 && sv[2] == sv[0] + 2 && sv[3] == sv[0] + 3;
         if (!ok) {
           bad = true;
         } else {
           dst[k] = d;
           full[k] = all;
+          run4[k] = consec && sizeof(Tin) == 1;
 #pragma unroll
           for (int i = 0; i < 4; ++i) src[k][i] = sv[i];
         }
       }
     }
   }
-  if (tid < MAX_SLOTS) {
-    int b = chunk_slot_bin[c * MAX_SLOTS + tid];
-    if (b >= n_bins) {
-      bad = true;
-      b = -1;
-    }
-    s_bin[tid] = b;
-  }
-  for (int i = tid; i < F * MAX_SLOTS; i += THREADS) (&s_sum[0][0])[i] = 0;
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
   uint32_t range_bad = 0;
   const int64_t total_bytes = T * npix * static_cast<int64_t>(sizeof(Tin));
   const uint8_t* fbytes = reinterpret_cast<const uint8_t*>(frames);
-  __syncthreads();
 
   auto issue = [&](int64_t t0, int buf) {
     for (int w = tid; w < F * C::WORDS; w += THREADS) {
@@ -380,48 +365,44 @@ __global__ void __launch_bounds__(THREADS, 4)
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       const int64_t t = t0 + f;
-      const bool live = t < T;
+      if (t >= T) break;
       const int delta = static_cast<int>(((t * npix + p0) * static_cast<int64_t>(sizeof(Tin))) & 15);
-      const uint8_t* sb = &s_buf[buf][f][delta];
+      const uint8_t* base = &s_buf[buf][f][0];
       uint8_t* row = packed + t * packed_cols;
 #pragma unroll
       for (int k = 0; k < WPT; ++k) {
+        if (dst[k] < 0) continue;
         uint32_t word = 0;
+        if (run4[k]) {
+          // 4 consecutive source bytes at byte offset o: two aligned words and a funnel shift
+          const uint32_t o = static_cast<uint32_t>(delta) + src[k][0];
+          const uint32_t* wp = reinterpret_cast<const uint32_t*>(base + (o & ~3u));
+          word = __funnelshift_r(wp[0], wp[1], 8 * (o & 3u));
+          // a byte > 16: ((b + 0x6F) | b) has bit 7 set (bytes are < 256, no carry between them)
+          range_bad |= ((word & 0x7F7F7F7Fu) + 0x6F6F6F6Fu | word) & 0x80808080u;
+        } else {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const bool has = src[k][i] != NO_SRC;
-          const uint32_t so = has ? src[k][i] : 0u;
-          uint32_t v = sizeof(Tin) == 1 ? static_cast<uint32_t>(sb[so])
-                                        : static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(sb + 2 * so));
-          v = has ? v : 0u;
-          range_bad |= v > 16u ? 1u : 0u;
-          word |= (v & 0xFFu) << (8 * i);
-        }
-        if (live && dst[k] >= 0) {
-          if (full[k]) {
-            *reinterpret_cast<uint32_t*>(row + dst[k]) = word;
-          } else {
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-              if (src[k][i] != NO_SRC) row[dst[k] + i] = static_cast<uint8_t>(word >> (8 * i));
+          for (int i = 0; i < 4; ++i) {
+            if (src[k][i] != NO_SRC) {
+              const uint32_t v = sizeof(Tin) == 1
+                                     ? static_cast<uint32_t>(base[delta + src[k][i]])
+                                     : static_cast<uint32_t>(
+                                           *reinterpret_cast<const uint16_t*>(base + delta + 2 * src[k][i]));
+              range_bad |= v > 16u ? 1u : 0u;
+              word |= (v & 0xFFu) << (8 * i);
+            }
           }
         }
-        const uint32_t bs = live ? __dp4a(word, 0x01010101u, 0u) : 0u;
-        const uint32_t vs = __reduce_add_sync(0xffffffffu, bs);  // the warp's words share one bin
-        if (lane == 0 && vs) atomicAdd(&s_sum[f][slot[k]], vs);
+        if (full[k]) {
+          *reinterpret_cast<uint32_t*>(row + dst[k]) = word;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (src[k][i] != NO_SRC) row[dst[k] + i] = static_cast<uint8_t>(word >> (8 * i));
+        }
       }
     }
-    __syncthreads();
-    for (int i = tid; i < F * MAX_SLOTS; i += THREADS) {
-      const int f = i / MAX_SLOTS, sl = i - f * MAX_SLOTS;
-      const uint32_t sv = s_sum[f][sl];
-      if (sv) {
-        const int b = s_bin[sl];
-        if (b >= 0 && t0 + f < T)
-          atomicAdd(&sums[static_cast<int64_t>(b) * T + t0 + f], static_cast<unsigned long long>(sv));
-        s_sum[f][sl] = 0;
-      }
-    }
+    // the buffer just read is refilled by the copies issued at the next step
     __syncthreads();
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -502,16 +483,13 @@ extern "C" int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_
 
 extern "C" int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
                             const int32_t* chunk_word_off_dev, const int32_t* word_dst_dev,
-                            const uint32_t* word_src_dev, const int32_t* chunk_slot_bin_dev, int64_t n_chunks,
-                            void* packed_dev, int64_t packed_cols, int64_t* sums_dev, int32_t n_bins,
+                            const uint32_t* word_src_dev, int64_t n_chunks, void* packed_dev, int64_t packed_cols,
                             int32_t* err_dev, void* stream) {
   using namespace g2;
-  if (!frames_dev || !chunk_word_off_dev || !word_dst_dev || !word_src_dev || !chunk_slot_bin_dev || !packed_dev ||
-      !sums_dev || !err_dev)
+  if (!frames_dev || !chunk_word_off_dev || !word_dst_dev || !word_src_dev || !packed_dev || !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || nframes <= 0 || npix <= 0 ||
-      n_chunks != (npix + G2_PACK_CHUNK - 1) / G2_PACK_CHUNK || packed_cols <= 0 || packed_cols % G2_PAD != 0 ||
-      n_bins <= 0)
+      n_chunks != (npix + G2_PACK_CHUNK - 1) / G2_PACK_CHUNK || packed_cols <= 0 || packed_cols % G2_PAD != 0)
     return G2_ERR_ARG;
   if (!aligned(packed_dev, 16) || !aligned(frames_dev, 16) || !aligned(word_src_dev, 8)) return G2_ERR_ARG;
   if (n_chunks == 0) return G2_OK;
@@ -527,15 +505,14 @@ extern "C" int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t 
   dim3 grid(static_cast<unsigned>(n_chunks), static_cast<unsigned>(gy));
   auto* ws = reinterpret_cast<const uint2*>(word_src_dev);
   auto* out = reinterpret_cast<uint8_t*>(packed_dev);
-  auto* sm = reinterpret_cast<unsigned long long*>(sums_dev);
   if (elem_bytes == 1)
     pack::pack_e4m3_kernel<uint8_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
-        reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, chunk_word_off_dev, word_dst_dev, ws,
-        chunk_slot_bin_dev, out, packed_cols, sm, n_bins, err_dev);
+        reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, chunk_word_off_dev, word_dst_dev, ws, out,
+        packed_cols, err_dev);
   else
     pack::pack_e4m3_kernel<uint16_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
-        reinterpret_cast<const uint16_t*>(frames_dev), nframes, npix, chunk_word_off_dev, word_dst_dev, ws,
-        chunk_slot_bin_dev, out, packed_cols, sm, n_bins, err_dev);
+        reinterpret_cast<const uint16_t*>(frames_dev), nframes, npix, chunk_word_off_dev, word_dst_dev, ws, out,
+        packed_cols, err_dev);
   return launch_status();
 }
 

@@ -32,7 +32,7 @@ struct JobsParam {
 __device__ __forceinline__ bool item_ok(const g2_gram_item& w, int n_jobs, int64_t numer_len) {
   return w.job >= 0 && w.job < n_jobs && w.k_len > 0 && (w.k_len % KT) == 0 && (w.a_k0 % KT) == 0 &&
          (w.b_k0 % KT) == 0 && w.nframes > 0 && w.shift >= 0 && w.shift <= 32 && w.out_off >= 0 &&
-         w.out_off + w.nframes <= numer_len;
+         w.out_off + w.nframes <= numer_len && w.s_off < 0;
 }
 
 // Load rows [r0, r0+128) x cols [k, k+32) of a packed matrix: 512 chunks of
@@ -177,7 +177,7 @@ extern "C" int g2_plain_direct(const g2_job* jobs, int32_t n_jobs, const g2_gram
   for (int j = 0; j < n_jobs; ++j) {
     const g2_job& jb = jobs[j];
     if (!jb.packed_dev || !aligned(jb.packed_dev, 16) || jb.nframes <= 0 || jb.nframes >= (1ll << 31) ||
-        jb.packed_cols <= 0 || jb.packed_cols % G2_PAD != 0 || jb.elem_kind != G2_KIND_FP16)
+        jb.packed_cols <= 0 || jb.packed_cols % G2_PAD != 0 || jb.elem_kind != G2_KIND_FP16 || jb.ones_row != 0)
       return G2_ERR_ARG;
     jp.packed[j] = reinterpret_cast<const uint16_t*>(jb.packed_dev);
     jp.cols[j] = jb.packed_cols;

@@ -179,17 +179,27 @@ class DenseEngine:
             self._layouts[mode] = L
         return self._layouts[mode]
 
-    def _packed_buffer(self, nbytes, mode):
-        """The packed operand buffer; zeroed whenever its layout changes, since
-        the pack kernel writes only the binned columns (padding stays 0)."""
+    def _packed_buffer(self, L):
+        """The packed operand buffer, [T (+1)][packed_cols]; zeroed whenever its
+        layout changes, since the pack kernels write only the binned columns
+        (padding stays 0).  e4m3 layouts get the row of ones after the frames."""
         torch = _torch()
+        rows = self.T + (1 if L.ones_row else 0)
+        nbytes = rows * L.packed_bytes_per_frame
+        fresh = False
         if self.packed is None or self.packed.numel() < nbytes:
             self.packed = None
             self.packed = torch.zeros(nbytes, dtype=torch.uint8, device=self.dev)
-            self._packed_mode = mode
-        elif self._packed_mode != mode:
+            fresh = True
+        elif self._packed_mode != L.mode:
             self.packed.zero_()
-            self._packed_mode = mode
+            fresh = True
+        if fresh:
+            self._packed_mode = L.mode
+            if L.ones_row:
+                row = torch.from_numpy(L.ones_row_values().view(np.uint8)).to(self.dev)
+                off = self.T * L.packed_bytes_per_frame
+                self.packed[off:off + row.numel()].copy_(row)
         return self.packed
 
     # -- stages ----------------------------------------------------------
@@ -213,7 +223,7 @@ class DenseEngine:
 
     def pack(self, frames_dev, mode):
         L = self._layout(mode)
-        packed = self._packed_buffer(self.T * L.packed_bytes_per_frame, mode)
+        packed = self._packed_buffer(L)
         self.sums.zero_()
         L.d_piece_emax.zero_()
         self.err.zero_()
@@ -221,8 +231,8 @@ class DenseEngine:
         if mode == MODE_E4M3:
             _lib.check(self.lib.g2_pack_e4m3(
                 ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_word_off),
-                ptr(L.d_word_dst), ptr(L.d_word_src), ptr(L.d_chunk_slot_bin), L.n_chunks, ptr(packed),
-                L.packed_cols, ptr(self.sums), self.n_bins, ptr(self.err), st), "g2_pack_e4m3")
+                ptr(L.d_word_dst), ptr(L.d_word_src), L.n_chunks, ptr(packed), L.packed_cols, ptr(self.err), st),
+                "g2_pack_e4m3")
             return L
         _lib.check(self.lib.g2_pack_frames(
             ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_entry_off),
@@ -235,7 +245,8 @@ class DenseEngine:
         key = (L.mode, self.method, tuple(grams))
         if key not in self._items_cache:
             torch = _torch()
-            items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method)
+            items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method,
+                               s_base=0 if (L.ones_row and self.method == "tc") else None)
             dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
             if len(self._items_cache) > 8:
                 self._items_cache.clear()
@@ -244,11 +255,12 @@ class DenseEngine:
 
     def numerator(self, L, items_dev, n_items):
         self.numer.zero_()
-        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind)])
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, L.ones_row)])
         st = stream_handle(self.dev)
         if self.method == "tc":
             _lib.check(self.lib.g2_gram_tc(jobs, 1, ptr(items_dev), n_items, ptr(self.numer), self.numer.numel(),
-                                           ptr(self.err), self.grid, st), "g2_gram_tc")
+                                           ptr(self.sums), self.sums.numel(), ptr(self.err), self.grid, st),
+                       "g2_gram_tc")
         else:
             _lib.check(self.lib.g2_plain_direct(jobs, 1, ptr(items_dev), n_items, ptr(self.numer),
                                                 self.numer.numel(), ptr(self.err), st), "g2_plain_direct")

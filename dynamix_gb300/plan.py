@@ -136,29 +136,14 @@ class PackLayout:
             wslot = np.zeros(uw.size, dtype=np.int64)
             wslot[widx] = slot
             wchunk = uw // nq
-            wdst = (uw % nq) * 4
-            # slot-uniform warp tiles: the words of one (chunk, slot) run are
-            # padded to a multiple of 32 with empty words (no sources, dst -1),
-            # so every warp of the kernel reduces one bin
-            run = wchunk * PACK_MAX_SLOTS + wslot
-            urun, run_start, run_len = np.unique(run, return_index=True, return_counts=True)
-            padded = (run_len + 31) // 32 * 32
-            out_start = np.concatenate([[0], np.cumsum(padded)])[:-1]
-            pos = np.repeat(out_start - run_start, run_len) + np.arange(uw.size)
-            total = int(padded.sum())
-            self.word_dst = np.full(total, -1, dtype=np.int32)
-            self.word_dst[pos] = wdst
-            ws = np.empty((total, 2), dtype=np.uint32)
-            ws[:, 0] = 0xFFF | (0xFFF << 12) | (0xFF << 24)
-            empty_slot = np.repeat(urun % PACK_MAX_SLOTS, padded)
-            ws[:, 1] = (0xF | (0xFFF << 4) | (empty_slot << 16)).astype(np.uint32)
-            ws[pos, 0] = (srcs[:, 0] | (srcs[:, 1] << 12) | ((srcs[:, 2] & 0xFF) << 24)).astype(np.uint32)
-            ws[pos, 1] = ((srcs[:, 2] >> 8) | (srcs[:, 3] << 4) | (wslot << 16)).astype(np.uint32)
-            self.word_src = ws
-            pchunk = np.repeat(urun // PACK_MAX_SLOTS, padded)
-            self.chunk_word_off = np.searchsorted(pchunk, np.arange(self.n_chunks + 1)).astype(np.int32)
-            if total and np.diff(self.chunk_word_off).max() > PACK_WORDS_PER_CHUNK:
+            self.chunk_word_off = np.searchsorted(wchunk, np.arange(self.n_chunks + 1)).astype(np.int32)
+            if uw.size and np.diff(self.chunk_word_off).max() > PACK_WORDS_PER_CHUNK:
                 raise ValueError("more than %d packed words in one chunk" % PACK_WORDS_PER_CHUNK)
+            self.word_dst = ((uw % nq) * 4).astype(np.int32)
+            ws = np.empty((uw.size, 2), dtype=np.uint32)
+            ws[:, 0] = (srcs[:, 0] | (srcs[:, 1] << 12) | ((srcs[:, 2] & 0xFF) << 24)).astype(np.uint32)
+            ws[:, 1] = ((srcs[:, 2] >> 8) | (srcs[:, 3] << 4) | (wslot << 16)).astype(np.uint32)
+            self.word_src = ws
 
     def segment_emax(self, piece_emax):
         """Per 64-column output segment, the sum over its pieces of the pieces'
@@ -174,6 +159,19 @@ class PackLayout:
     @property
     def packed_bytes_per_frame(self):
         return self.packed_cols * self.elem_bytes
+
+    @property
+    def ones_row(self):
+        """e4m3 jobs carry a row of ones after the last frame: the Gram turns
+        it into the bin sums (G(t, ones) = S(t))."""
+        return self.mode == MODE_E4M3
+
+    def ones_row_values(self):
+        """Row of ones: 1 in every binned column, 0 in the bin padding."""
+        row = np.zeros(self.packed_cols, dtype=np.uint8 if self.elem_bytes == 1 else np.uint16)
+        for b in range(self.n_bins):
+            row[self.plane0[b]:self.plane0[b] + self.npix[b]] = 1
+        return row
 
     def grams(self):
         """The Grams to run per bin: (bin, a_plane_off, b_plane_off, kpad, shift)."""
@@ -228,15 +226,16 @@ def k_chunks(emax_a, emax_b, limit=EXACT_LIMIT):
 _TILE_CACHE = {}
 
 
-def _tiles(T, bm, bn, super_rows=SUPER_ROWS):
-    """(i0, j0) of every bm x bn block holding some t' >= t (t, t' < T).
+def _tiles(T, bm, bn, super_rows=SUPER_ROWS, extra_col=False):
+    """(i0, j0) of every bm x bn block holding some t' >= t (t, t' < T); with
+    ``extra_col`` the columns run to T inclusive (the row of ones).
 
     Ordered by square super-tiles of ``super_rows`` frames per side (upper
     triangle, row-major), then row-major inside a super-tile."""
-    key = (T, bm, bn, super_rows)
+    key = (T, bm, bn, super_rows, extra_col)
     if key not in _TILE_CACHE:
         ni = -(-T // bm)
-        nj = -(-T // bn)
+        nj = -(-(T + (1 if extra_col else 0)) // bn)
         ii, jj = np.meshgrid(np.arange(ni), np.arange(nj), indexing="ij")
         i0 = (ii * bm).ravel()
         j0 = (jj * bn).ravel()
@@ -247,17 +246,20 @@ def _tiles(T, bm, bn, super_rows=SUPER_ROWS):
     return _TILE_CACHE[key]
 
 
-def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc"):
+def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc", s_base=None):
     """Build the item list of one job.
 
     ``chunked_grams``: iterable of ``(bin, a_off, b_off, k0, k_len, shift)`` with
     columns relative to the job's packed matrix.  ``kind`` selects the block
     shape (tensor-core 128x256 or plain 128x128).  Items are sorted by k_len
     (descending, stable) so that the persistent kernel's static round-robin
-    schedule starts with the longest items.
+    schedule starts with the longest items.  ``s_base`` (tensor-core items of a
+    job whose packed matrix carries the row of ones): element offset of the
+    job's bin sums; the blocks then also cover that row and add S_b(t) at
+    ``s_base + b * T + t``.
     """
     bm, bn = (TC_BM, TC_BN) if kind == "tc" else (PLAIN_BM, PLAIN_BN)
-    i0, j0 = _tiles(int(T), bm, bn)
+    i0, j0 = _tiles(int(T), bm, bn, extra_col=s_base is not None)
     parts = []
     for (b, a_off, b_off, k0, klen, shift) in chunked_grams:
         it = np.empty(i0.size, dtype=ITEM_DTYPE)
@@ -270,6 +272,7 @@ def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc"):
         it["shift"] = shift
         it["nframes"] = T
         it["out_off"] = out_base + b * T
+        it["s_off"] = -1 if s_base is None else s_base + b * T
         parts.append(it)
     if not parts:
         return np.empty(0, dtype=ITEM_DTYPE)

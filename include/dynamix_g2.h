@@ -50,7 +50,7 @@ extern "C" {
 #define G2_PACK_CHUNK 2048 /* source pixels per pack chunk */
 #define G2_PACK_MAX_SLOTS  32   /* distinct bins per chunk */
 #define G2_PACK_MAX_PIECES 512  /* (64-column segment x chunk) pieces per chunk */
-#define G2_PACK_WORDS_PER_CHUNK 1024 /* 4-column words per chunk (g2_pack_e4m3) */
+#define G2_PACK_WORDS_PER_CHUNK 512 /* 4-column words per chunk (g2_pack_e4m3) */
 #define G2_MAX_JOBS   32
 
 /* element kinds of a packed operand matrix */
@@ -60,7 +60,11 @@ extern "C" {
 /* One unit of Gram work: rows [i0, i0+BM) of the A operand against rows
  * [j0, j0+BN) of the B operand over packed columns [a_k0, a_k0+k_len) and
  * [b_k0, b_k0+k_len).  The lag-diagonal sums of the t' >= t part are added,
- * multiplied by 2^shift, to numer[out_off + tau] for 0 <= tau < nframes. */
+ * multiplied by 2^shift, to numer[out_off + tau] for 0 <= tau < nframes; rows
+ * and columns >= nframes never enter them.  When the job's packed matrix has a
+ * row of ones at row nframes (g2_job.ones_row) and s_off >= 0, the column of
+ * that row holds the bin sums: G(t, nframes) = sum_k A(t, k) = S(t), added to
+ * sums[s_off + t] for t < nframes. */
 typedef struct g2_gram_item {
     int32_t job;       /* index into the jobs array of the launch */
     int32_t i0;        /* first frame of the A rows */
@@ -71,6 +75,7 @@ typedef struct g2_gram_item {
     int32_t shift;     /* weight 2^shift (0, 8 or 16 for byte-split planes) */
     int32_t nframes;   /* T of the job */
     int64_t out_off;   /* element offset of N_b(0) in numer */
+    int64_t s_off;     /* element offset of S_b(0) in sums, or -1 */
 } g2_gram_item;
 
 /* A dense job: its packed operand matrix, row-major [nframes][packed_cols]
@@ -82,7 +87,8 @@ typedef struct g2_job {
     int64_t nframes;
     int64_t packed_cols;   /* multiple of G2_PAD */
     int32_t elem_kind;     /* G2_KIND_FP16 or G2_KIND_E4M3 */
-    int32_t reserved;
+    int32_t ones_row;      /* 1: row nframes of the packed matrix holds 1 in every
+                              binned column and 0 in the padding (bin sums) */
 } g2_job;
 
 /* ---- host utilities ---------------------------------------------------- */
@@ -133,14 +139,14 @@ int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, 
  * G2_PACK_WORDS_PER_CHUNK; word w covers packed columns word_dst[w] ..
  * word_dst[w]+3 of one bin, word_src[2w], word_src[2w+1] hold the 4 chunk-local
  * source offsets (12 bits each, 0xFFF = column owned by another chunk) and the
- * bin slot (bits 16-20 of word_src[2w+1]); word_dst[w] = -1 marks an empty
- * word.  Every aligned group of 32 words of a chunk must belong to one bin
- * slot (the bin sums are reduced per warp).  Adds S_b(t) into sums_dev; a
- * count above 16 sets G2_DEVERR_RANGE.  Same role as g2_pack_frames mode 2. */
+ * bin slot (bits 16-20 of word_src[2w+1], unused here).  Bit 0 of
+ * word_src[2w+1] >> 21 set means the 4 sources are consecutive pixels.  A
+ * count above 16 sets G2_DEVERR_RANGE.  The bin sums are not computed here:
+ * g2_gram_tc takes them from the row of ones (g2_job.ones_row).  Same packed
+ * result as g2_pack_frames mode 2. */
 int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
                  const int32_t* chunk_word_off_dev, const int32_t* word_dst_dev,
-                 const uint32_t* word_src_dev, const int32_t* chunk_slot_bin_dev, int64_t n_chunks,
-                 void* packed_dev, int64_t packed_cols, int64_t* sums_dev, int32_t n_bins,
+                 const uint32_t* word_src_dev, int64_t n_chunks, void* packed_dev, int64_t packed_cols,
                  int32_t* err_dev, void* stream);
 
 /* Largest count over the binned pixels (col_src >= 0): picks split 0/1.
@@ -160,7 +166,8 @@ int g2_binned_max(const void* frames_dev, int32_t elem_bytes, int64_t nframes, i
  * items_dev: n_items g2_gram_item (BM=128, BN=256).  grid <= 0: one CTA per SM.
  */
 int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
-               uint64_t* numer_dev, int64_t numer_len, int32_t* err_dev, int32_t grid, void* stream);
+               uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
+               int32_t* err_dev, int32_t grid, void* stream);
 
 /* ---- G5: plain direct kernel (CUDA cores, integer) ----------------------
  * The same-GPU non-tensor-core comparator: the direct integer numerator of

@@ -42,7 +42,7 @@ def test_argument_errors_are_caught_on_host(built_lib):
     # null pointers / bad sizes are rejected before any CUDA call
     assert built_lib.g2_denominator(None, 1, 10, None, None) == 1
     assert built_lib.g2_finalize(None, None, None, 1, 10, None, None, None) == 1
-    assert built_lib.g2_gram_tc(None, 0, None, 0, None, 0, None, 0, None) == 1
+    assert built_lib.g2_gram_tc(None, 0, None, 0, None, 0, None, 0, None, 0, None) == 1
     assert built_lib.g2_pack_frames(None, 1, 1, 1, None, None, None, None, None, None, 1, 0, None, 128, None, 1,
                                     None, 0, None, None) == 1
     assert built_lib.g2_normalize_static(None, None, None, 1, 10, None, None, None) == 1
@@ -50,8 +50,8 @@ def test_argument_errors_are_caught_on_host(built_lib):
 
 def test_item_layout_matches_c_struct():
     from dynamix_gb300 import _lib
-    assert _lib.ITEM_DTYPE.itemsize == 40
+    assert _lib.ITEM_DTYPE.itemsize == 48
     assert ctypes.sizeof(_lib.Job) == 32
     assert list(_lib.ITEM_DTYPE.names) == ["job", "i0", "j0", "a_k0", "b_k0", "k_len", "shift", "nframes",
-                                           "out_off"]
+                                           "out_off", "s_off"]
     assert np.dtype(_lib.ITEM_DTYPE).fields["out_off"][1] == 32

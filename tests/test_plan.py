@@ -59,18 +59,29 @@ def emulate_pack(frames, L):
     return packed, emax
 
 
-def run_items(packed, items, n_rows, T, bm, bn):
+def run_items(packed, items, n_rows, T, bm, bn, ones=None):
+    """What the Gram kernels add for each item: lag sums over t <= t' < T and,
+    when the packed matrix carries the row of ones (``ones``), the bin sums
+    from that row's column.  Returns N (and S when ``ones`` is given)."""
     N = np.zeros(n_rows * T, dtype=np.int64)
-    P = np.concatenate([packed, np.zeros((bn, packed.shape[1]), dtype=np.int64)])
+    S = np.zeros(n_rows * T, dtype=np.int64)
+    rows = [packed] + ([ones[None, :].astype(np.int64)] if ones is not None else [])
+    P = np.concatenate(rows + [np.zeros((bn + bm, packed.shape[1]), dtype=np.int64)])
     for it in items:
         i0, j0, a0, b0, kl = int(it["i0"]), int(it["j0"]), int(it["a_k0"]), int(it["b_k0"]), int(it["k_len"])
         G = P[i0:i0 + bm, a0:a0 + kl] @ P[j0:j0 + bn, b0:b0 + kl].T
         assert G.max(initial=0) <= plan.EXACT_LIMIT
         r, c = np.meshgrid(np.arange(bm), np.arange(bn), indexing="ij")
-        tau = (j0 + c) - (i0 + r)
-        ok = (tau >= 0) & (tau < T)
+        t, tp = i0 + r, j0 + c
+        tau = tp - t
+        ok = (tau >= 0) & (t < T) & (tp < T)
         np.add.at(N, int(it["out_off"]) + tau[ok], G[ok] << int(it["shift"]))
-    return N.reshape(n_rows, T)
+        if it["s_off"] >= 0:
+            sel = (tp == T) & (t < T)
+            np.add.at(S, int(it["s_off"]) + t[sel], G[sel])
+    if ones is None:
+        return N.reshape(n_rows, T)
+    return N.reshape(n_rows, T), S.reshape(n_rows, T)
 
 
 @pytest.mark.parametrize("mode", [0, 1, 2])
@@ -87,11 +98,18 @@ def test_item_semantics_reproduce_oracle(name, kind, mode):
     if mode == 2 and fr.max() > plan.E4M3_MAX_EXACT:
         pytest.skip("counts do not fit e4m3")
     packed, emax = emulate_pack(fr, L)
+    if mode == plan.MODE_E4M3:
+        emax = plan.e4m3_segment_bound(L)
     grams = plan.chunk_grams(L, emax)
-    items = plan.gram_items(T, grams, kind=kind)
     bm, bn = (TC_BM, TC_BN) if kind == "tc" else (PLAIN_BM, PLAIN_BN)
-    N = run_items(packed, items, nb, T, bm, bn)
     ref = o.g2_exact(fr, qm)
+    if L.ones_row and kind == "tc":
+        items = plan.gram_items(T, grams, kind=kind, s_base=0)
+        N, S = run_items(packed, items, nb, T, bm, bn, ones=L.ones_row_values())
+        assert np.array_equal(S, ref["sums"])
+    else:
+        items = plan.gram_items(T, grams, kind=kind)
+        N = run_items(packed, items, nb, T, bm, bn)
     assert np.array_equal(N, ref["numerator"])
 
 
@@ -175,12 +193,7 @@ def test_e4m3_word_tables_decode_to_entries():
     y = L.word_src[:, 1].astype(np.int64)
     srcs = np.stack([x & 0xFFF, (x >> 12) & 0xFFF, (x >> 24) | ((y & 0xF) << 8), (y >> 4) & 0xFFF], axis=1)
     live = L.word_dst >= 0
-    assert np.all(L.word_dst[live] % 4 == 0)
-    assert np.all(srcs[~live] == 0xFFF)
-    # every aligned group of 32 words of a chunk names one bin slot
-    assert np.all(np.diff(L.chunk_word_off) % 32 == 0)
-    wslot = (y >> 16) & 31
-    assert np.all(wslot.reshape(-1, 32) == wslot.reshape(-1, 32)[:, :1])
+    assert live.all() and np.all(L.word_dst % 4 == 0)
     for w in np.flatnonzero(live):
         for i in range(4):
             if srcs[w, i] != 0xFFF:
