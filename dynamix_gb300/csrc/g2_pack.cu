@@ -38,6 +38,7 @@ struct Cfg {
   static constexpr int CHUNK_BYTES = CH * static_cast<int>(sizeof(Tin));
   static constexpr int BUF = CHUNK_BYTES + 16;
   static constexpr int WORDS = CHUNK_BYTES / 16 + 1;  // 16-byte words covering one unaligned chunk
+  static_assert(BUF % 16 == 0, "staging rows must keep 16-byte cp.async destinations aligned");
 };
 
 template <typename Tin, int MODE>
@@ -280,7 +281,9 @@ __global__ void __launch_bounds__(THREADS, 4)
                      int32_t* __restrict__ err) {
   using C = Cfg<Tin>;
   constexpr int F = C::F;
-  __shared__ __align__(16) uint8_t s_buf[2][F][C::BUF + 4];
+  // rows stay multiples of 16 bytes (cp.async destinations); the 16 spare bytes
+  // cover the second word of the funnel-shift read at the end of a chunk
+  __shared__ __align__(16) uint8_t s_buf[2][F][C::BUF + 16];
 
   const int tid = threadIdx.x;
   const int64_t c = blockIdx.x;
