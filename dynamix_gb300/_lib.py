@@ -22,7 +22,7 @@ DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE = 1, 2, 4
 
 BK = 64          # source segment width (pixels)
 PAD = 128        # packed bins and packed_cols are multiples of this
-PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 32, 512, 512
+PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 32, 512, 768
 TC_BM, TC_BN = 128, 256
 PLAIN_BM, PLAIN_BN = 128, 128
 MAX_JOBS = 32

@@ -50,7 +50,7 @@ extern "C" {
 #define G2_PACK_CHUNK 2048 /* source pixels per pack chunk */
 #define G2_PACK_MAX_SLOTS  32   /* distinct bins per chunk */
 #define G2_PACK_MAX_PIECES 512  /* (64-column segment x chunk) pieces per chunk */
-#define G2_PACK_WORDS_PER_CHUNK 512 /* 4-column words per chunk (g2_pack_e4m3) */
+#define G2_PACK_WORDS_PER_CHUNK 768 /* 4-column words per chunk: 2048/4 + partial words at bin edges */
 #define G2_MAX_JOBS   32
 
 /* element kinds of a packed operand matrix */
