@@ -273,7 +273,7 @@ def run_ours(args):
         peak, peak_src = 2.0 * bf16, "%s bf16_tflops x 2 (dense e4m3 rate, derived)" % peak_kind
     else:
         peak, peak_src = bf16, "%s bf16_tflops (dense f16 rate)" % peak_kind
-    pack_bytes = T * H * W + T * info["packed_cols"] * 2
+    pack_bytes = T * H * W + T * info["packed_cols"] * (1 if info.get("mode") == "e4m3" else 2)
     pack_avg = sum(pack_ms) / len(pack_ms)
     traffic = profile_traffic("gram_tc_dense_514x1030_%s.md" % info.get("mode"))
 
