@@ -340,3 +340,139 @@ class DenseEngine:
         S = self.sums[: self.n_bins].cpu().numpy()
         if S.size and float(S.max()) ** 2 * self.T >= 2.0 ** 63:
             raise OverflowError("denominator exceeds int64 for these counts")
+
+
+def _events_to_device(vol_times, vol_data, offsets, npix, dev):
+    """Validate the event arrays (layout of dynamix's FramesCompressor) and
+    move them to the device: times int32, counts uint8/uint16, offsets uint32."""
+    torch = _torch()
+
+    def host(a):
+        return a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+
+    offs = host(offsets)
+    if offs.ndim != 1 or offs.size != npix + 1:
+        raise ValueError("offsets should have size %d, got %s" % (npix + 1, offs.shape))
+    offs64 = offs.astype(np.int64)
+    if offs64[0] != 0 or np.any(np.diff(offs64) < 0):
+        raise ValueError("offsets must start at 0 and be non-decreasing")
+    n_ev = int(offs64[-1])
+    if n_ev >= 2 ** 32:
+        raise ValueError("too many events for uint32 offsets")
+    t = vol_times if isinstance(vol_times, torch.Tensor) else np.asarray(vol_times)
+    d = vol_data if isinstance(vol_data, torch.Tensor) else np.asarray(vol_data)
+    if t.ndim != 1 or d.ndim != 1 or t.shape[0] != d.shape[0]:
+        raise ValueError("vol_times and vol_data must be 1-D arrays of the same size")
+    if t.shape[0] < n_ev:
+        raise ValueError("offsets reference %d events but only %d are given" % (n_ev, t.shape[0]))
+
+    def to_dev_int(a, dtype_np, dtype_t):
+        if isinstance(a, torch.Tensor):
+            return a[:n_ev].to(dev).to(dtype_t).contiguous()
+        return torch.from_numpy(np.ascontiguousarray(a[:n_ev]).astype(dtype_np, copy=False)).to(dev)
+
+    d_np_kind = d.dtype.kind if not isinstance(d, torch.Tensor) else ("u" if d.dtype in (torch.uint8,) else "i")
+    times_d = to_dev_int(t, np.int32, torch.int32)
+    if isinstance(d, torch.Tensor):
+        dd = d[:n_ev].to(dev)
+    else:
+        dd = torch.from_numpy(np.ascontiguousarray(d[:n_ev]))
+        dd = dd.to(dev)
+    if dd.dtype.is_floating_point:
+        if n_ev and not bool(torch.all(dd == torch.round(dd))):
+            raise TypeError("event counts must be integers")
+    mx = int(dd.max().item()) if n_ev else 0
+    mn = int(dd.min().item()) if n_ev else 0
+    if mn < 0:
+        raise ValueError("counts must be non-negative")
+    if mx > 65535:
+        raise ValueError("counts above 65535 are not supported")
+    data_d = dd.to(torch.uint8) if mx <= 255 else dd.to(torch.int32).to(torch.uint16)
+    if n_ev:
+        tmin, tmax = int(times_d.min().item()), int(times_d.max().item())
+    else:
+        tmin = tmax = 0
+    offs_d = torch.from_numpy(offs64.astype(np.uint32).view(np.int32)).to(dev)
+    del d_np_kind
+    return times_d, data_d.contiguous(), offs_d, offs64, mx, (tmin, tmax)
+
+
+class EventEngine:
+    """Exact g2 from per-pixel event lists (G6 pair sums, then G3, G4)."""
+
+    def __init__(self, shape, nframes, qmask, n_bins, scale, device=None, ranges_per_sm=4):
+        torch = _torch()
+        self.lib = _lib.load()
+        self.dev = require_cuda(device)
+        self.shape = tuple(int(s) for s in shape)
+        self.npix = self.shape[0] * self.shape[1]
+        self.T = int(nframes)
+        if self.T >= 2 ** 31:
+            raise ValueError("too many frames")
+        self.n_bins = int(n_bins)
+        q = np.ascontiguousarray(qmask, dtype=np.int32).ravel()
+        self.qflat = np.where(q >= 1, q, 0)
+        order = np.argsort(self.qflat, kind="stable")
+        counts = np.bincount(self.qflat, minlength=self.n_bins + 1)[: self.n_bins + 1]
+        starts = np.concatenate([[0], np.cumsum(counts)])
+        self.binned = order[starts[1]:]                         # binned pixels, bin by bin
+        self.binned_bin = self.qflat[self.binned] - 1
+        self.ranges_per_sm = int(ranges_per_sm)
+        self.scale = torch.as_tensor(np.asarray(scale, dtype=np.float64), device=self.dev)
+        rows = max(self.n_bins, 1)
+        z = lambda dt: torch.zeros((rows, self.T), dtype=dt, device=self.dev)
+        self.sums, self.numer, self.denom = z(torch.int64), z(torch.int64), z(torch.int64)
+        self.g2_f32, self.g2_f64 = z(torch.float32), z(torch.float64)
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.last = {}
+
+    def plan_ranges(self, offs64):
+        """Cut the binned pixels with events into ranges of one bin each, of
+        about equal pair counts (the work of a CTA)."""
+        n = np.diff(offs64)[self.binned]
+        keep = n > 0
+        pix = self.binned[keep]
+        pb = self.binned_bin[keep]
+        pairs = n[keep] * (n[keep] + 1) // 2
+        total = int(pairs.sum())
+        sms = _torch().cuda.get_device_properties(self.dev).multi_processor_count
+        target = max(1, total // max(1, sms * self.ranges_per_sm))
+        cum = np.cumsum(pairs)
+        # range id = (bin, cumulative pairs // target), cut at bin changes
+        key = pb.astype(np.int64) * (total // target + 2) + (cum - pairs) // target
+        starts = np.flatnonzero(np.concatenate([[True], key[1:] != key[:-1]])) if pix.size else np.zeros(0, np.int64)
+        range_off = np.concatenate([starts, [pix.size]]).astype(np.int32)
+        range_bin = pb[starts].astype(np.int32) if pix.size else np.zeros(0, np.int32)
+        return pix.astype(np.int32), range_off, range_bin, total
+
+    def run(self, vol_times, vol_data, offsets):
+        torch = _torch()
+        times_d, data_d, offs_d, offs64, mx, (tmin, tmax) = _events_to_device(vol_times, vol_data, offsets,
+                                                                           self.npix, self.dev)
+        if offs64[-1] and (tmin < 0 or tmax >= self.T):
+            raise ValueError("event times must lie in [0, nframes)")
+        pix, range_off, range_bin, total = self.plan_ranges(offs64)
+        self.numer.zero_()
+        self.sums.zero_()
+        self.err.zero_()
+        st = stream_handle(self.dev)
+        if range_bin.size and self.n_bins:
+            d = lambda a: torch.from_numpy(a).to(self.dev)
+            pix_d, ro_d, rb_d = d(pix), d(range_off), d(range_bin)
+            _lib.check(self.lib.g2_event_pairsum(
+                ptr(times_d), ptr(data_d), data_d.element_size(), int(offs64[-1]), ptr(offs_d), self.npix,
+                ptr(pix_d), ptr(ro_d), ptr(rb_d), int(range_bin.size), self.T, self.n_bins, mx, ptr(self.numer),
+                ptr(self.sums), ptr(self.err), st), "g2_event_pairsum")
+        if self.n_bins:
+            _lib.check(self.lib.g2_denominator(ptr(self.sums), self.n_bins, self.T, ptr(self.denom), st),
+                       "g2_denominator")
+            _lib.check(self.lib.g2_finalize(ptr(self.numer), ptr(self.denom), ptr(self.scale), self.n_bins,
+                                            self.T, ptr(self.g2_f32), ptr(self.g2_f64), st), "g2_finalize")
+        self.last = {"n_events": int(offs64[-1]), "pairs": total, "n_ranges": int(range_bin.size),
+                     "max_count": mx}
+        return self.g2_f32[: self.n_bins]
+
+    def check_error(self):
+        code = int(self.err.item())
+        if code:
+            raise DeviceError(_lib.device_error_message(code))

@@ -1,0 +1,90 @@
+"""GPU parity of the event-list correlator against the CPU oracle."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import g2_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+def check(c, ref, g):
+    assert np.array_equal(c.sums, ref["sums"])
+    assert np.array_equal(c.numerator, ref["numerator"])
+    assert np.array_equal(c.denominator, ref["denominator"])
+    assert np.array_equal(g, ref["g2"].astype(np.float32), equal_nan=True)
+
+
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_cfg1_u8", "dense_u16"])
+def test_reference_event_layout(built_lib, cuda_device, name):
+    from dynamix_gb300.correlator import EventCorrelator
+    z = golden(name)
+    fr, qm = z["frames"], z["qmask"]
+    T = fr.shape[0]
+    ref = o.g2_exact(fr, qm)
+    c = EventCorrelator(fr.shape[1:], T, max_events_count=int(np.diff(z["ev_offsets"]).max()), qmask=qm)
+    g = c.correlate(z["ev_times"], z["ev_data"], z["ev_offsets"])
+    check(c, ref, g)
+    # the reference's own float32 g2 agrees to float32 rounding
+    rg = z["g2_ref"]
+    ok = np.isfinite(rg)
+    assert np.all(np.abs(g[ok] - rg[ok]) <= 2e-6 * np.abs(rg[ok]))
+
+
+def test_shuffled_events_and_scale_factor(built_lib, cuda_device):
+    from dynamix_gb300.correlator import EventCorrelator
+    z = golden("dense_small_u8")
+    fr, qm = z["frames"], z["qmask"]
+    T = fr.shape[0]
+    d, t, off = z["ev_data"].copy(), z["ev_times"].copy(), z["ev_offsets"]
+    rng = np.random.default_rng(0)
+    for p in range(off.size - 1):                       # order inside a pixel does not matter
+        s, e = off[p], off[p + 1]
+        perm = rng.permutation(e - s) + s
+        d[s:e], t[s:e] = d[perm], t[perm]
+    nb = int(qm.max())
+    sf = np.linspace(10, 50, nb)
+    c = EventCorrelator(fr.shape[1:], T, 64, qmask=qm, scale_factor=list(sf))
+    g = c.correlate(t, d.astype(np.int32), off.astype(np.int64))
+    ref = o.g2_exact(fr, qm, scale_factor=list(sf))
+    check(c, ref, g)
+
+
+def test_qmask_none_and_long_stack_global_path(built_lib, cuda_device):
+    """T above the shared-memory capacity uses the global-atomic kernel."""
+    from dynamix_gb300.correlator import EventCorrelator, FramesCompressor
+    rng = np.random.default_rng(3)
+    T, shape = 30000, (3, 4)
+    fr = (rng.random((T,) + shape) < 0.01).astype(np.uint8) * rng.integers(1, 4, (T,) + shape).astype(np.uint8)
+    d, t, off = FramesCompressor.compress_all_stack(fr)
+    c = EventCorrelator(shape, T, int(np.diff(off).max()))
+    g = c.correlate(t, d, off)
+    ref = o.event_correlate_exact(t, d, off, None, shape, T)
+    check(c, ref, g)
+
+
+def test_large_counts_use_global_path(built_lib, cuda_device):
+    from dynamix_gb300.correlator import EventCorrelator, FramesCompressor
+    rng = np.random.default_rng(4)
+    T, shape = 300, (6, 5)
+    fr = np.where(rng.random((T,) + shape) < 0.05, rng.integers(40000, 65535, (T,) + shape), 0).astype(np.uint16)
+    qm = np.ones(shape, np.int32)
+    qm[:, 3:] = 2
+    d, t, off = FramesCompressor.compress_all_stack(fr)
+    c = EventCorrelator(shape, T, 64, qmask=qm)
+    g = c.correlate(t, d, off)
+    check(c, o.g2_exact(fr, qm), g)
+
+
+def test_event_errors(built_lib, cuda_device):
+    from dynamix_gb300.correlator import EventCorrelator
+    z = golden("dense_small_u8")
+    fr = z["frames"]
+    c = EventCorrelator(fr.shape[1:], fr.shape[0], 4, total_events_count=10, allow_reallocate=False)
+    with pytest.raises(ValueError):
+        c.correlate(z["ev_times"], z["ev_data"], z["ev_offsets"])
+    c = EventCorrelator(fr.shape[1:], fr.shape[0] - 10, 4)
+    with pytest.raises(ValueError):                     # times beyond nframes
+        c.correlate(z["ev_times"], z["ev_data"], z["ev_offsets"])
+    with pytest.raises(AssertionError):
+        c.correlate(z["ev_times"], z["ev_data"], z["ev_offsets"][:-1])
