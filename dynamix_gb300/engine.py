@@ -344,57 +344,57 @@ class DenseEngine:
 
 def _events_to_device(vol_times, vol_data, offsets, npix, dev):
     """Validate the event arrays (layout of dynamix's FramesCompressor) and
-    move them to the device: times int32, counts uint8/uint16, offsets uint32."""
+    move them to the device: times int32, counts uint8/uint16, offsets uint32.
+    Returns (times, counts, offsets, host offsets int64, max count, (min t, max t))."""
     torch = _torch()
 
     def host(a):
         return a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
 
-    offs = host(offsets)
-    if offs.ndim != 1 or offs.size != npix + 1:
-        raise ValueError("offsets should have size %d, got %s" % (npix + 1, offs.shape))
-    offs64 = offs.astype(np.int64)
+    offs64 = host(offsets).astype(np.int64)
+    if offs64.ndim != 1 or offs64.size != npix + 1:
+        raise ValueError("offsets should have size %d, got %s" % (npix + 1, offs64.shape))
     if offs64[0] != 0 or np.any(np.diff(offs64) < 0):
         raise ValueError("offsets must start at 0 and be non-decreasing")
     n_ev = int(offs64[-1])
     if n_ev >= 2 ** 32:
         raise ValueError("too many events for uint32 offsets")
-    t = vol_times if isinstance(vol_times, torch.Tensor) else np.asarray(vol_times)
-    d = vol_data if isinstance(vol_data, torch.Tensor) else np.asarray(vol_data)
-    if t.ndim != 1 or d.ndim != 1 or t.shape[0] != d.shape[0]:
+    if np.ndim(vol_times) != 1 or np.ndim(vol_data) != 1 or len(vol_times) != len(vol_data):
         raise ValueError("vol_times and vol_data must be 1-D arrays of the same size")
-    if t.shape[0] < n_ev:
-        raise ValueError("offsets reference %d events but only %d are given" % (n_ev, t.shape[0]))
+    if len(vol_times) < n_ev:
+        raise ValueError("offsets reference %d events but only %d are given" % (n_ev, len(vol_times)))
 
-    def to_dev_int(a, dtype_np, dtype_t):
+    def to_dev(a):
         if isinstance(a, torch.Tensor):
-            return a[:n_ev].to(dev).to(dtype_t).contiguous()
-        return torch.from_numpy(np.ascontiguousarray(a[:n_ev]).astype(dtype_np, copy=False)).to(dev)
+            t = a[:n_ev]
+            if t.dtype == torch.uint16:
+                t = t.to(torch.int32)
+            return t.to(dev)
+        a = np.ascontiguousarray(np.asarray(a)[:n_ev])
+        if a.dtype == np.uint16 or a.dtype == np.uint32:
+            a = a.astype(np.int64)
+        return torch.from_numpy(a).to(dev)
 
-    d_np_kind = d.dtype.kind if not isinstance(d, torch.Tensor) else ("u" if d.dtype in (torch.uint8,) else "i")
-    times_d = to_dev_int(t, np.int32, torch.int32)
-    if isinstance(d, torch.Tensor):
-        dd = d[:n_ev].to(dev)
-    else:
-        dd = torch.from_numpy(np.ascontiguousarray(d[:n_ev]))
-        dd = dd.to(dev)
-    if dd.dtype.is_floating_point:
-        if n_ev and not bool(torch.all(dd == torch.round(dd))):
+    times = to_dev(vol_times)
+    if times.dtype.is_floating_point:
+        raise TypeError("event times must be integers")
+    times = times.to(torch.int32).contiguous()
+    counts = to_dev(vol_data)
+    if counts.dtype.is_floating_point:
+        if n_ev and not bool(torch.all(counts == torch.round(counts))):
             raise TypeError("event counts must be integers")
-    mx = int(dd.max().item()) if n_ev else 0
-    mn = int(dd.min().item()) if n_ev else 0
+    counts = counts.to(torch.int32) if counts.dtype != torch.int64 else counts
+    mx = int(counts.max().item()) if n_ev else 0
+    mn = int(counts.min().item()) if n_ev else 0
     if mn < 0:
         raise ValueError("counts must be non-negative")
     if mx > 65535:
         raise ValueError("counts above 65535 are not supported")
-    data_d = dd.to(torch.uint8) if mx <= 255 else dd.to(torch.int32).to(torch.uint16)
-    if n_ev:
-        tmin, tmax = int(times_d.min().item()), int(times_d.max().item())
-    else:
-        tmin = tmax = 0
+    counts = counts.to(torch.uint8) if mx <= 255 else counts.to(torch.int32).to(torch.uint16)
+    tmin = int(times.min().item()) if n_ev else 0
+    tmax = int(times.max().item()) if n_ev else 0
     offs_d = torch.from_numpy(offs64.astype(np.uint32).view(np.int32)).to(dev)
-    del d_np_kind
-    return times_d, data_d.contiguous(), offs_d, offs64, mx, (tmin, tmax)
+    return times, counts.contiguous(), offs_d, offs64, mx, (tmin, tmax)
 
 
 class EventEngine:
