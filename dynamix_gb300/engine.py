@@ -446,11 +446,16 @@ class EventEngine:
         return pix.astype(np.int32), range_off, range_bin, total
 
     def run(self, vol_times, vol_data, offsets):
-        torch = _torch()
         times_d, data_d, offs_d, offs64, mx, (tmin, tmax) = _events_to_device(vol_times, vol_data, offsets,
                                                                            self.npix, self.dev)
         if offs64[-1] and (tmin < 0 or tmax >= self.T):
             raise ValueError("event times must lie in [0, nframes)")
+        return self.run_device(times_d, data_d, offs_d, offs64, mx)
+
+    def run_device(self, times_d, data_d, offs_d, offs64, mx):
+        """G6 + G3 + G4 on device-resident events (times int32, counts
+        uint8/uint16, offsets uint32 on the device; offsets also on the host)."""
+        torch = _torch()
         pix, range_off, range_bin, total = self.plan_ranges(offs64)
         self.numer.zero_()
         self.sums.zero_()
@@ -476,3 +481,89 @@ class EventEngine:
         code = int(self.err.item())
         if code:
             raise DeviceError(_lib.device_error_message(code))
+
+
+def _csr_to_device(data, indices, indptr, offsets, shape, nframes, dev):
+    """Validate a CSR stack (layout of dynamix's SparseCorrelator) and move it
+    to the device with one index type (uint32 when every index fits, else int64)."""
+    torch = _torch()
+    H, W = shape
+
+    def host(a):
+        return a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+
+    data, indices, indptr, offsets = (host(a).ravel() for a in (data, indices, indptr, offsets))
+    assert data.size == indices.size
+    assert indptr.size == (H + 1) * nframes
+    assert offsets.size == nframes + 1
+    n = int(data.size)
+    if data.dtype.kind == "f":
+        if n and not np.all(data == np.round(data)):
+            raise TypeError("counts must be integers")
+    if n and data.min() < 0:
+        raise ValueError("counts must be non-negative")
+    mx = int(data.max()) if n else 0
+    if mx > 65535:
+        raise ValueError("counts above 65535 are not supported")
+    big = max(int(offsets.max()) if offsets.size else 0, int(indptr.max()) if indptr.size else 0, n) >= 2 ** 32
+    idt = np.int64 if big else np.uint32
+    if n and (indices.min() < 0 or indices.max() >= W):
+        raise ValueError("column indices must lie in [0, width)")
+    d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a.astype(dt, copy=False)).view(
+        np.int64 if dt == np.int64 else np.int32)).to(dev)
+    data_d = torch.from_numpy(np.ascontiguousarray(data.astype(np.uint8 if mx <= 255 else np.uint16))).to(dev)
+    return (data_d, d(indices, idt), d(indptr, idt), d(offsets, idt), 8 if big else 4, n, mx)
+
+
+class SparseEngine:
+    """Exact g2 from per-frame CSR: transpose to event lists (G7), then G6-G4."""
+
+    def __init__(self, shape, nframes, qmask, n_bins, scale, device=None):
+        torch = _torch()
+        self.events = EventEngine(shape, nframes, qmask, n_bins, scale, device=device)
+        self.lib = self.events.lib
+        self.dev = self.events.dev
+        self.shape, self.T, self.npix = self.events.shape, self.events.T, self.events.npix
+        self.counts = torch.zeros(self.npix, dtype=torch.int32, device=self.dev)
+        self.ev_off = torch.zeros(self.npix + 1, dtype=torch.int32, device=self.dev)
+        n_tiles = -(-self.npix // 8192)
+        self.scan_scratch = torch.zeros(max(1, n_tiles), dtype=torch.int32, device=self.dev)
+        self.last = {}
+
+    def to_events(self, data_d, indices_d, indptr_d, offsets_d, ib, n, mx):
+        """CSR on the device -> (times, counts, offsets) event lists on the device."""
+        torch = _torch()
+        st = stream_handle(self.dev)
+        err = self.events.err
+        err.zero_()
+        self.counts.zero_()
+        H, W = self.shape
+        _lib.check(self.lib.g2_csr_count(ptr(indices_d), ptr(indptr_d), ptr(offsets_d), ib, n, self.T, H, W,
+                                         ptr(self.counts), ptr(err), st), "g2_csr_count")
+        _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
+                                                  ptr(self.scan_scratch), self.scan_scratch.numel(), st),
+                   "g2_exclusive_scan_u32")
+        times_d = torch.empty(max(1, n), dtype=torch.int32, device=self.dev)
+        evdata_d = torch.empty(max(1, n), dtype=data_d.dtype, device=self.dev)
+        self.counts.zero_()                              # reused as the scatter cursor
+        _lib.check(self.lib.g2_csr_scatter(ptr(data_d), data_d.element_size(), ptr(indices_d), ptr(indptr_d),
+                                           ptr(offsets_d), ib, n, self.T, H, W, ptr(self.ev_off), ptr(self.counts),
+                                           ptr(times_d), ptr(evdata_d), ptr(err), st), "g2_csr_scatter")
+        offs64 = self.ev_off.cpu().numpy().view(np.uint32).astype(np.int64)
+        code = int(err.item())
+        if code:
+            raise DeviceError(_lib.device_error_message(code))
+        if offs64[-1] != n:
+            raise DeviceError("CSR transposition lost elements")
+        return times_d, evdata_d, self.ev_off, offs64
+
+    def run(self, data, indices, indptr, offsets):
+        data_d, indices_d, indptr_d, offsets_d, ib, n, mx = _csr_to_device(data, indices, indptr, offsets,
+                                                                          self.shape, self.T, self.dev)
+        times_d, evdata_d, offs_d, offs64 = self.to_events(data_d, indices_d, indptr_d, offsets_d, ib, n, mx)
+        out = self.events.run_device(times_d, evdata_d, offs_d, offs64, mx)
+        self.last = dict(self.events.last, n_elements=n)
+        return out
+
+    def check_error(self):
+        self.events.check_error()

@@ -195,6 +195,31 @@ int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, int32_t ele
                      int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev, int32_t* err_dev,
                      void* stream);
 
+/* ---- G7: CSR frames -> per-pixel event lists ----------------------------
+ * Replaces the CSR path of SparseCorrelator (dynamix/correlator/intensity.py:
+ * 70-128: compute_sums and correlator_oneQ_Nt, correlator.cl:19-217): the CSR
+ * stack is transposed to the event layout and correlated by g2_event_pairsum.
+ * CSR of frame t: elements [offsets[t], offsets[t+1]) of data (count,
+ * elem_bytes 1 or 2) and indices (column); indptr[t*(height+1) + r] ..
+ * indptr[t*(height+1) + r + 1] are the elements of row r relative to
+ * offsets[t].  indices, indptr and offsets share one integer type of
+ * index_bytes (4 = uint32, 8 = int64).
+ * g2_csr_count adds 1 to counts[r*width + col] per element (caller zeroes).
+ * g2_exclusive_scan_u32 writes out[i] = sum(in[0..i)) for i <= n (out has n+1
+ * entries; totals below 2^32); scratch holds ceil(n / 8192) entries.
+ * g2_csr_scatter writes element (t, v) of pixel p to slot ev_offsets[p] +
+ * (cursor[p]++) of ev_times / ev_data (cursor zeroed by the caller). */
+int g2_csr_count(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
+                 int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
+                 uint32_t* counts_dev, int32_t* err_dev, void* stream);
+int g2_exclusive_scan_u32(const uint32_t* in_dev, int64_t n, uint32_t* out_dev, uint32_t* scratch_dev,
+                          int64_t scratch_len, void* stream);
+int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                   const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
+                   int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
+                   uint32_t* cursor_dev, int32_t* ev_times_dev, void* ev_data_dev, int32_t* err_dev,
+                   void* stream);
+
 /* ---- G3: denominator ----------------------------------------------------
  * Replaces correlate_1D (dynamix/resources/opencl/densecorrelator.cl:156-176),
  * the denominator loop of normalize_correlation (evtcorrelator.cl:70-73) and
