@@ -55,8 +55,8 @@ SIGNATURES = {
     "g2_binned_max": (C.c_int, [_p, _i32, _i64, _i64, _p, _i64, _p, _p]),
     "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
-    "g2_event_pairsum": (C.c_int, [_p, _p, _i32, _i64, _p, _i64, _p, _p, _p, _i32, _i32, _i32, _i32, _p, _p, _p,
-                                   _p]),
+    "g2_event_pairsum": (C.c_int, [_p, _p, _i32, _i64, _p, _i64, _p, _p, _p, _i32, _p, _i32, _i32, _i32, _i32, _p,
+                                   _p, _p, _p]),
     "g2_csr_count": (C.c_int, [_p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p]),
     "g2_exclusive_scan_u32": (C.c_int, [_p, _i64, _p, _p, _i64, _p]),
     "g2_csr_scatter": (C.c_int, [_p, _i32, _p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),

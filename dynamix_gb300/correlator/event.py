@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from ..engine import EventEngine
+from ..engine_sparse import EventEngine
 from .common import BaseCorrelator
 
 
@@ -49,6 +49,12 @@ class EventCorrelator(BaseCorrelator):
                 self.total_events_count = numels
             else:
                 raise ValueError("Too many events and allow_reallocate was set to False")
+
+    def correlate_device(self, vol_times, vol_data, offsets):
+        """Run on the device and return the float32 g2 device tensor
+        ``(n_bins, nframes)`` (no copy back).  CUDA tensors are used in place."""
+        self._check_event_arrays(vol_times, vol_data, offsets)
+        return self.engine.run(vol_times, vol_data, offsets)
 
     def correlate(self, vol_times, vol_data, offsets):
         self._check_event_arrays(vol_times, vol_data, offsets)

@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from ..engine import SparseEngine
+from ..engine_sparse import SparseEngine
 from .common import BaseCorrelator
 
 
@@ -34,6 +34,12 @@ class SparseCorrelator(BaseCorrelator):
         self.profile = profile
         self.engine = SparseEngine(self.shape, self.nframes, self.qmask, self.n_bins, self._scale_array(),
                                    device=self.extra_options.get("device"))
+
+    def correlate_device(self, data, indices, indptr, offsets):
+        """Run on the device and return the float32 g2 device tensor
+        ``(n_bins, nframes)`` (no copy back).  Inputs may be numpy arrays or
+        tensors; CUDA tensors are used in place."""
+        return self.engine.run(data, indices, indptr, offsets)
 
     def correlate(self, data, indices, indptr, offsets, output=None):
         out = self.engine.run(data, indices, indptr, offsets)

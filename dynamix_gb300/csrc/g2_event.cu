@@ -7,10 +7,10 @@
 // (evtcorrelator.cl:3-47 restated; the order of events within a pixel does not
 // matter because the lag is |t_j - t_i|.)
 //
-// The host lists the binned pixels bin by bin and cuts that list into ranges
-// of one bin each, balanced by pair count.  One CTA per range keeps the bin's
-// lag histogram and frame-sum histogram as uint32 counters in shared memory
-// (2 x T words).  A warp takes one pixel at a time, stages up to EV of its
+// The host lists the binned pixels bin by bin (once per q-mask) and gives each
+// CTA a contiguous slice of that list, cut into ranges of one bin each.  A CTA
+// keeps the current bin's lag histogram and frame-sum histogram as uint32
+// counters in shared memory (2 x T words) and flushes them at each range end.  A warp takes one pixel at a time, stages up to EV of its
 // events in shared memory as (t << 16 | v) and walks the pairs: for each i (warp
 // uniform) the lanes take j = i + lane, i + lane + 32, ...  A counter whose
 // value reaches 2^31 is drained with an atomic exchange into the int64 global
@@ -44,7 +44,8 @@ template <typename Tv>
 __global__ void __launch_bounds__(THREADS, 1)
     pairs_smem_kernel(const int32_t* __restrict__ times, const Tv* __restrict__ data,
                       const uint32_t* __restrict__ offsets, const int32_t* __restrict__ pix_list,
-                      const int32_t* __restrict__ range_off, const int32_t* __restrict__ range_bin, int64_t n_events,
+                      const int32_t* __restrict__ range_off, const int32_t* __restrict__ range_bin,
+                      const int32_t* __restrict__ cta_range_off, int n_ranges, int64_t n_events,
                       int64_t npix, int32_t T, int n_bins, unsigned long long* __restrict__ numer,
                       unsigned long long* __restrict__ sums, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
@@ -52,79 +53,85 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint32_t* shist = sm + T;         // [T] frame sums
   uint32_t* evbuf = sm + 2 * T;     // [WARPS][2][EV] staged events (t << 16 | v)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x;
-  const int bin = range_bin[r];
-  if (bin < 0 || bin >= n_bins) {
-    if (threadIdx.x == 0) atomicOr(err, G2_DEVERR_BOUNDS);
-    return;
-  }
-  for (int i = threadIdx.x; i < 2 * T; i += THREADS) sm[i] = 0;
-  __syncthreads();
-  unsigned long long* gN = numer + static_cast<int64_t>(bin) * T;
-  unsigned long long* gS = sums + static_cast<int64_t>(bin) * T;
   uint32_t* bufA = evbuf + warp * 2 * EV;
   uint32_t* bufB = bufA + EV;
   bool bad = false;
-
-  for (int li = range_off[r] + warp; li < range_off[r + 1]; li += WARPS) {
-    const int32_t p = pix_list[li];
-    if (p < 0 || p >= npix) {
+  for (int i = threadIdx.x; i < 2 * T; i += THREADS) sm[i] = 0;
+  // this CTA's ranges (a contiguous slice of the bin-ordered pixel list, cut
+  // at bin boundaries); the counters are flushed once per range
+  const int r_end = min(cta_range_off[blockIdx.x + 1], n_ranges);
+  for (int r = max(cta_range_off[blockIdx.x], 0); r < r_end; ++r) {
+    const int bin = range_bin[r];
+    if (bin < 0 || bin >= n_bins) {
       bad = true;
-      continue;
+      continue;  // uniform over the CTA
     }
-    const int64_t base = offsets[p];
-    const int64_t end = offsets[p + 1];
-    if (end < base || end > n_events) {
-      bad = true;
-      continue;
-    }
-    const int n = static_cast<int>(end - base);
-    for (int ib = 0; ib < n; ib += EV) {
-      const int na = min(EV, n - ib);
-      for (int e = lane; e < na; e += 32) {
-        const int32_t t = times[base + ib + e];
-        const uint32_t v = static_cast<uint32_t>(data[base + ib + e]);
-        const bool ok = t >= 0 && t < T;
-        bad |= !ok;
-        bufA[e] = ok ? (static_cast<uint32_t>(t) << 16) | v : 0u;
-        if (ok && v) add_counter(&shist[t], &gS[t], v);
+    __syncthreads();  // counters zeroed (start, or the previous flush)
+    unsigned long long* gN = numer + static_cast<int64_t>(bin) * T;
+    unsigned long long* gS = sums + static_cast<int64_t>(bin) * T;
+    for (int li = range_off[r] + warp; li < range_off[r + 1]; li += WARPS) {
+      const int32_t p = pix_list[li];
+      if (p < 0 || p >= npix) {
+        bad = true;
+        continue;
       }
-      __syncwarp();
-      for (int jb = ib; jb < n; jb += EV) {
-        const int nb = min(EV, n - jb);
-        const uint32_t* B = bufA;
-        if (jb != ib) {
-          for (int e = lane; e < nb; e += 32) {
-            const int32_t t = times[base + jb + e];
-            const uint32_t v = static_cast<uint32_t>(data[base + jb + e]);
-            bufB[e] = (t >= 0 && t < T) ? (static_cast<uint32_t>(t) << 16) | v : 0u;
-          }
-          __syncwarp();
-          B = bufB;
-        }
-        for (int i = 0; i < na; ++i) {
-          const uint32_t wi = bufA[i];
-          const uint32_t vi = wi & 0xFFFFu;
-          if (vi == 0) continue;  // warp-uniform
-          const int ti = static_cast<int>(wi >> 16);
-          for (int j = (jb == ib ? i : 0) + lane; j < nb; j += 32) {
-            const uint32_t wj = B[j];
-            const uint32_t vj = wj & 0xFFFFu;
-            const int lag = abs(static_cast<int>(wj >> 16) - ti);
-            const uint32_t prod = vi * vj;
-            if (prod) add_counter(&hist[lag], &gN[lag], prod);
-          }
+      const int64_t base = offsets[p];
+      const int64_t end = offsets[p + 1];
+      if (end < base || end > n_events) {
+        bad = true;
+        continue;
+      }
+      const int n = static_cast<int>(end - base);
+      for (int ib = 0; ib < n; ib += EV) {
+        const int na = min(EV, n - ib);
+        for (int e = lane; e < na; e += 32) {
+          const int32_t t = times[base + ib + e];
+          const uint32_t v = static_cast<uint32_t>(data[base + ib + e]);
+          const bool ok = t >= 0 && t < T;
+          bad |= !ok;
+          bufA[e] = ok ? (static_cast<uint32_t>(t) << 16) | v : 0u;
+          if (ok && v) add_counter(&shist[t], &gS[t], v);
         }
         __syncwarp();
+        for (int jb = ib; jb < n; jb += EV) {
+          const int nb = min(EV, n - jb);
+          const uint32_t* B = bufA;
+          if (jb != ib) {
+            for (int e = lane; e < nb; e += 32) {
+              const int32_t t = times[base + jb + e];
+              const uint32_t v = static_cast<uint32_t>(data[base + jb + e]);
+              bufB[e] = (t >= 0 && t < T) ? (static_cast<uint32_t>(t) << 16) | v : 0u;
+            }
+            __syncwarp();
+            B = bufB;
+          }
+          for (int i = 0; i < na; ++i) {
+            const uint32_t wi = bufA[i];
+            const uint32_t vi = wi & 0xFFFFu;
+            if (vi == 0) continue;  // warp-uniform
+            const int ti = static_cast<int>(wi >> 16);
+            for (int j = (jb == ib ? i : 0) + lane; j < nb; j += 32) {
+              const uint32_t wj = B[j];
+              const uint32_t vj = wj & 0xFFFFu;
+              const int lag = abs(static_cast<int>(wj >> 16) - ti);
+              const uint32_t prod = vi * vj;
+              if (prod) add_counter(&hist[lag], &gN[lag], prod);
+            }
+          }
+          __syncwarp();
+        }
       }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < T; i += THREADS) {
+      const uint32_t h = hist[i], sh = shist[i];
+      if (h) atomicAdd(&gN[i], static_cast<unsigned long long>(h));
+      if (sh) atomicAdd(&gS[i], static_cast<unsigned long long>(sh));
+      hist[i] = 0;
+      shist[i] = 0;
     }
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
-  __syncthreads();
-  for (int i = threadIdx.x; i < T; i += THREADS) {
-    if (hist[i]) atomicAdd(&gN[i], static_cast<unsigned long long>(hist[i]));
-    if (shist[i]) atomicAdd(&gS[i], static_cast<unsigned long long>(shist[i]));
-  }
 }
 
 // Every pair added straight to the global int64 sums (long stacks, large counts).
@@ -133,20 +140,23 @@ __global__ void __launch_bounds__(256)
     pairs_global_kernel(const int32_t* __restrict__ times, const Tv* __restrict__ data,
                         const uint32_t* __restrict__ offsets, const int32_t* __restrict__ pix_list,
                         const int32_t* __restrict__ range_off, const int32_t* __restrict__ range_bin,
-                        int64_t n_events, int64_t npix, int32_t T, int n_bins,
+                        const int32_t* __restrict__ cta_range_off, int n_ranges, int64_t n_events, int64_t npix,
+                        int32_t T,
+                        int n_bins,
                         unsigned long long* __restrict__ numer, unsigned long long* __restrict__ sums,
                         int32_t* __restrict__ err) {
   const int warps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x;
+  bool bad = false;
+  const int r_end = min(cta_range_off[blockIdx.x + 1], n_ranges);
+  for (int r = max(cta_range_off[blockIdx.x], 0); r < r_end; ++r) {
   const int bin = range_bin[r];
   if (bin < 0 || bin >= n_bins) {
-    if (threadIdx.x == 0) atomicOr(err, G2_DEVERR_BOUNDS);
-    return;
+    bad = true;
+    continue;
   }
   unsigned long long* gN = numer + static_cast<int64_t>(bin) * T;
   unsigned long long* gS = sums + static_cast<int64_t>(bin) * T;
-  bool bad = false;
   for (int li = range_off[r] + warp; li < range_off[r + 1]; li += warps) {
     const int32_t p = pix_list[li];
     if (p < 0 || p >= npix) {
@@ -177,6 +187,7 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
+  }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
 
@@ -186,17 +197,18 @@ __global__ void __launch_bounds__(256)
 extern "C" int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, int32_t elem_bytes,
                                 int64_t n_events, const uint32_t* offsets_dev, int64_t npix,
                                 const int32_t* pix_list_dev, const int32_t* range_off_dev,
-                                const int32_t* range_bin_dev, int32_t n_ranges, int32_t nframes, int32_t n_bins,
+                                const int32_t* range_bin_dev, int32_t n_ranges, const int32_t* cta_range_off_dev,
+                                int32_t n_ctas, int32_t nframes, int32_t n_bins,
                                 int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev, int32_t* err_dev,
                                 void* stream) {
   using namespace g2;
-  if (!times_dev || !data_dev || !offsets_dev || !pix_list_dev || !range_off_dev || !range_bin_dev || !numer_dev ||
-      !sums_dev || !err_dev)
+  if (!times_dev || !data_dev || !offsets_dev || !pix_list_dev || !range_off_dev || !range_bin_dev ||
+      !cta_range_off_dev || !numer_dev || !sums_dev || !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || n_events < 0 || npix <= 0 || n_ranges < 0 || nframes <= 0 ||
       n_bins <= 0 || max_count < 0)
     return G2_ERR_ARG;
-  if (n_ranges == 0) return G2_OK;
+  if (n_ranges == 0 || n_ctas <= 0) return G2_OK;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return G2_ERR_CUDA;
   int smem_optin = 0;
@@ -214,26 +226,26 @@ extern "C" int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, 
       if (cudaFuncSetAttribute(ev::pairs_smem_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(smem)) != cudaSuccess)
         return G2_ERR_CUDA;
-      ev::pairs_smem_kernel<uint8_t><<<n_ranges, ev::THREADS, smem, st>>>(
+      ev::pairs_smem_kernel<uint8_t><<<n_ctas, ev::THREADS, smem, st>>>(
           times_dev, reinterpret_cast<const uint8_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, n_events, npix, nframes, n_bins, N, S, err_dev);
+          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
     } else {
       if (cudaFuncSetAttribute(ev::pairs_smem_kernel<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(smem)) != cudaSuccess)
         return G2_ERR_CUDA;
-      ev::pairs_smem_kernel<uint16_t><<<n_ranges, ev::THREADS, smem, st>>>(
+      ev::pairs_smem_kernel<uint16_t><<<n_ctas, ev::THREADS, smem, st>>>(
           times_dev, reinterpret_cast<const uint16_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, n_events, npix, nframes, n_bins, N, S, err_dev);
+          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
     }
   } else {
     if (elem_bytes == 1)
-      ev::pairs_global_kernel<uint8_t><<<n_ranges, 256, 0, st>>>(
+      ev::pairs_global_kernel<uint8_t><<<n_ctas, 256, 0, st>>>(
           times_dev, reinterpret_cast<const uint8_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, n_events, npix, nframes, n_bins, N, S, err_dev);
+          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
     else
-      ev::pairs_global_kernel<uint16_t><<<n_ranges, 256, 0, st>>>(
+      ev::pairs_global_kernel<uint16_t><<<n_ctas, 256, 0, st>>>(
           times_dev, reinterpret_cast<const uint16_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, n_events, npix, nframes, n_bins, N, S, err_dev);
+          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
   }
   return launch_status();
 }

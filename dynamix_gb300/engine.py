@@ -340,230 +340,3 @@ class DenseEngine:
         S = self.sums[: self.n_bins].cpu().numpy()
         if S.size and float(S.max()) ** 2 * self.T >= 2.0 ** 63:
             raise OverflowError("denominator exceeds int64 for these counts")
-
-
-def _events_to_device(vol_times, vol_data, offsets, npix, dev):
-    """Validate the event arrays (layout of dynamix's FramesCompressor) and
-    move them to the device: times int32, counts uint8/uint16, offsets uint32.
-    Returns (times, counts, offsets, host offsets int64, max count, (min t, max t))."""
-    torch = _torch()
-
-    def host(a):
-        return a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
-
-    offs64 = host(offsets).astype(np.int64)
-    if offs64.ndim != 1 or offs64.size != npix + 1:
-        raise ValueError("offsets should have size %d, got %s" % (npix + 1, offs64.shape))
-    if offs64[0] != 0 or np.any(np.diff(offs64) < 0):
-        raise ValueError("offsets must start at 0 and be non-decreasing")
-    n_ev = int(offs64[-1])
-    if n_ev >= 2 ** 32:
-        raise ValueError("too many events for uint32 offsets")
-    if np.ndim(vol_times) != 1 or np.ndim(vol_data) != 1 or len(vol_times) != len(vol_data):
-        raise ValueError("vol_times and vol_data must be 1-D arrays of the same size")
-    if len(vol_times) < n_ev:
-        raise ValueError("offsets reference %d events but only %d are given" % (n_ev, len(vol_times)))
-
-    def to_dev(a):
-        if isinstance(a, torch.Tensor):
-            t = a[:n_ev]
-            if t.dtype == torch.uint16:
-                t = t.to(torch.int32)
-            return t.to(dev)
-        a = np.ascontiguousarray(np.asarray(a)[:n_ev])
-        if a.dtype == np.uint16 or a.dtype == np.uint32:
-            a = a.astype(np.int64)
-        return torch.from_numpy(a).to(dev)
-
-    times = to_dev(vol_times)
-    if times.dtype.is_floating_point:
-        raise TypeError("event times must be integers")
-    times = times.to(torch.int32).contiguous()
-    counts = to_dev(vol_data)
-    if counts.dtype.is_floating_point:
-        if n_ev and not bool(torch.all(counts == torch.round(counts))):
-            raise TypeError("event counts must be integers")
-    counts = counts.to(torch.int32) if counts.dtype != torch.int64 else counts
-    mx = int(counts.max().item()) if n_ev else 0
-    mn = int(counts.min().item()) if n_ev else 0
-    if mn < 0:
-        raise ValueError("counts must be non-negative")
-    if mx > 65535:
-        raise ValueError("counts above 65535 are not supported")
-    counts = counts.to(torch.uint8) if mx <= 255 else counts.to(torch.int32).to(torch.uint16)
-    tmin = int(times.min().item()) if n_ev else 0
-    tmax = int(times.max().item()) if n_ev else 0
-    offs_d = torch.from_numpy(offs64.astype(np.uint32).view(np.int32)).to(dev)
-    return times, counts.contiguous(), offs_d, offs64, mx, (tmin, tmax)
-
-
-class EventEngine:
-    """Exact g2 from per-pixel event lists (G6 pair sums, then G3, G4)."""
-
-    def __init__(self, shape, nframes, qmask, n_bins, scale, device=None, ranges_per_sm=4):
-        torch = _torch()
-        self.lib = _lib.load()
-        self.dev = require_cuda(device)
-        self.shape = tuple(int(s) for s in shape)
-        self.npix = self.shape[0] * self.shape[1]
-        self.T = int(nframes)
-        if self.T >= 2 ** 31:
-            raise ValueError("too many frames")
-        self.n_bins = int(n_bins)
-        q = np.ascontiguousarray(qmask, dtype=np.int32).ravel()
-        self.qflat = np.where(q >= 1, q, 0)
-        order = np.argsort(self.qflat, kind="stable")
-        counts = np.bincount(self.qflat, minlength=self.n_bins + 1)[: self.n_bins + 1]
-        starts = np.concatenate([[0], np.cumsum(counts)])
-        self.binned = order[starts[1]:]                         # binned pixels, bin by bin
-        self.binned_bin = self.qflat[self.binned] - 1
-        self.ranges_per_sm = int(ranges_per_sm)
-        self.scale = torch.as_tensor(np.asarray(scale, dtype=np.float64), device=self.dev)
-        rows = max(self.n_bins, 1)
-        z = lambda dt: torch.zeros((rows, self.T), dtype=dt, device=self.dev)
-        self.sums, self.numer, self.denom = z(torch.int64), z(torch.int64), z(torch.int64)
-        self.g2_f32, self.g2_f64 = z(torch.float32), z(torch.float64)
-        self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
-        self.last = {}
-
-    def plan_ranges(self, offs64):
-        """Cut the binned pixels with events into ranges of one bin each, of
-        about equal pair counts (the work of a CTA)."""
-        n = np.diff(offs64)[self.binned]
-        keep = n > 0
-        pix = self.binned[keep]
-        pb = self.binned_bin[keep]
-        pairs = n[keep] * (n[keep] + 1) // 2
-        total = int(pairs.sum())
-        sms = _torch().cuda.get_device_properties(self.dev).multi_processor_count
-        target = max(1, total // max(1, sms * self.ranges_per_sm))
-        cum = np.cumsum(pairs)
-        # range id = (bin, cumulative pairs // target), cut at bin changes
-        key = pb.astype(np.int64) * (total // target + 2) + (cum - pairs) // target
-        starts = np.flatnonzero(np.concatenate([[True], key[1:] != key[:-1]])) if pix.size else np.zeros(0, np.int64)
-        range_off = np.concatenate([starts, [pix.size]]).astype(np.int32)
-        range_bin = pb[starts].astype(np.int32) if pix.size else np.zeros(0, np.int32)
-        return pix.astype(np.int32), range_off, range_bin, total
-
-    def run(self, vol_times, vol_data, offsets):
-        times_d, data_d, offs_d, offs64, mx, (tmin, tmax) = _events_to_device(vol_times, vol_data, offsets,
-                                                                           self.npix, self.dev)
-        if offs64[-1] and (tmin < 0 or tmax >= self.T):
-            raise ValueError("event times must lie in [0, nframes)")
-        return self.run_device(times_d, data_d, offs_d, offs64, mx)
-
-    def run_device(self, times_d, data_d, offs_d, offs64, mx):
-        """G6 + G3 + G4 on device-resident events (times int32, counts
-        uint8/uint16, offsets uint32 on the device; offsets also on the host)."""
-        torch = _torch()
-        pix, range_off, range_bin, total = self.plan_ranges(offs64)
-        self.numer.zero_()
-        self.sums.zero_()
-        self.err.zero_()
-        st = stream_handle(self.dev)
-        if range_bin.size and self.n_bins:
-            d = lambda a: torch.from_numpy(a).to(self.dev)
-            pix_d, ro_d, rb_d = d(pix), d(range_off), d(range_bin)
-            _lib.check(self.lib.g2_event_pairsum(
-                ptr(times_d), ptr(data_d), data_d.element_size(), int(offs64[-1]), ptr(offs_d), self.npix,
-                ptr(pix_d), ptr(ro_d), ptr(rb_d), int(range_bin.size), self.T, self.n_bins, mx, ptr(self.numer),
-                ptr(self.sums), ptr(self.err), st), "g2_event_pairsum")
-        if self.n_bins:
-            _lib.check(self.lib.g2_denominator(ptr(self.sums), self.n_bins, self.T, ptr(self.denom), st),
-                       "g2_denominator")
-            _lib.check(self.lib.g2_finalize(ptr(self.numer), ptr(self.denom), ptr(self.scale), self.n_bins,
-                                            self.T, ptr(self.g2_f32), ptr(self.g2_f64), st), "g2_finalize")
-        self.last = {"n_events": int(offs64[-1]), "pairs": total, "n_ranges": int(range_bin.size),
-                     "max_count": mx}
-        return self.g2_f32[: self.n_bins]
-
-    def check_error(self):
-        code = int(self.err.item())
-        if code:
-            raise DeviceError(_lib.device_error_message(code))
-
-
-def _csr_to_device(data, indices, indptr, offsets, shape, nframes, dev):
-    """Validate a CSR stack (layout of dynamix's SparseCorrelator) and move it
-    to the device with one index type (uint32 when every index fits, else int64)."""
-    torch = _torch()
-    H, W = shape
-
-    def host(a):
-        return a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
-
-    data, indices, indptr, offsets = (host(a).ravel() for a in (data, indices, indptr, offsets))
-    assert data.size == indices.size
-    assert indptr.size == (H + 1) * nframes
-    assert offsets.size == nframes + 1
-    n = int(data.size)
-    if data.dtype.kind == "f":
-        if n and not np.all(data == np.round(data)):
-            raise TypeError("counts must be integers")
-    if n and data.min() < 0:
-        raise ValueError("counts must be non-negative")
-    mx = int(data.max()) if n else 0
-    if mx > 65535:
-        raise ValueError("counts above 65535 are not supported")
-    big = max(int(offsets.max()) if offsets.size else 0, int(indptr.max()) if indptr.size else 0, n) >= 2 ** 32
-    idt = np.int64 if big else np.uint32
-    if n and (indices.min() < 0 or indices.max() >= W):
-        raise ValueError("column indices must lie in [0, width)")
-    d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a.astype(dt, copy=False)).view(
-        np.int64 if dt == np.int64 else np.int32)).to(dev)
-    data_d = torch.from_numpy(np.ascontiguousarray(data.astype(np.uint8 if mx <= 255 else np.uint16))).to(dev)
-    return (data_d, d(indices, idt), d(indptr, idt), d(offsets, idt), 8 if big else 4, n, mx)
-
-
-class SparseEngine:
-    """Exact g2 from per-frame CSR: transpose to event lists (G7), then G6-G4."""
-
-    def __init__(self, shape, nframes, qmask, n_bins, scale, device=None):
-        torch = _torch()
-        self.events = EventEngine(shape, nframes, qmask, n_bins, scale, device=device)
-        self.lib = self.events.lib
-        self.dev = self.events.dev
-        self.shape, self.T, self.npix = self.events.shape, self.events.T, self.events.npix
-        self.counts = torch.zeros(self.npix, dtype=torch.int32, device=self.dev)
-        self.ev_off = torch.zeros(self.npix + 1, dtype=torch.int32, device=self.dev)
-        n_tiles = -(-self.npix // 8192)
-        self.scan_scratch = torch.zeros(max(1, n_tiles), dtype=torch.int32, device=self.dev)
-        self.last = {}
-
-    def to_events(self, data_d, indices_d, indptr_d, offsets_d, ib, n, mx):
-        """CSR on the device -> (times, counts, offsets) event lists on the device."""
-        torch = _torch()
-        st = stream_handle(self.dev)
-        err = self.events.err
-        err.zero_()
-        self.counts.zero_()
-        H, W = self.shape
-        _lib.check(self.lib.g2_csr_count(ptr(indices_d), ptr(indptr_d), ptr(offsets_d), ib, n, self.T, H, W,
-                                         ptr(self.counts), ptr(err), st), "g2_csr_count")
-        _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
-                                                  ptr(self.scan_scratch), self.scan_scratch.numel(), st),
-                   "g2_exclusive_scan_u32")
-        times_d = torch.empty(max(1, n), dtype=torch.int32, device=self.dev)
-        evdata_d = torch.empty(max(1, n), dtype=data_d.dtype, device=self.dev)
-        self.counts.zero_()                              # reused as the scatter cursor
-        _lib.check(self.lib.g2_csr_scatter(ptr(data_d), data_d.element_size(), ptr(indices_d), ptr(indptr_d),
-                                           ptr(offsets_d), ib, n, self.T, H, W, ptr(self.ev_off), ptr(self.counts),
-                                           ptr(times_d), ptr(evdata_d), ptr(err), st), "g2_csr_scatter")
-        offs64 = self.ev_off.cpu().numpy().view(np.uint32).astype(np.int64)
-        code = int(err.item())
-        if code:
-            raise DeviceError(_lib.device_error_message(code))
-        if offs64[-1] != n:
-            raise DeviceError("CSR transposition lost elements")
-        return times_d, evdata_d, self.ev_off, offs64
-
-    def run(self, data, indices, indptr, offsets):
-        data_d, indices_d, indptr_d, offsets_d, ib, n, mx = _csr_to_device(data, indices, indptr, offsets,
-                                                                          self.shape, self.T, self.dev)
-        times_d, evdata_d, offs_d, offs64 = self.to_events(data_d, indices_d, indptr_d, offsets_d, ib, n, mx)
-        out = self.events.run_device(times_d, evdata_d, offs_d, offs64, mx)
-        self.last = dict(self.events.last, n_elements=n)
-        return out
-
-    def check_error(self):
-        self.events.check_error()

@@ -1,0 +1,313 @@
+"""Device pipelines of the event-list and sparse (CSR) correlators.
+
+Event lists (G6): per pixel, its events (frame, count) in the layout of
+dynamix's FramesCompressor.  The binned pixels are listed bin by bin once per
+q-mask and that list is cut into one contiguous slice per CTA (split at bin
+boundaries), so a call needs no host-side planning: the pair-sum kernel adds
+N and S, then G3 (denominator) and G4 (g2) follow.
+
+CSR (G7): per-frame CSR in the layout of dynamix's SparseCorrelator, transposed
+on the device (count, scan, scatter) into event lists, then the same G6-G4.
+
+Inputs that already live on the GPU are validated there (no host round trip);
+numpy inputs are validated on the host before the copy.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+from .engine import DeviceError, _torch, ptr, require_cuda, stream_handle
+
+
+def _is_cuda(a):
+    torch = _torch()
+    return isinstance(a, torch.Tensor) and a.is_cuda
+
+
+def _int_counts_to_device(counts, n, dev):
+    """Validated non-negative integer counts -> device uint8 (max <= 255) or
+    uint16 tensor; returns (tensor, max)."""
+    torch = _torch()
+    if isinstance(counts, torch.Tensor):
+        c = counts[:n]
+        if c.dtype == torch.uint16:
+            c = c.to(torch.int32)
+        c = c.to(dev)
+    else:
+        a = np.ascontiguousarray(np.asarray(counts)[:n])
+        if a.dtype.kind not in "iuf":
+            raise TypeError("counts must be integers")
+        if a.dtype == np.uint16 or a.dtype == np.uint32:
+            a = a.astype(np.int64)
+        c = torch.from_numpy(a).to(dev)
+    if c.dtype.is_floating_point:
+        if n and not bool(torch.all(c == torch.round(c))):
+            raise TypeError("counts must be integers")
+        c = c.to(torch.int32)
+    if n == 0:
+        return torch.zeros(1, dtype=torch.uint8, device=dev), 0
+    if c.dtype == torch.uint8:
+        return c.contiguous(), int(c.max().item())
+    lo, hi = torch.aminmax(c)
+    if int(lo.item()) < 0:
+        raise ValueError("counts must be non-negative")
+    mx = int(hi.item())
+    if mx > 65535:
+        raise ValueError("counts above 65535 are not supported")
+    out = c.to(torch.uint8) if mx <= 255 else c.to(torch.int32).to(torch.uint16)
+    return out.contiguous(), mx
+
+
+def events_to_device(vol_times, vol_data, offsets, npix, nframes, dev):
+    """Validate event arrays and move them to the device.
+
+    Returns ``(times int32, counts uint8/uint16, offsets uint32 (as int32),
+    n_events, max_count)``.  Raises ValueError for a bad layout or times
+    outside [0, nframes)."""
+    torch = _torch()
+    if np.ndim(vol_times) != 1 or np.ndim(vol_data) != 1 or np.ndim(offsets) != 1:
+        raise ValueError("event arrays must be 1-D")
+    if len(vol_times) != len(vol_data):
+        raise ValueError("vol_times and vol_data must have the same size")
+    if len(offsets) != npix + 1:
+        raise ValueError("offsets should have size %d, got %d" % (npix + 1, len(offsets)))
+    if _is_cuda(offsets):
+        o = offsets.to(dev).to(torch.int64)
+        if int(o[0].item()) != 0 or not bool(torch.all(o[1:] >= o[:-1])):
+            raise ValueError("offsets must start at 0 and be non-decreasing")
+        n_ev = int(o[-1].item())
+    else:
+        o = np.asarray(offsets).astype(np.int64)
+        if o[0] != 0 or np.any(np.diff(o) < 0):
+            raise ValueError("offsets must start at 0 and be non-decreasing")
+        n_ev = int(o[-1])
+    if n_ev >= 2 ** 32:
+        raise ValueError("too many events for uint32 offsets")
+    if len(vol_times) < n_ev:
+        raise ValueError("offsets reference %d events but only %d are given" % (n_ev, len(vol_times)))
+    if isinstance(o, np.ndarray):
+        offs_d = torch.from_numpy(o.astype(np.uint32).view(np.int32)).to(dev)
+    else:
+        offs_d = o.to(torch.int32)                     # values < 2^31 here; uint32 bit pattern otherwise
+    if isinstance(vol_times, torch.Tensor):
+        times = vol_times[:n_ev].to(dev)
+    else:
+        times = torch.from_numpy(np.ascontiguousarray(np.asarray(vol_times)[:n_ev])).to(dev)
+    if times.dtype.is_floating_point:
+        raise TypeError("event times must be integers")
+    times = times.to(torch.int32).contiguous()
+    if n_ev:
+        tmin, tmax = (int(x.item()) for x in torch.aminmax(times))
+        if tmin < 0 or tmax >= nframes:
+            raise ValueError("event times must lie in [0, nframes)")
+    counts, mx = _int_counts_to_device(vol_data, n_ev, dev)
+    return times, counts, offs_d, n_ev, mx
+
+
+def csr_to_device(data, indices, indptr, offsets, shape, nframes, dev):
+    """Validate a CSR stack and move it to the device with one index type
+    (uint32 when every index fits, else int64).  Returns
+    ``(data, indices, indptr, offsets, index_bytes, n_elements, max_count)``."""
+    torch = _torch()
+    H, W = shape
+    for a in (data, indices, indptr, offsets):
+        assert np.ndim(a) == 1
+    assert len(data) == len(indices)
+    assert len(indptr) == (H + 1) * nframes
+    assert len(offsets) == nframes + 1
+    n = int(len(data))
+
+    def dev_int(a):
+        if isinstance(a, torch.Tensor):
+            t = a.to(dev)
+            return t.to(torch.int64) if t.dtype in (torch.uint16, torch.uint32) else t
+        a = np.asarray(a)
+        if a.dtype == np.uint32 or a.dtype == np.uint64:
+            a = a.astype(np.int64)
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    ind, ip, off = dev_int(indices), dev_int(indptr), dev_int(offsets)
+    big = max(int(off[-1].item()), int(ip.max().item()) if ip.numel() else 0, n) >= 2 ** 31
+    if n:
+        lo, hi = torch.aminmax(ind)
+        if int(lo.item()) < 0 or int(hi.item()) >= W:
+            raise ValueError("column indices must lie in [0, width)")
+    it = torch.int64 if big else torch.int32
+    ind, ip, off = (x.to(it).contiguous() for x in (ind, ip, off))
+    counts, mx = _int_counts_to_device(data, n, dev)
+    return counts, ind, ip, off, 8 if big else 4, n, mx
+
+
+def cta_ranges(binned_bin, n_ctas):
+    """Static work split of the pair-sum kernel.
+
+    ``binned_bin`` is the bin of every binned pixel, the pixels listed bin by
+    bin.  The list is cut into ``n_ctas`` (at most one per pixel) contiguous
+    slices of equal size, and each slice at the bin changes inside it, giving
+    ranges of pixels of one bin.  Returns int32 ``(range_off [n_ranges + 1],
+    range_bin [n_ranges], cta_range_off [n_ctas + 1])``: CTA c handles ranges
+    ``cta_range_off[c] .. cta_range_off[c+1]``, range r the pixels
+    ``range_off[r] .. range_off[r+1]`` of the list."""
+    binned_bin = np.asarray(binned_bin, dtype=np.int32)
+    n = binned_bin.size
+    n_ctas = max(1, min(int(n_ctas), n))
+    bounds = (np.arange(n_ctas + 1, dtype=np.int64) * n) // n_ctas
+    cuts = set(bounds.tolist())
+    if n:
+        cuts.update((np.flatnonzero(np.diff(binned_bin)) + 1).tolist())
+    starts = np.array(sorted(c for c in cuts if c < n), dtype=np.int64)
+    range_off = np.concatenate([starts, [n]]).astype(np.int32)
+    range_bin = binned_bin[starts].astype(np.int32) if n else np.zeros(0, np.int32)
+    cta_range_off = np.searchsorted(starts, bounds).astype(np.int32)
+    return range_off, range_bin, cta_range_off
+
+
+class EventEngine:
+    """Exact g2 from per-pixel event lists (G6 pair sums, then G3, G4)."""
+
+    SMEM_CTAS_PER_SM = 1   # the shared-memory kernel holds 2 x T counters per CTA
+    GLOBAL_CTAS_PER_SM = 8
+
+    def __init__(self, shape, nframes, qmask, n_bins, scale, device=None):
+        torch = _torch()
+        self.lib = _lib.load()
+        self.dev = require_cuda(device)
+        self.shape = tuple(int(s) for s in shape)
+        self.npix = self.shape[0] * self.shape[1]
+        self.T = int(nframes)
+        if self.T >= 2 ** 31:
+            raise ValueError("too many frames")
+        self.n_bins = int(n_bins)
+        q = np.ascontiguousarray(qmask, dtype=np.int32).ravel()
+        q = np.where(q >= 1, q, 0)
+        order = np.argsort(q, kind="stable")
+        counts = np.bincount(q, minlength=self.n_bins + 1)[: self.n_bins + 1]
+        self.binned = order[counts[0]:].astype(np.int32)          # binned pixels, bin by bin
+        self.binned_bin = (q[self.binned] - 1).astype(np.int32)
+        sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
+        self.pix_list = torch.from_numpy(self.binned).to(self.dev)
+        self.plans = {k: self._plan(sms * n) for k, n in
+                      (("smem", self.SMEM_CTAS_PER_SM), ("global", self.GLOBAL_CTAS_PER_SM))}
+        self.scale = torch.as_tensor(np.asarray(scale, dtype=np.float64), device=self.dev)
+        rows = max(self.n_bins, 1)
+        z = lambda dt: torch.zeros((rows, self.T), dtype=dt, device=self.dev)
+        self.sums, self.numer, self.denom = z(torch.int64), z(torch.int64), z(torch.int64)
+        self.g2_f32, self.g2_f64 = z(torch.float32), z(torch.float64)
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.last = {}
+        self.profile = False
+        self._events = []
+
+    def _mark(self, name):
+        """With ``profile`` set, record a CUDA event named ``name`` on the stream."""
+        if self.profile:
+            torch = _torch()
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(torch.cuda.current_stream(self.dev))
+            self._events.append((name, e))
+
+    def take_events(self):
+        ev, self._events = self._events, []
+        return ev
+
+    @staticmethod
+    def stage_times(events):
+        """{stage: ms} from consecutive marks (stage = the name of its end mark)."""
+        out = {}
+        for (_, a), (name, b) in zip(events, events[1:]):
+            out[name] = out.get(name, 0.0) + a.elapsed_time(b)
+        return out
+
+    def _plan(self, n_ctas):
+        torch = _torch()
+        range_off, range_bin, cta_range_off = cta_ranges(self.binned_bin, n_ctas)
+        d = lambda a: torch.from_numpy(a).to(self.dev)
+        return d(range_off), d(range_bin), d(cta_range_off), int(range_bin.size), int(cta_range_off.size - 1)
+
+    def run(self, vol_times, vol_data, offsets):
+        times, counts, offs, n_ev, mx = events_to_device(vol_times, vol_data, offsets, self.npix, self.T,
+                                                         self.dev)
+        return self.run_device(times, counts, offs, n_ev, mx)
+
+    def run_device(self, times, counts, offs, n_ev, mx):
+        """G6 + G3 + G4 on validated device events."""
+        self.numer.zero_()
+        self.sums.zero_()
+        self.err.zero_()
+        st = stream_handle(self.dev)
+        use_smem = self.T * 8 + 32768 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
+        ro, rb, cro, n_ranges, n_ctas = self.plans["smem" if use_smem else "global"]
+        self._mark("start_pairs")
+        if n_ranges and self.n_bins and n_ev:
+            _lib.check(self.lib.g2_event_pairsum(
+                ptr(times), ptr(counts), counts.element_size(), n_ev, ptr(offs), self.npix, ptr(self.pix_list),
+                ptr(ro), ptr(rb), n_ranges, ptr(cro), n_ctas, self.T, self.n_bins, mx, ptr(self.numer),
+                ptr(self.sums), ptr(self.err), st), "g2_event_pairsum")
+        self._mark("pairsum")
+        if self.n_bins:
+            _lib.check(self.lib.g2_denominator(ptr(self.sums), self.n_bins, self.T, ptr(self.denom), st),
+                       "g2_denominator")
+            _lib.check(self.lib.g2_finalize(ptr(self.numer), ptr(self.denom), ptr(self.scale), self.n_bins,
+                                            self.T, ptr(self.g2_f32), ptr(self.g2_f64), st), "g2_finalize")
+        self._mark("normalize")
+        self.last = {"n_events": n_ev, "max_count": mx, "kernel": "smem" if use_smem else "global",
+                     "n_ranges": n_ranges, "n_ctas": n_ctas}
+        return self.g2_f32[: self.n_bins]
+
+    def check_error(self):
+        code = int(self.err.item())
+        if code:
+            raise DeviceError(_lib.device_error_message(code))
+
+
+class SparseEngine:
+    """Exact g2 from per-frame CSR: transpose to event lists (G7), then G6-G4."""
+
+    def __init__(self, shape, nframes, qmask, n_bins, scale, device=None):
+        torch = _torch()
+        self.events = EventEngine(shape, nframes, qmask, n_bins, scale, device=device)
+        self.lib = self.events.lib
+        self.dev = self.events.dev
+        self.shape, self.T, self.npix = self.events.shape, self.events.T, self.events.npix
+        self.counts = torch.zeros(self.npix, dtype=torch.int32, device=self.dev)
+        self.ev_off = torch.zeros(self.npix + 1, dtype=torch.int32, device=self.dev)
+        self.scan_scratch = torch.zeros(max(1, -(-self.npix // 8192)), dtype=torch.int32, device=self.dev)
+        self._ev_cap = 0
+        self.last = {}
+
+    def to_events(self, data, indices, indptr, offsets, ib, n):
+        """CSR on the device -> (times, counts, offsets) event lists on the device."""
+        torch = _torch()
+        st = stream_handle(self.dev)
+        err = self.events.err
+        err.zero_()
+        self.counts.zero_()
+        H, W = self.shape
+        self.events._mark("start_transpose")
+        _lib.check(self.lib.g2_csr_count(ptr(indices), ptr(indptr), ptr(offsets), ib, n, self.T, H, W,
+                                         ptr(self.counts), ptr(err), st), "g2_csr_count")
+        _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
+                                                  ptr(self.scan_scratch), self.scan_scratch.numel(), st),
+                   "g2_exclusive_scan_u32")
+        if n > self._ev_cap or not hasattr(self, "ev_times") or self.ev_data.dtype != data.dtype:
+            self._ev_cap = max(n, 1)
+            self.ev_times = torch.empty(self._ev_cap, dtype=torch.int32, device=self.dev)
+            self.ev_data = torch.empty(self._ev_cap, dtype=data.dtype, device=self.dev)
+        self.counts.zero_()                              # reused as the scatter cursor
+        _lib.check(self.lib.g2_csr_scatter(ptr(data), data.element_size(), ptr(indices), ptr(indptr), ptr(offsets),
+                                           ib, n, self.T, H, W, ptr(self.ev_off), ptr(self.counts),
+                                           ptr(self.ev_times), ptr(self.ev_data), ptr(err), st), "g2_csr_scatter")
+        self.events._mark("transpose")
+        return self.ev_times, self.ev_data, self.ev_off
+
+    def run(self, data, indices, indptr, offsets):
+        counts, ind, ip, off, ib, n, mx = csr_to_device(data, indices, indptr, offsets, self.shape, self.T,
+                                                        self.dev)
+        times, evdata, evoff = self.to_events(counts, ind, ip, off, ib, n)
+        out = self.events.run_device(times, evdata, evoff, n, mx)
+        self.last = dict(self.events.last, n_elements=n)
+        return out
+
+    def check_error(self):
+        self.events.check_error()

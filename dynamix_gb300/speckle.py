@@ -89,3 +89,47 @@ def speckle_torch(nframes, shape, rho, mu, seed=0, dtype="uint8", max_count=None
             out[t:t + n] = cnt.to(tdtype)
         t += n
     return out
+
+
+def speckle_csr_torch(nframes, shape, rho, mu, seed=0, device="cuda", chunk=64, max_count=255):
+    """Seeded AR(1) speckle stack generated on the device and stored directly
+    as per-frame CSR (the layout of dynamix's SparseCorrelator): returns
+    ``(data uint8, indices int32, indptr int32 [(H+1)*T], offsets int64 [T+1])``
+    device tensors.  Frames are built ``chunk`` at a time, so a sparse stack far
+    larger than device memory as dense frames (e.g. 2162 x 2068 x 20000) fits."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    H, W = shape
+    s = math.sqrt(max(0.0, 1.0 - rho * rho))
+    inv = 1.0 / math.sqrt(2.0)
+    re = torch.randn((H, W), generator=g, device=device) * inv
+    im = torch.randn((H, W), generator=g, device=device) * inv
+    buf = torch.empty((min(chunk, nframes), H, W), dtype=torch.float32, device=device)
+    datas, cols, indptr_rows, counts = [], [], [], []
+    t = 0
+    while t < nframes:
+        n = min(chunk, nframes - t)
+        for k in range(n):
+            if t + k:
+                re.mul_(rho).add_(torch.randn((H, W), generator=g, device=device), alpha=s * inv)
+                im.mul_(rho).add_(torch.randn((H, W), generator=g, device=device), alpha=s * inv)
+            torch.mul(re, re, out=buf[k]).addcmul_(im, im).mul_(mu)
+        cnt = torch.poisson(buf[:n], generator=g).clamp_(max=max_count).to(torch.uint8)
+        nz = torch.nonzero(cnt)                                    # (frame, row, col), lexicographic
+        datas.append(cnt[nz[:, 0], nz[:, 1], nz[:, 2]])
+        cols.append(nz[:, 2].to(torch.int32))
+        rows = torch.bincount(nz[:, 0] * H + nz[:, 1], minlength=n * H).view(n, H)
+        ip = torch.zeros((n, H + 1), dtype=torch.int64, device=device)
+        ip[:, 1:] = torch.cumsum(rows, dim=1)
+        indptr_rows.append(ip.to(torch.int32))
+        counts.append(ip[:, -1])
+        t += n
+    data = torch.cat(datas)
+    indices = torch.cat(cols)
+    indptr = torch.cat(indptr_rows).reshape(-1)
+    per_frame = torch.cat(counts)
+    offsets = torch.zeros(nframes + 1, dtype=torch.int64, device=device)
+    offsets[1:] = torch.cumsum(per_frame, dim=0)
+    return data, indices, indptr, offsets

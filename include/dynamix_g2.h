@@ -184,14 +184,16 @@ int g2_plain_direct(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* item
  * data_dev (count, elem_bytes 1 or 2), the layout of FramesCompressor
  * (event.py:267-284); their order within a pixel does not matter.  pix_list
  * holds binned pixels grouped by bin; range r covers pix_list[range_off[r] ..
- * range_off[r+1]) of bin range_bin[r] (0-based).  For every pair i <= j of a
+ * range_off[r+1]) of bin range_bin[r] (0-based); CTA c of the n_ctas launched
+ * processes ranges [cta_range_off[c], cta_range_off[c+1]).  For every pair i <= j of a
  * pixel's events adds v_i v_j to numer[bin * nframes + |t_j - t_i|] and v_i to
  * sums[bin * nframes + t_i] (int64 as uint64, caller zeroes them).  max_count
  * is an upper bound of the counts (selects the shared-memory kernel). */
 int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, int32_t elem_bytes,
                      int64_t n_events, const uint32_t* offsets_dev, int64_t npix,
                      const int32_t* pix_list_dev, const int32_t* range_off_dev,
-                     const int32_t* range_bin_dev, int32_t n_ranges, int32_t nframes, int32_t n_bins,
+                     const int32_t* range_bin_dev, int32_t n_ranges, const int32_t* cta_range_off_dev,
+                     int32_t n_ctas, int32_t nframes, int32_t n_bins,
                      int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev, int32_t* err_dev,
                      void* stream);
 

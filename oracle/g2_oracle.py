@@ -25,6 +25,8 @@ agrees with this restatement to float32 rounding; the tests pin that.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 __all__ = [
@@ -292,3 +294,65 @@ def csr_correlate_exact(data, indices, indptr, offsets, shape, nframes, qmask=No
             s, e = indptr[t, r], indptr[t, r + 1]
             dense[t, r, indices[o + s:o + e]] = data[o + s:o + e]
     return g2_exact(dense, qmask, scale_factor)
+
+
+def event_pairsum_c(vol_times, vol_data, offsets, qmask, shape, nframes, n_threads=None, pixels=None):
+    """N and S (int64) of the event lists with the C restatement
+    (``g2_oracle.c``), over all binned pixels or the listed ``pixels``.
+    Same sums as :func:`event_correlate_exact`; threads give the same result."""
+    from .build_oracle import load
+    qm, n_bins, bins, sf, npix = bins_from_qmask(qmask, shape)
+    qf = qm.ravel()
+    pix = np.flatnonzero(qf > 0) if pixels is None else np.asarray(pixels, dtype=np.int64)
+    pix = pix[qf[pix] > 0].astype(np.int32)
+    b = (qf[pix] - 1).astype(np.int32)
+    T = int(nframes)
+    data = np.ascontiguousarray(vol_data)
+    if data.dtype not in (np.uint8, np.uint16):
+        data = data.astype(np.uint16 if data.size and data.max() > 255 else np.uint8)
+    times = np.ascontiguousarray(vol_times, dtype=np.int32)
+    offs = np.ascontiguousarray(offsets, dtype=np.uint32)
+    N = np.zeros((n_bins, T), np.int64)
+    S = np.zeros((n_bins, T), np.int64)
+    ptr = lambda a: a.ctypes.data
+    rc = load().g2o_event_pairsum(ptr(times), ptr(data), data.itemsize, ptr(offs), ptr(pix), ptr(b), pix.size, T,
+                                  n_bins, ptr(N), ptr(S), int(n_threads or os.cpu_count() or 1))
+    if rc:
+        raise ValueError("g2o_event_pairsum failed with status %d" % rc)
+    return N, S
+
+
+def reference_event_correlate(vol_times, vol_data, offsets, qmask, shape, nframes, scale_factors=None,
+                              n_threads=1):
+    """Run the reference's own ``event_correlator`` and ``normalize_correlation``
+    (``evtcorrelator.cl``, compiled as C into ``oracle/_ref``) with the launch
+    arguments of ``EventCorrelator.correlate`` (``event.py:162-204``).
+    Returns ``{"res_int": int32, "sums": uint32, "g2": float32}`` of shape
+    (n_bins, nframes), or None when the reference sources are not present."""
+    from .build_oracle import load_ref
+    qm, n_bins, bins, sf, npix = bins_from_qmask(qmask, shape, scale_factors)
+    data = np.ascontiguousarray(vol_data)
+    tag = {1: "u8", 2: "u16"}.get(data.itemsize)
+    if tag is None or data.dtype.kind not in "ui":
+        raise TypeError("event data must be 8- or 16-bit integers")
+    lib = load_ref(tag)
+    if lib is None:
+        return None
+    offs = np.ascontiguousarray(offsets, dtype=np.uint32)
+    if offs.size > 1 and int(np.diff(offs.astype(np.int64)).max()) > lib.g2r_max_evt_count():
+        raise ValueError("a pixel has more events than the compiled MAX_EVT_COUNT")
+    H, W = shape
+    T = int(nframes)
+    times = np.ascontiguousarray(vol_times, dtype=np.int32)
+    qmi = np.ascontiguousarray(qm, dtype=np.int32)
+    res_int = np.zeros((n_bins, T), np.int32)
+    sums = np.zeros((n_bins, T), np.uint32)
+    res = np.zeros((n_bins, T), np.float32)
+    sfa = np.ascontiguousarray(sf, dtype=np.float32)
+    ptr = lambda a: a.ctypes.data
+    # event.py:185-190 launches over shape[::-1] = (W, H) and passes shape[1] as image_height
+    rc = lib.g2r_event_correlate(ptr(times), ptr(data), ptr(offs), ptr(qmi), ptr(res_int), ptr(sums), ptr(res),
+                                 ptr(sfa), W, H, W, T, n_bins, int(n_threads))
+    if rc:
+        raise ValueError("g2r_event_correlate failed with status %d" % rc)
+    return {"res_int": res_int, "sums": sums, "g2": res}

@@ -35,3 +35,23 @@ def test_progressive_compression_rejects_overflow():
         c.process_frame(f)
     with pytest.raises(ValueError):
         c.process_frame(fr[3])
+
+
+@pytest.mark.parametrize("n_ctas", [1, 3, 152, 5000])
+def test_cta_ranges_cover_each_pixel_once(n_ctas):
+    from dynamix_gb300.engine_sparse import cta_ranges
+    rng = np.random.default_rng(n_ctas)
+    bins = np.sort(rng.integers(0, 9, 1234)).astype(np.int32)
+    ro, rb, cro = cta_ranges(bins, n_ctas)
+    assert ro[0] == 0 and ro[-1] == bins.size and np.all(np.diff(ro) > 0)
+    assert cro[0] == 0 and cro[-1] == rb.size and np.all(np.diff(cro) >= 1)
+    for r in range(rb.size):                         # every range holds one bin
+        assert np.all(bins[ro[r]:ro[r + 1]] == rb[r])
+    sizes = [ro[cro[c + 1]] - ro[cro[c]] for c in range(cro.size - 1)]
+    assert max(sizes) - min(sizes) <= 1              # equal slices
+
+
+def test_cta_ranges_empty():
+    from dynamix_gb300.engine_sparse import cta_ranges
+    ro, rb, cro = cta_ranges(np.zeros(0, np.int32), 152)
+    assert ro.tolist() == [0] and rb.size == 0 and cro.tolist() == [0, 0]

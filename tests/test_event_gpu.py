@@ -88,3 +88,41 @@ def test_event_errors(built_lib, cuda_device):
         c.correlate(z["ev_times"], z["ev_data"], z["ev_offsets"])
     with pytest.raises(AssertionError):
         c.correlate(z["ev_times"], z["ev_data"], z["ev_offsets"][:-1])
+
+
+@pytest.mark.parametrize("bright", [False, True])
+def test_many_pixels_bins_cut_across_ctas(built_lib, cuda_device, bright):
+    """More binned pixels than CTAs, bins split between CTAs and CTAs holding
+    several bins; bright counts take the global-atomic kernel."""
+    from dynamix_gb300.correlator import EventCorrelator, FramesCompressor
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    T, shape = 400, (40, 50)
+    fr = speckle_numpy(T, shape, 0.95, 0.2, seed=11, dtype=np.uint16 if bright else np.uint8)
+    if bright:
+        fr = (fr.astype(np.int64) * 20000 % 65536).astype(np.uint16)
+    qm = annular_qmask(shape, 7, 2, 30)
+    d, t, off = FramesCompressor.compress_all_stack(fr)
+    c = EventCorrelator(shape, T, int(np.diff(off).max()), qmask=qm)
+    g = c.correlate(t, d, off)
+    assert c.engine.last["kernel"] == ("global" if bright else "smem")
+    check(c, o.g2_exact(fr, qm), g)
+
+
+@pytest.mark.parametrize("name", ["event_ref_u8", "event_ref_u16", "event_ref_tall_u8"])
+def test_against_reference_event_kernel(built_lib, cuda_device, name):
+    """Bit-exact N and S against the reference's own event kernel (rows the
+    reference reaches; it skips rows y >= width of a tall image)."""
+    from dynamix_gb300.correlator import EventCorrelator
+    z = golden(name)
+    T, H, W = z["frames"].shape
+    qm = z["qmask"].copy()
+    qm[W:] = 0
+    sf = list(o.bins_from_qmask(z["qmask"], (H, W))[3])       # scale of the whole q-mask, as the reference
+    c = EventCorrelator((H, W), T, int(np.diff(z["ev_offsets"]).max()), qmask=qm, scale_factor=sf)
+    g = c.correlate(z["ev_times"], z["ev_data"], z["ev_offsets"])
+    assert np.array_equal(c.numerator, z["res_int"].astype(np.int64))
+    assert np.array_equal(c.sums, z["sums"].astype(np.int64))
+    rg = z["g2"]
+    ok = np.isfinite(rg)
+    assert np.array_equal(ok, np.isfinite(g))
+    assert np.all(np.abs(g[ok] - rg[ok]) <= 1e-5 * np.abs(rg[ok]))
