@@ -38,6 +38,14 @@ WORKLOAD = {
     "l2": "inputs (5.3 GB) larger than L2; no flush",
 }
 CPU_SAMPLE_FRAMES = 2048
+SPARSE_WORKLOAD = {
+    "workload": "sparse_2162x2068_u8_T20000_32bins",
+    "frame_shape": [2162, 2068], "nframes": 20000, "dtype": "uint8", "n_bins": 32,
+    "qmask": "32 equal annuli r 20-1000 px around (1081, 1034)", "rho": 0.99, "mean_photons": 0.005, "seed": 4,
+    "layout": "per-frame CSR (uint8 values, int32 column indices and row pointers, int64 frame offsets)",
+    "l2": "inputs (~2.4 GB CSR, ~2.3 GB event lists) larger than L2; no flush",
+}
+CPU_SAMPLE_PIXEL_STRIDE = 16
 
 
 def parse():
@@ -49,7 +57,10 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparator")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--frames", type=int, default=WORKLOAD["nframes"], help="override T (testing only)")
+    p.add_argument("--frames", type=int, default=None, help="override T (testing only)")
+    p.add_argument("--workload", default="dense", choices=["dense", "sparse", "event", "serving"],
+                   help="dense: 514x1030x10k u8 Gram path (default); sparse / event: 2162x2068x20k CSR or "
+                        "per-pixel event lists through the pair-sum path")
     return p.parse_args()
 
 
@@ -351,8 +362,405 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------- sparse / event
+def make_sparse_workload(dev, T):
+    from dynamix_gb300.speckle import annular_qmask, speckle_csr_torch
+    H, W = SPARSE_WORKLOAD["frame_shape"]
+    qmask = annular_qmask((H, W), SPARSE_WORKLOAD["n_bins"], 20.0, 1000.0, center=(1081, 1034))
+    csr = speckle_csr_torch(T, (H, W), SPARSE_WORKLOAD["rho"], SPARSE_WORKLOAD["mean_photons"],
+                            seed=SPARSE_WORKLOAD["seed"], device=dev)
+    return csr, qmask
+
+
+def event_stats(ev_off, qmask):
+    """(binned events, pair operations sum_p n_p (n_p + 1) / 2 over binned pixels)."""
+    import torch
+    n = (ev_off[1:].to(torch.int64) - ev_off[:-1].to(torch.int64))
+    binned = torch.from_numpy((qmask.ravel() > 0)).to(n.device)
+    nb = n[binned]
+    return int(nb.sum().item()), int((nb * (nb + 1) // 2).sum().item())
+
+
+def cpu_event_sample(times, data, offs, qmask, shape, T, stride):
+    """Seconds of the C pair-sum restatement on every ``stride``-th binned
+    pixel (all host threads), and the pair operations of that sample."""
+    import numpy as np
+    from oracle.g2_oracle import event_pairsum_c
+    pix = np.flatnonzero(qmask.ravel() > 0)[::stride]
+    n = (offs[pix + 1].astype(np.int64) - offs[pix].astype(np.int64))
+    pairs = int((n * (n + 1) // 2).sum())
+    t0 = time.perf_counter()
+    event_pairsum_c(times, data, offs, qmask, shape, T, pixels=pix)
+    return time.perf_counter() - t0, pairs
+
+
+def run_sparse(args):
+    import numpy as np
+    import torch
+
+    from dynamix_gb300 import build as b
+    from dynamix_gb300.correlator import EventCorrelator, SparseCorrelator
+
+    rank, world, local = dist_info()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    b.build(force=False)
+    T = args.frames
+    H, W = SPARSE_WORKLOAD["frame_shape"]
+    (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T)
+    offsets = offsets.to(torch.int32)              # one index type (int32) for the whole CSR stack
+    sc = SparseCorrelator((H, W), T, qmask=qmask)
+    ev_times, ev_data, ev_off = (x.clone() for x in sc.engine.to_events(data, indices, indptr, offsets, 4,
+                                                                          int(data.numel())))
+    torch.cuda.synchronize(dev)
+    n_elem = int(data.numel())
+    n_binned_events, pairs = event_stats(ev_off, qmask)
+    if args.workload == "event":
+        corr = EventCorrelator((H, W), T, 1, qmask=qmask)
+        inputs = (ev_times, ev_data, ev_off)
+        events_engine = corr.engine
+        del data, indices, indptr, offsets
+    else:
+        corr = sc
+        inputs = (data, indices, indptr, offsets)
+        events_engine = sc.engine.events
+        del ev_times, ev_data
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(max(args.warmup, 3)):
+        corr.correlate_device(*inputs)
+    corr.engine.check_error()
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    sampler = ClockSampler(uuid)
+    events_engine.profile = True
+    barrier()
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step_events = []
+    for _ in range(args.steps):
+        corr.correlate_device(*inputs)
+        step_events.append(events_engine.take_events())
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    events_engine.profile = False
+    corr.engine.check_error()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    stages = {}
+    for ev in step_events:
+        for k, v in events_engine.stage_times(ev).items():
+            stages[k] = stages.get(k, 0.0) + v / args.steps
+    info = dict(events_engine.last)
+
+    # algorithmic bytes per step (each array read or written once)
+    npix = H * W
+    P_b = int((qmask > 0).sum())
+    n_bins = SPARSE_WORKLOAD["n_bins"]
+    transpose_bytes = 14 * n_elem + 8 * (H + 1) * T + 16 * npix
+    pair_bytes = 5 * n_binned_events + 12 * P_b + 16 * n_bins * T
+    norm_bytes = 6 * 8 * n_bins * T
+    step_bytes = pair_bytes + norm_bytes + (transpose_bytes if args.workload == "sparse" else 0)
+    peaks, peak_kind = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    pair_ms = stages.get("pairsum", float("nan"))
+    achieved = pair_bytes / (pair_ms / 1e3) / 1e9
+    stage_report = {"pairsum": {"ms": pair_ms, "GB_per_s": achieved, "bytes": pair_bytes,
+                                "pair_ops_per_s": pairs / (pair_ms / 1e3)},
+                    "normalize": {"ms": stages.get("normalize", float("nan")), "bytes": norm_bytes}}
+    launches = 3   # pair sums, denominator, finalize
+    if args.workload == "sparse":
+        tms = stages.get("transpose", float("nan"))
+        stage_report["transpose"] = {"ms": tms, "GB_per_s": transpose_bytes / (tms / 1e3) / 1e9,
+                                     "bytes": transpose_bytes, "kernels": "count, scan (3), scatter"}
+        launches += 5
+    cfg = dict(SPARSE_WORKLOAD, nframes=T, workload=SPARSE_WORKLOAD["workload"].replace(
+        "sparse", "sparse_csr" if args.workload == "sparse" else "event_lists"),
+        parallelism="replicas" if world > 1 else "single", n_elements=n_elem,
+        binned_pixels=P_b, binned_events=n_binned_events, pair_ops=pairs)
+    line = {
+        "metric": "g2_frames_per_s", "value": world * T / (ms / 1e3), "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+        "hbm_GB_per_s_step": step_bytes / (ms / 1e3) / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": profile_traffic("event_pairsum_2162x2068_T20000.md"), "kernel": "g2_event_pairsum",
+                     "peak_source": "%s hbm_gbs" % peak_kind, "algorithmic_bytes_per_launch": pair_bytes,
+                     "launch_ms": pair_ms,
+                     "note": "bound by shared-memory atomics (one per event pair), not by HBM"},
+        "stages": stage_report, "clocks": clocks, "gpu_launches": launches * args.steps, "plan": info,
+    }
+
+    if not args.no_e2e:
+        host = [x.cpu().pin_memory() for x in inputs]
+        corr.correlate(*host)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            corr.correlate(*host)
+        barrier()
+        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+        line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
+                       "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in host)),
+                       "d2h_bytes_per_step": int(n_bins * T * 4 + 4), "ms_per_step": e2e_ms}
+        del host
+
+    if not args.no_cpu and rank == 0:
+        if args.workload == "event":
+            t_h, d_h, o_h = (x.cpu().numpy() for x in inputs)
+        else:
+            t_h, d_h, o_h = (x.cpu().numpy() for x in sc.engine.to_events(*inputs, 4, n_elem))
+        o_h = o_h.view(np.uint32)
+        secs, sample_pairs = cpu_event_sample(t_h, d_h, o_h, qmask, (H, W), T, CPU_SAMPLE_PIXEL_STRIDE)
+        ncores = os.cpu_count()
+        full = secs * pairs / max(sample_pairs, 1)
+        line["cpu_baseline"] = {
+            "value": T / full, "unit": "frames/s", "cores": ncores, "kind": "port",
+            "sample": "event pair sums (C restatement of evtcorrelator.cl:3-47, int64, %d threads) over every "
+                      "%dth binned pixel: %d pair ops in %.2f s, scaled by pair ops to the %d of all %d frames; "
+                      "the CSR-to-event step is not included" % (ncores, CPU_SAMPLE_PIXEL_STRIDE, sample_pairs,
+                                                                secs, pairs, T)}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_sparse_reference(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    T = args.frames
+    H, W = SPARSE_WORKLOAD["frame_shape"]
+    dev = torch.device("cuda", local)
+    from dynamix_gb300 import build as b
+    from dynamix_gb300.correlator import SparseCorrelator
+    b.build(force=False)
+    # the CSR stack is generated on the device and turned into event lists there
+    (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T)
+    offsets = offsets.to(torch.int32)
+    sc = SparseCorrelator((H, W), T, qmask=qmask)
+    t_h, d_h, o_h = (x.cpu().numpy() for x in sc.engine.to_events(data, indices, indptr, offsets, 4,
+                                                                   int(data.numel())))
+    o_h = o_h.view(np.uint32)
+    del data, indices, indptr, offsets, sc
+    ev_off = torch.from_numpy(o_h.view(np.int32))
+    _, pairs = event_stats(ev_off, qmask)
+    for _ in range(args.warmup):
+        cpu_event_sample(t_h, d_h, o_h, qmask, (H, W), T, CPU_SAMPLE_PIXEL_STRIDE * 4)
+    ts = []
+    for _ in range(args.steps):
+        secs, sp = cpu_event_sample(t_h, d_h, o_h, qmask, (H, W), T, CPU_SAMPLE_PIXEL_STRIDE * 4)
+        ts.append(secs * pairs / max(sp, 1))
+    t = sum(ts) / len(ts)
+    v = T / t
+    ncores = os.cpu_count()
+    line = {
+        "metric": "g2_frames_per_s", "value": v, "unit": "frames/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": dict(SPARSE_WORKLOAD, nframes=T, workload=SPARSE_WORKLOAD["workload"].replace(
+            "sparse", "event_lists")),
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": ncores, "kind": "port",
+                         "sample": "each step: event pair sums (C restatement, %d threads) over every %dth binned "
+                                   "pixel, scaled by pair ops to all %d pair ops" % (
+                                       ncores, CPU_SAMPLE_PIXEL_STRIDE * 4, pairs)},
+        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------- serving mix
+SERVING_WORKLOAD = {
+    "workload": "serving_mix",
+    "frame_shapes": [[256, 256], [514, 1030], [1062, 1028]], "nframes": "log-uniform 500-20000",
+    "n_bins": "uniform 4-64", "dtype": "uint8 or uint16 (even odds)", "rho": 0.99, "mean_photons": 1.0,
+    "qmask": "n_bins equal annuli r 0 to 0.4 min(H, W) around the frame centre", "seed": 5, "jobs": 24,
+    "hbm_budget_gb": 150,
+    "inputs": "device-resident frame pools (one per shape and dtype, 20,000 frames); a job's frames are the "
+              "first T frames of its pool, used in place (the server copies nothing in)",
+}
+
+
+def make_serving_jobs(dev, n_jobs, seed):
+    import numpy as np
+    import torch
+    from dynamix_gb300.speckle import annular_qmask, speckle_torch
+    rng = np.random.default_rng(seed)
+    shapes = [tuple(s) for s in SERVING_WORKLOAD["frame_shapes"]]
+    spec = []
+    for _ in range(n_jobs):
+        shape = shapes[int(rng.integers(len(shapes)))]
+        T = int(round(math.exp(rng.uniform(math.log(500), math.log(20000)))))
+        nb = int(rng.integers(4, 65))
+        u16 = bool(rng.integers(2))
+        spec.append((shape, T, nb, u16))
+    pools = {}
+    for shape in shapes:
+        need = [T for s, T, _, _ in spec if s == shape]
+        if not need:
+            continue
+        u8 = speckle_torch(max(need), shape, SERVING_WORKLOAD["rho"], SERVING_WORKLOAD["mean_photons"],
+                           seed=seed + shapes.index(shape), device=dev)
+        pools[(shape, False)] = u8
+        if any(s == shape and u for s, _, _, u in spec):
+            w = torch.empty(u8.shape, dtype=torch.int16, device=dev)
+            w.copy_(u8)
+            pools[(shape, True)] = w.view(torch.uint16)
+    masks = {}
+    jobs = []
+    for shape, T, nb, u16 in spec:
+        if (shape, nb) not in masks:
+            masks[(shape, nb)] = annular_qmask(shape, nb, 0.0, 0.4 * min(shape))
+        qm = masks[(shape, nb)]
+        npx = int((qm > 0).sum())
+        jobs.append({"frames": pools[(shape, u16)][:T], "qmask": qm, "shape": shape, "T": T, "n_bins": nb,
+                     "dtype": "uint16" if u16 else "uint8", "gram_ops": float(npx) * T * (T + 1)})
+    return jobs, pools
+
+
+def drive(server, jobs, arrivals):
+    """Submit job i at ``arrivals[i]`` seconds after the start, serve until all
+    are done; returns (requests, wall seconds)."""
+    t0 = time.perf_counter()
+    reqs = [None] * len(jobs)
+    nxt = 0
+    while True:
+        now = time.perf_counter() - t0
+        while nxt < len(jobs) and arrivals[nxt] <= now:
+            reqs[nxt] = server.submit(jobs[nxt]["frames"], jobs[nxt]["qmask"])
+            reqs[nxt].t_submit = t0 + arrivals[nxt]
+            nxt += 1
+        worked = server.step()
+        if nxt == len(jobs) and server.idle():
+            break
+        if not worked:
+            time.sleep(0.0001)
+    wall = time.perf_counter() - t0
+    for r in reqs:
+        r.wait()
+    return reqs, wall
+
+
+def latency_summary(reqs, wall, jobs):
+    import numpy as np
+    lat = np.array([r.latency for r in reqs]) * 1e3
+    frames = sum(j["T"] for j in jobs)
+    ops = sum(j["gram_ops"] for j in jobs)
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "wall_s": wall,
+            "jobs_per_s": len(reqs) / wall, "frames_per_s": frames / wall, "gram_tops": ops / wall / 1e12}
+
+
+def run_serving(args):
+    import numpy as np
+    import torch
+
+    from dynamix_gb300 import build as b
+    from dynamix_gb300.serving import G2Server
+
+    rank, world, local = dist_info()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    b.build(force=False)
+    n_jobs = SERVING_WORKLOAD["jobs"]
+    t_gen = time.perf_counter()
+    jobs, pools = make_serving_jobs(dev, n_jobs, SERVING_WORKLOAD["seed"])
+    torch.cuda.synchronize(dev)
+    t_gen = time.perf_counter() - t_gen
+    budget = SERVING_WORKLOAD["hbm_budget_gb"] * 1e9
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+
+    def server(kind):
+        if kind == "batched":
+            return G2Server(hbm_budget=budget)
+        if kind == "one_at_a_time":
+            return G2Server(hbm_budget=budget, max_active=1, slice_ops=1e30)
+        return G2Server(hbm_budget=budget, max_active=1, slice_ops=1e30, method="plain")
+
+    # warm-up (layouts of every q-mask, allocator pools) and the reference results
+    ref, _ = drive(server("batched"), jobs, [0.0] * n_jobs)
+    # service capacity of one-job-at-a-time execution (all jobs queued at t = 0)
+    seq_reqs, seq_wall = drive(server("one_at_a_time"), jobs, [0.0] * n_jobs)
+    capacity = n_jobs / seq_wall
+    rng = np.random.default_rng(SERVING_WORKLOAD["seed"] + 100)
+    gaps = rng.exponential(1.0, n_jobs)
+    sampler = ClockSampler(uuid)
+    sampler.start()
+    sweep = []
+    identical = True
+    for load in (0.5, 0.8, 1.0, 1.5):
+        rate = load * capacity
+        arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
+        row = {"load_vs_one_at_a_time_capacity": load, "rate_jobs_per_s": rate}
+        for kind in ("batched", "one_at_a_time"):
+            reqs, wall = drive(server(kind), jobs, arrivals)
+            row[kind] = latency_summary(reqs, wall, jobs)
+            identical &= all(np.array_equal(r.numerator, q.numerator) and np.array_equal(r.denominator, q.denominator)
+                             for r, q in zip(reqs, ref))
+        row["p99_speedup"] = row["one_at_a_time"]["p99_ms"] / row["batched"]["p99_ms"]
+        sweep.append(row)
+    clocks = sampler.stop()
+    plain = None
+    if not args.no_plain:
+        p_reqs, p_wall = drive(server("plain"), jobs, [0.0] * n_jobs)
+        plain = latency_summary(p_reqs, p_wall, jobs)
+        identical &= all(np.array_equal(r.numerator, q.numerator) for r, q in zip(p_reqs, ref))
+    top = sweep[-1]
+    line = {
+        "metric": "serving_p99_latency_ms", "value": top["batched"]["p99_ms"], "unit": "ms", "n_gpus": 1,
+        "steps": n_jobs, "warmup": 1, "higher_is_better": False, "scaling": "none", "vs_baseline": None,
+        "dtype": "u8/u16", "data": "synthetic",
+        "config": dict(SERVING_WORKLOAD, pool_generation_s=t_gen),
+        "jobs": [{k: (list(v) if k == "shape" else v) for k, v in j.items() if k not in ("frames", "qmask")}
+                 for j in jobs],
+        "one_at_a_time_capacity_jobs_per_s": capacity, "sweep": sweep,
+        "plain_one_at_a_time_all_queued": plain, "results_identical_across_runs": bool(identical),
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "serving":
+        return run_serving(args)
+    if args.workload in ("sparse", "event"):
+        if args.frames is None:
+            args.frames = SPARSE_WORKLOAD["nframes"]
+        return (run_sparse_reference if args.impl == "reference" else run_sparse)(args)
+    if args.frames is None:
+        args.frames = WORKLOAD["nframes"]
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -39,11 +39,12 @@ class EventCorrelator(BaseCorrelator):
         self.total_events_count = total_events_count or max_events_count * int(np.prod(self.shape))
 
     def _check_event_arrays(self, vol_times, vol_data, offsets):
+        # event.py:104-115; len() also serves device tensors
         for arr in (vol_times, vol_data, offsets):
             assert np.ndim(arr) == 1
-        assert np.size(vol_times) == np.size(vol_data)
-        assert np.size(offsets) == int(np.prod(self.shape)) + 1
-        numels = int(np.size(vol_data))
+        assert len(vol_times) == len(vol_data)
+        assert len(offsets) == int(np.prod(self.shape)) + 1
+        numels = len(vol_data)
         if numels > self.total_events_count:
             if self.allow_reallocate:
                 self.total_events_count = numels

@@ -6,13 +6,18 @@
 // indptr[t * (H+1) + r] .. indptr[t * (H+1) + r + 1] are the elements of row r
 // relative to offsets[t]; indices[] is the column inside the row, data[] the
 // count.  The transposition is a counting sort by pixel:
-//   1. count   : events per pixel (global atomics)
+//   1. count   : events per pixel
 //   2. scan    : exclusive prefix sum of the counts -> event offsets
-//   3. scatter : each element takes the next slot of its pixel (atomic
-//                cursor) and writes (t, v); the order inside a pixel is free
-//                because G6 uses |t_j - t_i|.
-// A warp walks one row of one frame (rows hold a handful of elements), a
-// block one frame.
+//   3. scatter : each element goes to the slot of its pixel given by the
+//                number of earlier frames holding that pixel.
+// Row kernels (image rows up to ROW_MAX_W pixels): one warp owns one image row
+// for all frames, its lanes take 32 consecutive frames at a time, and the
+// per-pixel counters of the row live in the warp's shared memory, so neither
+// pass needs a global atomic.  The scatter ranks the elements of a 32-frame
+// batch per pixel with a bit mask (bit = frame of the batch), so every pixel's
+// events come out in ascending frame order -- the layout FramesCompressor
+// builds (event.py:267-284).  Wider rows use the walk kernels (a warp per row
+// of a frame, global atomics, order inside a pixel unspecified).
 #include "g2_ptx.cuh"
 #include "g2_host.h"
 
@@ -40,7 +45,7 @@ __global__ void __launch_bounds__(THREADS)
     for (int r = warp; r < H; r += WARPS) {
       const int64_t s = base + static_cast<int64_t>(ip[r]);
       const int64_t e = base + static_cast<int64_t>(ip[r + 1]);
-      if (s < base || e < s || e > fend || e > n_elem) {
+      if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
         bad = true;
         continue;
       }
@@ -64,6 +69,121 @@ __global__ void __launch_bounds__(THREADS)
         }
       }
     }
+  }
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+constexpr int ROW_MAX_W = 29000;       // 2 x W words of shared memory per warp in the scatter
+
+// Counts of one image row over all frames (one warp per row).
+template <typename Ti>
+__global__ void __launch_bounds__(256)
+    row_count_kernel(const Ti* __restrict__ indices, const Ti* __restrict__ indptr, const Ti* __restrict__ offsets,
+                     int64_t n_elem, int32_t T, int32_t H, int32_t W, int rows_per_cta,
+                     uint32_t* __restrict__ counts, int32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * rows_per_cta + warp;
+  if (warp >= rows_per_cta || r >= H) return;  // warp-uniform; no block barrier below
+  uint32_t* cnt = sm + static_cast<int64_t>(warp) * W;
+  for (int i = lane; i < W; i += 32) cnt[i] = 0;
+  __syncwarp();
+  bool bad = false;
+  for (int64_t t0 = 0; t0 < T; t0 += 32) {
+    const int64_t t = t0 + lane;
+    if (t >= T) continue;
+    const int64_t base = static_cast<int64_t>(offsets[t]);
+    const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
+    const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
+    const int64_t s = base + static_cast<int64_t>(ip[0]);
+    const int64_t e = base + static_cast<int64_t>(ip[1]);
+    if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+      bad = true;
+      continue;
+    }
+#pragma unroll 4
+    for (int64_t k = s; k < e; ++k) {
+      const int64_t col = static_cast<int64_t>(indices[k]);
+      if (col < 0 || col >= W) {
+        bad = true;
+        continue;
+      }
+      atomicAdd(&cnt[col], 1u);
+    }
+  }
+  __syncwarp();
+  uint32_t* out = counts + static_cast<int64_t>(r) * W;
+  for (int i = lane; i < W; i += 32)
+    if (cnt[i]) out[i] += cnt[i];  // the row belongs to this warp alone
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// Scatter of one image row over all frames, events of a pixel in frame order.
+template <typename Tv, typename Ti>
+__global__ void __launch_bounds__(256)
+    row_scatter_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices, const Ti* __restrict__ indptr,
+                       const Ti* __restrict__ offsets, int64_t n_elem, int32_t T, int32_t H, int32_t W,
+                       int rows_per_cta, const uint32_t* __restrict__ ev_off, int32_t* __restrict__ ev_times,
+                       Tv* __restrict__ ev_data, int32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * rows_per_cta + warp;
+  if (warp >= rows_per_cta || r >= H) return;  // warp-uniform; no block barrier below
+  uint32_t* cur = sm + static_cast<int64_t>(warp) * 2 * W;  // next free slot of each pixel
+  uint32_t* msk = cur + W;                                    // frames of the batch holding the pixel
+  const uint32_t* row_off = ev_off + static_cast<int64_t>(r) * W;
+  for (int i = lane; i < W; i += 32) {
+    cur[i] = row_off[i];
+    msk[i] = 0;
+  }
+  __syncwarp();
+  bool bad = false;
+  const uint32_t bit = 1u << lane;
+  for (int64_t t0 = 0; t0 < T; t0 += 32) {
+    const int64_t t = t0 + lane;
+    int64_t s = 0, e = 0;
+    if (t < T) {
+      const int64_t base = static_cast<int64_t>(offsets[t]);
+      const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
+      const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
+      s = base + static_cast<int64_t>(ip[0]);
+      e = base + static_cast<int64_t>(ip[1]);
+      if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+        bad = true;
+        s = e = 0;
+      }
+    }
+    // 1. mark the frames of the batch that hold each pixel
+    for (int64_t k = s; k < e; ++k) {
+      const int64_t col = static_cast<int64_t>(indices[k]);
+      if (col < 0 || col >= W) continue;  // reported by the count pass
+      if (atomicOr(&msk[col], bit) & bit) bad = true;  // a column twice in one row
+    }
+    __syncwarp();
+    // 2. slot = next free slot + earlier frames of the batch holding the pixel
+    for (int64_t k = s; k < e; ++k) {
+      const int64_t col = static_cast<int64_t>(indices[k]);
+      if (col < 0 || col >= W) continue;
+      const uint32_t slot = cur[col] + __popc(msk[col] & (bit - 1u));
+      if (slot < row_off[col + 1]) {
+        ev_times[slot] = static_cast<int32_t>(t);
+        ev_data[slot] = data[k];
+      } else {
+        bad = true;
+      }
+    }
+    __syncwarp();
+    // 3. the last frame of the batch holding the pixel advances its cursor
+    for (int64_t k = s; k < e; ++k) {
+      const int64_t col = static_cast<int64_t>(indices[k]);
+      if (col < 0 || col >= W) continue;
+      const uint32_t m = msk[col];
+      if (m != 0u && (m >> lane) == 1u) {
+        cur[col] += __popc(m);
+        msk[col] = 0u;
+      }
+    }
+    __syncwarp();
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
@@ -197,6 +317,59 @@ int walk(const void* data, int32_t elem_bytes, const void* indices, const void* 
 }
 }  // namespace
 
+namespace {
+// Warps (image rows) per CTA so that a CTA holds about 64 KB of row counters.
+int rows_per_cta(int32_t W, int words_per_px) {
+  const int64_t per_row = static_cast<int64_t>(W) * words_per_px * 4;
+  int64_t r = 65536 / per_row;
+  return static_cast<int>(r < 1 ? 1 : (r > 8 ? 8 : r));
+}
+
+template <typename K>
+bool allow_smem(K kernel, int64_t bytes) {
+  if (bytes <= 48 * 1024) return true;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)) ==
+         cudaSuccess;
+}
+
+int row_count(const void* indices, const void* indptr, const void* offsets, int32_t index_bytes, int64_t n_elem,
+              int32_t T, int32_t H, int32_t W, uint32_t* counts, int32_t* err, void* stream) {
+  using namespace g2;
+  const int rpc = rows_per_cta(W, 1);
+  const int64_t smem = static_cast<int64_t>(rpc) * W * 4;
+  const unsigned grid = static_cast<unsigned>((H + rpc - 1) / rpc);
+  cudaStream_t st = as_stream(stream);
+  if (index_bytes == 4) {
+    if (!allow_smem(csr::row_count_kernel<uint32_t>, smem)) return G2_ERR_CUDA;
+    csr::row_count_kernel<uint32_t><<<grid, rpc * 32, smem, st>>>(
+        reinterpret_cast<const uint32_t*>(indices), reinterpret_cast<const uint32_t*>(indptr),
+        reinterpret_cast<const uint32_t*>(offsets), n_elem, T, H, W, rpc, counts, err);
+  } else {
+    if (!allow_smem(csr::row_count_kernel<int64_t>, smem)) return G2_ERR_CUDA;
+    csr::row_count_kernel<int64_t><<<grid, rpc * 32, smem, st>>>(
+        reinterpret_cast<const int64_t*>(indices), reinterpret_cast<const int64_t*>(indptr),
+        reinterpret_cast<const int64_t*>(offsets), n_elem, T, H, W, rpc, counts, err);
+  }
+  return launch_status();
+}
+
+template <typename Tv, typename Ti>
+int row_scatter_t(const void* data, const void* indices, const void* indptr, const void* offsets, int64_t n_elem,
+                  int32_t T, int32_t H, int32_t W, const uint32_t* ev_off, int32_t* ev_times, void* ev_data,
+                  int32_t* err, cudaStream_t st) {
+  using namespace g2;
+  const int rpc = rows_per_cta(W, 2);
+  const int64_t smem = static_cast<int64_t>(rpc) * W * 8;
+  const unsigned grid = static_cast<unsigned>((H + rpc - 1) / rpc);
+  if (!allow_smem(csr::row_scatter_kernel<Tv, Ti>, smem)) return G2_ERR_CUDA;
+  csr::row_scatter_kernel<Tv, Ti><<<grid, rpc * 32, smem, st>>>(
+      reinterpret_cast<const Tv*>(data), reinterpret_cast<const Ti*>(indices), reinterpret_cast<const Ti*>(indptr),
+      reinterpret_cast<const Ti*>(offsets), n_elem, T, H, W, rpc, ev_off, ev_times, reinterpret_cast<Tv*>(ev_data),
+      err);
+  return launch_status();
+}
+}  // namespace
+
 extern "C" int g2_csr_count(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
                             int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
                             uint32_t* counts_dev, int32_t* err_dev, void* stream) {
@@ -204,6 +377,9 @@ extern "C" int g2_csr_count(const void* indices_dev, const void* indptr_dev, con
   if (!indices_dev || !indptr_dev || !offsets_dev || !counts_dev || !err_dev) return G2_ERR_ARG;
   if ((index_bytes != 4 && index_bytes != 8) || n_elem < 0 || nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
+  if (width <= csr::ROW_MAX_W)
+    return row_count(indices_dev, indptr_dev, offsets_dev, index_bytes, n_elem, nframes, height, width, counts_dev,
+                     err_dev, stream);
   return walk<false>(indices_dev, 1, indices_dev, indptr_dev, offsets_dev, index_bytes, n_elem, nframes, height,
                      width, counts_dev, nullptr, nullptr, nullptr, err_dev, stream);
 }
@@ -235,6 +411,20 @@ extern "C" int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const vo
   if ((elem_bytes != 1 && elem_bytes != 2) || (index_bytes != 4 && index_bytes != 8) || n_elem < 0 ||
       nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
+  if (width <= csr::ROW_MAX_W) {
+    cudaStream_t st = as_stream(stream);
+    if (elem_bytes == 1 && index_bytes == 4)
+      return row_scatter_t<uint8_t, uint32_t>(data_dev, indices_dev, indptr_dev, offsets_dev, n_elem, nframes, height,
+                                              width, ev_offsets_dev, ev_times_dev, ev_data_dev, err_dev, st);
+    if (elem_bytes == 1)
+      return row_scatter_t<uint8_t, int64_t>(data_dev, indices_dev, indptr_dev, offsets_dev, n_elem, nframes, height,
+                                             width, ev_offsets_dev, ev_times_dev, ev_data_dev, err_dev, st);
+    if (index_bytes == 4)
+      return row_scatter_t<uint16_t, uint32_t>(data_dev, indices_dev, indptr_dev, offsets_dev, n_elem, nframes,
+                                               height, width, ev_offsets_dev, ev_times_dev, ev_data_dev, err_dev, st);
+    return row_scatter_t<uint16_t, int64_t>(data_dev, indices_dev, indptr_dev, offsets_dev, n_elem, nframes, height,
+                                            width, ev_offsets_dev, ev_times_dev, ev_data_dev, err_dev, st);
+  }
   return walk<true>(data_dev, elem_bytes, indices_dev, indptr_dev, offsets_dev, index_bytes, n_elem, nframes,
                     height, width, cursor_dev, ev_offsets_dev, ev_times_dev, ev_data_dev, err_dev, stream);
 }

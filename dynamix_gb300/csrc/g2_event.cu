@@ -26,11 +26,12 @@
 namespace g2 {
 namespace ev {
 
-constexpr int THREADS = 512;
+constexpr int THREADS = 768;
 constexpr int WARPS = THREADS / 32;
-constexpr int EV = 256;                    // events of one pixel staged per block of pairs
+constexpr int EV = 128;                    // events of one pixel staged per block of pairs
 constexpr uint32_t DRAIN = 1u << 31;
 constexpr int SMEM_FIXED = WARPS * 2 * EV * 4;
+constexpr int SMEM_STATIC = WARPS * 8;    // block-reduction slots
 
 __device__ __forceinline__ void add_counter(uint32_t* c, unsigned long long* g, uint32_t x) {
   const uint32_t old = atomicAdd(c, x);
@@ -40,15 +41,74 @@ __device__ __forceinline__ void add_counter(uint32_t* c, unsigned long long* g, 
   }
 }
 
+// Pair sums of one pixel's events by one warp.  FAST: every counter of the
+// range is known to stay below 2^32 (checked per range from its event count),
+// so the shared adds need no returned value (the warp does not wait on them)
+// and no drain check.
+template <bool FAST, typename Tv>
+__device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, const Tv* __restrict__ data,
+                                            int64_t base, int n, int T, uint32_t maxc, uint32_t* hist,
+                                            uint32_t* shist, unsigned long long* gN, unsigned long long* gS,
+                                            uint32_t* bufA, uint32_t* bufB, int lane, bool& bad) {
+  for (int ib = 0; ib < n; ib += EV) {
+    const int na = min(EV, n - ib);
+    for (int e = lane; e < na; e += 32) {
+      const int32_t t = times[base + ib + e];
+      const uint32_t v = static_cast<uint32_t>(data[base + ib + e]);
+      const bool ok = t >= 0 && t < T && v <= maxc;
+      bad |= !ok;
+      bufA[e] = ok ? (static_cast<uint32_t>(t) << 16) | v : 0u;
+      if (ok && v) {
+        if (FAST)
+          atomicAdd(&shist[t], v);
+        else
+          add_counter(&shist[t], &gS[t], v);
+      }
+    }
+    __syncwarp();
+    for (int jb = ib; jb < n; jb += EV) {
+      const int nb = min(EV, n - jb);
+      const uint32_t* B = bufA;
+      if (jb != ib) {
+        for (int e = lane; e < nb; e += 32) {
+          const int32_t t = times[base + jb + e];
+          const uint32_t v = static_cast<uint32_t>(data[base + jb + e]);
+          bufB[e] = (t >= 0 && t < T && v <= maxc) ? (static_cast<uint32_t>(t) << 16) | v : 0u;
+        }
+        __syncwarp();
+        B = bufB;
+      }
+      for (int i = 0; i < na; ++i) {
+        const uint32_t wi = bufA[i];
+        const uint32_t vi = wi & 0xFFFFu;
+        if (vi == 0) continue;  // warp-uniform
+        const int ti = static_cast<int>(wi >> 16);
+        for (int j = (jb == ib ? i : 0) + lane; j < nb; j += 32) {
+          const uint32_t wj = B[j];
+          const int lag = abs(static_cast<int>(wj >> 16) - ti);
+          const uint32_t prod = vi * (wj & 0xFFFFu);
+          if (FAST) {
+            atomicAdd(&hist[lag], prod);  // a zero product (invalid event) adds nothing
+          } else if (prod) {
+            add_counter(&hist[lag], &gN[lag], prod);
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
 template <typename Tv>
 __global__ void __launch_bounds__(THREADS, 1)
     pairs_smem_kernel(const int32_t* __restrict__ times, const Tv* __restrict__ data,
                       const uint32_t* __restrict__ offsets, const int32_t* __restrict__ pix_list,
                       const int32_t* __restrict__ range_off, const int32_t* __restrict__ range_bin,
                       const int32_t* __restrict__ cta_range_off, int n_ranges, int64_t n_events,
-                      int64_t npix, int32_t T, int n_bins, unsigned long long* __restrict__ numer,
+                      int64_t npix, int32_t T, int n_bins, uint32_t maxc, unsigned long long* __restrict__ numer,
                       unsigned long long* __restrict__ sums, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
+  __shared__ unsigned long long s_red[WARPS];
   uint32_t* hist = sm;              // [T] lag sums of this range's bin
   uint32_t* shist = sm + T;         // [T] frame sums
   uint32_t* evbuf = sm + 2 * T;     // [WARPS][2][EV] staged events (t << 16 | v)
@@ -57,6 +117,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint32_t* bufB = bufA + EV;
   bool bad = false;
   for (int i = threadIdx.x; i < 2 * T; i += THREADS) sm[i] = 0;
+  const unsigned long long max2 = static_cast<unsigned long long>(maxc) * maxc;
   // this CTA's ranges (a contiguous slice of the bin-ordered pixel list, cut
   // at bin boundaries); the counters are flushed once per range
   const int r_end = min(cta_range_off[blockIdx.x + 1], n_ranges);
@@ -66,7 +127,23 @@ __global__ void __launch_bounds__(THREADS, 1)
       bad = true;
       continue;  // uniform over the CTA
     }
-    __syncthreads();  // counters zeroed (start, or the previous flush)
+    // events of the range: a lag counter gains at most max^2 per event and a
+    // frame counter at most max per pixel, so max^2 * events < 2^32 keeps
+    // every counter of the range in uint32 without draining
+    unsigned long long ev = 0;
+    for (int li = range_off[r] + threadIdx.x; li < range_off[r + 1]; li += THREADS) {
+      const int32_t p = pix_list[li];
+      if (p >= 0 && p < npix) {
+        const uint32_t a = offsets[p], b = offsets[p + 1];
+        if (b >= a) ev += b - a;
+      }
+    }
+    for (int o = 16; o; o >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, o);
+    if (lane == 0) s_red[warp] = ev;
+    __syncthreads();  // also: counters zeroed (start, or the previous flush)
+    unsigned long long tot = 0;
+    for (int w = 0; w < WARPS; ++w) tot += s_red[w];
+    const bool fast = max2 == 0 || tot < (1ull << 32) / max2;
     unsigned long long* gN = numer + static_cast<int64_t>(bin) * T;
     unsigned long long* gS = sums + static_cast<int64_t>(bin) * T;
     for (int li = range_off[r] + warp; li < range_off[r + 1]; li += WARPS) {
@@ -82,45 +159,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         continue;
       }
       const int n = static_cast<int>(end - base);
-      for (int ib = 0; ib < n; ib += EV) {
-        const int na = min(EV, n - ib);
-        for (int e = lane; e < na; e += 32) {
-          const int32_t t = times[base + ib + e];
-          const uint32_t v = static_cast<uint32_t>(data[base + ib + e]);
-          const bool ok = t >= 0 && t < T;
-          bad |= !ok;
-          bufA[e] = ok ? (static_cast<uint32_t>(t) << 16) | v : 0u;
-          if (ok && v) add_counter(&shist[t], &gS[t], v);
-        }
-        __syncwarp();
-        for (int jb = ib; jb < n; jb += EV) {
-          const int nb = min(EV, n - jb);
-          const uint32_t* B = bufA;
-          if (jb != ib) {
-            for (int e = lane; e < nb; e += 32) {
-              const int32_t t = times[base + jb + e];
-              const uint32_t v = static_cast<uint32_t>(data[base + jb + e]);
-              bufB[e] = (t >= 0 && t < T) ? (static_cast<uint32_t>(t) << 16) | v : 0u;
-            }
-            __syncwarp();
-            B = bufB;
-          }
-          for (int i = 0; i < na; ++i) {
-            const uint32_t wi = bufA[i];
-            const uint32_t vi = wi & 0xFFFFu;
-            if (vi == 0) continue;  // warp-uniform
-            const int ti = static_cast<int>(wi >> 16);
-            for (int j = (jb == ib ? i : 0) + lane; j < nb; j += 32) {
-              const uint32_t wj = B[j];
-              const uint32_t vj = wj & 0xFFFFu;
-              const int lag = abs(static_cast<int>(wj >> 16) - ti);
-              const uint32_t prod = vi * vj;
-              if (prod) add_counter(&hist[lag], &gN[lag], prod);
-            }
-          }
-          __syncwarp();
-        }
-      }
+      if (fast)
+        pixel_pairs<true>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
+      else
+        pixel_pairs<false>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < T; i += THREADS) {
@@ -216,7 +258,7 @@ extern "C" int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, 
     return G2_ERR_CUDA;
   const int64_t smem = static_cast<int64_t>(nframes) * 8 + ev::SMEM_FIXED;
   // shared counters need t < 2^16 (packed with the count) and products < 2^31
-  const bool use_smem = smem <= smem_optin && nframes <= 65535 &&
+  const bool use_smem = smem + ev::SMEM_STATIC <= smem_optin && nframes <= 65535 &&
                         static_cast<int64_t>(max_count) * max_count < (1ll << 31);
   auto* N = reinterpret_cast<unsigned long long*>(numer_dev);
   auto* S = reinterpret_cast<unsigned long long*>(sums_dev);
@@ -228,14 +270,16 @@ extern "C" int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, 
         return G2_ERR_CUDA;
       ev::pairs_smem_kernel<uint8_t><<<n_ctas, ev::THREADS, smem, st>>>(
           times_dev, reinterpret_cast<const uint8_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
+          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins,
+          static_cast<uint32_t>(max_count), N, S, err_dev);
     } else {
       if (cudaFuncSetAttribute(ev::pairs_smem_kernel<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(smem)) != cudaSuccess)
         return G2_ERR_CUDA;
       ev::pairs_smem_kernel<uint16_t><<<n_ctas, ev::THREADS, smem, st>>>(
           times_dev, reinterpret_cast<const uint16_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
+          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins,
+          static_cast<uint32_t>(max_count), N, S, err_dev);
     }
   } else {
     if (elem_bytes == 1)

@@ -97,7 +97,7 @@ class DenseEngine:
     MODES = {"fp16": MODE_FP16, "bytes": MODE_BYTES, "e4m3": MODE_E4M3}
 
     def __init__(self, shape, nframes, qmask, n_bins, scale, device=None, method="tc",
-                 exact_limit=EXACT_LIMIT, grid=0, operand="auto"):
+                 exact_limit=EXACT_LIMIT, grid=0, operand="auto", numer=None, sums=None, layouts=None):
         torch = _torch()
         self.lib = _lib.load()
         self.dev = require_cuda(device)
@@ -119,14 +119,16 @@ class DenseEngine:
         self.scale = torch.as_tensor(np.asarray(scale, dtype=np.float64), device=self.dev)
         rows = max(self.n_bins, 1)
         z = lambda dt: torch.zeros((rows, self.T), dtype=dt, device=self.dev)
-        self.sums = z(torch.int64)
-        self.numer = z(torch.int64)
+        # N and S may be views into a caller's arena (grouped launches address
+        # several jobs' sums through one base pointer)
+        self.sums = z(torch.int64) if sums is None else sums
+        self.numer = z(torch.int64) if numer is None else numer
         self.denom = z(torch.int64)
         self.g2_f32 = z(torch.float32)
         self.g2_f64 = z(torch.float64)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.maxval = torch.zeros(1, dtype=torch.int32, device=self.dev)
-        self._layouts = {}
+        self._layouts = {} if layouts is None else layouts   # may be shared by engines of one q-mask
         self._items_cache = {}
         self.packed = None
         self.last = {}

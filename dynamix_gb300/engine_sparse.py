@@ -230,13 +230,17 @@ class EventEngine:
                                                          self.dev)
         return self.run_device(times, counts, offs, n_ev, mx)
 
-    def run_device(self, times, counts, offs, n_ev, mx):
-        """G6 + G3 + G4 on validated device events."""
+    def run_device(self, times, counts, offs, n_ev, mx, reset_error=True):
+        """G6 + G3 + G4 on validated device events (``reset_error=False`` keeps
+        the flags an earlier stage of the same call has set)."""
         self.numer.zero_()
         self.sums.zero_()
-        self.err.zero_()
+        if reset_error:
+            self.err.zero_()
         st = stream_handle(self.dev)
-        use_smem = self.T * 8 + 32768 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
+        # the C side makes the same choice (shared counters for 2 x T frames,
+        # times below 2^16, products below 2^31)
+        use_smem = self.T * 8 + 24576 + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
         ro, rb, cro, n_ranges, n_ctas = self.plans["smem" if use_smem else "global"]
         self._mark("start_pairs")
         if n_ranges and self.n_bins and n_ev:
@@ -305,7 +309,7 @@ class SparseEngine:
         counts, ind, ip, off, ib, n, mx = csr_to_device(data, indices, indptr, offsets, self.shape, self.T,
                                                         self.dev)
         times, evdata, evoff = self.to_events(counts, ind, ip, off, ib, n)
-        out = self.events.run_device(times, evdata, evoff, n, mx)
+        out = self.events.run_device(times, evdata, evoff, n, mx, reset_error=False)
         self.last = dict(self.events.last, n_elements=n)
         return out
 

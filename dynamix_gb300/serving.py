@@ -1,0 +1,557 @@
+"""Continuous-batching g2 service on one GPU.
+
+Correlation jobs (a dense ``(T, H, W)`` stack and its q-mask, any frame shape
+and length) arrive while others run.  The server
+
+* admits a job when one of its ``max_active`` slots and enough of its HBM
+  budget are free (the budget covers the job's frames while they are on the
+  device and its packed operand; the frames are released as soon as they are
+  packed);
+* copies the frames in (when they come from host memory) and packs them on a
+  side stream, while the tensor cores work on the jobs admitted earlier;
+* runs the Gram work of all active jobs as a sequence of grouped persistent
+  launches (``g2_gram_tc`` takes up to ``G2_MAX_JOBS`` jobs per launch): each
+  launch takes a slice of every active job's tiles, shortest remaining job
+  first, so a short job that arrives behind a long one finishes in a few
+  launches instead of waiting for it;
+* finishes a job whose last tiles were launched (denominator and g2 on the
+  compute stream, results copied to pinned host memory) and hands the result
+  to the caller.
+
+N and S of all active jobs live in two int64 arenas, so that one launch
+addresses every job's sums through one base pointer.  Results are exact
+(integer N, S, D) and therefore identical whether a job runs alone or in a
+mix.
+
+There is no reference counterpart: dynamix correlates one stack per call
+(``correlator/dense.py:118-142``).  Each job computes exactly what
+``MatMulCorrelator.correlate`` computes (g2 normalised by the bin's pixel
+count unless a scale factor is given).
+"""
+from __future__ import annotations
+
+import collections
+import itertools
+import threading
+import time
+
+import numpy as np
+
+from . import _lib
+from .engine import DenseEngine, DeviceError, _torch, frames_to_device, ptr, require_cuda, stream_handle
+from .plan import MODE_BYTES, MODE_E4M3, MODE_FP16, gram_items
+
+TC_OPS_PER_ITEM_COL = 2 * 128 * 256       # int ops of one 128 x 256 tile per unit of k_len
+
+
+class ArenaFull(Exception):
+    pass
+
+
+class Arena:
+    """First-fit allocator of element ranges in a fixed device array."""
+
+    def __init__(self, n):
+        self.n = int(n)
+        self.free = [(0, self.n)]          # sorted (start, length)
+
+    def alloc(self, k):
+        k = int(k)
+        for i, (s, ln) in enumerate(self.free):
+            if ln >= k:
+                if ln == k:
+                    self.free.pop(i)
+                else:
+                    self.free[i] = (s + k, ln - k)
+                return s
+        raise ArenaFull(k)
+
+    def release(self, s, k):
+        self.free.append((int(s), int(k)))
+        self.free.sort()
+        merged = []
+        for s0, l0 in self.free:
+            if merged and merged[-1][0] + merged[-1][1] == s0:
+                merged[-1] = (merged[-1][0], merged[-1][1] + l0)
+            else:
+                merged.append((s0, l0))
+        self.free = merged
+
+    @property
+    def used(self):
+        return self.n - sum(ln for _, ln in self.free)
+
+
+def plan_slice(remaining, item_ops, next_items, slice_ops):
+    """Items each active job contributes to one grouped launch.
+
+    ``remaining[j]``: int ops job j still needs; ``item_ops[j]``: ops of each of
+    its items (launch order); ``next_items[j]``: its first item not launched.
+    Jobs are served shortest remaining first; a job gets what is left of
+    ``slice_ops`` but at least ``slice_ops / (2 n)`` and at least one item, so
+    every job advances in every launch.  Returns ``(job, n_items, ops)`` in
+    that order, jobs with nothing left omitted."""
+    n = len(remaining)
+    if n == 0:
+        return []
+    floor = float(slice_ops) / (2 * n)
+    left = float(slice_ops)
+    out = []
+    for j in sorted(range(n), key=lambda j: (remaining[j], j)):
+        k0 = int(next_items[j])
+        ops = np.asarray(item_ops[j], dtype=np.float64)[k0:]
+        if ops.size == 0:
+            continue
+        cum = np.cumsum(ops)
+        k = min(max(1, int(np.searchsorted(cum, max(left, floor), side="right"))), ops.size)
+        out.append((j, k, float(cum[k - 1])))
+        left -= float(cum[k - 1])
+    return out
+
+
+def admit_order(needs, used, budget, free_slots):
+    """Indices of queued jobs (in arrival order, ``needs`` = their bytes) that
+    can start now: first fit in arrival order under ``budget`` with ``used``
+    bytes held and ``free_slots`` slots; a job larger than the whole budget is
+    reported separately.  Returns ``(admit, too_large)``."""
+    admit, too_large = [], []
+    for i, need in enumerate(needs):
+        if need > budget:
+            too_large.append(i)
+            continue
+        if len(admit) >= free_slots:
+            break
+        if used + need <= budget:
+            admit.append(i)
+            used += need
+    return admit, too_large
+
+
+class Request:
+    """Handle of a submitted job.  ``wait()`` blocks until the result is there;
+    ``g2`` (float32 ``(n_bins, T)``), ``numerator``, ``sums``, ``denominator``
+    (int64) are host arrays afterwards; ``latency`` is seconds from submission
+    to result."""
+
+    _ids = itertools.count()
+
+    def __init__(self, frames, qmask, scale_factor):
+        self.id = next(self._ids)
+        self.frames = frames
+        self.qmask = qmask
+        self.scale_factor = scale_factor
+        self.t_submit = time.perf_counter()
+        self.t_admit = None
+        self.t_done = None
+        self.error = None
+        self.g2 = self.numerator = self.sums = self.denominator = None
+        self.info = {}
+        self._done = threading.Event()
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.t_submit
+
+    def done(self):
+        return self._done.is_set()
+
+    def wait(self, timeout=None):
+        if not self._done.wait(timeout):
+            raise TimeoutError("job %d not finished" % self.id)
+        if self.error is not None:
+            raise self.error
+        return self.g2
+
+
+class _Job:
+    """Server-side state of one request."""
+
+    def __init__(self, req, shape, T, qmask, n_bins, scale, elem_bytes, from_host):
+        self.req = req
+        self.shape = shape
+        self.T = T
+        self.qmask = qmask
+        self.n_bins = n_bins
+        self.scale = scale
+        self.elem_bytes = elem_bytes
+        self.from_host = from_host
+        self.engine = None
+        self.layout = None
+        self.items = None          # numpy ITEM_DTYPE, job field rewritten per launch
+        self.item_ops = None       # int ops of each item
+        self.next_item = 0
+        self.remaining_ops = 0
+        self.arena_off = None
+        self.reserved = 0          # bytes of the HBM budget held
+        self.frames_dev = None
+        self.host_out = None
+        self.done_event = None
+
+    @property
+    def rows(self):
+        return max(self.n_bins, 1)
+
+
+class G2Server:
+    """See the module docstring.  ``hbm_budget``: bytes of device memory the
+    server may hold for admitted jobs (frames in flight + packed operands);
+    ``arena_elems``: int64 elements of each of the N and S arenas (the sum of
+    ``n_bins * T`` over the active jobs must fit); ``slice_ops``: tensor-core
+    int ops per grouped launch."""
+
+    def __init__(self, hbm_budget=150e9, max_active=_lib.MAX_JOBS, arena_elems=1 << 25, slice_ops=2e13,
+                 device=None, method="tc"):
+        torch = _torch()
+        self.lib = _lib.load()
+        self.dev = require_cuda(device)
+        self.budget = int(hbm_budget)
+        self.max_active = min(int(max_active), _lib.MAX_JOBS)
+        self.slice_ops = float(slice_ops)
+        self.method = method
+        self.arena = Arena(arena_elems)
+        self.numer_arena = torch.zeros(int(arena_elems), dtype=torch.int64, device=self.dev)
+        self.sums_arena = torch.zeros(int(arena_elems), dtype=torch.int64, device=self.dev)
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.compute = torch.cuda.Stream(self.dev)
+        self.side = torch.cuda.Stream(self.dev)
+        self.queue = collections.deque()
+        self.active = []
+        self.finishing = []
+        self._inflight = []        # (event, pinned items, device items, jobs) per grouped launch
+        self.used = 0
+        self.lock = threading.Lock()
+        self._layouts = {}         # (shape, qmask digest, n_bins) -> shared layout dict
+        self.stats = {"launches": 0, "items": 0, "admitted": 0, "finished": 0, "max_active": 0,
+                      "max_used_bytes": 0}
+        self._thread = None
+        self._stop = False
+
+    # -- client side -----------------------------------------------------
+    def submit(self, frames, qmask=None, scale_factor=None):
+        """Queue a job; ``frames`` (T, H, W) u8/u16 as a CUDA tensor (used in
+        place), a CPU tensor (pinned memory gives an asynchronous copy) or a
+        numpy array.  Returns a :class:`Request`."""
+        req = Request(frames, qmask, scale_factor)
+        with self.lock:
+            self.queue.append(req)
+        return req
+
+    def start(self):
+        """Serve from a background thread until :meth:`stop`."""
+        self._stop = False
+        self._thread = threading.Thread(target=self._loop, daemon=True)
+        self._thread.start()
+
+    def stop(self):
+        self._stop = True
+        if self._thread is not None:
+            self._thread.join()
+            self._thread = None
+
+    def _loop(self):
+        torch = _torch()
+        torch.cuda.set_device(self.dev)
+        while not self._stop:
+            if not self.step():
+                time.sleep(0.0002)
+
+    def idle(self):
+        with self.lock:
+            return not (self.queue or self.active or self.finishing or self._inflight)
+
+    def run_until_idle(self):
+        while not self.idle():
+            if not self.step():
+                time.sleep(0.0002)
+
+    # -- scheduling --------------------------------------------------------
+    def step(self):
+        """One scheduling round: launch the next grouped Gram slice, admit and
+        pack new jobs while it runs, hand over finished results.  Returns True
+        when it did any work."""
+        launched = self._launch_slice()
+        admitted = self._admit()
+        reaped = self._reap()
+        return launched or admitted or reaped
+
+    def _params(self, req):
+        """(shape, T, qmask int32, n_bins, scale, layouts) of a request, the
+        q-mask derived data cached per mask."""
+        import hashlib
+
+        from .correlator.common import BaseCorrelator
+        fr = req.frames
+        if fr is None or len(getattr(fr, "shape", ())) != 3:
+            raise ValueError("frames must be a (T, H, W) stack")
+        T, H, W = (int(x) for x in fr.shape)
+        qm = None if req.qmask is None else np.ascontiguousarray(req.qmask, dtype=np.int32)
+        digest = hashlib.blake2b(qm.tobytes() if qm is not None else b"all", digest_size=16).hexdigest()
+        sf = req.scale_factor
+        key = (H, W, digest, None if sf is None else repr(sf))
+        if key not in self._layouts:
+            bc = BaseCorrelator()
+            if qm is None:
+                bc._set_parameters((H, W), T, None, sf, {})
+            else:
+                bc._set_shape((H, W))
+                bc.nframes = T
+                bc.qmask = qm
+                bc.n_bins = int(qm.max()) if qm.size else 0
+                bc.bins = np.arange(1, bc.n_bins + 1, dtype=np.int32)
+                if sf is None:
+                    cnt = np.bincount(qm.ravel()[qm.ravel() > 0], minlength=bc.n_bins + 1)
+                    bc.scale_factors = {b: int(cnt[b]) for b in bc.bins}
+                else:
+                    bc._set_scale_factor(sf)
+            if len(self._layouts) > 64:
+                self._layouts.clear()
+            self._layouts[key] = (bc.qmask, bc.n_bins, bc._scale_array(), {})
+        qmask, n_bins, scale, layouts = self._layouts[key]
+        return (H, W), T, qmask, n_bins, scale, layouts
+
+    def _estimate(self, job, layouts):
+        """Bytes of the budget a job needs at its peak: frames copied to the
+        device plus the widest packed operand its counts may need."""
+        from .plan import PackLayout
+        key = ("fp16_cols",)
+        if key not in layouts:
+            layouts[key] = PackLayout(job.qmask, job.n_bins, MODE_FP16).packed_cols
+        cols = layouts[key]
+        frames = job.T * job.shape[0] * job.shape[1] * job.elem_bytes if job.from_host else 0
+        return frames + (job.T + 1) * cols * (2 if job.elem_bytes == 1 else 4)
+
+    def _make_job(self, req):
+        """Server-side job of a request (built once, kept on the request)."""
+        torch = _torch()
+        if getattr(req, "_job", None) is None:
+            shape, T, qmask, n_bins, scale, layouts = self._params(req)
+            fr = req.frames
+            from_host = not (isinstance(fr, torch.Tensor) and fr.is_cuda)
+            dt = fr.dtype if isinstance(fr, torch.Tensor) else np.asarray(fr).dtype
+            elem = 1 if dt in (torch.uint8, np.uint8) else 2     # other integer types become u8 or u16
+            job = _Job(req, shape, T, qmask, n_bins, scale, elem, from_host)
+            req._job = (job, layouts, self._estimate(job, layouts))
+        return req._job
+
+    def _admit(self):
+        with self.lock:
+            pending = list(self.queue)
+        free = self.max_active - len(self.active) - len(self.finishing)
+        if not pending or free <= 0:
+            return False
+        cands = []
+        for req in pending:
+            try:
+                cands.append((req,) + self._make_job(req))
+            except Exception as e:                 # malformed request: fail it, keep serving
+                self._dequeue(req)
+                self._fail(req, e)
+        admit, too_large = admit_order([c[3] for c in cands], self.used, self.budget, free)
+        for i in too_large:
+            req, job, layouts, need = cands[i]
+            self._dequeue(req)
+            self._fail(req, MemoryError("job needs %.1f GB, the budget is %.1f GB" % (need / 1e9,
+                                                                                      self.budget / 1e9)))
+        admitted = False
+        for i in admit:
+            req, job, layouts, need = cands[i]
+            try:
+                job.arena_off = self.arena.alloc(job.rows * job.T)
+            except ArenaFull:
+                continue                           # stays queued until sums space frees up
+            self._dequeue(req)
+            job.reserved = need
+            self.used += need
+            try:
+                self._start(job, layouts)
+            except Exception as e:
+                self._release(job)
+                self._fail(req, e)
+                continue
+            admitted = True
+        return admitted
+
+    def _dequeue(self, req):
+        with self.lock:
+            if req in self.queue:
+                self.queue.remove(req)
+
+    def _start(self, job, layouts):
+        """Frames to the device and packed, on the side stream; the tiles of
+        the job are then ready for the grouped launches."""
+        torch = _torch()
+        req = job.req
+        req.t_admit = time.perf_counter()
+        off, n = job.arena_off, job.rows * job.T
+        numer = self.numer_arena[off:off + n].view(job.rows, job.T)
+        sums = self.sums_arena[off:off + n].view(job.rows, job.T)
+        with torch.cuda.stream(self.side):
+            numer.zero_()                           # the pack zeroes the sums
+            fr = req.frames
+            if (isinstance(fr, torch.Tensor) and not fr.is_cuda and fr.dtype in (torch.uint8, torch.uint16)
+                    and fr.is_pinned() and fr.is_contiguous()):
+                frames_dev = torch.empty(fr.shape, dtype=fr.dtype, device=self.dev)
+                frames_dev.copy_(fr, non_blocking=True)         # asynchronous on the side stream
+            else:
+                frames_dev = frames_to_device(fr, self.dev)      # validates, converts, or uses in place
+            eng = DenseEngine(job.shape, job.T, job.qmask, job.n_bins, job.scale, device=self.dev,
+                              method=self.method, numer=numer, sums=sums, layouts=layouts)
+            job.engine = eng
+            if job.n_bins:
+                mode = eng.choose_mode(frames_dev)
+                L, grams = eng._pack_and_plan(frames_dev, mode)   # synchronises the side stream
+                job.layout = L
+                items = gram_items(job.T, grams, job=0, out_base=off, kind=self.method,
+                                   s_base=off if (L.ones_row and self.method == "tc") else None)
+            else:
+                items = np.empty(0, dtype=_lib.ITEM_DTYPE)
+            ready = torch.cuda.Event()
+            ready.record(self.side)
+        self.compute.wait_event(ready)
+        del frames_dev                              # packed: the frames are no longer needed
+        if eng.packed is not None:
+            eng.packed.record_stream(self.compute)
+        packed_bytes = 0 if eng.packed is None else eng.packed.numel()
+        self.used -= job.reserved
+        job.reserved = packed_bytes
+        self.used += packed_bytes
+        job.items = items
+        job.item_ops = items["k_len"].astype(np.float64) * TC_OPS_PER_ITEM_COL
+        job.remaining_ops = float(job.item_ops.sum())
+        job.next_item = 0
+        req.info.update(mode=None if job.layout is None else ["fp16", "bytes", "e4m3"][job.layout.mode],
+                        n_items=int(items.size), packed_bytes=int(packed_bytes))
+        req.frames = None                           # the server keeps no reference to the input
+        self.active.append(job)
+        if items.size == 0:
+            self._finish(job)                       # no binned pixel: nothing to correlate
+        self.stats["admitted"] += 1
+        self.stats["max_active"] = max(self.stats["max_active"], len(self.active))
+        self.stats["max_used_bytes"] = max(self.stats["max_used_bytes"], self.used)
+
+    def _launch_slice(self):
+        """One grouped persistent launch over a slice of every active job's
+        tiles (shortest remaining job first; each job gets at least
+        1 / (2 n_active) of the slice so none starves)."""
+        torch = _torch()
+        self._retire_launches()
+        if not self.active or len(self._inflight) >= 2:
+            return False
+        act = self.active
+        plan = plan_slice([j.remaining_ops for j in act], [j.item_ops for j in act], [j.next_item for j in act],
+                          self.slice_ops)
+        parts, jobs, taken = [], [], []
+        for idx, k, ops in plan:
+            job = act[idx]
+            it = job.items[job.next_item:job.next_item + k].copy()
+            it["job"] = len(jobs)
+            parts.append(it)
+            L = job.layout
+            jobs.append((job.engine.packed.data_ptr(), job.T, L.packed_cols, L.kind, L.ones_row))
+            taken.append((job, k, ops))
+        if not parts:
+            return False
+        items = np.concatenate(parts)
+        items = items[np.argsort(-items["k_len"].astype(np.int64), kind="stable")]
+        host = torch.from_numpy(items.view(np.uint8).copy()).pin_memory()
+        with torch.cuda.stream(self.compute):
+            dev_items = torch.empty(host.numel(), dtype=torch.uint8, device=self.dev)
+            dev_items.copy_(host, non_blocking=True)
+            jarr = _lib.jobs_array(jobs)
+            st = stream_handle(self.dev)
+            if self.method == "tc":
+                _lib.check(self.lib.g2_gram_tc(jarr, len(jobs), ptr(dev_items), items.size, ptr(self.numer_arena),
+                                               self.numer_arena.numel(), ptr(self.sums_arena),
+                                               self.sums_arena.numel(), ptr(self.err), 0, st), "g2_gram_tc")
+            else:                                   # the CUDA-core comparator, same items and sums
+                _lib.check(self.lib.g2_plain_direct(jarr, len(jobs), ptr(dev_items), items.size,
+                                                    ptr(self.numer_arena), self.numer_arena.numel(), ptr(self.err),
+                                                    st), "g2_plain_direct")
+            ev = torch.cuda.Event()
+            ev.record(self.compute)
+        members = []
+        for job, k, ops in taken:
+            job.next_item += k
+            job.remaining_ops -= ops
+            members.append(job)
+        self._inflight.append((ev, host, dev_items, members))
+        self.stats["launches"] += 1
+        self.stats["items"] += int(items.size)
+        for job in [j for j in self.active if j.next_item >= j.items.size]:
+            self._finish(job)
+        return True
+
+    def _retire_launches(self):
+        """Drop launches that completed; a raised device error flag fails the
+        jobs of that launch."""
+        keep = []
+        for rec in self._inflight:
+            ev, host, dev_items, members = rec
+            if ev.query():
+                code = int(self.err.item())
+                if code:
+                    self.err.zero_()
+                    for job in members:
+                        job.req.info["device_error"] = code
+            else:
+                keep.append(rec)
+        self._inflight = keep
+
+    def _finish(self, job):
+        """Denominator, g2 and the copies to pinned host memory, queued on the
+        compute stream after the job's last tiles."""
+        torch = _torch()
+        self.active.remove(job)
+        eng = job.engine
+        with torch.cuda.stream(self.compute):
+            if job.n_bins:
+                eng.normalise()
+            rows = job.rows
+            out = {k: torch.empty((rows, job.T), dtype=dt, pin_memory=True) for k, dt in
+                   (("g2", torch.float32), ("numerator", torch.int64), ("sums", torch.int64),
+                    ("denominator", torch.int64))}
+            for k, src in (("g2", eng.g2_f32), ("numerator", eng.numer), ("sums", eng.sums),
+                           ("denominator", eng.denom)):
+                out[k].copy_(src, non_blocking=True)
+            job.done_event = torch.cuda.Event()
+            job.done_event.record(self.compute)
+        job.host_out = out
+        eng.packed = None                        # freed once the compute stream is past it
+        self.used -= job.reserved
+        job.reserved = 0
+        self.finishing.append(job)
+
+    def _reap(self):
+        done = [j for j in self.finishing if j.done_event.query()]
+        for job in done:
+            self.finishing.remove(job)
+            req = job.req
+            out = job.host_out
+            nb = job.n_bins
+            req.g2 = out["g2"].numpy()[:nb]
+            req.numerator = out["numerator"].numpy()[:nb]
+            req.sums = out["sums"].numpy()[:nb]
+            req.denominator = out["denominator"].numpy()[:nb]
+            code = req.info.get("device_error", 0) | int(job.engine.err.item())
+            if code:
+                req.error = DeviceError(_lib.device_error_message(code))
+            elif nb and req.sums.size and float(req.sums.max()) ** 2 * job.T >= 2.0 ** 63:
+                req.error = OverflowError("denominator exceeds int64 for these counts")
+            self._release(job)
+            req.t_done = time.perf_counter()
+            self.stats["finished"] += 1
+            req._done.set()
+        return bool(done)
+
+    def _release(self, job):
+        if job.arena_off is not None:
+            self.arena.release(job.arena_off, job.rows * job.T)
+            job.arena_off = None
+        self.used -= job.reserved
+        job.reserved = 0
+        job.engine = None
+
+    def _fail(self, req, err):
+        req.error = err
+        req.t_done = time.perf_counter()
+        req._done.set()

@@ -54,3 +54,45 @@ def test_csr_layout_errors(built_lib, cuda_device):
         c.correlate(data, bad, indptr, offsets)
     with pytest.raises(ValueError):
         SparseCorrelator((H, W), T, bins=3)
+
+
+@pytest.mark.parametrize("name,index_dtype", [("dense_small_u8", np.uint32), ("dense_u16", np.int64),
+                                              ("dense_cfg1_u8", np.uint32)])
+def test_csr_to_events_is_frames_compressor_layout(built_lib, cuda_device, name, index_dtype):
+    """The device transposition yields exactly FramesCompressor's layout:
+    pixel-major, frames ascending within a pixel (event.py:267-284)."""
+    import torch
+    from dynamix_gb300.engine_sparse import SparseEngine, csr_to_device
+    z = golden(name)
+    fr = z["frames"]
+    T, H, W = fr.shape
+    csr = o.frames_to_csr(fr, index_dtype=index_dtype)
+    eng = SparseEngine((H, W), T, np.ones((H, W), np.int32), 1, [1.0])
+    counts, ind, ip, off, ib, n, mx = csr_to_device(*csr, (H, W), T, eng.dev)
+    times, data, evoff = eng.to_events(counts, ind, ip, off, ib, n)
+    torch.cuda.synchronize()
+    eng.check_error()
+    d_ref, t_ref, o_ref = o.compress_all_stack(fr)
+    assert np.array_equal(evoff.cpu().numpy().view(np.uint32), o_ref)
+    assert np.array_equal(times[:n].cpu().numpy(), t_ref)
+    assert np.array_equal(data[:n].cpu().numpy().astype(np.int64), d_ref.astype(np.int64))
+
+
+def test_csr_duplicate_column_is_reported(built_lib, cuda_device):
+    from dynamix_gb300.correlator import SparseCorrelator
+    from dynamix_gb300.engine import DeviceError
+    fr = np.zeros((3, 2, 8), np.uint8)
+    fr[:, 0, 2] = 1
+    fr[1, 1, 5] = 2
+    data, indices, indptr, offsets = o.frames_to_csr(fr)
+    indices = indices.copy()
+    # frame 0, row 0 holds one element; make frame 1's row 0 name column 2 twice
+    data2 = np.insert(data, 1, 1)
+    indices2 = np.insert(indices, 1, 2)
+    ip = indptr.reshape(3, 3).astype(np.int64)
+    ip[1, 1:] += 1
+    off = offsets.astype(np.int64)
+    off[2:] += 1
+    c = SparseCorrelator((2, 8), 3)
+    with pytest.raises(DeviceError):
+        c.correlate(data2, indices2.astype(np.uint32), ip.ravel().astype(np.uint32), off.astype(np.uint32))
