@@ -43,8 +43,12 @@ class _DenseBase(BaseCorrelator):
         """Run on the device and return the float32 g2 device tensor (no copy back).
 
         ``frames``: (nframes, H, W) counts as a numpy array, a CPU tensor or a
-        CUDA tensor (uint8 / uint16 tensors are used as they are)."""
+        CUDA tensor (uint8 / uint16 tensors are used as they are).  A pinned
+        uint8 CPU tensor is copied in chunks that overlap the packing and the
+        Gram; it must stay alive until the result is read."""
         eng = self.engine
+        if eng.pipelined_ok(frames) and not frames.is_cuda:
+            return eng.run(frames)
         frames_dev = frames_to_device(frames, eng.dev)
         out = eng.run(frames_dev)
         return out

@@ -119,6 +119,10 @@ __global__ void __launch_bounds__(256)
 }
 
 // Scatter of one image row over all frames, events of a pixel in frame order.
+// A lane keeps the first KREG elements of its (frame, row) segment in
+// registers across the three phases of a batch; longer segments reload the rest.
+constexpr int KREG = 16;
+
 template <typename Tv, typename Ti>
 __global__ void __launch_bounds__(256)
     row_scatter_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices, const Ti* __restrict__ indptr,
@@ -132,6 +136,7 @@ __global__ void __launch_bounds__(256)
   uint32_t* cur = sm + static_cast<int64_t>(warp) * 2 * W;  // next free slot of each pixel
   uint32_t* msk = cur + W;                                    // frames of the batch holding the pixel
   const uint32_t* row_off = ev_off + static_cast<int64_t>(r) * W;
+  const uint32_t n_total = ev_off[static_cast<int64_t>(H) * W];
   for (int i = lane; i < W; i += 32) {
     cur[i] = row_off[i];
     msk[i] = 0;
@@ -153,39 +158,205 @@ __global__ void __launch_bounds__(256)
         s = e = 0;
       }
     }
-    // 1. mark the frames of the batch that hold each pixel
-    for (int64_t k = s; k < e; ++k) {
-      const int64_t col = static_cast<int64_t>(indices[k]);
-      if (col < 0 || col >= W) continue;  // reported by the count pass
-      if (atomicOr(&msk[col], bit) & bit) bad = true;  // a column twice in one row
+    const int len = static_cast<int>(e - s);
+    int32_t col[KREG];
+    Tv val[KREG];
+    // 1. load the segment and mark the frames of the batch holding each pixel
+#pragma unroll
+    for (int j = 0; j < KREG; ++j) {
+      col[j] = -1;
+      if (j < len) {
+        const int64_t c = static_cast<int64_t>(indices[s + j]);
+        val[j] = data[s + j];
+        col[j] = (c >= 0 && c < W) ? static_cast<int32_t>(c) : -1;  // bad columns: reported by the count pass
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < KREG; ++j)
+      if (col[j] >= 0 && (atomicOr(&msk[col[j]], bit) & bit)) bad = true;  // a column twice in one row
+    for (int j = KREG; j < len; ++j) {
+      const int64_t c = static_cast<int64_t>(indices[s + j]);
+      if (c >= 0 && c < W && (atomicOr(&msk[c], bit) & bit)) bad = true;
     }
     __syncwarp();
     // 2. slot = next free slot + earlier frames of the batch holding the pixel
-    for (int64_t k = s; k < e; ++k) {
-      const int64_t col = static_cast<int64_t>(indices[k]);
-      if (col < 0 || col >= W) continue;
-      const uint32_t slot = cur[col] + __popc(msk[col] & (bit - 1u));
-      if (slot < row_off[col + 1]) {
+#pragma unroll
+    for (int j = 0; j < KREG; ++j) {
+      if (col[j] >= 0) {
+        const uint32_t slot = cur[col[j]] + __popc(msk[col[j]] & (bit - 1u));
+        if (slot < n_total) {
+          ev_times[slot] = static_cast<int32_t>(t);
+          ev_data[slot] = val[j];
+        } else {
+          bad = true;
+        }
+      }
+    }
+    for (int j = KREG; j < len; ++j) {
+      const int64_t c = static_cast<int64_t>(indices[s + j]);
+      if (c < 0 || c >= W) continue;
+      const uint32_t slot = cur[c] + __popc(msk[c] & (bit - 1u));
+      if (slot < n_total) {
         ev_times[slot] = static_cast<int32_t>(t);
-        ev_data[slot] = data[k];
+        ev_data[slot] = data[s + j];
       } else {
         bad = true;
       }
     }
     __syncwarp();
     // 3. the last frame of the batch holding the pixel advances its cursor
-    for (int64_t k = s; k < e; ++k) {
-      const int64_t col = static_cast<int64_t>(indices[k]);
-      if (col < 0 || col >= W) continue;
-      const uint32_t m = msk[col];
+#pragma unroll
+    for (int j = 0; j < KREG; ++j) {
+      if (col[j] >= 0) {
+        const uint32_t m = msk[col[j]];
+        if (m != 0u && (m >> lane) == 1u) {
+          cur[col[j]] += __popc(m);
+          msk[col[j]] = 0u;
+        }
+      }
+    }
+    for (int j = KREG; j < len; ++j) {
+      const int64_t c = static_cast<int64_t>(indices[s + j]);
+      if (c < 0 || c >= W) continue;
+      const uint32_t m = msk[c];
       if (m != 0u && (m >> lane) == 1u) {
-        cur[col] += __popc(m);
-        msk[col] = 0u;
+        cur[c] += __popc(m);
+        msk[c] = 0u;
       }
     }
     __syncwarp();
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// Scatter into packed event words (t << 16 | v; frames < 2^16), one CTA per
+// image row: its warps split the row's columns (a warp's lanes still take 32
+// consecutive frames), so a pixel's slot cursor and batch mask are touched by
+// one warp only.  The CTA asks for ROW_SMEM_FLOOR bytes of shared memory so
+// that few rows are in flight at once: the sectors being filled (one per
+// pixel of every row in flight) then stay in L2 until they are complete.
+constexpr int PK_WARPS = 8;
+constexpr int ROW_SMEM_FLOOR = 56 * 1024;
+
+template <typename Tv, typename Ti>
+__global__ void __launch_bounds__(PK_WARPS * 32)
+    row_scatter_packed_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices,
+                              const Ti* __restrict__ indptr, const Ti* __restrict__ offsets, int64_t n_elem,
+                              int32_t T, int32_t H, int32_t W, const uint32_t* __restrict__ ev_off,
+                              uint32_t* __restrict__ ev_words, int32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x;
+  if (r >= H) return;
+  uint32_t* cur = sm;        // [W] next free slot of each pixel of the row
+  uint32_t* msk = sm + W;    // [W] frames of the batch holding the pixel
+  const uint32_t* row_off = ev_off + static_cast<int64_t>(r) * W;
+  const uint32_t n_total = ev_off[static_cast<int64_t>(H) * W];
+  for (int i = threadIdx.x; i < W; i += blockDim.x) {
+    cur[i] = row_off[i];
+    msk[i] = 0;
+  }
+  __syncthreads();
+  // this warp's columns [c0, c1)
+  const int per = (W + PK_WARPS - 1) / PK_WARPS;
+  const int c0 = min(W, warp * per), c1 = min(W, c0 + per);
+  bool bad = false;
+  const uint32_t bit = 1u << lane;
+  for (int64_t t0 = 0; t0 < T; t0 += 32) {
+    const int64_t t = t0 + lane;
+    int64_t s = 0, e = 0;
+    if (t < T) {
+      const int64_t base = static_cast<int64_t>(offsets[t]);
+      const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
+      const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
+      s = base + static_cast<int64_t>(ip[0]);
+      e = base + static_cast<int64_t>(ip[1]);
+      if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+        bad = true;
+        s = e = 0;
+      }
+    }
+    const int len = static_cast<int>(e - s);
+    int32_t col[KREG];
+    uint32_t val[KREG];
+#pragma unroll
+    for (int j = 0; j < KREG; ++j) {
+      col[j] = -1;
+      if (j < len) {
+        const int64_t c = static_cast<int64_t>(indices[s + j]);
+        if (c >= c0 && c < c1) {
+          col[j] = static_cast<int32_t>(c);
+          val[j] = static_cast<uint32_t>(data[s + j]);
+        }
+      }
+    }
+    // 1. mark the frames of the batch holding each pixel
+#pragma unroll
+    for (int j = 0; j < KREG; ++j)
+      if (col[j] >= 0 && (atomicOr(&msk[col[j]], bit) & bit)) bad = true;  // a column twice in one row
+    for (int j = KREG; j < len; ++j) {
+      const int64_t c = static_cast<int64_t>(indices[s + j]);
+      if (c >= c0 && c < c1 && (atomicOr(&msk[c], bit) & bit)) bad = true;
+    }
+    __syncwarp();
+    // 2. slot = next free slot + earlier frames of the batch holding the pixel
+    const uint32_t tw = static_cast<uint32_t>(t) << 16;
+#pragma unroll
+    for (int j = 0; j < KREG; ++j) {
+      if (col[j] >= 0) {
+        const uint32_t slot = cur[col[j]] + __popc(msk[col[j]] & (bit - 1u));
+        if (slot < n_total)
+          ev_words[slot] = tw | val[j];
+        else
+          bad = true;
+      }
+    }
+    for (int j = KREG; j < len; ++j) {
+      const int64_t c = static_cast<int64_t>(indices[s + j]);
+      if (c < c0 || c >= c1) continue;
+      const uint32_t slot = cur[c] + __popc(msk[c] & (bit - 1u));
+      if (slot < n_total)
+        ev_words[slot] = tw | static_cast<uint32_t>(data[s + j]);
+      else
+        bad = true;
+    }
+    __syncwarp();
+    // 3. the last frame of the batch holding the pixel advances its cursor
+#pragma unroll
+    for (int j = 0; j < KREG; ++j) {
+      if (col[j] >= 0) {
+        const uint32_t m = msk[col[j]];
+        if (m != 0u && (m >> lane) == 1u) {
+          cur[col[j]] += __popc(m);
+          msk[col[j]] = 0u;
+        }
+      }
+    }
+    for (int j = KREG; j < len; ++j) {
+      const int64_t c = static_cast<int64_t>(indices[s + j]);
+      if (c < c0 || c >= c1) continue;
+      const uint32_t m = msk[c];
+      if (m != 0u && (m >> lane) == 1u) {
+        cur[c] += __popc(m);
+        msk[c] = 0u;
+      }
+    }
+    __syncwarp();
+  }
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// Packed words -> (times int32, data) arrays.
+template <typename Tv>
+__global__ void __launch_bounds__(256)
+    unpack_events_kernel(const uint32_t* __restrict__ words, int64_t n, int32_t* __restrict__ times,
+                         Tv* __restrict__ data) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const uint32_t w = words[i];
+    times[i] = static_cast<int32_t>(w >> 16);
+    data[i] = static_cast<Tv>(w & 0xFFFFu);
+  }
 }
 
 // Exclusive scan of n uint32 into uint32 (the total must stay below 2^32):
@@ -427,4 +598,55 @@ extern "C" int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const vo
   }
   return walk<true>(data_dev, elem_bytes, indices_dev, indptr_dev, offsets_dev, index_bytes, n_elem, nframes,
                     height, width, cursor_dev, ev_offsets_dev, ev_times_dev, ev_data_dev, err_dev, stream);
+}
+
+extern "C" int g2_csr_scatter_packed(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                                     const void* indptr_dev, const void* offsets_dev, int32_t index_bytes,
+                                     int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
+                                     const uint32_t* ev_offsets_dev, uint32_t* ev_words_dev, int32_t* err_dev,
+                                     void* stream) {
+  using namespace g2;
+  if (!data_dev || !indices_dev || !indptr_dev || !offsets_dev || !ev_offsets_dev || !ev_words_dev || !err_dev)
+    return G2_ERR_ARG;
+  if ((elem_bytes != 1 && elem_bytes != 2) || (index_bytes != 4 && index_bytes != 8) || n_elem < 0 ||
+      nframes <= 0 || height <= 0 || width <= 0)
+    return G2_ERR_ARG;
+  if (nframes > 65536 || width > csr::ROW_MAX_W) return G2_ERR_UNSUPPORTED;
+  const int64_t need = static_cast<int64_t>(width) * 8;
+  const int64_t smem = need > csr::ROW_SMEM_FLOOR ? need : csr::ROW_SMEM_FLOOR;
+  cudaStream_t st = as_stream(stream);
+#define G2_PK(TV, TI)                                                                                           \
+  do {                                                                                                          \
+    if (!allow_smem(csr::row_scatter_packed_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                          \
+    csr::row_scatter_packed_kernel<TV, TI><<<static_cast<unsigned>(height), csr::PK_WARPS * 32, smem, st>>>(     \
+        reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev),                        \
+        reinterpret_cast<const TI*>(indptr_dev), reinterpret_cast<const TI*>(offsets_dev), n_elem, nframes,     \
+        height, width, ev_offsets_dev, ev_words_dev, err_dev);                                                  \
+  } while (0)
+  if (elem_bytes == 1 && index_bytes == 4) G2_PK(uint8_t, uint32_t);
+  else if (elem_bytes == 1) G2_PK(uint8_t, int64_t);
+  else if (index_bytes == 4) G2_PK(uint16_t, uint32_t);
+  else G2_PK(uint16_t, int64_t);
+#undef G2_PK
+  return launch_status();
+}
+
+extern "C" int g2_events_unpack(const uint32_t* ev_words_dev, int64_t n_events, int32_t elem_bytes,
+                                int32_t* ev_times_dev, void* ev_data_dev, void* stream) {
+  using namespace g2;
+  if (!ev_words_dev || !ev_times_dev || !ev_data_dev || n_events < 0 || (elem_bytes != 1 && elem_bytes != 2))
+    return G2_ERR_ARG;
+  if (n_events == 0) return G2_OK;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  int64_t blocks = (n_events + 255) / 256;
+  if (blocks > static_cast<int64_t>(sms) * 16) blocks = static_cast<int64_t>(sms) * 16;
+  cudaStream_t st = as_stream(stream);
+  if (elem_bytes == 1)
+    csr::unpack_events_kernel<uint8_t><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+        ev_words_dev, n_events, ev_times_dev, reinterpret_cast<uint8_t*>(ev_data_dev));
+  else
+    csr::unpack_events_kernel<uint16_t><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+        ev_words_dev, n_events, ev_times_dev, reinterpret_cast<uint16_t*>(ev_data_dev));
+  return launch_status();
 }

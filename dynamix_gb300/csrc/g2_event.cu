@@ -41,11 +41,27 @@ __device__ __forceinline__ void add_counter(uint32_t* c, unsigned long long* g, 
   }
 }
 
+// One event as (t << 16) | v with its validity: from the caller's split
+// arrays (times int32, data u8/u16) or from packed words (t << 16 | v).
+template <bool PACKED, typename Tv>
+__device__ __forceinline__ uint32_t load_event(const int32_t* __restrict__ times, const Tv* __restrict__ data,
+                                               int64_t i, int T, uint32_t maxc, bool& ok) {
+  if (PACKED) {
+    const uint32_t w = reinterpret_cast<const uint32_t*>(times)[i];
+    ok = static_cast<int>(w >> 16) < T && (w & 0xFFFFu) <= maxc;
+    return w;
+  }
+  const int32_t t = times[i];
+  const uint32_t v = static_cast<uint32_t>(data[i]);
+  ok = t >= 0 && t < T && v <= maxc;
+  return (static_cast<uint32_t>(t) << 16) | v;
+}
+
 // Pair sums of one pixel's events by one warp.  FAST: every counter of the
 // range is known to stay below 2^32 (checked per range from its event count),
 // so the shared adds need no returned value (the warp does not wait on them)
 // and no drain check.
-template <bool FAST, typename Tv>
+template <bool FAST, bool PACKED, typename Tv>
 __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, const Tv* __restrict__ data,
                                             int64_t base, int n, int T, uint32_t maxc, uint32_t* hist,
                                             uint32_t* shist, unsigned long long* gN, unsigned long long* gS,
@@ -53,11 +69,12 @@ __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, c
   for (int ib = 0; ib < n; ib += EV) {
     const int na = min(EV, n - ib);
     for (int e = lane; e < na; e += 32) {
-      const int32_t t = times[base + ib + e];
-      const uint32_t v = static_cast<uint32_t>(data[base + ib + e]);
-      const bool ok = t >= 0 && t < T && v <= maxc;
+      bool ok;
+      const uint32_t w = load_event<PACKED>(times, data, base + ib + e, T, maxc, ok);
+      const int t = static_cast<int>(w >> 16);
+      const uint32_t v = w & 0xFFFFu;
       bad |= !ok;
-      bufA[e] = ok ? (static_cast<uint32_t>(t) << 16) | v : 0u;
+      bufA[e] = ok ? w : 0u;
       if (ok && v) {
         if (FAST)
           atomicAdd(&shist[t], v);
@@ -71,9 +88,9 @@ __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, c
       const uint32_t* B = bufA;
       if (jb != ib) {
         for (int e = lane; e < nb; e += 32) {
-          const int32_t t = times[base + jb + e];
-          const uint32_t v = static_cast<uint32_t>(data[base + jb + e]);
-          bufB[e] = (t >= 0 && t < T && v <= maxc) ? (static_cast<uint32_t>(t) << 16) | v : 0u;
+          bool ok;
+          const uint32_t w = load_event<PACKED>(times, data, base + jb + e, T, maxc, ok);
+          bufB[e] = ok ? w : 0u;
         }
         __syncwarp();
         B = bufB;
@@ -99,7 +116,7 @@ __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, c
   }
 }
 
-template <typename Tv>
+template <bool PACKED, typename Tv>
 __global__ void __launch_bounds__(THREADS, 1)
     pairs_smem_kernel(const int32_t* __restrict__ times, const Tv* __restrict__ data,
                       const uint32_t* __restrict__ offsets, const int32_t* __restrict__ pix_list,
@@ -160,9 +177,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       const int n = static_cast<int>(end - base);
       if (fast)
-        pixel_pairs<true>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
+        pixel_pairs<true, PACKED>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
       else
-        pixel_pairs<false>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
+        pixel_pairs<false, PACKED>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < T; i += THREADS) {
@@ -177,7 +194,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // Every pair added straight to the global int64 sums (long stacks, large counts).
-template <typename Tv>
+template <bool PACKED, typename Tv>
 __global__ void __launch_bounds__(256)
     pairs_global_kernel(const int32_t* __restrict__ times, const Tv* __restrict__ data,
                         const uint32_t* __restrict__ offsets, const int32_t* __restrict__ pix_list,
@@ -213,18 +230,22 @@ __global__ void __launch_bounds__(256)
     }
     const int64_t n = end - base;
     for (int64_t i = 0; i < n; ++i) {
-      const int32_t ti = times[base + i];
-      const unsigned long long vi = data[base + i];
-      if (ti < 0 || ti >= T) {
+      bool oki;
+      const uint32_t wi = load_event<PACKED>(times, data, base + i, T, 0xFFFFu, oki);
+      const int32_t ti = static_cast<int32_t>(wi >> 16);
+      const unsigned long long vi = wi & 0xFFFFu;
+      if (!oki) {
         bad = true;
         continue;
       }
       if (lane == 0 && vi) atomicAdd(&gS[ti], vi);
       if (!vi) continue;
       for (int64_t j = i + lane; j < n; j += 32) {
-        const int32_t tj = times[base + j];
-        const unsigned long long vj = data[base + j];
-        if (tj < 0 || tj >= T || !vj) continue;
+        bool okj;
+        const uint32_t wj = load_event<PACKED>(times, data, base + j, T, 0xFFFFu, okj);
+        const int32_t tj = static_cast<int32_t>(wj >> 16);
+        const unsigned long long vj = wj & 0xFFFFu;
+        if (!okj || !vj) continue;
         atomicAdd(&gN[abs(tj - ti)], vi * vj);
       }
     }
@@ -236,20 +257,14 @@ __global__ void __launch_bounds__(256)
 }  // namespace ev
 }  // namespace g2
 
-extern "C" int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, int32_t elem_bytes,
-                                int64_t n_events, const uint32_t* offsets_dev, int64_t npix,
-                                const int32_t* pix_list_dev, const int32_t* range_off_dev,
-                                const int32_t* range_bin_dev, int32_t n_ranges, const int32_t* cta_range_off_dev,
-                                int32_t n_ctas, int32_t nframes, int32_t n_bins,
-                                int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev, int32_t* err_dev,
-                                void* stream) {
+namespace {
+template <bool PACKED>
+int pairsum(const int32_t* times_dev, const void* data_dev, int32_t elem_bytes, int64_t n_events,
+            const uint32_t* offsets_dev, int64_t npix, const int32_t* pix_list_dev, const int32_t* range_off_dev,
+            const int32_t* range_bin_dev, int32_t n_ranges, const int32_t* cta_range_off_dev, int32_t n_ctas,
+            int32_t nframes, int32_t n_bins, int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev,
+            int32_t* err_dev, void* stream) {
   using namespace g2;
-  if (!times_dev || !data_dev || !offsets_dev || !pix_list_dev || !range_off_dev || !range_bin_dev ||
-      !cta_range_off_dev || !numer_dev || !sums_dev || !err_dev)
-    return G2_ERR_ARG;
-  if ((elem_bytes != 1 && elem_bytes != 2) || n_events < 0 || npix <= 0 || n_ranges < 0 || nframes <= 0 ||
-      n_bins <= 0 || max_count < 0)
-    return G2_ERR_ARG;
   if (n_ranges == 0 || n_ctas <= 0) return G2_OK;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return G2_ERR_CUDA;
@@ -263,33 +278,67 @@ extern "C" int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, 
   auto* N = reinterpret_cast<unsigned long long*>(numer_dev);
   auto* S = reinterpret_cast<unsigned long long*>(sums_dev);
   cudaStream_t st = as_stream(stream);
-  if (use_smem) {
-    if (elem_bytes == 1) {
-      if (cudaFuncSetAttribute(ev::pairs_smem_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(smem)) != cudaSuccess)
-        return G2_ERR_CUDA;
-      ev::pairs_smem_kernel<uint8_t><<<n_ctas, ev::THREADS, smem, st>>>(
-          times_dev, reinterpret_cast<const uint8_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins,
-          static_cast<uint32_t>(max_count), N, S, err_dev);
-    } else {
-      if (cudaFuncSetAttribute(ev::pairs_smem_kernel<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(smem)) != cudaSuccess)
-        return G2_ERR_CUDA;
-      ev::pairs_smem_kernel<uint16_t><<<n_ctas, ev::THREADS, smem, st>>>(
-          times_dev, reinterpret_cast<const uint16_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins,
-          static_cast<uint32_t>(max_count), N, S, err_dev);
-    }
-  } else {
-    if (elem_bytes == 1)
-      ev::pairs_global_kernel<uint8_t><<<n_ctas, 256, 0, st>>>(
-          times_dev, reinterpret_cast<const uint8_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
-    else
-      ev::pairs_global_kernel<uint16_t><<<n_ctas, 256, 0, st>>>(
-          times_dev, reinterpret_cast<const uint16_t*>(data_dev), offsets_dev, pix_list_dev, range_off_dev,
-          range_bin_dev, cta_range_off_dev, n_ranges, n_events, npix, nframes, n_bins, N, S, err_dev);
-  }
+  const uint32_t maxc = static_cast<uint32_t>(max_count);
+#define G2_PAIRS(TV)                                                                                              \
+  do {                                                                                                            \
+    const TV* d = reinterpret_cast<const TV*>(data_dev);                                                          \
+    if (use_smem) {                                                                                               \
+      if (cudaFuncSetAttribute(ev::pairs_smem_kernel<PACKED, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                               static_cast<int>(smem)) != cudaSuccess)                                            \
+        return G2_ERR_CUDA;                                                                                       \
+      ev::pairs_smem_kernel<PACKED, TV><<<n_ctas, ev::THREADS, smem, st>>>(                                       \
+          times_dev, d, offsets_dev, pix_list_dev, range_off_dev, range_bin_dev, cta_range_off_dev, n_ranges,     \
+          n_events, npix, nframes, n_bins, maxc, N, S, err_dev);                                                  \
+    } else {                                                                                                      \
+      ev::pairs_global_kernel<PACKED, TV><<<n_ctas, 256, 0, st>>>(times_dev, d, offsets_dev, pix_list_dev,       \
+                                                                  range_off_dev, range_bin_dev, cta_range_off_dev, \
+                                                                  n_ranges, n_events, npix, nframes, n_bins, N, S, \
+                                                                  err_dev);                                       \
+    }                                                                                                             \
+  } while (0)
+  if (elem_bytes == 1)
+    G2_PAIRS(uint8_t);
+  else
+    G2_PAIRS(uint16_t);
+#undef G2_PAIRS
   return launch_status();
+}
+}  // namespace
+
+extern "C" int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, int32_t elem_bytes,
+                                int64_t n_events, const uint32_t* offsets_dev, int64_t npix,
+                                const int32_t* pix_list_dev, const int32_t* range_off_dev,
+                                const int32_t* range_bin_dev, int32_t n_ranges, const int32_t* cta_range_off_dev,
+                                int32_t n_ctas, int32_t nframes, int32_t n_bins,
+                                int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev, int32_t* err_dev,
+                                void* stream) {
+  using namespace g2;
+  if (!times_dev || !data_dev || !offsets_dev || !pix_list_dev || !range_off_dev || !range_bin_dev ||
+      !cta_range_off_dev || !numer_dev || !sums_dev || !err_dev)
+    return G2_ERR_ARG;
+  if ((elem_bytes != 1 && elem_bytes != 2) || n_events < 0 || npix <= 0 || n_ranges < 0 || nframes <= 0 ||
+      n_bins <= 0 || max_count < 0 || max_count > 65535)
+    return G2_ERR_ARG;
+  return pairsum<false>(times_dev, data_dev, elem_bytes, n_events, offsets_dev, npix, pix_list_dev, range_off_dev,
+                        range_bin_dev, n_ranges, cta_range_off_dev, n_ctas, nframes, n_bins, max_count, numer_dev,
+                        sums_dev, err_dev, stream);
+}
+
+extern "C" int g2_event_pairsum_packed(const uint32_t* words_dev, int64_t n_events, const uint32_t* offsets_dev,
+                                       int64_t npix, const int32_t* pix_list_dev, const int32_t* range_off_dev,
+                                       const int32_t* range_bin_dev, int32_t n_ranges,
+                                       const int32_t* cta_range_off_dev, int32_t n_ctas, int32_t nframes,
+                                       int32_t n_bins, int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev,
+                                       int32_t* err_dev, void* stream) {
+  using namespace g2;
+  if (!words_dev || !offsets_dev || !pix_list_dev || !range_off_dev || !range_bin_dev || !cta_range_off_dev ||
+      !numer_dev || !sums_dev || !err_dev)
+    return G2_ERR_ARG;
+  if (n_events < 0 || npix <= 0 || n_ranges < 0 || nframes <= 0 || nframes > 65536 || n_bins <= 0 ||
+      max_count < 0 || max_count > 65535)
+    return G2_ERR_ARG;
+  // the data pointer is unused on the packed path; elem_bytes 1 selects one instantiation
+  return pairsum<true>(reinterpret_cast<const int32_t*>(words_dev), words_dev, 1, n_events, offsets_dev, npix,
+                       pix_list_dev, range_off_dev, range_bin_dev, n_ranges, cta_range_off_dev, n_ctas, nframes,
+                       n_bins, max_count, numer_dev, sums_dev, err_dev, stream);
 }

@@ -20,8 +20,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .plan import (E4M3_MAX_EXACT, EXACT_LIMIT, FP16_MAX_EXACT, MODE_BYTES, MODE_E4M3, MODE_FP16, PackLayout,
-                   chunk_grams, e4m3_segment_bound, gram_items)
+from .plan import (E4M3_MAX_EXACT, EXACT_LIMIT, FP16_MAX_EXACT, MODE_BYTES, MODE_E4M3, MODE_FP16, TC_BN,
+                   PackLayout, chunk_grams, e4m3_segment_bound, gram_items)
 
 
 def _torch():
@@ -134,6 +134,7 @@ class DenseEngine:
         self.last = {}
         self._u8_hint = MODE_E4M3 if method == "tc" else MODE_FP16
         self._packed_mode = None
+        self.pipeline = True      # chunked copy/pack/Gram overlap where it applies
         self.profile = False      # record CUDA events around every stage
         self.stage_ms = {}
         self._events = []
@@ -312,8 +313,119 @@ class DenseEngine:
                 self._u8_hint = MODE_E4M3        # every count <= 16: the next call can use e4m3
             return L, grams
 
+    # -- chunked pipeline (e4m3) ---------------------------------------------
+    PIPE_CHUNKS = 8
+
+    def _pipe_plan(self, L):
+        """Items of the e4m3 Gram grouped by the frame chunk whose packing
+        makes them ready (a tile needs frames up to its last column), LPT order
+        inside a group; cached per layout."""
+        key = ("pipe", L.mode, self.T, self.exact_limit, self.grid)
+        if key not in self._items_cache:
+            torch = _torch()
+            grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit)
+            items = gram_items(self.T, grams, job=0, out_base=0, kind="tc", s_base=0 if L.ones_row else None)
+            T = self.T
+            n = max(1, min(self.PIPE_CHUNKS, T // 256))
+            step = -(-(-(-T // n)) // 128) * 128               # chunk of frames, a multiple of 128
+            bounds = np.array(list(range(0, T, step)) + [T], dtype=np.int64)
+            need = np.minimum(items["j0"].astype(np.int64) + TC_BN, T)
+            grp = np.searchsorted(bounds[1:], need, side="left")
+            order = np.argsort(grp, kind="stable")
+            items, grp = items[order], grp[order]
+            starts = np.searchsorted(grp, np.arange(bounds.size), side="left")
+            dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
+            if len(self._items_cache) > 8:
+                self._items_cache.clear()
+            self._items_cache[key] = (items, dev_items, bounds, starts, len(grams))
+        return self._items_cache[key]
+
+    def _streams(self):
+        if getattr(self, "_side_streams", None) is None:
+            torch = _torch()
+            self._side_streams = (torch.cuda.Stream(self.dev), torch.cuda.Stream(self.dev))
+        return self._side_streams
+
+    def _frames_buffer(self, like):
+        torch = _torch()
+        buf = getattr(self, "_frames_buf", None)
+        if buf is None or buf.dtype != like.dtype or tuple(buf.shape) != tuple(like.shape):
+            self._frames_buf = None
+            self._frames_buf = torch.empty(like.shape, dtype=like.dtype, device=self.dev)
+        return self._frames_buf
+
+    def pipelined_ok(self, frames):
+        """The chunked pipeline applies to u8 stacks on the tensor-core path
+        while their counts are known (or expected) to be <= 16."""
+        torch = _torch()
+        return (self.method == "tc" and self.operand in ("auto", "e4m3") and self.pipeline
+                and isinstance(frames, torch.Tensor) and frames.dtype == torch.uint8
+                and (self.operand == "e4m3" or self._u8_hint == MODE_E4M3) and self.n_bins > 0
+                and (frames.is_cuda or (frames.is_pinned() and frames.is_contiguous())))
+
+    def run_pipelined(self, frames):
+        """G1 + G2 chunk by chunk of frames: copy (host input) -> pack -> the
+        Gram tiles that chunk completes, on three streams, so copies, packing
+        and tensor-core work overlap; then G3 + G4.  One synchronisation at the
+        end reads the error word; counts above 16 rerun on fp16 operands."""
+        torch = _torch()
+        L = self._layout(MODE_E4M3)
+        packed = self._packed_buffer(L)
+        items, dev_items, bounds, starts, n_grams = self._pipe_plan(L)
+        host = not frames.is_cuda
+        frames_dev = self._frames_buffer(frames) if host else frames
+        if not host and frames_dev.data_ptr() % 16:
+            frames_dev = frames_dev.clone()
+        cur = torch.cuda.current_stream(self.dev)
+        copy_s, pack_s = self._streams()
+        self._events = []
+        self._mark("pipeline")
+        self.numer.zero_()
+        self.sums.zero_()
+        self.err.zero_()
+        start = torch.cuda.Event()
+        start.record(cur)                     # the previous call's work and the zeroing are done first
+        copy_s.wait_event(start)
+        pack_s.wait_event(start)
+        npix, pc = self.npix, L.packed_cols
+        jobs = _lib.jobs_array([(packed.data_ptr(), self.T, pc, L.kind, L.ones_row)])
+        item_bytes = _lib.ITEM_DTYPE.itemsize
+        for c in range(bounds.size - 1):
+            t0, t1 = int(bounds[c]), int(bounds[c + 1])
+            if host:
+                with torch.cuda.stream(copy_s):
+                    frames_dev[t0:t1].copy_(frames[t0:t1], non_blocking=True)
+                    e = torch.cuda.Event()
+                    e.record(copy_s)
+                pack_s.wait_event(e)
+            _lib.check(self.lib.g2_pack_e4m3(
+                frames_dev.data_ptr() + t0 * npix, 1, t1 - t0, npix, ptr(L.d_chunk_word_off), ptr(L.d_word_dst),
+                ptr(L.d_word_src), L.n_chunks, packed.data_ptr() + t0 * pc, pc, ptr(self.err),
+                pack_s.cuda_stream), "g2_pack_e4m3")
+            e = torch.cuda.Event()
+            e.record(pack_s)
+            cur.wait_event(e)
+            k0, k1 = int(starts[c]), int(starts[c + 1])
+            if k1 > k0:
+                _lib.check(self.lib.g2_gram_tc(jobs, 1, dev_items.data_ptr() + k0 * item_bytes, k1 - k0,
+                                               ptr(self.numer), self.numer.numel(), ptr(self.sums),
+                                               self.sums.numel(), ptr(self.err), self.grid, cur.cuda_stream),
+                           "g2_gram_tc")
+        self._mark("normalise")
+        self.normalise()
+        self._mark("end")
+        if host:
+            self._frames_host_ref = frames            # alive until the copies are done
+        code = int(self.err.item())
+        if code & _lib.DEVERR_RANGE and self.operand == "auto":
+            self._u8_hint = MODE_FP16                 # counts above 16: rerun on fp16 operands
+            return self.run(frames_dev, pipelined=False)
+        self.last = {"mode": "e4m3", "split": int(L.split), "n_items": int(items.size), "n_grams": n_grams,
+                     "packed_cols": L.packed_cols, "pipeline_chunks": int(bounds.size - 1)}
+        return self.g2_f32[: self.n_bins]
+
     # -- whole pipeline ----------------------------------------------------
-    def run(self, frames_dev):
+    def run(self, frames_dev, pipelined=True):
         """Run G1..G4 on a device stack; returns the float32 g2 device tensor.
 
         Synchronises once after G1 to read the segment energies (K split)."""
@@ -322,6 +434,10 @@ class DenseEngine:
                                                                     tuple(frames_dev.shape)))
         if self.n_bins == 0:
             return self.g2_f32[:0]
+        if pipelined and self.pipelined_ok(frames_dev):
+            return self.run_pipelined(frames_dev)
+        if not frames_dev.is_cuda:
+            frames_dev = frames_to_device(frames_dev, self.dev)
         self._events = []
         self._mark("split")
         mode = self.choose_mode(frames_dev)

@@ -231,8 +231,10 @@ class EventEngine:
         return self.run_device(times, counts, offs, n_ev, mx)
 
     def run_device(self, times, counts, offs, n_ev, mx, reset_error=True):
-        """G6 + G3 + G4 on validated device events (``reset_error=False`` keeps
-        the flags an earlier stage of the same call has set)."""
+        """G6 + G3 + G4 on validated device events: ``times`` int32 with
+        ``counts``, or packed words ``(t << 16) | v`` with ``counts=None``
+        (``reset_error=False`` keeps the flags an earlier stage of the same
+        call has set)."""
         self.numer.zero_()
         self.sums.zero_()
         if reset_error:
@@ -243,7 +245,12 @@ class EventEngine:
         use_smem = self.T * 8 + 24576 + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
         ro, rb, cro, n_ranges, n_ctas = self.plans["smem" if use_smem else "global"]
         self._mark("start_pairs")
-        if n_ranges and self.n_bins and n_ev:
+        if n_ranges and self.n_bins and n_ev and counts is None:     # packed words (t << 16) | v
+            _lib.check(self.lib.g2_event_pairsum_packed(
+                ptr(times), n_ev, ptr(offs), self.npix, ptr(self.pix_list), ptr(ro), ptr(rb), n_ranges, ptr(cro),
+                n_ctas, self.T, self.n_bins, mx, ptr(self.numer), ptr(self.sums), ptr(self.err), st),
+                "g2_event_pairsum_packed")
+        elif n_ranges and self.n_bins and n_ev:
             _lib.check(self.lib.g2_event_pairsum(
                 ptr(times), ptr(counts), counts.element_size(), n_ev, ptr(offs), self.npix, ptr(self.pix_list),
                 ptr(ro), ptr(rb), n_ranges, ptr(cro), n_ctas, self.T, self.n_bins, mx, ptr(self.numer),
@@ -280,37 +287,83 @@ class SparseEngine:
         self._ev_cap = 0
         self.last = {}
 
-    def to_events(self, data, indices, indptr, offsets, ib, n):
-        """CSR on the device -> (times, counts, offsets) event lists on the device."""
-        torch = _torch()
+    ROW_MAX_W = 29000
+
+    @property
+    def packed(self):
+        """Events travel as packed words (t << 16) | v: frames < 2^16 and rows
+        the row-owned kernels take."""
+        return self.T <= 65535 and self.shape[1] <= self.ROW_MAX_W
+
+    def _counts_and_offsets(self, indices, indptr, offsets, ib, n):
         st = stream_handle(self.dev)
-        err = self.events.err
-        err.zero_()
-        self.counts.zero_()
         H, W = self.shape
-        self.events._mark("start_transpose")
+        self.counts.zero_()
         _lib.check(self.lib.g2_csr_count(ptr(indices), ptr(indptr), ptr(offsets), ib, n, self.T, H, W,
-                                         ptr(self.counts), ptr(err), st), "g2_csr_count")
+                                         ptr(self.counts), ptr(self.events.err), st), "g2_csr_count")
         _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
                                                   ptr(self.scan_scratch), self.scan_scratch.numel(), st),
                    "g2_exclusive_scan_u32")
-        if n > self._ev_cap or not hasattr(self, "ev_times") or self.ev_data.dtype != data.dtype:
-            self._ev_cap = max(n, 1)
-            self.ev_times = torch.empty(self._ev_cap, dtype=torch.int32, device=self.dev)
-            self.ev_data = torch.empty(self._ev_cap, dtype=data.dtype, device=self.dev)
+
+    def _buffer(self, name, n, dtype):
+        torch = _torch()
+        buf = getattr(self, name, None)
+        if buf is None or buf.numel() < max(n, 1) or buf.dtype != dtype:
+            setattr(self, name, None)
+            buf = torch.empty(max(n, 1), dtype=dtype, device=self.dev)
+            setattr(self, name, buf)
+        return buf
+
+    def to_words(self, data, indices, indptr, offsets, ib, n):
+        """CSR on the device -> packed event words and event offsets (uint32
+        as int32) on the device; requires :attr:`packed`."""
+        torch = _torch()
+        H, W = self.shape
+        self.events._mark("start_transpose")
+        self._counts_and_offsets(indices, indptr, offsets, ib, n)
+        words = self._buffer("ev_words", n, torch.int32)
+        _lib.check(self.lib.g2_csr_scatter_packed(ptr(data), data.element_size(), ptr(indices), ptr(indptr),
+                                                  ptr(offsets), ib, n, self.T, H, W, ptr(self.ev_off), ptr(words),
+                                                  ptr(self.events.err), stream_handle(self.dev)),
+                   "g2_csr_scatter_packed")
+        self.events._mark("transpose")
+        return words, self.ev_off
+
+    def to_events(self, data, indices, indptr, offsets, ib, n):
+        """CSR on the device -> (times int32, counts, offsets) event lists on
+        the device, in the FramesCompressor layout (frames ascending within a
+        pixel when :attr:`packed`, else in an unspecified order)."""
+        torch = _torch()
+        self.events.err.zero_()
+        times = self._buffer("ev_times", n, torch.int32)
+        evdata = self._buffer("ev_data", n, data.dtype)
+        if self.packed:
+            words, off = self.to_words(data, indices, indptr, offsets, ib, n)
+            _lib.check(self.lib.g2_events_unpack(ptr(words), n, data.element_size(), ptr(times), ptr(evdata),
+                                                 stream_handle(self.dev)), "g2_events_unpack")
+            return times, evdata, off
+        H, W = self.shape
+        self.events._mark("start_transpose")
+        self._counts_and_offsets(indices, indptr, offsets, ib, n)
         self.counts.zero_()                              # reused as the scatter cursor
         _lib.check(self.lib.g2_csr_scatter(ptr(data), data.element_size(), ptr(indices), ptr(indptr), ptr(offsets),
                                            ib, n, self.T, H, W, ptr(self.ev_off), ptr(self.counts),
-                                           ptr(self.ev_times), ptr(self.ev_data), ptr(err), st), "g2_csr_scatter")
+                                           ptr(times), ptr(evdata), ptr(self.events.err), stream_handle(self.dev)),
+                   "g2_csr_scatter")
         self.events._mark("transpose")
-        return self.ev_times, self.ev_data, self.ev_off
+        return times, evdata, self.ev_off
 
     def run(self, data, indices, indptr, offsets):
         counts, ind, ip, off, ib, n, mx = csr_to_device(data, indices, indptr, offsets, self.shape, self.T,
                                                         self.dev)
-        times, evdata, evoff = self.to_events(counts, ind, ip, off, ib, n)
-        out = self.events.run_device(times, evdata, evoff, n, mx, reset_error=False)
-        self.last = dict(self.events.last, n_elements=n)
+        if self.packed:
+            self.events.err.zero_()
+            words, evoff = self.to_words(counts, ind, ip, off, ib, n)
+            out = self.events.run_device(words, None, evoff, n, mx, reset_error=False)
+        else:
+            times, evdata, evoff = self.to_events(counts, ind, ip, off, ib, n)
+            out = self.events.run_device(times, evdata, evoff, n, mx, reset_error=False)
+        self.last = dict(self.events.last, n_elements=n, packed=self.packed)
         return out
 
     def check_error(self):

@@ -197,6 +197,14 @@ int g2_event_pairsum(const int32_t* times_dev, const void* data_dev, int32_t ele
                      int32_t max_count, uint64_t* numer_dev, uint64_t* sums_dev, int32_t* err_dev,
                      void* stream);
 
+/* g2_event_pairsum on packed event words (t << 16) | v (as written by
+ * g2_csr_scatter_packed), nframes <= 65536; same plan arguments and sums. */
+int g2_event_pairsum_packed(const uint32_t* words_dev, int64_t n_events, const uint32_t* offsets_dev,
+                            int64_t npix, const int32_t* pix_list_dev, const int32_t* range_off_dev,
+                            const int32_t* range_bin_dev, int32_t n_ranges, const int32_t* cta_range_off_dev,
+                            int32_t n_ctas, int32_t nframes, int32_t n_bins, int32_t max_count,
+                            uint64_t* numer_dev, uint64_t* sums_dev, int32_t* err_dev, void* stream);
+
 /* ---- G7: CSR frames -> per-pixel event lists ----------------------------
  * Replaces the CSR path of SparseCorrelator (dynamix/correlator/intensity.py:
  * 70-128: compute_sums and correlator_oneQ_Nt, correlator.cl:19-217): the CSR
@@ -221,6 +229,19 @@ int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices
                    int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
                    uint32_t* cursor_dev, int32_t* ev_times_dev, void* ev_data_dev, int32_t* err_dev,
                    void* stream);
+
+/* Packed variants (frames < 2^16, image rows up to 29,000 pixels).
+ * g2_csr_scatter_packed writes each element as one word (t << 16) | v into
+ * ev_words_dev[ev_offsets[p] ..), frames ascending within a pixel (no cursor
+ * array); g2_events_unpack splits such words into ev_times (int32) and ev_data
+ * (elem_bytes 1 or 2), the FramesCompressor layout (event.py:267-284).
+ * Returns G2_ERR_UNSUPPORTED when nframes > 65536 or width > 29,000. */
+int g2_csr_scatter_packed(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                          const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
+                          int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
+                          uint32_t* ev_words_dev, int32_t* err_dev, void* stream);
+int g2_events_unpack(const uint32_t* ev_words_dev, int64_t n_events, int32_t elem_bytes, int32_t* ev_times_dev,
+                     void* ev_data_dev, void* stream);
 
 /* ---- G3: denominator ----------------------------------------------------
  * Replaces correlate_1D (dynamix/resources/opencl/densecorrelator.cl:156-176),

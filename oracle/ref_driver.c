@@ -5,7 +5,7 @@
  * correlator/event.py:162-204): event_correlator over the (W, H) grid, then
  * normalize_correlation over (nframes, n_bins).  The caller passes the scalar
  * arguments exactly as the reference does, including its image_height
- * argument (event.py:189 passes shape[1]).  Work-items run on n_threads POSIX
+ * argument (event.py:183 passes shape[1]).  Work-items run on n_threads POSIX
  * threads, rows split among them; the kernels' atomics are real atomics.
  */
 #include <pthread.h>

@@ -11,7 +11,7 @@ a container where the reference sources are available::
 Each fixture holds the event lists, the q-mask and the reference's outputs:
 ``res_int`` (int32 numerator), ``sums`` (uint32 frame sums) and ``g2``
 (float32).  ``event_ref_tall_u8`` is an image taller than wide: the reference
-passes ``shape[1]`` as ``image_height`` (``event.py:189``), so it drops the rows
+passes ``shape[1]`` as ``image_height`` (``event.py:183``), so it drops the rows
 ``y >= width``; the fixture records that behaviour.
 """
 from __future__ import annotations

@@ -3,7 +3,7 @@
 Fixtures ``event_ref_*.npz`` hold the outputs of ``evtcorrelator.cl``
 (``event_correlator`` + ``normalize_correlation``), compiled as C and run on the
 CPU by ``tests/golden/make_event_golden.py``.  The reference launches with
-``image_height = shape[1]`` (``event.py:189``) and so ignores the rows
+``image_height = shape[1]`` (``event.py:183``) and so ignores the rows
 ``y >= width`` of a tall image; the oracle reproduces its sums once those rows
 are masked out.
 """

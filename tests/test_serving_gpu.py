@@ -49,7 +49,7 @@ def test_mix_matches_oracle_and_alone(built_lib, cuda_device):
             inp = fr                                         # numpy
         reqs.append(srv.submit(inp, qm))
     srv.run_until_idle()
-    assert srv.stats["launches"] > len(jobs)
+    assert srv.stats["launches"] >= 3          # jobs span several grouped launches
     assert srv.stats["max_active"] >= 2
     for r, (fr, qm) in zip(reqs, jobs):
         r.wait()

@@ -96,3 +96,23 @@ def test_csr_duplicate_column_is_reported(built_lib, cuda_device):
     c = SparseCorrelator((2, 8), 3)
     with pytest.raises(DeviceError):
         c.correlate(data2, indices2.astype(np.uint32), ip.ravel().astype(np.uint32), off.astype(np.uint32))
+
+
+def test_wide_rows_take_the_walk_kernels(built_lib, cuda_device):
+    """Rows wider than the row-owned kernels take (29,000 px): global-atomic
+    transposition, events unordered within a pixel, same exact sums."""
+    from dynamix_gb300.correlator import SparseCorrelator
+    rng = np.random.default_rng(8)
+    T, H, W = 40, 2, 29010
+    fr = (rng.random((T, H, W)) < 0.002).astype(np.uint8) * rng.integers(1, 5, (T, H, W)).astype(np.uint8)
+    qm = np.zeros((H, W), np.int32)
+    qm[:, :10000] = 1
+    qm[:, 20000:] = 2
+    csr = o.frames_to_csr(fr)
+    c = SparseCorrelator((H, W), T, qmask=qm)
+    g = c.correlate(*csr)
+    assert c.engine.last["packed"] is False
+    ref = o.g2_exact(fr, qm)
+    assert np.array_equal(c.numerator, ref["numerator"])
+    assert np.array_equal(c.sums, ref["sums"])
+    assert np.array_equal(g, ref["g2"].astype(np.float32), equal_nan=True)
