@@ -55,6 +55,8 @@ SIGNATURES = {
     "g2_binned_max": (C.c_int, [_p, _i32, _i64, _i64, _p, _i64, _p, _p]),
     "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
+    "g2_gram_std": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p, _p, _p, _i64, _p, _i32, _p]),
+    "g2_std_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
     "g2_event_pairsum": (C.c_int, [_p, _p, _i32, _i64, _p, _i64, _p, _p, _p, _i32, _p, _i32, _i32, _i32, _i32, _p,
                                    _p, _p, _p]),
     "g2_event_pairsum_packed": (C.c_int, [_p, _i64, _p, _i64, _p, _p, _p, _i32, _p, _i32, _i32, _i32, _i32, _p,
@@ -63,6 +65,7 @@ SIGNATURES = {
     "g2_exclusive_scan_u32": (C.c_int, [_p, _i64, _p, _p, _i64, _p]),
     "g2_csr_scatter": (C.c_int, [_p, _i32, _p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),
     "g2_csr_scatter_packed": (C.c_int, [_p, _i32, _p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p]),
+    "g2_events_sort_windows": (C.c_int, [_p, _p, _i64, _p]),
     "g2_events_unpack": (C.c_int, [_p, _i64, _i32, _p, _p, _p]),
     "g2_denominator": (C.c_int, [_p, _i32, _i64, _p, _p]),
     "g2_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),

@@ -54,12 +54,18 @@ class _DenseBase(BaseCorrelator):
         return out
 
     def correlate(self, frames, calc_std=False):
-        if calc_std:
-            raise NotImplementedError("calc_std is not available on the GPU path yet")
+        """g2 as float32 ``(n_bins, nframes)``; with ``calc_std`` a
+        ``CorrelationResult(res, dev)`` whose ``dev`` is the deviation of
+        dense.py:58-66 (float32, computed in float on the tensor cores and
+        reduced in float64; NaN where the reference divides by zero)."""
         out = self.correlate_device(frames)
         res = out.cpu().numpy()
         self.engine.check_error()
         self.engine.check_denominator_range()
+        if calc_std:
+            dev = self.engine.deviation().cpu().numpy()
+            self.engine.check_error()
+            return CorrelationResult(res, dev)
         return res
 
     # exact intermediate results of the last call (int64 / float64 numpy)
@@ -107,14 +113,16 @@ class DenseCorrelator(_DenseBase):
 
 
 def py_dense_correlator(xpcs_data, mask, calc_std=False):
-    """g2 of the pixels ``mask > 0`` of a (T, H, W) stack, float64 (T,).
+    """g2 of the pixels ``mask > 0`` of a (T, H, W) stack, float64 (T,), or
+    ``CorrelationResult(res, dev)`` with ``calc_std``.
 
-    Same contract as dense.py:32-70 (without ``calc_std``), evaluated on the GPU."""
+    Same contract as dense.py:32-70, evaluated on the GPU."""
     mask = np.asarray(mask)
     q = (mask > 0).astype(np.int32)
     T = np.shape(xpcs_data)[0]
     corr = MatMulCorrelator(q.shape, T, qmask=q)
-    if calc_std:
-        raise NotImplementedError("calc_std is not available on the GPU path yet")
     corr.correlate(xpcs_data)
+    if calc_std:
+        corr.engine.deviation()
+        return CorrelationResult(corr.g2_fp64[0], corr.engine.dev_f64[0].cpu().numpy())
     return corr.g2_fp64[0]

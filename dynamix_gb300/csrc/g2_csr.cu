@@ -229,121 +229,103 @@ __global__ void __launch_bounds__(256)
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
 
-// Scatter into packed event words (t << 16 | v; frames < 2^16), one CTA per
-// image row: its warps split the row's columns (a warp's lanes still take 32
-// consecutive frames), so a pixel's slot cursor and batch mask are touched by
-// one warp only.  The CTA asks for ROW_SMEM_FLOOR bytes of shared memory so
-// that few rows are in flight at once: the sectors being filled (one per
-// pixel of every row in flight) then stay in L2 until they are complete.
-constexpr int PK_WARPS = 8;
-constexpr int ROW_SMEM_FLOOR = 56 * 1024;
-
+// Scatter into packed event words (t << 16 | v; frames < 2^16): one warp owns
+// one image row for all frames (lanes = 32 consecutive frames), the row's slot
+// cursors in its shared memory, one shared atomic per element.  Pixels' events
+// come out ordered by 32-frame batch, in any order inside a batch (the pair
+// sums do not depend on it; sort_windows_kernel restores frame order where the
+// FramesCompressor layout is wanted).  Column indices must increase strictly
+// inside a row (sorted CSR, as correlator.cl:185-197 assumes); a repeated or
+// descending column is reported.
 template <typename Tv, typename Ti>
-__global__ void __launch_bounds__(PK_WARPS * 32)
+__global__ void __launch_bounds__(256)
     row_scatter_packed_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices,
                               const Ti* __restrict__ indptr, const Ti* __restrict__ offsets, int64_t n_elem,
-                              int32_t T, int32_t H, int32_t W, const uint32_t* __restrict__ ev_off,
+                              int32_t T, int32_t H, int32_t W, int rows_per_cta, const uint32_t* __restrict__ ev_off,
                               uint32_t* __restrict__ ev_words, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x;
-  if (r >= H) return;
-  uint32_t* cur = sm;        // [W] next free slot of each pixel of the row
-  uint32_t* msk = sm + W;    // [W] frames of the batch holding the pixel
+  const int r = blockIdx.x * rows_per_cta + warp;
+  if (warp >= rows_per_cta || r >= H) return;  // warp-uniform; no block barrier below
+  uint32_t* cur = sm + static_cast<int64_t>(warp) * W;
   const uint32_t* row_off = ev_off + static_cast<int64_t>(r) * W;
   const uint32_t n_total = ev_off[static_cast<int64_t>(H) * W];
-  for (int i = threadIdx.x; i < W; i += blockDim.x) {
-    cur[i] = row_off[i];
-    msk[i] = 0;
-  }
-  __syncthreads();
-  // this warp's columns [c0, c1)
-  const int per = (W + PK_WARPS - 1) / PK_WARPS;
-  const int c0 = min(W, warp * per), c1 = min(W, c0 + per);
+  for (int i = lane; i < W; i += 32) cur[i] = row_off[i];
+  __syncwarp();
   bool bad = false;
-  const uint32_t bit = 1u << lane;
   for (int64_t t0 = 0; t0 < T; t0 += 32) {
     const int64_t t = t0 + lane;
-    int64_t s = 0, e = 0;
-    if (t < T) {
-      const int64_t base = static_cast<int64_t>(offsets[t]);
-      const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
-      const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
-      s = base + static_cast<int64_t>(ip[0]);
-      e = base + static_cast<int64_t>(ip[1]);
-      if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
-        bad = true;
-        s = e = 0;
-      }
+    if (t >= T) continue;
+    const int64_t base = static_cast<int64_t>(offsets[t]);
+    const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
+    const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
+    const int64_t s = base + static_cast<int64_t>(ip[0]);
+    const int64_t e = base + static_cast<int64_t>(ip[1]);
+    if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+      bad = true;
+      continue;
     }
-    const int len = static_cast<int>(e - s);
-    int32_t col[KREG];
-    uint32_t val[KREG];
-#pragma unroll
-    for (int j = 0; j < KREG; ++j) {
-      col[j] = -1;
-      if (j < len) {
-        const int64_t c = static_cast<int64_t>(indices[s + j]);
-        if (c >= c0 && c < c1) {
-          col[j] = static_cast<int32_t>(c);
-          val[j] = static_cast<uint32_t>(data[s + j]);
-        }
-      }
-    }
-    // 1. mark the frames of the batch holding each pixel
-#pragma unroll
-    for (int j = 0; j < KREG; ++j)
-      if (col[j] >= 0 && (atomicOr(&msk[col[j]], bit) & bit)) bad = true;  // a column twice in one row
-    for (int j = KREG; j < len; ++j) {
-      const int64_t c = static_cast<int64_t>(indices[s + j]);
-      if (c >= c0 && c < c1 && (atomicOr(&msk[c], bit) & bit)) bad = true;
-    }
-    __syncwarp();
-    // 2. slot = next free slot + earlier frames of the batch holding the pixel
     const uint32_t tw = static_cast<uint32_t>(t) << 16;
-#pragma unroll
-    for (int j = 0; j < KREG; ++j) {
-      if (col[j] >= 0) {
-        const uint32_t slot = cur[col[j]] + __popc(msk[col[j]] & (bit - 1u));
-        if (slot < n_total)
-          ev_words[slot] = tw | val[j];
-        else
-          bad = true;
+    int64_t prev = -1;
+#pragma unroll 4
+    for (int64_t k = s; k < e; ++k) {
+      const int64_t c = static_cast<int64_t>(indices[k]);
+      if (c <= prev || c >= W) {
+        bad = true;
+        if (c < 0 || c >= W) continue;
       }
-    }
-    for (int j = KREG; j < len; ++j) {
-      const int64_t c = static_cast<int64_t>(indices[s + j]);
-      if (c < c0 || c >= c1) continue;
-      const uint32_t slot = cur[c] + __popc(msk[c] & (bit - 1u));
+      prev = c;
+      const uint32_t slot = atomicAdd(&cur[c], 1u);
       if (slot < n_total)
-        ev_words[slot] = tw | static_cast<uint32_t>(data[s + j]);
+        ev_words[slot] = tw | static_cast<uint32_t>(data[k]);
       else
         bad = true;
     }
-    __syncwarp();
-    // 3. the last frame of the batch holding the pixel advances its cursor
-#pragma unroll
-    for (int j = 0; j < KREG; ++j) {
-      if (col[j] >= 0) {
-        const uint32_t m = msk[col[j]];
-        if (m != 0u && (m >> lane) == 1u) {
-          cur[col[j]] += __popc(m);
-          msk[col[j]] = 0u;
-        }
-      }
-    }
-    for (int j = KREG; j < len; ++j) {
-      const int64_t c = static_cast<int64_t>(indices[s + j]);
-      if (c < c0 || c >= c1) continue;
-      const uint32_t m = msk[c];
-      if (m != 0u && (m >> lane) == 1u) {
-        cur[c] += __popc(m);
-        msk[c] = 0u;
-      }
-    }
-    __syncwarp();
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// Frame order inside each pixel's list of packed words that is already ordered
+// by 32-frame window (t >> 5): a warp per pixel takes 32 words at a time and
+// ranks each word inside its window group by shuffles; a group that may run on
+// past the 32 words waits for the next round.
+__global__ void __launch_bounds__(256)
+    sort_windows_kernel(uint32_t* __restrict__ words, const uint32_t* __restrict__ ev_off, int64_t npix) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x >> 5) + (threadIdx.x >> 5); p < npix;
+       p += warps) {
+    const int64_t s = ev_off[p];
+    const int64_t n = static_cast<int64_t>(ev_off[p + 1]) - s;
+    int64_t c0 = 0;
+    while (c0 + 1 < n) {
+      const bool has = c0 + lane < n;
+      const uint32_t w = has ? words[s + c0 + lane] : 0xFFFFFFFFu;
+      const uint32_t win = has ? (w >> 21) : 0xFFFFFFFFu;          // (t >> 5)
+      const uint32_t prev_win = __shfl_up_sync(0xffffffffu, win, 1);
+      const uint32_t heads = __ballot_sync(0xffffffffu, has && (lane == 0 || win != prev_win));
+      const int avail = static_cast<int>(n - c0 < 32 ? n - c0 : 32);
+      int commit = avail;
+      if (c0 + 32 < n) {                                            // the last group may continue
+        const int last_head = 31 - __clz(heads);
+        commit = last_head > 0 ? last_head : 32;
+      }
+      const uint32_t le = heads & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
+      const int start = le ? 31 - __clz(le) : 0;
+      const uint32_t gt = heads & ~(lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
+      const int gend = min(gt ? __ffs(gt) - 1 : 32, commit);
+      const uint32_t t = w >> 16;
+      int rank = 0;
+      for (int j = 0; j < 32; ++j) {
+        const uint32_t tj = __shfl_sync(0xffffffffu, t, j);
+        rank += (j >= start && j < gend && (tj < t || (tj == t && j < lane))) ? 1 : 0;
+      }
+      __syncwarp();
+      if (lane < commit) words[s + c0 + start + rank] = w;
+      __syncwarp();
+      c0 += commit;
+    }
+  }
 }
 
 // Packed words -> (times int32, data) arrays.
@@ -612,22 +594,36 @@ extern "C" int g2_csr_scatter_packed(const void* data_dev, int32_t elem_bytes, c
       nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
   if (nframes > 65536 || width > csr::ROW_MAX_W) return G2_ERR_UNSUPPORTED;
-  const int64_t need = static_cast<int64_t>(width) * 8;
-  const int64_t smem = need > csr::ROW_SMEM_FLOOR ? need : csr::ROW_SMEM_FLOOR;
+  const int rpc = rows_per_cta(width, 1);
+  const int64_t smem = static_cast<int64_t>(rpc) * width * 4;
+  const unsigned grid = static_cast<unsigned>((height + rpc - 1) / rpc);
   cudaStream_t st = as_stream(stream);
 #define G2_PK(TV, TI)                                                                                           \
   do {                                                                                                          \
     if (!allow_smem(csr::row_scatter_packed_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                          \
-    csr::row_scatter_packed_kernel<TV, TI><<<static_cast<unsigned>(height), csr::PK_WARPS * 32, smem, st>>>(     \
+    csr::row_scatter_packed_kernel<TV, TI><<<grid, rpc * 32, smem, st>>>(                                       \
         reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev),                        \
         reinterpret_cast<const TI*>(indptr_dev), reinterpret_cast<const TI*>(offsets_dev), n_elem, nframes,     \
-        height, width, ev_offsets_dev, ev_words_dev, err_dev);                                                  \
+        height, width, rpc, ev_offsets_dev, ev_words_dev, err_dev);                                             \
   } while (0)
   if (elem_bytes == 1 && index_bytes == 4) G2_PK(uint8_t, uint32_t);
   else if (elem_bytes == 1) G2_PK(uint8_t, int64_t);
   else if (index_bytes == 4) G2_PK(uint16_t, uint32_t);
   else G2_PK(uint16_t, int64_t);
 #undef G2_PK
+  return launch_status();
+}
+
+extern "C" int g2_events_sort_windows(uint32_t* ev_words_dev, const uint32_t* ev_offsets_dev, int64_t npix,
+                                      void* stream) {
+  using namespace g2;
+  if (!ev_words_dev || !ev_offsets_dev || npix <= 0) return G2_ERR_ARG;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  int64_t blocks = (npix + 7) / 8;
+  if (blocks > static_cast<int64_t>(sms) * 16) blocks = static_cast<int64_t>(sms) * 16;
+  csr::sort_windows_kernel<<<static_cast<unsigned>(blocks), 256, 0, as_stream(stream)>>>(ev_words_dev,
+                                                                                       ev_offsets_dev, npix);
   return launch_status();
 }
 

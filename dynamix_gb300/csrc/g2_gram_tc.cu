@@ -49,6 +49,22 @@ constexpr uint32_t IDESC = idesc_f32acc(BM, BN);  // same bits for fp16 and e4m3
 
 constexpr int SMEM_BAR_OFF = STAGES * STAGE_BYTES;
 constexpr int SMEM_BYTES = 1024 /*alignment slack*/ + SMEM_BAR_OFF + 256 + 2 * NDIAG_PAD * 4;
+// deviation mode: per TMEM buffer the lag centres, sums of d, sums of d^2 and
+// zero-denominator counts (4 x NDIAG_PAD words)
+constexpr int STD_WORDS = 4 * NDIAG_PAD;
+constexpr int SMEM_BYTES_STD = 1024 + SMEM_BAR_OFF + 256 + 2 * STD_WORDS * 4;
+
+// Outputs of the deviation mode (calc_std of dense.py:58-66): for every pair
+// t' >= t of one bin, r = P G(t,t') / (S(t) S(t')) and d = r - centre(tau);
+// the lag sums of d and d^2 (float per block, double in memory) and the count
+// of pairs with S(t) S(t') = 0.
+struct StdOut {
+  const long long* S;      // bin sums, indexed by item.s_off + t
+  const float* centre;     // per lag, indexed by item.out_off + tau
+  double* sum_d;           // indexed by item.out_off + tau
+  double* sum_d2;
+  unsigned int* zeros;
+};
 
 struct MapsParam {
   CUtensorMap a[G2_MAX_JOBS];
@@ -75,19 +91,26 @@ __device__ __forceinline__ bool named_bar_any(uint32_t id, uint32_t n, bool v) {
 
 // Every role applies the same test, so a malformed item is skipped by all of
 // them consistently (the epilogue records G2_DEVERR_BOUNDS).
+// In the deviation mode ``shift`` carries the bin's pixel count and ``s_off``
+// the offset of its sums.
+template <bool STD>
 __device__ __forceinline__ bool item_ok(const g2_gram_item& w, const MapsParam& maps, int n_jobs,
                                         int64_t numer_len, int64_t sums_len) {
   if (w.job < 0 || w.job >= n_jobs) return false;
   const int bk = stage_elems(maps.kind[w.job]);
-  return w.k_len > 0 && (w.k_len % bk) == 0 && (w.a_k0 % bk) == 0 && (w.b_k0 % bk) == 0 && w.nframes > 0 &&
-         w.shift >= 0 && w.shift <= 32 && w.out_off >= 0 && w.out_off + w.nframes <= numer_len &&
+  const bool shape = w.k_len > 0 && (w.k_len % bk) == 0 && (w.a_k0 % bk) == 0 && (w.b_k0 % bk) == 0 &&
+                     w.nframes > 0 && w.out_off >= 0 && w.out_off + w.nframes <= numer_len;
+  if (STD) return shape && w.shift > 0 && w.s_off >= 0 && w.s_off + w.nframes <= sums_len;
+  return shape && w.shift >= 0 && w.shift <= 32 &&
          (w.s_off < 0 || (maps.ones[w.job] && w.shift == 0 && w.s_off + w.nframes <= sums_len));
 }
 
+template <bool STD>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     gram_tc_kernel(const __grid_constant__ MapsParam maps, int n_jobs, const g2_gram_item* __restrict__ items,
                    int64_t n_items, unsigned long long* __restrict__ numer, int64_t numer_len,
-                   unsigned long long* __restrict__ sums, int64_t sums_len, int32_t* __restrict__ err) {
+                   unsigned long long* __restrict__ sums, int64_t sums_len, int32_t* __restrict__ err,
+                   const StdOut so) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
@@ -117,7 +140,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     *abort_flag = 0;
     fence_mbar_init();
   }
-  for (int i = threadIdx.x; i < 2 * NDIAG_PAD; i += NUM_THREADS) diag[i] = 0;
+  for (int i = threadIdx.x; i < (STD ? 2 * STD_WORDS : 2 * NDIAG_PAD); i += NUM_THREADS) diag[i] = 0;
   if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
   tc_fence_before();
   __syncthreads();
@@ -133,7 +156,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) continue;
+        if (!item_ok<STD>(w, maps, n_jobs, numer_len, sums_len)) continue;
         const CUtensorMap* ma = &maps.a[w.job];
         const CUtensorMap* mb = &maps.b[w.job];
         const int bk = stage_elems(maps.kind[w.job]);
@@ -171,7 +194,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) continue;
+        if (!item_ok<STD>(w, maps, n_jobs, numer_len, sums_len)) continue;
         const bool fp8 = maps.kind[w.job] == G2_KIND_E4M3;
         const int buf = static_cast<int>(local & 1);
         const uint32_t ap = static_cast<uint32_t>((local >> 1) & 1);
@@ -221,7 +244,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     int64_t local = 0;
     for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x, ++local) {
       const g2_gram_item w = items[it];
-      if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) {
+      if (!item_ok<STD>(w, maps, n_jobs, numer_len, sums_len)) {
         if (etid == 0) atomicOr(err, G2_DEVERR_BOUNDS);
         --local;
         continue;
@@ -240,8 +263,61 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       // lag sums; the column of the row of ones, when this block holds it,
       // goes to the bin sums instead
       const bool row_live = w.i0 + row < w.nframes;
-      const int ones_col = w.s_off >= 0 ? w.nframes - w.j0 : -1;  // -1 or >= BN: not in this block
       const int col_end = min(BN, w.nframes - w.j0);                // columns < col_end are frames
+      const int lag0 = w.j0 - w.i0 - (BM - 1);
+      if (STD) {
+        // ---------------------------------------- deviation mode epilogue
+        float* cen = reinterpret_cast<float*>(diag) + (local & 1) * STD_WORDS;
+        float* sd = cen + NDIAG_PAD;
+        float* sd2 = sd + NDIAG_PAD;
+        unsigned int* zc = reinterpret_cast<unsigned int*>(sd2 + NDIAG_PAD);
+        for (int d = etid; d < NDIAG; d += EPI_THREADS) {
+          const int tau = lag0 + d;
+          const float c = (tau >= 0 && tau < w.nframes) ? so.centre[w.out_off + tau] : 0.0f;
+          cen[d] = isfinite(c) ? c : 0.0f;
+        }
+        named_bar_sync(1, EPI_THREADS);
+        const float P = static_cast<float>(w.shift);
+        const float St = row_live ? static_cast<float>(so.S[w.s_off + w.i0 + row]) : 0.0f;
+#pragma unroll 1
+        for (int cc = 0; cc < BN / 32; ++cc) {
+          uint32_t v[32];
+          __syncwarp();
+          tmem_ld_32x32b_x32(tbase + static_cast<uint32_t>(cc * 32), v);
+          tmem_wait_ld();
+          if (!row_live) continue;
+          const int dbase = cc * 32 - row + (BM - 1);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            if (cc * 32 + j >= col_end || dbase + j < (BM - 1) - (w.j0 - w.i0)) continue;  // t' >= T or t' < t
+            const float den = St * static_cast<float>(so.S[w.s_off + w.j0 + cc * 32 + j]);
+            if (den == 0.0f) {
+              atomicAdd(&zc[dbase + j], 1u);
+            } else {
+              const float r = P * (__uint_as_float(v[j]) * unscale) / den;
+              const float dv = r - cen[dbase + j];
+              atomicAdd(&sd[dbase + j], dv);
+              atomicAdd(&sd2[dbase + j], dv * dv);
+            }
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&acce[buf]);
+        named_bar_sync(1, EPI_THREADS);
+        for (int d = etid; d < NDIAG; d += EPI_THREADS) {
+          const int tau = lag0 + d;
+          if (tau >= 0 && tau < w.nframes) {
+            if (sd[d] != 0.0f) atomicAdd(&so.sum_d[w.out_off + tau], static_cast<double>(sd[d]));
+            if (sd2[d] != 0.0f) atomicAdd(&so.sum_d2[w.out_off + tau], static_cast<double>(sd2[d]));
+            if (zc[d]) atomicAdd(&so.zeros[w.out_off + tau], zc[d]);
+          }
+          sd[d] = 0.0f;
+          sd2[d] = 0.0f;
+          zc[d] = 0u;
+        }
+        continue;
+      }
+      const int ones_col = w.s_off >= 0 ? w.nframes - w.j0 : -1;  // -1 or >= BN: not in this block
 #pragma unroll 1
       for (int cc = 0; cc < BN / 32; ++cc) {
         uint32_t v[32];
@@ -264,7 +340,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       tc_fence_before();
       mbar_arrive(&acce[buf]);
       named_bar_sync(1, EPI_THREADS);
-      const int lag0 = w.j0 - w.i0 - (BM - 1);
       for (int d = etid; d < NDIAG; d += EPI_THREADS) {
         const uint32_t s = dacc[d];
         if (s) {
@@ -288,14 +363,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 }  // namespace tc
 }  // namespace g2
 
-extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
-                          uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
-                          int32_t* err_dev, int32_t grid, void* stream) {
+namespace {
+template <bool STD>
+int launch_gram(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len, int32_t* err_dev,
+                int32_t grid, void* stream, const g2::tc::StdOut& so) {
   using namespace g2;
-  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !numer_dev || numer_len <= 0 || !err_dev ||
-      sums_len < 0 || (sums_len > 0 && !sums_dev))
-    return G2_ERR_ARG;
-  if (n_items > 0 && !items_dev) return G2_ERR_ARG;
   for (int j = 0; j < n_jobs; ++j) {
     const g2_job& jb = jobs[j];
     if (!jb.packed_dev || !aligned(jb.packed_dev, 16) || jb.nframes <= 0 || jb.nframes >= (1ll << 31) ||
@@ -319,15 +392,48 @@ extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item
     maps.kind[j] = jobs[j].elem_kind;
     maps.ones[j] = jobs[j].ones_row;
   }
-  if (cudaFuncSetAttribute(tc::gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES) !=
+  const int smem = STD ? tc::SMEM_BYTES_STD : tc::SMEM_BYTES;
+  if (cudaFuncSetAttribute(tc::gram_tc_kernel<STD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
       cudaSuccess)
     return G2_ERR_CUDA;
   int sms = sm_count_current();
   if (sms <= 0) return G2_ERR_CUDA;
   int64_t g = grid > 0 ? grid : sms;
   if (g > n_items) g = n_items;
-  tc::gram_tc_kernel<<<static_cast<unsigned>(g), tc::NUM_THREADS, tc::SMEM_BYTES, as_stream(stream)>>>(
+  tc::gram_tc_kernel<STD><<<static_cast<unsigned>(g), tc::NUM_THREADS, smem, as_stream(stream)>>>(
       maps, n_jobs, items_dev, n_items, reinterpret_cast<unsigned long long*>(numer_dev), numer_len,
-      reinterpret_cast<unsigned long long*>(sums_dev), sums_len, err_dev);
+      reinterpret_cast<unsigned long long*>(sums_dev), sums_len, err_dev, so);
   return launch_status();
+}
+}  // namespace
+
+extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                          uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
+                          int32_t* err_dev, int32_t grid, void* stream) {
+  using namespace g2;
+  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !numer_dev || numer_len <= 0 || !err_dev ||
+      sums_len < 0 || (sums_len > 0 && !sums_dev))
+    return G2_ERR_ARG;
+  if (n_items > 0 && !items_dev) return G2_ERR_ARG;
+  const tc::StdOut none = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  return launch_gram<false>(jobs, n_jobs, items_dev, n_items, numer_dev, numer_len, sums_dev, sums_len, err_dev,
+                            grid, stream, none);
+}
+
+extern "C" int g2_gram_std(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                           const int64_t* sums_dev, int64_t sums_len, const float* centre_dev, double* sum_d_dev,
+                           double* sum_d2_dev, uint32_t* zeros_dev, int64_t out_len, int32_t* err_dev,
+                           int32_t grid, void* stream) {
+  using namespace g2;
+  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !sums_dev || sums_len <= 0 || !centre_dev ||
+      !sum_d_dev || !sum_d2_dev || !zeros_dev || out_len <= 0 || !err_dev)
+    return G2_ERR_ARG;
+  if (n_items > 0 && !items_dev) return G2_ERR_ARG;
+  const tc::StdOut so = {reinterpret_cast<const long long*>(sums_dev), centre_dev, sum_d_dev, sum_d2_dev,
+                         zeros_dev};
+  // out_len bounds out_off + tau, sums_len bounds s_off + t; numer and sums
+  // are not written in this mode
+  return launch_gram<true>(jobs, n_jobs, items_dev, n_items, reinterpret_cast<uint64_t*>(sum_d_dev), out_len,
+                           reinterpret_cast<uint64_t*>(const_cast<int64_t*>(sums_dev)), sums_len, err_dev, grid,
+                           stream, so);
 }

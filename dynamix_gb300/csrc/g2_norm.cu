@@ -1,7 +1,8 @@
 // G3 (denominator) and G4 (finalize).
 //
 // G3: D[r][tau] = sum_t S[r][t] * S[r][t+tau] in int64 for every row r (one row
-// per (job, bin)).  A block owns 256 consecutive lags of one row and walks t in
+// per (job, bin)).  A block owns 1024 lags of one row (4 per thread, strided by
+// the block size so the shared loads stay conflict-free) and walks t in
 // shared-memory windows of 1024 frames; the shifted window is padded with
 // zeros beyond T, so no per-term bounds test is needed.
 // Replaces correlate_1D (densecorrelator.cl:156-176), the sum loop of
@@ -18,33 +19,65 @@
 namespace g2 {
 namespace norm {
 
-constexpr int LAGS = 256;
-constexpr int WIN = 1024;
+constexpr int THR = 256;
+constexpr int LPT = 4;               // lags per thread, strided by THR
+constexpr int LAGS = THR * LPT;      // lags per block
+constexpr int WIN = 1024;            // frames per shared window
 
-__global__ void __launch_bounds__(LAGS)
+// S values are split into 32-bit halves in shared memory.  Windows whose
+// values all fit in 32 bits (the usual case: a bin sum is at most
+// pixels x max count) take one 32 x 32 -> 64-bit multiply-add per term;
+// others add the cross terms too (arithmetic mod 2^64, exact while D < 2^63,
+// which the host checks).
+__global__ void __launch_bounds__(THR)
     denom_kernel(const long long* __restrict__ S, int64_t T, long long* __restrict__ D) {
-  __shared__ long long s1[WIN];
-  __shared__ long long s2[WIN + LAGS];
+  __shared__ uint32_t lo1[WIN], hi1[WIN];
+  __shared__ uint32_t lo2[WIN + LAGS], hi2[WIN + LAGS];
   const int64_t r = blockIdx.y;
   const int64_t tau0 = static_cast<int64_t>(blockIdx.x) * LAGS;
   const long long* row = S + r * T;
-  long long acc = 0;
+  unsigned long long acc[LPT] = {0, 0, 0, 0};
   for (int64_t t0 = 0; t0 < T - tau0; t0 += WIN) {
-    for (int i = threadIdx.x; i < WIN; i += LAGS) {
+    bool wide = false;
+    for (int i = threadIdx.x; i < WIN; i += THR) {
       const int64_t t = t0 + i;
-      s1[i] = t < T ? row[t] : 0;
+      const unsigned long long v = t < T ? static_cast<unsigned long long>(row[t]) : 0ull;
+      lo1[i] = static_cast<uint32_t>(v);
+      hi1[i] = static_cast<uint32_t>(v >> 32);
+      wide |= (v >> 32) != 0;
     }
-    for (int i = threadIdx.x; i < WIN + LAGS; i += LAGS) {
+    for (int i = threadIdx.x; i < WIN + LAGS; i += THR) {
       const int64_t t = t0 + tau0 + i;
-      s2[i] = t < T ? row[t] : 0;
+      const unsigned long long v = t < T ? static_cast<unsigned long long>(row[t]) : 0ull;
+      lo2[i] = static_cast<uint32_t>(v);
+      hi2[i] = static_cast<uint32_t>(v >> 32);
+      wide |= (v >> 32) != 0;
     }
-    __syncthreads();
-#pragma unroll 8
-    for (int i = 0; i < WIN; ++i) acc += s1[i] * s2[i + threadIdx.x];
+    const int n = static_cast<int>(T - tau0 - t0 < WIN ? T - tau0 - t0 : WIN);  // terms with t + tau0 < T
+    if (__syncthreads_or(wide)) {
+      for (int i = 0; i < n; ++i) {
+        const unsigned long long a_lo = lo1[i], a_hi = hi1[i];
+#pragma unroll
+        for (int k = 0; k < LPT; ++k) {
+          const int j = i + threadIdx.x + k * THR;
+          acc[k] += a_lo * lo2[j] + ((a_hi * lo2[j] + a_lo * hi2[j]) << 32);
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int i = 0; i < n; ++i) {
+        const uint32_t a = lo1[i];
+#pragma unroll
+        for (int k = 0; k < LPT; ++k) acc[k] += static_cast<unsigned long long>(a) * lo2[i + threadIdx.x + k * THR];
+      }
+    }
     __syncthreads();
   }
-  const int64_t tau = tau0 + threadIdx.x;
-  if (tau < T) D[r * T + tau] = acc;
+#pragma unroll
+  for (int k = 0; k < LPT; ++k) {
+    const int64_t tau = tau0 + threadIdx.x + k * THR;
+    if (tau < T) D[r * T + tau] = static_cast<long long>(acc[k]);
+  }
 }
 
 __global__ void finalize_kernel(const long long* __restrict__ N, const long long* __restrict__ D,
@@ -60,8 +93,43 @@ __global__ void finalize_kernel(const long long* __restrict__ N, const long long
   }
 }
 
+// calc_std deviation (dense.py:58-66): dev(tau) = std_t(r) / sqrt(T - tau),
+// from the sums of d = r - centre and d^2 over the T - tau pairs of the lag
+// (population variance, as numpy's std); NaN when a pair had S(t) S(t') = 0
+// (the reference divides by zero there).
+__global__ void std_finalize_kernel(const double* __restrict__ sum_d, const double* __restrict__ sum_d2,
+                                    const unsigned int* __restrict__ zeros, int64_t rows, int64_t T,
+                                    float* __restrict__ d32, double* __restrict__ d64) {
+  const int64_t total = rows * T;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double n = static_cast<double>(T - i % T);
+    const double m = sum_d[i] / n;
+    const double var = fmax(sum_d2[i] / n - m * m, 0.0);
+    const double dev = zeros[i] ? __longlong_as_double(0x7ff8000000000000ll) : sqrt(var) / sqrt(n);
+    if (d32) d32[i] = static_cast<float>(dev);
+    if (d64) d64[i] = dev;
+  }
+}
+
 }  // namespace norm
 }  // namespace g2
+
+extern "C" int g2_std_finalize(const double* sum_d_dev, const double* sum_d2_dev, const uint32_t* zeros_dev,
+                               int32_t n_rows, int64_t nframes, float* dev_f32, double* dev_f64, void* stream) {
+  using namespace g2;
+  if (!sum_d_dev || !sum_d2_dev || !zeros_dev || n_rows < 0 || nframes <= 0 || (!dev_f32 && !dev_f64))
+    return G2_ERR_ARG;
+  if (n_rows == 0) return G2_OK;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  const int64_t total = static_cast<int64_t>(n_rows) * nframes;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > sms * 8) blocks = sms * 8;
+  norm::std_finalize_kernel<<<static_cast<unsigned>(blocks), 256, 0, as_stream(stream)>>>(
+      sum_d_dev, sum_d2_dev, zeros_dev, n_rows, nframes, dev_f32, dev_f64);
+  return launch_status();
+}
 
 extern "C" int g2_denominator(const int64_t* sums_dev, int32_t n_rows, int64_t nframes, int64_t* denom_dev,
                               void* stream) {
@@ -72,7 +140,7 @@ extern "C" int g2_denominator(const int64_t* sums_dev, int32_t n_rows, int64_t n
   const int64_t gx = (nframes + norm::LAGS - 1) / norm::LAGS;
   if (gx > 0x7fffffff) return G2_ERR_TOO_LARGE;
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(n_rows));
-  norm::denom_kernel<<<grid, norm::LAGS, 0, as_stream(stream)>>>(reinterpret_cast<const long long*>(sums_dev),
+  norm::denom_kernel<<<grid, norm::THR, 0, as_stream(stream)>>>(reinterpret_cast<const long long*>(sums_dev),
                                                                  nframes, reinterpret_cast<long long*>(denom_dev));
   return launch_status();
 }
@@ -133,7 +201,7 @@ extern "C" int g2_normalize_static(const int64_t* numer_dev, const int64_t* sums
   if (sms <= 0) return G2_ERR_CUDA;
   const int64_t gx = (nframes + norm::LAGS - 1) / norm::LAGS;
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(n_rows));
-  norm::denom_kernel<<<grid, norm::LAGS, 0, as_stream(stream)>>>(reinterpret_cast<const long long*>(sums_dev),
+  norm::denom_kernel<<<grid, norm::THR, 0, as_stream(stream)>>>(reinterpret_cast<const long long*>(sums_dev),
                                                                  nframes, denom);
   const int64_t total = static_cast<int64_t>(n_rows) * nframes;
   int64_t blocks = (total + 255) / 256;

@@ -133,6 +133,7 @@ class DenseEngine:
         self.packed = None
         self.last = {}
         self._u8_hint = MODE_E4M3 if method == "tc" else MODE_FP16
+        self._u16_hint = MODE_E4M3 if method == "tc" else MODE_FP16
         self._packed_mode = None
         self.pipeline = True      # chunked copy/pack/Gram overlap where it applies
         self.profile = False      # record CUDA events around every stage
@@ -217,12 +218,9 @@ class DenseEngine:
     def choose_mode(self, frames_dev):
         if self.operand != "auto":
             return self.MODES[self.operand]
-        if frames_dev.element_size() == 1:
-            return self._u8_hint
-        m = self._binned_max(frames_dev)
-        if m <= E4M3_MAX_EXACT and self.method == "tc":
-            return MODE_E4M3
-        return MODE_FP16 if m <= FP16_MAX_EXACT else MODE_BYTES
+        # start from the narrowest operand the last stack of this width needed;
+        # the pack kernels flag counts that do not fit and the step reruns wider
+        return self._u8_hint if frames_dev.element_size() == 1 else self._u16_hint
 
     def pack(self, frames_dev, mode):
         L = self._layout(mode)
@@ -292,12 +290,18 @@ class DenseEngine:
             else:
                 seg_emax = L.segment_emax(L.d_piece_emax.cpu().numpy().view(np.uint32))
             code = int(self.err.item())
+            wide = frames_dev.element_size() == 2
             if code & _lib.DEVERR_RANGE and mode == MODE_E4M3 and self.operand == "auto":
                 mode = MODE_FP16
-                self._u8_hint = MODE_FP16
+                if wide:
+                    self._u16_hint = MODE_FP16
+                else:
+                    self._u8_hint = MODE_FP16
                 continue
             if code & _lib.DEVERR_RANGE and mode == MODE_FP16 and self.operand == "auto":
                 mode = MODE_BYTES
+                if wide:
+                    self._u16_hint = MODE_BYTES
                 continue
             if code:
                 raise DeviceError(_lib.device_error_message(code))
@@ -308,9 +312,13 @@ class DenseEngine:
                     mode = MODE_BYTES
                     continue
                 raise
-            if (mode == MODE_FP16 and frames_dev.element_size() == 1 and self.method == "tc"
-                    and self.operand == "auto" and seg_emax.size and int(seg_emax.max()) < 17 * 17):
-                self._u8_hint = MODE_E4M3        # every count <= 16: the next call can use e4m3
+            if (mode == MODE_FP16 and self.method == "tc" and self.operand == "auto" and seg_emax.size
+                    and int(seg_emax.max()) < 17 * 17):
+                # every count <= 16: the next call can use e4m3
+                if frames_dev.element_size() == 1:
+                    self._u8_hint = MODE_E4M3
+                else:
+                    self._u16_hint = MODE_E4M3
             return L, grams
 
     # -- chunked pipeline (e4m3) ---------------------------------------------
@@ -452,6 +460,44 @@ class DenseEngine:
         self.last = {"mode": ["fp16", "bytes", "e4m3"][L.mode], "split": int(L.split), "n_items": int(items.size),
                      "n_grams": n_chunks, "packed_cols": L.packed_cols}
         return self.g2_f32[: self.n_bins]
+
+    def deviation(self):
+        """calc_std of the last run (dense.py:58-66): float32 device tensor
+        ``(n_bins, T)``; float64 in ``self.dev_f64``.  One more tensor-core pass
+        over the packed operand of the last run (u8/u16 counts <= 2048)."""
+        torch = _torch()
+        if self.method != "tc":
+            raise NotImplementedError("calc_std runs on the tensor-core path")
+        L = self._layouts.get(self._packed_mode)
+        if L is None or self.packed is None:
+            raise RuntimeError("deviation() needs a preceding run()")
+        if L.split:
+            raise NotImplementedError("calc_std needs counts <= 2048 (this stack uses byte planes)")
+        key = ("std", L.mode, self.T)
+        if key not in self._items_cache:
+            from .plan import std_items
+            npix = np.bincount(self.qmask.ravel()[self.qmask.ravel() > 0], minlength=self.n_bins + 1)[1:]
+            items = std_items(self.T, L, npix)
+            self._items_cache[key] = (items, torch.from_numpy(items.view(np.uint8).copy()).to(self.dev))
+        items, dev_items = self._items_cache[key]
+        rows = max(self.n_bins, 1)
+        if getattr(self, "_std_bufs", None) is None:
+            z = lambda dt: torch.zeros((rows, self.T), dtype=dt, device=self.dev)
+            self._std_bufs = (z(torch.float64), z(torch.float64), z(torch.int32), z(torch.float32), z(torch.float64))
+        sd, sd2, zeros, d32, d64 = self._std_bufs
+        sd.zero_()
+        sd2.zero_()
+        zeros.zero_()
+        st = stream_handle(self.dev)
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, L.ones_row)])
+        if items.size:
+            _lib.check(self.lib.g2_gram_std(jobs, 1, ptr(dev_items), items.size, ptr(self.sums), self.sums.numel(),
+                                            ptr(self.g2_f32), ptr(sd), ptr(sd2), ptr(zeros), sd.numel(),
+                                            ptr(self.err), self.grid, st), "g2_gram_std")
+        _lib.check(self.lib.g2_std_finalize(ptr(sd), ptr(sd2), ptr(zeros), self.n_bins, self.T, ptr(d32), ptr(d64),
+                                            st), "g2_std_finalize")
+        self.dev_f64 = d64
+        return d32[: self.n_bins]
 
     def check_denominator_range(self):
         """Raise if int64 D could have overflowed (checked from S on the host)."""

@@ -315,8 +315,9 @@ class SparseEngine:
         return buf
 
     def to_words(self, data, indices, indptr, offsets, ib, n):
-        """CSR on the device -> packed event words and event offsets (uint32
-        as int32) on the device; requires :attr:`packed`."""
+        """CSR on the device -> packed event words (ordered by 32-frame window
+        within a pixel) and event offsets (uint32 as int32) on the device;
+        requires :attr:`packed`."""
         torch = _torch()
         H, W = self.shape
         self.events._mark("start_transpose")
@@ -339,6 +340,8 @@ class SparseEngine:
         evdata = self._buffer("ev_data", n, data.dtype)
         if self.packed:
             words, off = self.to_words(data, indices, indptr, offsets, ib, n)
+            _lib.check(self.lib.g2_events_sort_windows(ptr(words), ptr(off), self.npix, stream_handle(self.dev)),
+                       "g2_events_sort_windows")
             _lib.check(self.lib.g2_events_unpack(ptr(words), n, data.element_size(), ptr(times), ptr(evdata),
                                                  stream_handle(self.dev)), "g2_events_unpack")
             return times, evdata, off

@@ -307,3 +307,34 @@ def e4m3_segment_bound(layout):
 def gram_macs(T, npix):
     """Algorithmic multiply-accumulates of the upper-triangle Grams (incl. diagonal)."""
     return int(np.sum(np.asarray(npix, dtype=np.int64))) * T * (T + 1) // 2
+
+
+def std_items(T, layout, npix, job=0):
+    """Items of the calc_std pass (``g2_gram_std``): for every bin one Gram
+    over its whole K (the deviation is a float statistic, so K is not split),
+    tiles of the upper triangle, ``shift`` = the bin's pixel count and
+    ``out_off`` = ``s_off`` = bin * T.  Needs a layout without byte planes."""
+    if layout.split:
+        raise ValueError("calc_std needs counts <= 2048 (no byte planes)")
+    i0, j0 = _tiles(int(T), TC_BM, TC_BN)
+    parts = []
+    for b in range(layout.n_bins):
+        kp = int(layout.kpad[b])
+        if kp == 0 or int(npix[b]) == 0:
+            continue
+        it = np.empty(i0.size, dtype=ITEM_DTYPE)
+        it["job"] = job
+        it["i0"] = i0
+        it["j0"] = j0
+        it["a_k0"] = int(layout.plane0[b])
+        it["b_k0"] = int(layout.plane0[b])
+        it["k_len"] = kp
+        it["shift"] = int(npix[b])
+        it["nframes"] = T
+        it["out_off"] = b * T
+        it["s_off"] = b * T
+        parts.append(it)
+    if not parts:
+        return np.empty(0, dtype=ITEM_DTYPE)
+    items = np.concatenate(parts)
+    return items[np.argsort(-items["k_len"].astype(np.int64), kind="stable")]

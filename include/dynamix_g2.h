@@ -232,16 +232,37 @@ int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices
 
 /* Packed variants (frames < 2^16, image rows up to 29,000 pixels).
  * g2_csr_scatter_packed writes each element as one word (t << 16) | v into
- * ev_words_dev[ev_offsets[p] ..), frames ascending within a pixel (no cursor
- * array); g2_events_unpack splits such words into ev_times (int32) and ev_data
- * (elem_bytes 1 or 2), the FramesCompressor layout (event.py:267-284).
+ * ev_words_dev[ev_offsets[p] ..), ordered by 32-frame window (t >> 5) and in
+ * any order inside a window (no cursor array; column indices must increase
+ * strictly within a row, else G2_DEVERR_BOUNDS); g2_events_sort_windows puts
+ * every pixel's words in frame order; g2_events_unpack splits words into
+ * ev_times (int32) and ev_data (elem_bytes 1 or 2) -- with the sort, the
+ * FramesCompressor layout (event.py:267-284).
  * Returns G2_ERR_UNSUPPORTED when nframes > 65536 or width > 29,000. */
 int g2_csr_scatter_packed(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
                           const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
                           int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
                           uint32_t* ev_words_dev, int32_t* err_dev, void* stream);
+int g2_events_sort_windows(uint32_t* ev_words_dev, const uint32_t* ev_offsets_dev, int64_t npix, void* stream);
 int g2_events_unpack(const uint32_t* ev_words_dev, int64_t n_events, int32_t elem_bytes, int32_t* ev_times_dev,
                      void* ev_data_dev, void* stream);
+
+/* ---- calc_std deviation (dense.py:58-66) ---------------------------------
+ * g2_gram_std runs the Gram tiles of the items again (full K per item, fp32
+ * accumulation: a float statistic, not an exact sum) and, for every pair
+ * t' >= t of a bin, r = P * G(t,t') / (S(t) S(t')) with P = item.shift (the
+ * bin's pixel count) and S read at item.s_off + t from sums_dev; it adds
+ * d = r - centre[item.out_off + tau] and d^2 to sum_d / sum_d2 (double) and
+ * counts pairs with S(t) S(t') = 0 in zeros (caller zeroes the three).  The
+ * centre (the bin's g2, say) keeps the variance free of cancellation.
+ * g2_std_finalize gives dev = std_t(r) / sqrt(T - tau), NaN where a zero
+ * denominator occurred (the reference divides by zero there). */
+int g2_gram_std(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                const int64_t* sums_dev, int64_t sums_len, const float* centre_dev, double* sum_d_dev,
+                double* sum_d2_dev, uint32_t* zeros_dev, int64_t out_len, int32_t* err_dev, int32_t grid,
+                void* stream);
+int g2_std_finalize(const double* sum_d_dev, const double* sum_d2_dev, const uint32_t* zeros_dev, int32_t n_rows,
+                    int64_t nframes, float* dev_f32, double* dev_f64, void* stream);
 
 /* ---- G3: denominator ----------------------------------------------------
  * Replaces correlate_1D (dynamix/resources/opencl/densecorrelator.cl:156-176),

@@ -234,3 +234,39 @@ def test_chunked_pipeline_matches_single_pass(built_lib, cuda_device, T):
     assert "pipeline_chunks" not in b.engine.last
     assert np.array_equal(a.numerator, b.numerator) and np.array_equal(a.sums, b.sums)
     assert np.array_equal(g, gb, equal_nan=True)
+
+
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_cfg1_u8", "dense_u16"])
+def test_calc_std(built_lib, cuda_device, name):
+    """calc_std (dense.py:58-66): against the float64 oracle to 1e-4 relative
+    (float products and ratios on the tensor cores, float64 reduction) and
+    against the reference's own float32 result to 1e-3; NaN exactly where the
+    reference divides by zero."""
+    from dynamix_gb300.correlator import MatMulCorrelator, py_dense_correlator
+    z = golden(name)
+    fr, qm = z["frames"], z["qmask"]
+    c = MatMulCorrelator(fr.shape[1:], fr.shape[0], qmask=qm)
+    res, dev = c.correlate(fr, calc_std=True)
+    ref = o.g2_exact(fr, qm)
+    assert np.array_equal(c.numerator, ref["numerator"])
+    assert np.array_equal(res, ref["g2"].astype(np.float32), equal_nan=True)
+    want = o.dense_std_exact(fr, qm)
+    got = c.engine.dev_f64[: c.n_bins].cpu().numpy()
+    assert np.array_equal(np.isfinite(got), np.isfinite(want))
+    ok = np.isfinite(want)
+    assert np.all(np.abs(got[ok] - want[ok]) <= 1e-4 * np.abs(want[ok]) + 1e-9)
+    assert np.allclose(dev, got.astype(np.float32), rtol=1e-6, equal_nan=True)
+    rs = z["g2_ref_std"].astype(np.float64)
+    okr = np.isfinite(rs) & (np.abs(rs) > 1e-6)
+    assert np.max(np.abs(got[okr] - rs[okr]) / np.abs(rs[okr])) < 1e-3
+    # one bin through py_dense_correlator
+    r1, d1 = py_dense_correlator(fr, qm == 1, calc_std=True)
+    assert np.allclose(d1, got[0], rtol=1e-9, equal_nan=True)
+
+
+def test_calc_std_byte_planes_not_supported(built_lib, cuda_device):
+    from dynamix_gb300.correlator import MatMulCorrelator
+    fr = np.full((40, 6, 6), 3000, np.uint16)
+    c = MatMulCorrelator((6, 6), 40)
+    with pytest.raises(NotImplementedError):
+        c.correlate(fr, calc_std=True)
