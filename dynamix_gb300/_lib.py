@@ -22,7 +22,7 @@ DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE = 1, 2, 4
 
 BK = 64          # source segment width (pixels)
 PAD = 128        # packed bins and packed_cols are multiples of this
-PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 32, 512, 768
+PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 128, 512, 768
 TC_BM, TC_BN = 128, 256
 PLAIN_BM, PLAIN_BN = 128, 128
 MAX_JOBS = 32
@@ -70,8 +70,11 @@ SIGNATURES = {
     "g2_denominator": (C.c_int, [_p, _i32, _i64, _p, _p]),
     "g2_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
     "g2_normalize_static": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
+    "g2_set_tuning": (C.c_int, [_i32, _i64]),
+    "g2_get_tuning": (_i64, [_i32]),
 }
 STATIC_DENOM_MAX = 1 << 19
+TUNE_CSR_SMEM = 0
 
 _lock = threading.Lock()
 _lib = None

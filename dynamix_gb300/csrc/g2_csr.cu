@@ -595,7 +595,9 @@ extern "C" int g2_csr_scatter_packed(const void* data_dev, int32_t elem_bytes, c
     return G2_ERR_ARG;
   if (nframes > 65536 || width > csr::ROW_MAX_W) return G2_ERR_UNSUPPORTED;
   const int rpc = rows_per_cta(width, 1);
-  const int64_t smem = static_cast<int64_t>(rpc) * width * 4;
+  int64_t smem = static_cast<int64_t>(rpc) * width * 4;
+  const int64_t floor_bytes = tuning(G2_TUNE_CSR_SMEM);
+  if (floor_bytes > smem) smem = floor_bytes < 227 * 1024 ? floor_bytes : 227 * 1024;
   const unsigned grid = static_cast<unsigned>((height + rpc - 1) / rpc);
   cudaStream_t st = as_stream(stream);
 #define G2_PK(TV, TI)                                                                                           \

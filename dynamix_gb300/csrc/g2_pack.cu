@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(THREADS, 3)
       const int32_t d = entry_dst[e0 + e];
       const uint32_t m = entry_meta[e0 + e];
       const int so = static_cast<int>(m & 2047u);
-      const int pc = static_cast<int>(m >> 16);
+      const int pc = static_cast<int>(m >> 18);
       if (d < 0 || d >= packed_cols || p0 + so >= npix || pc >= np) {
         bad = true;
       } else {
@@ -122,8 +122,8 @@ __global__ void __launch_bounds__(THREADS, 3)
     const unsigned amask = __ballot_sync(0xffffffffu, valid);
     gslot[k] = gpiece[k] = 0;
     if (valid) {
-      gslot[k] = __match_any_sync(amask, static_cast<int>((meta[k] >> 11) & 31u));
-      gpiece[k] = __match_any_sync(amask, static_cast<int>(meta[k] >> 16));
+      gslot[k] = __match_any_sync(amask, static_cast<int>((meta[k] >> 11) & 127u));
+      gpiece[k] = __match_any_sync(amask, static_cast<int>(meta[k] >> 18));
     }
   }
 
@@ -172,8 +172,8 @@ __global__ void __launch_bounds__(THREADS, 3)
     for (int k = 0; k < EPT; ++k) {
       if (dst[k] < 0) continue;
       const int so = static_cast<int>(meta[k] & 2047u);
-      const int sl = static_cast<int>((meta[k] >> 11) & 31u);
-      const int pc = static_cast<int>(meta[k] >> 16);
+      const int sl = static_cast<int>((meta[k] >> 11) & 127u);
+      const int pc = static_cast<int>(meta[k] >> 18);
       const bool lead_s = (__ffs(gslot[k]) - 1) == lane;
       const bool lead_p = (__ffs(gpiece[k]) - 1) == lane;
 #pragma unroll

@@ -136,6 +136,10 @@ class DenseEngine:
         self._u16_hint = MODE_E4M3 if method == "tc" else MODE_FP16
         self._packed_mode = None
         self.pipeline = True      # chunked copy/pack/Gram overlap where it applies
+        self.pipe_chunks = self.PIPE_CHUNKS
+        self.super_rows = self.SUPER_ROWS
+        from .tune import apply_cached
+        apply_cached(self)        # launch shapes an earlier tuning run chose for this (T, pixels per bin)
         self.profile = False      # record CUDA events around every stage
         self.stage_ms = {}
         self._events = []
@@ -243,11 +247,12 @@ class DenseEngine:
         return L
 
     def items_for(self, L, grams):
-        key = (L.mode, self.method, tuple(grams))
+        key = (L.mode, self.method, tuple(grams), self.super_rows)
         if key not in self._items_cache:
             torch = _torch()
             items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method,
-                               s_base=0 if (L.ones_row and self.method == "tc") else None)
+                               s_base=0 if (L.ones_row and self.method == "tc") else None,
+                               super_rows=self.super_rows)
             dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
             if len(self._items_cache) > 8:
                 self._items_cache.clear()
@@ -323,18 +328,20 @@ class DenseEngine:
 
     # -- chunked pipeline (e4m3) ---------------------------------------------
     PIPE_CHUNKS = 8
+    SUPER_ROWS = 2048
 
     def _pipe_plan(self, L):
         """Items of the e4m3 Gram grouped by the frame chunk whose packing
         makes them ready (a tile needs frames up to its last column), LPT order
         inside a group; cached per layout."""
-        key = ("pipe", L.mode, self.T, self.exact_limit, self.grid)
+        key = ("pipe", L.mode, self.T, self.exact_limit, self.grid, self.pipe_chunks, self.super_rows)
         if key not in self._items_cache:
             torch = _torch()
             grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit)
-            items = gram_items(self.T, grams, job=0, out_base=0, kind="tc", s_base=0 if L.ones_row else None)
+            items = gram_items(self.T, grams, job=0, out_base=0, kind="tc", s_base=0 if L.ones_row else None,
+                               super_rows=self.super_rows)
             T = self.T
-            n = max(1, min(self.PIPE_CHUNKS, T // 256))
+            n = max(1, min(self.pipe_chunks, T // 256))
             step = -(-(-(-T // n)) // 128) * 128               # chunk of frames, a multiple of 128
             bounds = np.array(list(range(0, T, step)) + [T], dtype=np.int64)
             need = np.minimum(items["j0"].astype(np.int64) + TC_BN, T)

@@ -122,7 +122,7 @@ class PackLayout:
             self.piece_seg1 = self.piece_seg + self.kpad[piece_bin] // BK
         self.entry_dst = dst.astype(np.int32)
         src_off = pix - chunk * PACK_CHUNK
-        self.entry_meta = (src_off | (slot << 11) | (piece << 16)).astype(np.uint32)
+        self.entry_meta = (src_off | (slot << 11) | (piece << 18)).astype(np.uint32)
         self.bin_kpad = self.kpad.astype(np.int32)
         self.n_planes = 2 if self.split else 1
         # words of the byte-permutation pack (e4m3): 4 aligned packed columns of
@@ -246,7 +246,7 @@ def _tiles(T, bm, bn, super_rows=SUPER_ROWS, extra_col=False):
     return _TILE_CACHE[key]
 
 
-def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc", s_base=None):
+def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc", s_base=None, super_rows=SUPER_ROWS):
     """Build the item list of one job.
 
     ``chunked_grams``: iterable of ``(bin, a_off, b_off, k0, k_len, shift)`` with
@@ -259,7 +259,7 @@ def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc", s_base=None):
     ``s_base + b * T + t``.
     """
     bm, bn = (TC_BM, TC_BN) if kind == "tc" else (PLAIN_BM, PLAIN_BN)
-    i0, j0 = _tiles(int(T), bm, bn, extra_col=s_base is not None)
+    i0, j0 = _tiles(int(T), bm, bn, super_rows=int(super_rows), extra_col=s_base is not None)
     parts = []
     for (b, a_off, b_off, k0, klen, shift) in chunked_grams:
         it = np.empty(i0.size, dtype=ITEM_DTYPE)

@@ -1,0 +1,106 @@
+"""Autotuner of the dense step's launch shapes.
+
+The tensor-core Gram's tile order and the chunked copy/pack/Gram pipeline have
+two free parameters that change speed but never results:
+
+* ``super_rows`` -- side, in frames, of the square super-tiles the 128 x 256
+  tiles are grouped in (concurrent CTAs share those frames in L2);
+* ``pipe_chunks`` -- number of frame chunks the step is split into (more
+  chunks overlap more of the copy and the packing with the Gram, fewer keep
+  each grouped launch long).
+
+:func:`tune_dense` times every candidate pair on the caller's own stack and
+keeps the fastest for the key ``(nframes, pixels per bin)``; engines built
+later for the same key pick it up (:func:`apply_cached`).  Choices are kept in
+memory and, when ``path`` is given (or ``DYNAMIX_G2_TUNE_CACHE`` is set), in
+a JSON file.
+"""
+from __future__ import annotations
+
+import json
+import os
+import threading
+
+import numpy as np
+
+DEFAULT_CANDIDATES = [(sr, pc) for sr in (1024, 2048, 4096) for pc in (4, 8, 12)]
+
+_lock = threading.Lock()
+_cache = {}
+_loaded_from = set()
+
+
+def key_of(T, qmask, n_bins):
+    q = np.asarray(qmask).ravel()
+    npix = np.bincount(q[q > 0], minlength=int(n_bins) + 1)[1:]
+    return "T=%d;P=%s" % (int(T), ",".join(str(int(p)) for p in npix))
+
+
+def _cache_path(path=None):
+    return path or os.environ.get("DYNAMIX_G2_TUNE_CACHE")
+
+
+def _load(path):
+    if not path or path in _loaded_from or not os.path.exists(path):
+        return
+    with open(path) as f:
+        data = json.load(f)
+    _cache.update({k: tuple(v) for k, v in data.items()})
+    _loaded_from.add(path)
+
+
+def lookup(key, path=None):
+    with _lock:
+        _load(_cache_path(path))
+        return _cache.get(key)
+
+
+def store(key, value, path=None):
+    with _lock:
+        _cache[key] = tuple(value)
+        p = _cache_path(path)
+        if p:
+            data = {}
+            if os.path.exists(p):
+                with open(p) as f:
+                    data = json.load(f)
+            data[key] = list(value)
+            tmp = p + ".%d.tmp" % os.getpid()
+            with open(tmp, "w") as f:
+                json.dump(data, f, indent=1, sort_keys=True)
+            os.replace(tmp, p)
+
+
+def apply_cached(engine, path=None):
+    """Set an engine's launch shapes from an earlier tuning of its key."""
+    v = lookup(key_of(engine.T, engine.qmask, engine.n_bins), path)
+    if v is not None:
+        engine.super_rows, engine.pipe_chunks = int(v[0]), int(v[1])
+    return v
+
+
+def tune_dense(correlator, frames, candidates=None, repeats=3, path=None):
+    """Time ``correlate_device(frames)`` for every ``(super_rows,
+    pipe_chunks)`` candidate (CUDA events, after one warm-up call each), keep
+    the fastest for this stack's key and return ``(best, {candidate: ms})``.
+    ``frames`` must stay the same stack for all candidates."""
+    import torch
+    eng = correlator.engine
+    times = {}
+    for sr, pc in (candidates or DEFAULT_CANDIDATES):
+        eng.super_rows, eng.pipe_chunks = int(sr), int(pc)
+        correlator.correlate_device(frames)
+        stream = torch.cuda.current_stream(eng.dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(repeats):
+            correlator.correlate_device(frames)
+        e1.record(stream)
+        e1.synchronize()
+        times[(int(sr), int(pc))] = e0.elapsed_time(e1) / repeats
+    eng.check_error()
+    best = min(times, key=times.get)
+    eng.super_rows, eng.pipe_chunks = best
+    store(key_of(eng.T, eng.qmask, eng.n_bins), best, path)
+    return best, times

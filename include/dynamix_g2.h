@@ -48,7 +48,7 @@ extern "C" {
 #define G2_PLAIN_BN   128
 #define G2_PAD        128  /* packed_cols and bin segments are multiples of this */
 #define G2_PACK_CHUNK 2048 /* source pixels per pack chunk */
-#define G2_PACK_MAX_SLOTS  32   /* distinct bins per chunk */
+#define G2_PACK_MAX_SLOTS  128  /* distinct bins per chunk */
 #define G2_PACK_MAX_PIECES 512  /* (64-column segment x chunk) pieces per chunk */
 #define G2_PACK_WORDS_PER_CHUNK 768 /* 4-column words per chunk: 2048/4 + partial words at bin edges */
 #define G2_MAX_JOBS   32
@@ -107,7 +107,7 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
  * pixels are cut into n_chunks = ceil(npix / G2_PACK_CHUNK) chunks.  The
  * binned pixels of chunk c are entries [chunk_entry_off[c], chunk_entry_off[c+1])
  * (in pixel order); entry e goes to packed column entry_dst[e] (plane 0) and
- * entry_meta[e] = offset in the chunk | local bin slot << 11 | local piece << 16.
+ * entry_meta[e] = offset in the chunk | local bin slot << 11 | local piece << 18.
  * chunk_slot_bin[c * G2_PACK_MAX_SLOTS + slot] is the 0-based bin of a slot (-1
  * unused).  A piece is one 64-column output segment within one chunk; chunk c
  * owns pieces [chunk_piece_off[c], chunk_piece_off[c+1]).
@@ -297,6 +297,18 @@ int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, const double
  * clearing); calls whose work overlaps on the GPU race on it.  This entry
  * point allocates nothing: no cudaMalloc, no cudaFree. */
 #define G2_STATIC_DENOM_MAX (1 << 19)
+
+/* ---- launch-shape settings (no reference counterpart) ---------------------
+ * Process-wide knobs read at launch time; 0 (the default) means the built-in
+ * choice.  They change launch shapes only, never results; an autotuner
+ * (dynamix_gb300.tune) times the candidates and sets the winners.
+ *   G2_TUNE_CSR_SMEM   bytes of shared memory the row-owned CSR scatter asks
+ *                      per CTA (more bytes: fewer image rows in flight, so the
+ *                      sectors being filled stay in L2) */
+#define G2_TUNE_CSR_SMEM 0
+#define G2_TUNE_COUNT 1
+int g2_set_tuning(int32_t key, int64_t value);
+int64_t g2_get_tuning(int32_t key);
 int g2_normalize_static(const int64_t* numer_dev, const int64_t* sums_dev, const double* scale_dev,
                         int32_t n_rows, int64_t nframes, float* g2_f32_dev, double* g2_f64_dev,
                         void* stream);

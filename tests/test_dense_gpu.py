@@ -270,3 +270,39 @@ def test_calc_std_byte_planes_not_supported(built_lib, cuda_device):
     c = MatMulCorrelator((6, 6), 40)
     with pytest.raises(NotImplementedError):
         c.correlate(fr, calc_std=True)
+
+
+def test_autotuner_keeps_results_exact(built_lib, cuda_device):
+    import torch
+    from dynamix_gb300 import tune
+    from dynamix_gb300.correlator import MatMulCorrelator
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    T, shape = 1200, (40, 52)
+    fr = speckle_numpy(T, shape, 0.99, 0.4, seed=5, dtype=np.uint8, max_count=16)
+    qm = annular_qmask(shape, 4, 2.0, 26.0)
+    c = MatMulCorrelator(shape, T, qmask=qm)
+    d = torch.from_numpy(fr).to(cuda_device)
+    best, times = tune.tune_dense(c, d, candidates=[(1024, 2), (2048, 4), (4096, 8)], repeats=1)
+    assert best in times and len(times) == 3
+    assert (c.engine.super_rows, c.engine.pipe_chunks) == best
+    g = c.correlate(d)
+    assert_exact(c, o.g2_exact(fr, qm), g)
+    c2 = MatMulCorrelator(shape, T, qmask=qm)            # same key: the choice is reused
+    assert (c2.engine.super_rows, c2.engine.pipe_chunks) == best
+
+
+@pytest.mark.parametrize("bright", [False, True])
+def test_64_narrow_bins(built_lib, cuda_device, bright):
+    """More than 32 bins inside one 2048-pixel pack chunk (fp16 / byte planes
+    carry per-chunk bin slots for S)."""
+    from dynamix_gb300.correlator import MatMulCorrelator
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    T, shape = 150, (256, 256)
+    fr = speckle_numpy(T, shape, 0.95, 3.0, seed=9, dtype=np.uint16)
+    if bright:
+        fr = (fr.astype(np.int64) * 700).astype(np.uint16)        # byte planes
+    qm = annular_qmask(shape, 64, 0.0, 102.4)
+    c = MatMulCorrelator(shape, T, qmask=qm)
+    g = c.correlate(fr)
+    assert c.engine.last["mode"] == ("bytes" if bright else "fp16")
+    assert_exact(c, o.g2_exact(fr, qm), g)

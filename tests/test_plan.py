@@ -25,8 +25,8 @@ def emulate_pack(frames, L):
     chunk = np.repeat(np.arange(L.n_chunks), np.diff(L.chunk_entry_off))
     meta = L.entry_meta.astype(np.int64)
     pix = chunk * PACK_CHUNK + (meta & 2047)
-    slot = (meta >> 11) & 31
-    piece = L.chunk_piece_off[chunk] + (meta >> 16)
+    slot = (meta >> 11) & 127
+    piece = L.chunk_piece_off[chunk] + (meta >> 18)
     b = L.chunk_slot_bin[chunk * PACK_MAX_SLOTS + slot]
     # the slot's bin is the bin whose columns hold the entry
     assert np.all((b >= 0) & (L.plane0[b] <= L.entry_dst) & (L.entry_dst < L.plane0[b] + L.kpad[b]))
@@ -199,6 +199,23 @@ def test_e4m3_word_tables_decode_to_entries():
             if srcs[w, i] != 0xFFF:
                 got.add((int(chunk_w[w] * PACK_CHUNK + srcs[w, i]), int(L.word_dst[w] + i)))
         # the slot names the bin whose columns hold the word
-        b = L.chunk_slot_bin[chunk_w[w] * PACK_MAX_SLOTS + ((y[w] >> 16) & 31)]
+        b = L.chunk_slot_bin[chunk_w[w] * PACK_MAX_SLOTS + ((y[w] >> 16) & 127)]
         assert L.plane0[b] <= L.word_dst[w] < L.plane0[b] + L.kpad[b]
     assert got == want
+
+
+@pytest.mark.parametrize("mode", [plan.MODE_FP16, plan.MODE_BYTES, plan.MODE_E4M3])
+def test_many_narrow_bins_share_a_chunk(mode):
+    """64 annuli on a 256-wide frame: a 2048-pixel chunk holds more than 32
+    bins (the serving mix has up to 64 bins on 256 x 256 frames)."""
+    qm = annular_qmask((256, 256), 64, 0.0, 102.4)
+    L = plan.PackLayout(qm, 64, mode)
+    chunk = np.repeat(np.arange(L.n_chunks), np.diff(L.chunk_entry_off))
+    slots = (L.entry_meta.astype(np.int64) >> 11) & 127
+    per_chunk = max(np.unique(slots[chunk == c]).size for c in range(L.n_chunks) if np.any(chunk == c))
+    assert per_chunk > 32
+    fr = speckle_numpy(3, (256, 256), 0.9, 3.0, seed=2, dtype=np.uint16 if mode == plan.MODE_BYTES else np.uint8)
+    if mode == plan.MODE_BYTES:
+        fr = fr * 300
+    if mode != plan.MODE_E4M3:
+        emulate_pack(fr, L)
