@@ -229,62 +229,6 @@ __global__ void __launch_bounds__(256)
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
 
-// Scatter into packed event words (t << 16 | v; frames < 2^16): one warp owns
-// one image row for all frames (lanes = 32 consecutive frames), the row's slot
-// cursors in its shared memory, one shared atomic per element.  Pixels' events
-// come out ordered by 32-frame batch, in any order inside a batch (the pair
-// sums do not depend on it; sort_windows_kernel restores frame order where the
-// FramesCompressor layout is wanted).  Column indices must increase strictly
-// inside a row (sorted CSR, as correlator.cl:185-197 assumes); a repeated or
-// descending column is reported.
-template <typename Tv, typename Ti>
-__global__ void __launch_bounds__(256)
-    row_scatter_packed_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices,
-                              const Ti* __restrict__ indptr, const Ti* __restrict__ offsets, int64_t n_elem,
-                              int32_t T, int32_t H, int32_t W, int rows_per_cta, const uint32_t* __restrict__ ev_off,
-                              uint32_t* __restrict__ ev_words, int32_t* __restrict__ err) {
-  extern __shared__ __align__(16) uint32_t sm[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * rows_per_cta + warp;
-  if (warp >= rows_per_cta || r >= H) return;  // warp-uniform; no block barrier below
-  uint32_t* cur = sm + static_cast<int64_t>(warp) * W;
-  const uint32_t* row_off = ev_off + static_cast<int64_t>(r) * W;
-  const uint32_t n_total = ev_off[static_cast<int64_t>(H) * W];
-  for (int i = lane; i < W; i += 32) cur[i] = row_off[i];
-  __syncwarp();
-  bool bad = false;
-  for (int64_t t0 = 0; t0 < T; t0 += 32) {
-    const int64_t t = t0 + lane;
-    if (t >= T) continue;
-    const int64_t base = static_cast<int64_t>(offsets[t]);
-    const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
-    const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
-    const int64_t s = base + static_cast<int64_t>(ip[0]);
-    const int64_t e = base + static_cast<int64_t>(ip[1]);
-    if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
-      bad = true;
-      continue;
-    }
-    const uint32_t tw = static_cast<uint32_t>(t) << 16;
-    int64_t prev = -1;
-#pragma unroll 4
-    for (int64_t k = s; k < e; ++k) {
-      const int64_t c = static_cast<int64_t>(indices[k]);
-      if (c <= prev || c >= W) {
-        bad = true;
-        if (c < 0 || c >= W) continue;
-      }
-      prev = c;
-      const uint32_t slot = atomicAdd(&cur[c], 1u);
-      if (slot < n_total)
-        ev_words[slot] = tw | static_cast<uint32_t>(data[k]);
-      else
-        bad = true;
-    }
-  }
-  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
-}
-
 // Frame order inside each pixel's list of packed words that is already ordered
 // by 32-frame window (t >> 5): a warp per pixel takes 32 words at a time and
 // ranks each word inside its window group by shuffles; a group that may run on
@@ -326,6 +270,138 @@ __global__ void __launch_bounds__(256)
       c0 += commit;
     }
   }
+}
+
+// Sub-blocked transposition (frames < 2^16): the frames are cut into
+// sub-blocks of SUBBLOCK frames.  The count pass keeps, per image row (one
+// warp, lanes = 32 consecutive frames), the per-pixel counts of each
+// sub-block (uint16) instead of one total.  The scatter runs one CTA per (8
+// consecutive sub-blocks, image row), a warp per sub-block with its own slot
+// cursors (the pixel's offset plus the counts of the earlier sub-blocks), so
+// the CTA writes, for every pixel of its row, one contiguous stretch of that
+// pixel's list (8 x 1024 frames of events) while it runs: the sectors it
+// fills are complete before they leave L2.  Events come out ordered by
+// 32-frame window within a pixel, in any order inside a window.
+constexpr int SUBBLOCK = 1024;
+constexpr int SB_PER_CTA = 8;
+
+template <typename Ti>
+__global__ void __launch_bounds__(256)
+    row_count_blocked_kernel(const Ti* __restrict__ indices, const Ti* __restrict__ indptr,
+                             const Ti* __restrict__ offsets, int64_t n_elem, int32_t T, int32_t H, int32_t W,
+                             int rows_per_cta, uint16_t* __restrict__ sb_counts, int32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * rows_per_cta + warp;
+  if (warp >= rows_per_cta || r >= H) return;  // warp-uniform; no block barrier below
+  uint32_t* cnt = sm + static_cast<int64_t>(warp) * W;
+  for (int i = lane; i < W; i += 32) cnt[i] = 0;
+  __syncwarp();
+  const int64_t npix = static_cast<int64_t>(H) * W;
+  bool bad = false;
+  for (int64_t sb0 = 0; sb0 < T; sb0 += SUBBLOCK) {
+    const int64_t sb_end = sb0 + SUBBLOCK < T ? sb0 + SUBBLOCK : T;
+    for (int64_t t0 = sb0; t0 < sb_end; t0 += 32) {
+      const int64_t t = t0 + lane;
+      if (t >= sb_end) continue;
+      const int64_t base = static_cast<int64_t>(offsets[t]);
+      const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
+      const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
+      const int64_t s = base + static_cast<int64_t>(ip[0]);
+      const int64_t e = base + static_cast<int64_t>(ip[1]);
+      if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+        bad = true;
+        continue;
+      }
+#pragma unroll 4
+      for (int64_t k = s; k < e; ++k) {
+        const int64_t col = static_cast<int64_t>(indices[k]);
+        if (col < 0 || col >= W) {
+          bad = true;
+          continue;
+        }
+        atomicAdd(&cnt[col], 1u);
+      }
+    }
+    __syncwarp();
+    uint16_t* out = sb_counts + (sb0 / SUBBLOCK) * npix + static_cast<int64_t>(r) * W;
+    for (int i = lane; i < W; i += 32) {
+      out[i] = static_cast<uint16_t>(cnt[i]);  // <= SUBBLOCK frames, one element each
+      cnt[i] = 0;
+    }
+    __syncwarp();
+  }
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// counts[p] += sum over sub-blocks of sb_counts[sb][p]
+__global__ void __launch_bounds__(256)
+    sum_subblocks_kernel(const uint16_t* __restrict__ sb_counts, int n_sb, int64_t npix,
+                         uint32_t* __restrict__ counts) {
+  for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < npix;
+       p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    uint32_t s = 0;
+    for (int b = 0; b < n_sb; ++b) s += sb_counts[b * npix + p];
+    counts[p] += s;
+  }
+}
+
+template <typename Tv, typename Ti>
+__global__ void __launch_bounds__(SB_PER_CTA * 32)
+    row_scatter_blocked_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices,
+                               const Ti* __restrict__ indptr, const Ti* __restrict__ offsets, int64_t n_elem,
+                               int32_t T, int32_t H, int32_t W, const uint32_t* __restrict__ ev_off,
+                               const uint16_t* __restrict__ sb_counts, uint32_t* __restrict__ ev_words,
+                               int32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.y;
+  const int64_t sb = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
+  const int64_t sb0 = sb * SUBBLOCK;
+  if (r >= H || sb0 >= T) return;  // warp-uniform; no block barrier below
+  const int64_t npix = static_cast<int64_t>(H) * W;
+  uint32_t* cur = sm + static_cast<int64_t>(warp) * W;
+  const int64_t row0 = static_cast<int64_t>(r) * W;
+  // the sub-block's first slot of each pixel: its offset plus the earlier sub-blocks
+  for (int i = lane; i < W; i += 32) {
+    uint32_t c = ev_off[row0 + i];
+    for (int64_t b = 0; b < sb; ++b) c += sb_counts[b * npix + row0 + i];
+    cur[i] = c;
+  }
+  __syncwarp();
+  const uint32_t n_total = ev_off[npix];
+  const int64_t sb_end = sb0 + SUBBLOCK < T ? sb0 + SUBBLOCK : T;
+  bool bad = false;
+  for (int64_t t0 = sb0; t0 < sb_end; t0 += 32) {
+    const int64_t t = t0 + lane;
+    if (t >= sb_end) continue;
+    const int64_t base = static_cast<int64_t>(offsets[t]);
+    const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
+    const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
+    const int64_t s = base + static_cast<int64_t>(ip[0]);
+    const int64_t e = base + static_cast<int64_t>(ip[1]);
+    if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+      bad = true;
+      continue;
+    }
+    const uint32_t tw = static_cast<uint32_t>(t) << 16;
+    int64_t prev = -1;
+#pragma unroll 4
+    for (int64_t k = s; k < e; ++k) {
+      const int64_t c = static_cast<int64_t>(indices[k]);
+      if (c <= prev || c >= W) {
+        bad = true;  // repeated, descending or out-of-range column
+        if (c < 0 || c >= W) continue;
+      }
+      prev = c;
+      const uint32_t slot = atomicAdd(&cur[c], 1u);
+      if (slot < n_total)
+        ev_words[slot] = tw | static_cast<uint32_t>(data[k]);
+      else
+        bad = true;
+    }
+  }
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
 
 // Packed words -> (times int32, data) arrays.
@@ -582,37 +658,73 @@ extern "C" int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const vo
                     height, width, cursor_dev, ev_offsets_dev, ev_times_dev, ev_data_dev, err_dev, stream);
 }
 
-extern "C" int g2_csr_scatter_packed(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
-                                     const void* indptr_dev, const void* offsets_dev, int32_t index_bytes,
-                                     int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
-                                     const uint32_t* ev_offsets_dev, uint32_t* ev_words_dev, int32_t* err_dev,
-                                     void* stream) {
+extern "C" int g2_csr_count_blocked(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
+                                    int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height,
+                                    int32_t width, uint32_t* counts_dev, uint16_t* sb_counts_dev, int32_t* err_dev,
+                                    void* stream) {
   using namespace g2;
-  if (!data_dev || !indices_dev || !indptr_dev || !offsets_dev || !ev_offsets_dev || !ev_words_dev || !err_dev)
+  if (!indices_dev || !indptr_dev || !offsets_dev || !counts_dev || !sb_counts_dev || !err_dev) return G2_ERR_ARG;
+  if ((index_bytes != 4 && index_bytes != 8) || n_elem < 0 || nframes <= 0 || height <= 0 || width <= 0)
+    return G2_ERR_ARG;
+  if (width > csr::ROW_MAX_W) return G2_ERR_UNSUPPORTED;
+  const int rpc = rows_per_cta(width, 1);
+  const int64_t smem = static_cast<int64_t>(rpc) * width * 4;
+  const unsigned grid = static_cast<unsigned>((height + rpc - 1) / rpc);
+  cudaStream_t st = as_stream(stream);
+  if (index_bytes == 4) {
+    if (!allow_smem(csr::row_count_blocked_kernel<uint32_t>, smem)) return G2_ERR_CUDA;
+    csr::row_count_blocked_kernel<uint32_t><<<grid, rpc * 32, smem, st>>>(
+        reinterpret_cast<const uint32_t*>(indices_dev), reinterpret_cast<const uint32_t*>(indptr_dev),
+        reinterpret_cast<const uint32_t*>(offsets_dev), n_elem, nframes, height, width, rpc, sb_counts_dev, err_dev);
+  } else {
+    if (!allow_smem(csr::row_count_blocked_kernel<int64_t>, smem)) return G2_ERR_CUDA;
+    csr::row_count_blocked_kernel<int64_t><<<grid, rpc * 32, smem, st>>>(
+        reinterpret_cast<const int64_t*>(indices_dev), reinterpret_cast<const int64_t*>(indptr_dev),
+        reinterpret_cast<const int64_t*>(offsets_dev), n_elem, nframes, height, width, rpc, sb_counts_dev, err_dev);
+  }
+  const int64_t npix = static_cast<int64_t>(height) * width;
+  const int n_sb = static_cast<int>((static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK);
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  int64_t blocks = (npix + 255) / 256;
+  if (blocks > static_cast<int64_t>(sms) * 16) blocks = static_cast<int64_t>(sms) * 16;
+  csr::sum_subblocks_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(sb_counts_dev, n_sb, npix, counts_dev);
+  return launch_status();
+}
+
+extern "C" int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                                      const void* indptr_dev, const void* offsets_dev, int32_t index_bytes,
+                                      int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
+                                      const uint32_t* ev_offsets_dev, const uint16_t* sb_counts_dev,
+                                      uint32_t* ev_words_dev, int32_t* err_dev, void* stream) {
+  using namespace g2;
+  if (!data_dev || !indices_dev || !indptr_dev || !offsets_dev || !ev_offsets_dev || !sb_counts_dev ||
+      !ev_words_dev || !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || (index_bytes != 4 && index_bytes != 8) || n_elem < 0 ||
       nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
   if (nframes > 65536 || width > csr::ROW_MAX_W) return G2_ERR_UNSUPPORTED;
-  const int rpc = rows_per_cta(width, 1);
-  int64_t smem = static_cast<int64_t>(rpc) * width * 4;
-  const int64_t floor_bytes = tuning(G2_TUNE_CSR_SMEM);
-  if (floor_bytes > smem) smem = floor_bytes < 227 * 1024 ? floor_bytes : 227 * 1024;
-  const unsigned grid = static_cast<unsigned>((height + rpc - 1) / rpc);
+  // warps (sub-blocks) per CTA: up to 8, each holding one row of cursors
+  int warps = static_cast<int>((227 * 1024) / (static_cast<int64_t>(width) * 4));
+  warps = warps < 1 ? 1 : (warps > csr::SB_PER_CTA ? csr::SB_PER_CTA : warps);
+  const int64_t smem = static_cast<int64_t>(warps) * width * 4;
+  const int64_t n_sb = (static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK;
+  const dim3 grid(static_cast<unsigned>((n_sb + warps - 1) / warps), static_cast<unsigned>(height));
   cudaStream_t st = as_stream(stream);
-#define G2_PK(TV, TI)                                                                                           \
+#define G2_BS(TV, TI)                                                                                           \
   do {                                                                                                          \
-    if (!allow_smem(csr::row_scatter_packed_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                          \
-    csr::row_scatter_packed_kernel<TV, TI><<<grid, rpc * 32, smem, st>>>(                                       \
+    if (!allow_smem(csr::row_scatter_blocked_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                         \
+    csr::row_scatter_blocked_kernel<TV, TI><<<grid, warps * 32, smem, st>>>(                                    \
         reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev),                        \
         reinterpret_cast<const TI*>(indptr_dev), reinterpret_cast<const TI*>(offsets_dev), n_elem, nframes,     \
-        height, width, rpc, ev_offsets_dev, ev_words_dev, err_dev);                                             \
+        height, width, ev_offsets_dev, sb_counts_dev, ev_words_dev, err_dev);                                   \
   } while (0)
-  if (elem_bytes == 1 && index_bytes == 4) G2_PK(uint8_t, uint32_t);
-  else if (elem_bytes == 1) G2_PK(uint8_t, int64_t);
-  else if (index_bytes == 4) G2_PK(uint16_t, uint32_t);
-  else G2_PK(uint16_t, int64_t);
-#undef G2_PK
+  if (elem_bytes == 1 && index_bytes == 4) G2_BS(uint8_t, uint32_t);
+  else if (elem_bytes == 1) G2_BS(uint8_t, int64_t);
+  else if (index_bytes == 4) G2_BS(uint16_t, uint32_t);
+  else G2_BS(uint16_t, int64_t);
+#undef G2_BS
   return launch_status();
 }
 

@@ -1,5 +1,4 @@
 // Host utilities of the C ABI: status strings, device queries, tensor maps.
-#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <cudaTypedefs.h>
@@ -49,22 +48,6 @@ int encode_tmap_2d(CUtensorMap* map, const void* base, int elem_bytes, uint64_t 
 }
 
 }  // namespace g2
-
-namespace g2 {
-namespace {
-std::atomic<int64_t> g_tuning[G2_TUNE_COUNT];
-}  // namespace
-
-int64_t tuning(int key) { return key >= 0 && key < G2_TUNE_COUNT ? g_tuning[key].load() : 0; }
-}  // namespace g2
-
-extern "C" int g2_set_tuning(int32_t key, int64_t value) {
-  if (key < 0 || key >= G2_TUNE_COUNT || value < 0) return G2_ERR_ARG;
-  g2::g_tuning[key].store(value);
-  return G2_OK;
-}
-
-extern "C" int64_t g2_get_tuning(int32_t key) { return g2::tuning(key); }
 
 extern "C" int g2_abi_version(void) { return G2_ABI_VERSION; }
 

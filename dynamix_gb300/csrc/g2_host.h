@@ -20,9 +20,6 @@ inline int launch_status() {
 // Current device's SM count (cached per device).
 int sm_count_current();
 
-// Launch-shape setting (g2_set_tuning); 0 when unset.
-int64_t tuning(int key);
-
 // Encode a 2-D tiled tensor map over a row-major [rows][cols] matrix of
 // 2-byte (fp16) or 1-byte (e4m3, as uint8) elements with a (box_cols x
 // box_rows) box, 128-byte swizzle, zero fill outside.

@@ -15,7 +15,10 @@ Dense pipeline (one job = one frame stack, all its q-bins):
 """
 from __future__ import annotations
 
+import collections
 import ctypes as C
+import hashlib
+import threading
 
 import numpy as np
 
@@ -84,6 +87,43 @@ def frames_to_device(frames, dev):
             raise ValueError("counts above 65535 are not supported")
     tgt = np.uint8 if (a.size == 0 or a.max() <= 255) else np.uint16
     return torch.from_numpy(np.ascontiguousarray(a.astype(tgt))).to(dev)
+
+
+_LAYOUTS = collections.OrderedDict()
+_LAYOUTS_LOCK = threading.Lock()
+_LAYOUTS_MAX = 48
+
+
+def device_layout(qmask, n_bins, mode, dev):
+    """The packing layout of a q-mask with its read-only tables on ``dev``,
+    shared process-wide (least recently used of 48 kept): building one costs
+    host time proportional to the frame size."""
+    torch = _torch()
+    q = np.ascontiguousarray(qmask, dtype=np.int32)
+    key = (str(dev), q.shape, hashlib.blake2b(q.tobytes(), digest_size=16).hexdigest(), int(n_bins), int(mode))
+    with _LAYOUTS_LOCK:
+        L = _LAYOUTS.get(key)
+        if L is not None:
+            _LAYOUTS.move_to_end(key)
+            return L
+    L = PackLayout(q, n_bins, mode)
+    d = lambda a: torch.as_tensor(a, device=dev)
+    L.d_col_src = d(L.col_src)
+    L.d_chunk_entry_off = d(L.chunk_entry_off)
+    L.d_entry_dst = d(L.entry_dst)
+    L.d_entry_meta = d(L.entry_meta.view(np.int32))
+    L.d_chunk_slot_bin = d(L.chunk_slot_bin)
+    L.d_chunk_piece_off = d(L.chunk_piece_off)
+    L.d_bin_kpad = d(L.bin_kpad)
+    if mode == MODE_E4M3:
+        L.d_chunk_word_off = d(L.chunk_word_off)
+        L.d_word_dst = d(L.word_dst)
+        L.d_word_src = d(L.word_src.view(np.int32))
+    with _LAYOUTS_LOCK:
+        _LAYOUTS[key] = L
+        while len(_LAYOUTS) > _LAYOUTS_MAX:
+            _LAYOUTS.popitem(last=False)
+    return L
 
 
 class DenseEngine:
@@ -169,23 +209,18 @@ class DenseEngine:
     # -- layout / buffers ------------------------------------------------
     def _layout(self, mode):
         if mode not in self._layouts:
-            torch = _torch()
-            L = PackLayout(self.qmask, self.n_bins, mode)
-            d = lambda a: torch.as_tensor(a, device=self.dev)
-            L.d_col_src = d(L.col_src)
-            L.d_chunk_entry_off = d(L.chunk_entry_off)
-            L.d_entry_dst = d(L.entry_dst)
-            L.d_entry_meta = d(L.entry_meta.view(np.int32))
-            L.d_chunk_slot_bin = d(L.chunk_slot_bin)
-            L.d_chunk_piece_off = d(L.chunk_piece_off)
-            L.d_bin_kpad = d(L.bin_kpad)
-            L.d_piece_emax = torch.zeros(max(1, L.n_pieces * L.n_planes), dtype=torch.int32, device=self.dev)
-            if mode == MODE_E4M3:
-                L.d_chunk_word_off = d(L.chunk_word_off)
-                L.d_word_dst = d(L.word_dst)
-                L.d_word_src = d(L.word_src.view(np.int32))
-            self._layouts[mode] = L
+            self._layouts[mode] = device_layout(self.qmask, self.n_bins, mode, self.dev)
         return self._layouts[mode]
+
+    def _piece_emax(self, L):
+        """This engine's buffer of per-piece energy maxima for layout L (the
+        layout itself may be shared by other engines)."""
+        torch = _torch()
+        bufs = self.__dict__.setdefault("_emax_bufs", {})
+        n = max(1, L.n_pieces * L.n_planes)
+        if L.mode not in bufs or bufs[L.mode].numel() < n:
+            bufs[L.mode] = torch.zeros(n, dtype=torch.int32, device=self.dev)
+        return bufs[L.mode]
 
     def _packed_buffer(self, L):
         """The packed operand buffer, [T (+1)][packed_cols]; zeroed whenever its
@@ -230,7 +265,8 @@ class DenseEngine:
         L = self._layout(mode)
         packed = self._packed_buffer(L)
         self.sums.zero_()
-        L.d_piece_emax.zero_()
+        emax = self._piece_emax(L)
+        emax.zero_()
         self.err.zero_()
         st = stream_handle(self.dev)
         if mode == MODE_E4M3:
@@ -243,7 +279,7 @@ class DenseEngine:
             ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_entry_off),
             ptr(L.d_entry_dst), ptr(L.d_entry_meta), ptr(L.d_chunk_slot_bin), ptr(L.d_chunk_piece_off),
             ptr(L.d_bin_kpad), L.n_chunks, mode, ptr(packed), L.packed_cols, ptr(self.sums), self.n_bins,
-            ptr(L.d_piece_emax), L.n_pieces, ptr(self.err), st), "g2_pack_frames")
+            ptr(emax), L.n_pieces, ptr(self.err), st), "g2_pack_frames")
         return L
 
     def items_for(self, L, grams):
@@ -293,7 +329,7 @@ class DenseEngine:
             if mode == MODE_E4M3:
                 seg_emax = e4m3_segment_bound(L)          # counts <= 16 bound every sum
             else:
-                seg_emax = L.segment_emax(L.d_piece_emax.cpu().numpy().view(np.uint32))
+                seg_emax = L.segment_emax(self._piece_emax(L).cpu().numpy().view(np.uint32))
             code = int(self.err.item())
             wide = frames_dev.element_size() == 2
             if code & _lib.DEVERR_RANGE and mode == MODE_E4M3 and self.operand == "auto":

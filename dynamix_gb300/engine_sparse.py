@@ -314,19 +314,30 @@ class SparseEngine:
             setattr(self, name, buf)
         return buf
 
+    SUBBLOCK = 1024
+
     def to_words(self, data, indices, indptr, offsets, ib, n):
         """CSR on the device -> packed event words (ordered by 32-frame window
         within a pixel) and event offsets (uint32 as int32) on the device;
-        requires :attr:`packed`."""
+        requires :attr:`packed`.  Sub-blocked: per-(1024-frame block, pixel)
+        counts, their totals' scan, then the scatter."""
         torch = _torch()
         H, W = self.shape
+        st = stream_handle(self.dev)
         self.events._mark("start_transpose")
-        self._counts_and_offsets(indices, indptr, offsets, ib, n)
+        n_sb = -(-self.T // self.SUBBLOCK)
+        sbc = self._buffer("sb_counts", n_sb * self.npix, torch.int16)
+        self.counts.zero_()
+        _lib.check(self.lib.g2_csr_count_blocked(ptr(indices), ptr(indptr), ptr(offsets), ib, n, self.T, H, W,
+                                                 ptr(self.counts), ptr(sbc), ptr(self.events.err), st),
+                   "g2_csr_count_blocked")
+        _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
+                                                  ptr(self.scan_scratch), self.scan_scratch.numel(), st),
+                   "g2_exclusive_scan_u32")
         words = self._buffer("ev_words", n, torch.int32)
-        _lib.check(self.lib.g2_csr_scatter_packed(ptr(data), data.element_size(), ptr(indices), ptr(indptr),
-                                                  ptr(offsets), ib, n, self.T, H, W, ptr(self.ev_off), ptr(words),
-                                                  ptr(self.events.err), stream_handle(self.dev)),
-                   "g2_csr_scatter_packed")
+        _lib.check(self.lib.g2_csr_scatter_blocked(ptr(data), data.element_size(), ptr(indices), ptr(indptr),
+                                                   ptr(offsets), ib, n, self.T, H, W, ptr(self.ev_off), ptr(sbc),
+                                                   ptr(words), ptr(self.events.err), st), "g2_csr_scatter_blocked")
         self.events._mark("transpose")
         return words, self.ev_off
 

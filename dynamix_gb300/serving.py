@@ -38,7 +38,8 @@ import time
 import numpy as np
 
 from . import _lib
-from .engine import DenseEngine, DeviceError, _torch, frames_to_device, ptr, require_cuda, stream_handle
+from .engine import (DenseEngine, DeviceError, _torch, device_layout, frames_to_device, ptr, require_cuda,
+                     stream_handle)
 from .plan import MODE_BYTES, MODE_E4M3, MODE_FP16, gram_items
 
 TC_OPS_PER_ITEM_COL = 2 * 128 * 256       # int ops of one 128 x 256 tile per unit of k_len
@@ -184,6 +185,10 @@ class _Job:
         self.arena_off = None
         self.reserved = 0          # bytes of the HBM budget held
         self.frames_dev = None
+        self.mode = None
+        self.pack_event = None
+        self.host_err = None
+        self.host_emax = None
         self.host_out = None
         self.done_event = None
 
@@ -220,7 +225,8 @@ class G2Server:
         self._inflight = []        # (event, pinned items, device items, jobs) per grouped launch
         self.used = 0
         self.lock = threading.Lock()
-        self._layouts = {}         # (shape, qmask digest, n_bins) -> shared layout dict
+        self._params_cache = {}    # (shape, qmask digest, scale) -> (qmask, n_bins, scale)
+        self.packing = []          # jobs whose copy-in / packing is in flight
         self.stats = {"launches": 0, "items": 0, "admitted": 0, "finished": 0, "max_active": 0,
                       "max_used_bytes": 0}
         self._thread = None
@@ -257,7 +263,7 @@ class G2Server:
 
     def idle(self):
         with self.lock:
-            return not (self.queue or self.active or self.finishing or self._inflight)
+            return not (self.queue or self.packing or self.active or self.finishing or self._inflight)
 
     def run_until_idle(self):
         while not self.idle():
@@ -266,17 +272,18 @@ class G2Server:
 
     # -- scheduling --------------------------------------------------------
     def step(self):
-        """One scheduling round: launch the next grouped Gram slice, admit and
-        pack new jobs while it runs, hand over finished results.  Returns True
-        when it did any work."""
+        """One scheduling round: launch the next grouped Gram slice, start the
+        copy-in and packing of newly admitted jobs (asynchronous, side stream),
+        promote jobs whose packing finished, hand over finished results.
+        Returns True when it did any work."""
         launched = self._launch_slice()
         admitted = self._admit()
+        packed = self._poll_packs()
         reaped = self._reap()
-        return launched or admitted or reaped
+        return launched or admitted or packed or reaped
 
     def _params(self, req):
-        """(shape, T, qmask int32, n_bins, scale, layouts) of a request, the
-        q-mask derived data cached per mask."""
+        """(shape, T, qmask int32, n_bins, scale) of a request, cached per q-mask."""
         import hashlib
 
         from .correlator.common import BaseCorrelator
@@ -288,11 +295,13 @@ class G2Server:
         digest = hashlib.blake2b(qm.tobytes() if qm is not None else b"all", digest_size=16).hexdigest()
         sf = req.scale_factor
         key = (H, W, digest, None if sf is None else repr(sf))
-        if key not in self._layouts:
+        if key not in self._params_cache:
             bc = BaseCorrelator()
             if qm is None:
                 bc._set_parameters((H, W), T, None, sf, {})
             else:
+                if qm.shape != (H, W):
+                    raise ValueError("qmask shape %s does not match frame shape %s" % (qm.shape, (H, W)))
                 bc._set_shape((H, W))
                 bc.nframes = T
                 bc.qmask = qm
@@ -303,20 +312,16 @@ class G2Server:
                     bc.scale_factors = {b: int(cnt[b]) for b in bc.bins}
                 else:
                     bc._set_scale_factor(sf)
-            if len(self._layouts) > 64:
-                self._layouts.clear()
-            self._layouts[key] = (bc.qmask, bc.n_bins, bc._scale_array(), {})
-        qmask, n_bins, scale, layouts = self._layouts[key]
-        return (H, W), T, qmask, n_bins, scale, layouts
+            if len(self._params_cache) > 64:
+                self._params_cache.clear()
+            self._params_cache[key] = (bc.qmask, bc.n_bins, bc._scale_array())
+        qmask, n_bins, scale = self._params_cache[key]
+        return (H, W), T, qmask, n_bins, scale
 
-    def _estimate(self, job, layouts):
+    def _estimate(self, job):
         """Bytes of the budget a job needs at its peak: frames copied to the
         device plus the widest packed operand its counts may need."""
-        from .plan import PackLayout
-        key = ("fp16_cols",)
-        if key not in layouts:
-            layouts[key] = PackLayout(job.qmask, job.n_bins, MODE_FP16).packed_cols
-        cols = layouts[key]
+        cols = device_layout(job.qmask, job.n_bins, MODE_FP16, self.dev).packed_cols if job.n_bins else 0
         frames = job.T * job.shape[0] * job.shape[1] * job.elem_bytes if job.from_host else 0
         return frames + (job.T + 1) * cols * (2 if job.elem_bytes == 1 else 4)
 
@@ -324,19 +329,19 @@ class G2Server:
         """Server-side job of a request (built once, kept on the request)."""
         torch = _torch()
         if getattr(req, "_job", None) is None:
-            shape, T, qmask, n_bins, scale, layouts = self._params(req)
+            shape, T, qmask, n_bins, scale = self._params(req)
             fr = req.frames
             from_host = not (isinstance(fr, torch.Tensor) and fr.is_cuda)
             dt = fr.dtype if isinstance(fr, torch.Tensor) else np.asarray(fr).dtype
             elem = 1 if dt in (torch.uint8, np.uint8) else 2     # other integer types become u8 or u16
             job = _Job(req, shape, T, qmask, n_bins, scale, elem, from_host)
-            req._job = (job, layouts, self._estimate(job, layouts))
+            req._job = (job, self._estimate(job))
         return req._job
 
     def _admit(self):
         with self.lock:
             pending = list(self.queue)
-        free = self.max_active - len(self.active) - len(self.finishing)
+        free = self.max_active - len(self.active) - len(self.finishing) - len(self.packing)
         if not pending or free <= 0:
             return False
         cands = []
@@ -346,15 +351,15 @@ class G2Server:
             except Exception as e:                 # malformed request: fail it, keep serving
                 self._dequeue(req)
                 self._fail(req, e)
-        admit, too_large = admit_order([c[3] for c in cands], self.used, self.budget, free)
+        admit, too_large = admit_order([c[2] for c in cands], self.used, self.budget, free)
         for i in too_large:
-            req, job, layouts, need = cands[i]
+            req, job, need = cands[i]
             self._dequeue(req)
             self._fail(req, MemoryError("job needs %.1f GB, the budget is %.1f GB" % (need / 1e9,
                                                                                       self.budget / 1e9)))
         admitted = False
         for i in admit:
-            req, job, layouts, need = cands[i]
+            req, job, need = cands[i]
             try:
                 job.arena_off = self.arena.alloc(job.rows * job.T)
             except ArenaFull:
@@ -363,7 +368,7 @@ class G2Server:
             job.reserved = need
             self.used += need
             try:
-                self._start(job, layouts)
+                self._start(job)
             except Exception as e:
                 self._release(job)
                 self._fail(req, e)
@@ -376,9 +381,11 @@ class G2Server:
             if req in self.queue:
                 self.queue.remove(req)
 
-    def _start(self, job, layouts):
-        """Frames to the device and packed, on the side stream; the tiles of
-        the job are then ready for the grouped launches."""
+    def _start(self, job):
+        """Queue the frames' copy-in and the packing on the side stream; the
+        error word (and, for fp16 operands, the segment energies) follow to
+        pinned host memory, and :meth:`_poll_packs` plans the job's tiles once
+        they have arrived -- the host never waits for the GPU here."""
         torch = _torch()
         req = job.req
         req.t_admit = time.perf_counter()
@@ -394,21 +401,79 @@ class G2Server:
                 frames_dev.copy_(fr, non_blocking=True)         # asynchronous on the side stream
             else:
                 frames_dev = frames_to_device(fr, self.dev)      # validates, converts, or uses in place
-            eng = DenseEngine(job.shape, job.T, job.qmask, job.n_bins, job.scale, device=self.dev,
-                              method=self.method, numer=numer, sums=sums, layouts=layouts)
-            job.engine = eng
-            if job.n_bins:
-                mode = eng.choose_mode(frames_dev)
-                L, grams = eng._pack_and_plan(frames_dev, mode)   # synchronises the side stream
-                job.layout = L
+            job.frames_dev = frames_dev
+            job.engine = DenseEngine(job.shape, job.T, job.qmask, job.n_bins, job.scale, device=self.dev,
+                                     method=self.method, numer=numer, sums=sums)
+        req.frames = None                           # the server keeps no reference to the input
+        if job.n_bins == 0:
+            self._promote(job, np.empty(0, dtype=_lib.ITEM_DTYPE))
+            return
+        job.mode = job.engine.choose_mode(frames_dev)
+        self._launch_pack(job)
+        self.packing.append(job)
+
+    def _launch_pack(self, job):
+        torch = _torch()
+        eng = job.engine
+        with torch.cuda.stream(self.side):
+            L = eng.pack(job.frames_dev, job.mode)
+            job.layout = L
+            job.host_err = torch.empty(1, dtype=torch.int32, pin_memory=True)
+            job.host_err.copy_(eng.err, non_blocking=True)
+            job.host_emax = None
+            if job.mode != MODE_E4M3:
+                emax = eng._piece_emax(L)
+                job.host_emax = torch.empty(emax.numel(), dtype=torch.int32, pin_memory=True)
+                job.host_emax.copy_(emax, non_blocking=True)
+            job.pack_event = torch.cuda.Event()
+            job.pack_event.record(self.side)
+
+    def _poll_packs(self):
+        """Plan the tiles of every job whose packing has finished (a count
+        that does not fit the operand repacks wider)."""
+        from .plan import chunk_grams, e4m3_segment_bound
+        done = [j for j in self.packing if j.pack_event.query()]
+        for job in done:
+            self.packing.remove(job)
+            eng, L = job.engine, job.layout
+            try:
+                code = int(job.host_err[0])
+                wider = {MODE_E4M3: MODE_FP16, MODE_FP16: MODE_BYTES}.get(job.mode)
+                if code & _lib.DEVERR_RANGE and wider is not None:
+                    job.mode = wider
+                    self._launch_pack(job)
+                    self.packing.append(job)
+                    continue
+                if code:
+                    raise DeviceError(_lib.device_error_message(code))
+                if job.mode == MODE_E4M3:
+                    seg_emax = e4m3_segment_bound(L)
+                else:
+                    seg_emax = L.segment_emax(job.host_emax.numpy().view(np.uint32))
+                try:
+                    grams = chunk_grams(L, seg_emax, eng.exact_limit)
+                except OverflowError:
+                    if job.mode == MODE_BYTES:
+                        raise
+                    job.mode = MODE_BYTES
+                    self._launch_pack(job)
+                    self.packing.append(job)
+                    continue
+                off = job.arena_off
                 items = gram_items(job.T, grams, job=0, out_base=off, kind=self.method,
                                    s_base=off if (L.ones_row and self.method == "tc") else None)
-            else:
-                items = np.empty(0, dtype=_lib.ITEM_DTYPE)
-            ready = torch.cuda.Event()
-            ready.record(self.side)
-        self.compute.wait_event(ready)
-        del frames_dev                              # packed: the frames are no longer needed
+            except Exception as e:
+                self._release(job)
+                self._fail(job.req, e)
+                continue
+            self.compute.wait_event(job.pack_event)
+            self._promote(job, items)
+        return bool(done)
+
+    def _promote(self, job, items):
+        """A packed job joins the grouped launches."""
+        eng = job.engine
+        job.frames_dev = None                      # packed: the frames are no longer needed
         if eng.packed is not None:
             eng.packed.record_stream(self.compute)
         packed_bytes = 0 if eng.packed is None else eng.packed.numel()
@@ -419,9 +484,8 @@ class G2Server:
         job.item_ops = items["k_len"].astype(np.float64) * TC_OPS_PER_ITEM_COL
         job.remaining_ops = float(job.item_ops.sum())
         job.next_item = 0
-        req.info.update(mode=None if job.layout is None else ["fp16", "bytes", "e4m3"][job.layout.mode],
-                        n_items=int(items.size), packed_bytes=int(packed_bytes))
-        req.frames = None                           # the server keeps no reference to the input
+        job.req.info.update(mode=None if job.layout is None else ["fp16", "bytes", "e4m3"][job.layout.mode],
+                            n_items=int(items.size), packed_bytes=int(packed_bytes))
         self.active.append(job)
         if items.size == 0:
             self._finish(job)                       # no binned pixel: nothing to correlate

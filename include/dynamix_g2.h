@@ -230,19 +230,28 @@ int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices
                    uint32_t* cursor_dev, int32_t* ev_times_dev, void* ev_data_dev, int32_t* err_dev,
                    void* stream);
 
-/* Packed variants (frames < 2^16, image rows up to 29,000 pixels).
- * g2_csr_scatter_packed writes each element as one word (t << 16) | v into
- * ev_words_dev[ev_offsets[p] ..), ordered by 32-frame window (t >> 5) and in
- * any order inside a window (no cursor array; column indices must increase
- * strictly within a row, else G2_DEVERR_BOUNDS); g2_events_sort_windows puts
- * every pixel's words in frame order; g2_events_unpack splits words into
- * ev_times (int32) and ev_data (elem_bytes 1 or 2) -- with the sort, the
- * FramesCompressor layout (event.py:267-284).
- * Returns G2_ERR_UNSUPPORTED when nframes > 65536 or width > 29,000. */
-int g2_csr_scatter_packed(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
-                          const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
-                          int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
-                          uint32_t* ev_words_dev, int32_t* err_dev, void* stream);
+/* Sub-blocked variants with packed event words (frames < 2^16, image rows up
+ * to 29,000 pixels): the frames are cut into sub-blocks of 1024.
+ * g2_csr_count_blocked writes sb_counts_dev[sb * H*W + p] (uint16, the
+ * elements of pixel p in sub-block sb; ceil(nframes / 1024) * H*W entries)
+ * and adds each pixel's total to counts_dev (caller zeroes).
+ * g2_csr_scatter_blocked writes each element as one word (t << 16) | v into
+ * ev_words_dev[ev_offsets[p] ..) (ev_offsets: exclusive scan of the totals),
+ * ordered by 32-frame window (t >> 5) and in any order inside a window;
+ * column indices must increase strictly within a row (sorted CSR), else
+ * G2_DEVERR_BOUNDS.  g2_events_sort_windows puts every pixel's words in frame
+ * order; g2_events_unpack splits words into ev_times (int32) and ev_data
+ * (elem_bytes 1 or 2) -- with the sort, the FramesCompressor layout
+ * (event.py:267-284).  G2_ERR_UNSUPPORTED when nframes > 65536 (scatter) or
+ * width > 29,000. */
+int g2_csr_count_blocked(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
+                         int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
+                         uint32_t* counts_dev, uint16_t* sb_counts_dev, int32_t* err_dev, void* stream);
+int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                           const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
+                           int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
+                           const uint16_t* sb_counts_dev, uint32_t* ev_words_dev, int32_t* err_dev,
+                           void* stream);
 int g2_events_sort_windows(uint32_t* ev_words_dev, const uint32_t* ev_offsets_dev, int64_t npix, void* stream);
 int g2_events_unpack(const uint32_t* ev_words_dev, int64_t n_events, int32_t elem_bytes, int32_t* ev_times_dev,
                      void* ev_data_dev, void* stream);
@@ -298,17 +307,6 @@ int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, const double
  * point allocates nothing: no cudaMalloc, no cudaFree. */
 #define G2_STATIC_DENOM_MAX (1 << 19)
 
-/* ---- launch-shape settings (no reference counterpart) ---------------------
- * Process-wide knobs read at launch time; 0 (the default) means the built-in
- * choice.  They change launch shapes only, never results; an autotuner
- * (dynamix_gb300.tune) times the candidates and sets the winners.
- *   G2_TUNE_CSR_SMEM   bytes of shared memory the row-owned CSR scatter asks
- *                      per CTA (more bytes: fewer image rows in flight, so the
- *                      sectors being filled stay in L2) */
-#define G2_TUNE_CSR_SMEM 0
-#define G2_TUNE_COUNT 1
-int g2_set_tuning(int32_t key, int64_t value);
-int64_t g2_get_tuning(int32_t key);
 int g2_normalize_static(const int64_t* numer_dev, const int64_t* sums_dev, const double* scale_dev,
                         int32_t n_rows, int64_t nframes, float* g2_f32_dev, double* g2_f64_dev,
                         void* stream);
