@@ -285,11 +285,48 @@ __global__ void __launch_bounds__(256)
 constexpr int SUBBLOCK = 1024;
 constexpr int SB_PER_CTA = 8;
 
+// Row bounds transposed to row-major: rb[r * T + t] = offsets[t] + indptr[t][r]
+// (absolute element index of the start of row r in frame t; r = H is the
+// frame's end), so that a warp walking one row over 32 consecutive frames
+// reads its bounds with one coalesced load.  Malformed pointers are reported
+// and replaced by an empty row.
 template <typename Ti>
 __global__ void __launch_bounds__(256)
-    row_count_blocked_kernel(const Ti* __restrict__ indices, const Ti* __restrict__ indptr,
-                             const Ti* __restrict__ offsets, int64_t n_elem, int32_t T, int32_t H, int32_t W,
-                             int rows_per_cta, uint16_t* __restrict__ sb_counts, int32_t* __restrict__ err) {
+    row_bounds_kernel(const Ti* __restrict__ indptr, const Ti* __restrict__ offsets, int64_t n_elem, int32_t T,
+                      int32_t H, uint32_t* __restrict__ rb, int32_t* __restrict__ err) {
+  __shared__ uint32_t tile[32][33];
+  const int64_t t0 = static_cast<int64_t>(blockIdx.x) * 32, r0 = static_cast<int64_t>(blockIdx.y) * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  bool bad = false;
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t t = t0 + k, r = r0 + tx;
+    uint32_t v = 0;
+    if (t < T && r <= H) {
+      const int64_t base = static_cast<int64_t>(offsets[t]);
+      const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
+      const int64_t a = base + static_cast<int64_t>(indptr[t * static_cast<int64_t>(H + 1) + r]);
+      if (base < 0 || a < base || a > fend || fend > n_elem) {
+        bad = true;
+        v = static_cast<uint32_t>(base < 0 ? 0 : (base > n_elem ? n_elem : base));
+      } else {
+        v = static_cast<uint32_t>(a);
+      }
+    }
+    tile[k][tx] = v;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t r = r0 + k, t = t0 + tx;
+    if (t < T && r <= H) rb[r * T + t] = tile[tx][k];
+  }
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+template <typename Ti>
+__global__ void __launch_bounds__(256)
+    row_count_blocked_kernel(const Ti* __restrict__ indices, const uint32_t* __restrict__ rb, int64_t n_elem,
+                             int32_t T, int32_t H, int32_t W, int rows_per_cta, uint16_t* __restrict__ sb_counts,
+                             int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * rows_per_cta + warp;
@@ -304,12 +341,9 @@ __global__ void __launch_bounds__(256)
     for (int64_t t0 = sb0; t0 < sb_end; t0 += 32) {
       const int64_t t = t0 + lane;
       if (t >= sb_end) continue;
-      const int64_t base = static_cast<int64_t>(offsets[t]);
-      const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
-      const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
-      const int64_t s = base + static_cast<int64_t>(ip[0]);
-      const int64_t e = base + static_cast<int64_t>(ip[1]);
-      if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+      const int64_t s = rb[static_cast<int64_t>(r) * T + t];
+      const int64_t e = rb[static_cast<int64_t>(r + 1) * T + t];
+      if (e < s || e > n_elem) {
         bad = true;
         continue;
       }
@@ -349,10 +383,9 @@ __global__ void __launch_bounds__(256)
 template <typename Tv, typename Ti>
 __global__ void __launch_bounds__(SB_PER_CTA * 32)
     row_scatter_blocked_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices,
-                               const Ti* __restrict__ indptr, const Ti* __restrict__ offsets, int64_t n_elem,
-                               int32_t T, int32_t H, int32_t W, const uint32_t* __restrict__ ev_off,
-                               const uint16_t* __restrict__ sb_counts, uint32_t* __restrict__ ev_words,
-                               int32_t* __restrict__ err) {
+                               const uint32_t* __restrict__ rb, int64_t n_elem, int32_t T, int32_t H, int32_t W,
+                               const uint32_t* __restrict__ ev_off, const uint16_t* __restrict__ sb_counts,
+                               uint32_t* __restrict__ ev_words, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.y;
@@ -365,6 +398,7 @@ __global__ void __launch_bounds__(SB_PER_CTA * 32)
   // the sub-block's first slot of each pixel: its offset plus the earlier sub-blocks
   for (int i = lane; i < W; i += 32) {
     uint32_t c = ev_off[row0 + i];
+#pragma unroll 8
     for (int64_t b = 0; b < sb; ++b) c += sb_counts[b * npix + row0 + i];
     cur[i] = c;
   }
@@ -375,30 +409,47 @@ __global__ void __launch_bounds__(SB_PER_CTA * 32)
   for (int64_t t0 = sb0; t0 < sb_end; t0 += 32) {
     const int64_t t = t0 + lane;
     if (t >= sb_end) continue;
-    const int64_t base = static_cast<int64_t>(offsets[t]);
-    const int64_t fend = static_cast<int64_t>(offsets[t + 1]);
-    const Ti* ip = indptr + t * static_cast<int64_t>(H + 1) + r;
-    const int64_t s = base + static_cast<int64_t>(ip[0]);
-    const int64_t e = base + static_cast<int64_t>(ip[1]);
-    if (base < 0 || s < base || e < s || e > fend || e > n_elem) {
+    const int64_t s = rb[static_cast<int64_t>(r) * T + t];
+    const int64_t e = rb[static_cast<int64_t>(r + 1) * T + t];
+    if (e < s || e > n_elem) {
       bad = true;
       continue;
     }
     const uint32_t tw = static_cast<uint32_t>(t) << 16;
     int64_t prev = -1;
-#pragma unroll 4
-    for (int64_t k = s; k < e; ++k) {
-      const int64_t c = static_cast<int64_t>(indices[k]);
-      if (c <= prev || c >= W) {
-        bad = true;  // repeated, descending or out-of-range column
-        if (c < 0 || c >= W) continue;
+    // four elements at a time without branches between them, so their loads,
+    // their shared-memory slot atomics and their stores overlap
+    for (int64_t k0 = s; k0 < e; k0 += 4) {
+      int64_t c[4];
+      uint32_t v[4];
+      bool in[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t k = k0 + j;
+        in[j] = k < e;
+        c[j] = in[j] ? static_cast<int64_t>(indices[k]) : 0;
+        v[j] = in[j] ? static_cast<uint32_t>(data[k]) : 0u;
       }
-      prev = c;
-      const uint32_t slot = atomicAdd(&cur[c], 1u);
-      if (slot < n_total)
-        ev_words[slot] = tw | static_cast<uint32_t>(data[k]);
-      else
-        bad = true;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (in[j]) {
+          bad |= c[j] <= prev || c[j] >= W;  // repeated, descending or out-of-range column
+          prev = c[j];
+          in[j] = c[j] >= 0 && c[j] < W;
+        }
+      }
+      uint32_t slot[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) slot[j] = in[j] ? atomicAdd(&cur[c[j]], 1u) : 0u;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (in[j]) {
+          if (slot[j] < n_total)
+            ev_words[slot[j]] = tw | v[j];
+          else
+            bad = true;
+        }
+      }
     }
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
@@ -660,27 +711,37 @@ extern "C" int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const vo
 
 extern "C" int g2_csr_count_blocked(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
                                     int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height,
-                                    int32_t width, uint32_t* counts_dev, uint16_t* sb_counts_dev, int32_t* err_dev,
-                                    void* stream) {
+                                    int32_t width, uint32_t* row_bounds_dev, uint32_t* counts_dev,
+                                    uint16_t* sb_counts_dev, int32_t* err_dev, void* stream) {
   using namespace g2;
-  if (!indices_dev || !indptr_dev || !offsets_dev || !counts_dev || !sb_counts_dev || !err_dev) return G2_ERR_ARG;
+  if (!indices_dev || !indptr_dev || !offsets_dev || !row_bounds_dev || !counts_dev || !sb_counts_dev || !err_dev)
+    return G2_ERR_ARG;
   if ((index_bytes != 4 && index_bytes != 8) || n_elem < 0 || nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
-  if (width > csr::ROW_MAX_W) return G2_ERR_UNSUPPORTED;
+  if (width > csr::ROW_MAX_W || n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
+  cudaStream_t st = as_stream(stream);
+  const dim3 tgrid(static_cast<unsigned>((nframes + 31) / 32), static_cast<unsigned>((height + 1 + 31) / 32));
+  if (index_bytes == 4)
+    csr::row_bounds_kernel<uint32_t><<<tgrid, 256, 0, st>>>(reinterpret_cast<const uint32_t*>(indptr_dev),
+                                                             reinterpret_cast<const uint32_t*>(offsets_dev), n_elem,
+                                                             nframes, height, row_bounds_dev, err_dev);
+  else
+    csr::row_bounds_kernel<int64_t><<<tgrid, 256, 0, st>>>(reinterpret_cast<const int64_t*>(indptr_dev),
+                                                            reinterpret_cast<const int64_t*>(offsets_dev), n_elem,
+                                                            nframes, height, row_bounds_dev, err_dev);
   const int rpc = rows_per_cta(width, 1);
   const int64_t smem = static_cast<int64_t>(rpc) * width * 4;
   const unsigned grid = static_cast<unsigned>((height + rpc - 1) / rpc);
-  cudaStream_t st = as_stream(stream);
   if (index_bytes == 4) {
     if (!allow_smem(csr::row_count_blocked_kernel<uint32_t>, smem)) return G2_ERR_CUDA;
     csr::row_count_blocked_kernel<uint32_t><<<grid, rpc * 32, smem, st>>>(
-        reinterpret_cast<const uint32_t*>(indices_dev), reinterpret_cast<const uint32_t*>(indptr_dev),
-        reinterpret_cast<const uint32_t*>(offsets_dev), n_elem, nframes, height, width, rpc, sb_counts_dev, err_dev);
+        reinterpret_cast<const uint32_t*>(indices_dev), row_bounds_dev, n_elem, nframes, height, width, rpc,
+        sb_counts_dev, err_dev);
   } else {
     if (!allow_smem(csr::row_count_blocked_kernel<int64_t>, smem)) return G2_ERR_CUDA;
     csr::row_count_blocked_kernel<int64_t><<<grid, rpc * 32, smem, st>>>(
-        reinterpret_cast<const int64_t*>(indices_dev), reinterpret_cast<const int64_t*>(indptr_dev),
-        reinterpret_cast<const int64_t*>(offsets_dev), n_elem, nframes, height, width, rpc, sb_counts_dev, err_dev);
+        reinterpret_cast<const int64_t*>(indices_dev), row_bounds_dev, n_elem, nframes, height, width, rpc,
+        sb_counts_dev, err_dev);
   }
   const int64_t npix = static_cast<int64_t>(height) * width;
   const int n_sb = static_cast<int>((static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK);
@@ -693,18 +754,18 @@ extern "C" int g2_csr_count_blocked(const void* indices_dev, const void* indptr_
 }
 
 extern "C" int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
-                                      const void* indptr_dev, const void* offsets_dev, int32_t index_bytes,
-                                      int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
-                                      const uint32_t* ev_offsets_dev, const uint16_t* sb_counts_dev,
-                                      uint32_t* ev_words_dev, int32_t* err_dev, void* stream) {
+                                      const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem,
+                                      int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
+                                      const uint16_t* sb_counts_dev, uint32_t* ev_words_dev, int32_t* err_dev,
+                                      void* stream) {
   using namespace g2;
-  if (!data_dev || !indices_dev || !indptr_dev || !offsets_dev || !ev_offsets_dev || !sb_counts_dev ||
-      !ev_words_dev || !err_dev)
+  if (!data_dev || !indices_dev || !row_bounds_dev || !ev_offsets_dev || !sb_counts_dev || !ev_words_dev ||
+      !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || (index_bytes != 4 && index_bytes != 8) || n_elem < 0 ||
       nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
-  if (nframes > 65536 || width > csr::ROW_MAX_W) return G2_ERR_UNSUPPORTED;
+  if (nframes > 65536 || width > csr::ROW_MAX_W || n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
   // warps (sub-blocks) per CTA: up to 8, each holding one row of cursors
   int warps = static_cast<int>((227 * 1024) / (static_cast<int64_t>(width) * 4));
   warps = warps < 1 ? 1 : (warps > csr::SB_PER_CTA ? csr::SB_PER_CTA : warps);
@@ -716,9 +777,8 @@ extern "C" int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, 
   do {                                                                                                          \
     if (!allow_smem(csr::row_scatter_blocked_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                         \
     csr::row_scatter_blocked_kernel<TV, TI><<<grid, warps * 32, smem, st>>>(                                    \
-        reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev),                        \
-        reinterpret_cast<const TI*>(indptr_dev), reinterpret_cast<const TI*>(offsets_dev), n_elem, nframes,     \
-        height, width, ev_offsets_dev, sb_counts_dev, ev_words_dev, err_dev);                                   \
+        reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev), row_bounds_dev, n_elem, \
+        nframes, height, width, ev_offsets_dev, sb_counts_dev, ev_words_dev, err_dev);                          \
   } while (0)
   if (elem_bytes == 1 && index_bytes == 4) G2_BS(uint8_t, uint32_t);
   else if (elem_bytes == 1) G2_BS(uint8_t, int64_t);

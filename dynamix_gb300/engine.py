@@ -94,13 +94,19 @@ _LAYOUTS_LOCK = threading.Lock()
 _LAYOUTS_MAX = 48
 
 
-def device_layout(qmask, n_bins, mode, dev):
+def qmask_digest(qmask):
+    q = np.ascontiguousarray(qmask, dtype=np.int32)
+    return "%s:%s" % (q.shape, hashlib.blake2b(q.tobytes(), digest_size=16).hexdigest())
+
+
+def device_layout(qmask, n_bins, mode, dev, digest=None):
     """The packing layout of a q-mask with its read-only tables on ``dev``,
     shared process-wide (least recently used of 48 kept): building one costs
-    host time proportional to the frame size."""
+    host time proportional to the frame size.  ``digest``: the q-mask's
+    :func:`qmask_digest` when the caller has it."""
     torch = _torch()
     q = np.ascontiguousarray(qmask, dtype=np.int32)
-    key = (str(dev), q.shape, hashlib.blake2b(q.tobytes(), digest_size=16).hexdigest(), int(n_bins), int(mode))
+    key = (str(dev), digest or qmask_digest(q), int(n_bins), int(mode))
     with _LAYOUTS_LOCK:
         L = _LAYOUTS.get(key)
         if L is not None:
@@ -137,7 +143,8 @@ class DenseEngine:
     MODES = {"fp16": MODE_FP16, "bytes": MODE_BYTES, "e4m3": MODE_E4M3}
 
     def __init__(self, shape, nframes, qmask, n_bins, scale, device=None, method="tc",
-                 exact_limit=EXACT_LIMIT, grid=0, operand="auto", numer=None, sums=None, layouts=None):
+                 exact_limit=EXACT_LIMIT, grid=0, operand="auto", numer=None, sums=None, layouts=None,
+                 qmask_digest=None):
         torch = _torch()
         self.lib = _lib.load()
         self.dev = require_cuda(device)
@@ -169,6 +176,7 @@ class DenseEngine:
         self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.maxval = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self._layouts = {} if layouts is None else layouts   # may be shared by engines of one q-mask
+        self._qdigest = qmask_digest
         self._items_cache = {}
         self.packed = None
         self.last = {}
@@ -178,6 +186,7 @@ class DenseEngine:
         self.pipeline = True      # chunked copy/pack/Gram overlap where it applies
         self.pipe_chunks = self.PIPE_CHUNKS
         self.super_rows = self.SUPER_ROWS
+        self.kslab = self.KSLAB
         from .tune import apply_cached
         apply_cached(self)        # launch shapes an earlier tuning run chose for this (T, pixels per bin)
         self.profile = False      # record CUDA events around every stage
@@ -209,7 +218,9 @@ class DenseEngine:
     # -- layout / buffers ------------------------------------------------
     def _layout(self, mode):
         if mode not in self._layouts:
-            self._layouts[mode] = device_layout(self.qmask, self.n_bins, mode, self.dev)
+            if getattr(self, "_qdigest", None) is None:
+                self._qdigest = qmask_digest(self.qmask)
+            self._layouts[mode] = device_layout(self.qmask, self.n_bins, mode, self.dev, self._qdigest)
         return self._layouts[mode]
 
     def _piece_emax(self, L):
@@ -347,7 +358,7 @@ class DenseEngine:
             if code:
                 raise DeviceError(_lib.device_error_message(code))
             try:
-                grams = chunk_grams(L, seg_emax, self.exact_limit)
+                grams = chunk_grams(L, seg_emax, self.exact_limit, self.kslab)
             except OverflowError:
                 if mode != MODE_BYTES and self.operand == "auto":
                     mode = MODE_BYTES
@@ -365,15 +376,16 @@ class DenseEngine:
     # -- chunked pipeline (e4m3) ---------------------------------------------
     PIPE_CHUNKS = 8
     SUPER_ROWS = 2048
+    KSLAB = 0                 # no cap on the K columns of one tile item
 
     def _pipe_plan(self, L):
         """Items of the e4m3 Gram grouped by the frame chunk whose packing
         makes them ready (a tile needs frames up to its last column), LPT order
         inside a group; cached per layout."""
-        key = ("pipe", L.mode, self.T, self.exact_limit, self.grid, self.pipe_chunks, self.super_rows)
+        key = ("pipe", L.mode, self.T, self.exact_limit, self.grid, self.pipe_chunks, self.super_rows, self.kslab)
         if key not in self._items_cache:
             torch = _torch()
-            grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit)
+            grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit, self.kslab)
             items = gram_items(self.T, grams, job=0, out_base=0, kind="tc", s_base=0 if L.ones_row else None,
                                super_rows=self.super_rows)
             T = self.T

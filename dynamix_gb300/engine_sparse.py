@@ -289,11 +289,10 @@ class SparseEngine:
 
     ROW_MAX_W = 29000
 
-    @property
-    def packed(self):
-        """Events travel as packed words (t << 16) | v: frames < 2^16 and rows
-        the row-owned kernels take."""
-        return self.T <= 65535 and self.shape[1] <= self.ROW_MAX_W
+    def packed_for(self, n):
+        """Events travel as packed words (t << 16) | v: frames < 2^16, rows the
+        row-owned kernels take, fewer than 2^32 elements."""
+        return self.T <= 65535 and self.shape[1] <= self.ROW_MAX_W and n < 2 ** 32
 
     def _counts_and_offsets(self, indices, indptr, offsets, ib, n):
         st = stream_handle(self.dev)
@@ -319,7 +318,7 @@ class SparseEngine:
     def to_words(self, data, indices, indptr, offsets, ib, n):
         """CSR on the device -> packed event words (ordered by 32-frame window
         within a pixel) and event offsets (uint32 as int32) on the device;
-        requires :attr:`packed`.  Sub-blocked: per-(1024-frame block, pixel)
+        requires :meth:`packed_for`.  Sub-blocked: per-(1024-frame block, pixel)
         counts, their totals' scan, then the scatter."""
         torch = _torch()
         H, W = self.shape
@@ -327,29 +326,30 @@ class SparseEngine:
         self.events._mark("start_transpose")
         n_sb = -(-self.T // self.SUBBLOCK)
         sbc = self._buffer("sb_counts", n_sb * self.npix, torch.int16)
+        rb = self._buffer("row_bounds", (H + 1) * self.T, torch.int32)
         self.counts.zero_()
         _lib.check(self.lib.g2_csr_count_blocked(ptr(indices), ptr(indptr), ptr(offsets), ib, n, self.T, H, W,
-                                                 ptr(self.counts), ptr(sbc), ptr(self.events.err), st),
+                                                 ptr(rb), ptr(self.counts), ptr(sbc), ptr(self.events.err), st),
                    "g2_csr_count_blocked")
         _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
                                                   ptr(self.scan_scratch), self.scan_scratch.numel(), st),
                    "g2_exclusive_scan_u32")
         words = self._buffer("ev_words", n, torch.int32)
-        _lib.check(self.lib.g2_csr_scatter_blocked(ptr(data), data.element_size(), ptr(indices), ptr(indptr),
-                                                   ptr(offsets), ib, n, self.T, H, W, ptr(self.ev_off), ptr(sbc),
-                                                   ptr(words), ptr(self.events.err), st), "g2_csr_scatter_blocked")
+        _lib.check(self.lib.g2_csr_scatter_blocked(ptr(data), data.element_size(), ptr(indices), ptr(rb), ib, n,
+                                                   self.T, H, W, ptr(self.ev_off), ptr(sbc), ptr(words),
+                                                   ptr(self.events.err), st), "g2_csr_scatter_blocked")
         self.events._mark("transpose")
         return words, self.ev_off
 
     def to_events(self, data, indices, indptr, offsets, ib, n):
         """CSR on the device -> (times int32, counts, offsets) event lists on
         the device, in the FramesCompressor layout (frames ascending within a
-        pixel when :attr:`packed`, else in an unspecified order)."""
+        pixel when :meth:`packed_for` holds, else in an unspecified order)."""
         torch = _torch()
         self.events.err.zero_()
         times = self._buffer("ev_times", n, torch.int32)
         evdata = self._buffer("ev_data", n, data.dtype)
-        if self.packed:
+        if self.packed_for(n):
             words, off = self.to_words(data, indices, indptr, offsets, ib, n)
             _lib.check(self.lib.g2_events_sort_windows(ptr(words), ptr(off), self.npix, stream_handle(self.dev)),
                        "g2_events_sort_windows")
@@ -370,14 +370,15 @@ class SparseEngine:
     def run(self, data, indices, indptr, offsets):
         counts, ind, ip, off, ib, n, mx = csr_to_device(data, indices, indptr, offsets, self.shape, self.T,
                                                         self.dev)
-        if self.packed:
+        packed = self.packed_for(n)
+        if packed:
             self.events.err.zero_()
             words, evoff = self.to_words(counts, ind, ip, off, ib, n)
             out = self.events.run_device(words, None, evoff, n, mx, reset_error=False)
         else:
             times, evdata, evoff = self.to_events(counts, ind, ip, off, ib, n)
             out = self.events.run_device(times, evdata, evoff, n, mx, reset_error=False)
-        self.last = dict(self.events.last, n_elements=n, packed=self.packed)
+        self.last = dict(self.events.last, n_elements=n, packed=packed)
         return out
 
     def check_error(self):

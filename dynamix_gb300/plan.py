@@ -281,19 +281,25 @@ def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc", s_base=None, supe
     return items[order]
 
 
-def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT):
+def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT, kslab=0):
     """Apply :func:`k_chunks` to every Gram of a layout, in units of PAD columns.
 
-    ``seg_emax`` is indexed by packed column // 64.  Returns the list of
-    ``(bin, a_off, b_off, k0, k_len, shift)``."""
+    ``seg_emax`` is indexed by packed column // 64.  ``kslab`` > 0 also caps
+    every chunk at that many columns (rounded down to PAD): the tiles that run
+    at the same time then share a narrower slab of K in L2.  Returns the list
+    of ``(bin, a_off, b_off, k0, k_len, shift)``."""
     per = PAD // BK
+    cap = max(1, int(kslab) // PAD) if kslab else 0
     out = []
     for (b, a_off, b_off, kp, shift) in layout.grams():
         nseg = kp // BK
         ea = np.asarray(seg_emax[a_off // BK: a_off // BK + nseg], dtype=np.float64).reshape(-1, per).sum(1)
         eb = np.asarray(seg_emax[b_off // BK: b_off // BK + nseg], dtype=np.float64).reshape(-1, per).sum(1)
         for (u0, u1) in k_chunks(ea, eb, limit):
-            out.append((b, a_off, b_off, u0 * PAD, (u1 - u0) * PAD, shift))
+            step = cap if cap else u1 - u0
+            for v0 in range(u0, u1, step):
+                v1 = min(u1, v0 + step)
+                out.append((b, a_off, b_off, v0 * PAD, (v1 - v0) * PAD, shift))
     return out
 
 

@@ -225,7 +225,8 @@ class G2Server:
         self._inflight = []        # (event, pinned items, device items, jobs) per grouped launch
         self.used = 0
         self.lock = threading.Lock()
-        self._params_cache = {}    # (shape, qmask digest, scale) -> (qmask, n_bins, scale)
+        self._params_cache = {}    # (shape, qmask digest, scale) -> (qmask, n_bins, scale, digest)
+        self._digest_cache = {}    # (id(qmask), H, W) -> (qmask, digest)
         self.packing = []          # jobs whose copy-in / packing is in flight
         self.stats = {"launches": 0, "items": 0, "admitted": 0, "finished": 0, "max_active": 0,
                       "max_used_bytes": 0}
@@ -292,7 +293,16 @@ class G2Server:
             raise ValueError("frames must be a (T, H, W) stack")
         T, H, W = (int(x) for x in fr.shape)
         qm = None if req.qmask is None else np.ascontiguousarray(req.qmask, dtype=np.int32)
-        digest = hashlib.blake2b(qm.tobytes() if qm is not None else b"all", digest_size=16).hexdigest()
+        # the same q-mask object is usually submitted again: hash it once
+        ident = (id(req.qmask), H, W)
+        cached = self._digest_cache.get(ident)
+        if cached is not None and cached[0] is req.qmask:
+            digest = cached[1]
+        else:
+            digest = hashlib.blake2b(qm.tobytes() if qm is not None else b"all", digest_size=16).hexdigest()
+            if len(self._digest_cache) > 256:
+                self._digest_cache.clear()
+            self._digest_cache[ident] = (req.qmask, digest)
         sf = req.scale_factor
         key = (H, W, digest, None if sf is None else repr(sf))
         if key not in self._params_cache:
@@ -314,14 +324,15 @@ class G2Server:
                     bc._set_scale_factor(sf)
             if len(self._params_cache) > 64:
                 self._params_cache.clear()
-            self._params_cache[key] = (bc.qmask, bc.n_bins, bc._scale_array())
-        qmask, n_bins, scale = self._params_cache[key]
-        return (H, W), T, qmask, n_bins, scale
+            self._params_cache[key] = (bc.qmask, bc.n_bins, bc._scale_array(), "%s:%s" % ((H, W), digest))
+        qmask, n_bins, scale, qd = self._params_cache[key]
+        return (H, W), T, qmask, n_bins, scale, qd
 
     def _estimate(self, job):
         """Bytes of the budget a job needs at its peak: frames copied to the
         device plus the widest packed operand its counts may need."""
-        cols = device_layout(job.qmask, job.n_bins, MODE_FP16, self.dev).packed_cols if job.n_bins else 0
+        cols = (device_layout(job.qmask, job.n_bins, MODE_FP16, self.dev, job.qdigest).packed_cols
+                if job.n_bins else 0)
         frames = job.T * job.shape[0] * job.shape[1] * job.elem_bytes if job.from_host else 0
         return frames + (job.T + 1) * cols * (2 if job.elem_bytes == 1 else 4)
 
@@ -329,12 +340,13 @@ class G2Server:
         """Server-side job of a request (built once, kept on the request)."""
         torch = _torch()
         if getattr(req, "_job", None) is None:
-            shape, T, qmask, n_bins, scale = self._params(req)
+            shape, T, qmask, n_bins, scale, qd = self._params(req)
             fr = req.frames
             from_host = not (isinstance(fr, torch.Tensor) and fr.is_cuda)
             dt = fr.dtype if isinstance(fr, torch.Tensor) else np.asarray(fr).dtype
             elem = 1 if dt in (torch.uint8, np.uint8) else 2     # other integer types become u8 or u16
             job = _Job(req, shape, T, qmask, n_bins, scale, elem, from_host)
+            job.qdigest = qd if req.qmask is not None else None
             req._job = (job, self._estimate(job))
         return req._job
 
@@ -403,7 +415,7 @@ class G2Server:
                 frames_dev = frames_to_device(fr, self.dev)      # validates, converts, or uses in place
             job.frames_dev = frames_dev
             job.engine = DenseEngine(job.shape, job.T, job.qmask, job.n_bins, job.scale, device=self.dev,
-                                     method=self.method, numer=numer, sums=sums)
+                                     method=self.method, numer=numer, sums=sums, qmask_digest=job.qdigest)
         req.frames = None                           # the server keeps no reference to the input
         if job.n_bins == 0:
             self._promote(job, np.empty(0, dtype=_lib.ITEM_DTYPE))

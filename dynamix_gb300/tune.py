@@ -1,13 +1,16 @@
 """Autotuner of the dense step's launch shapes.
 
 The tensor-core Gram's tile order and the chunked copy/pack/Gram pipeline have
-two free parameters that change speed but never results:
+free parameters that change speed but never results:
 
 * ``super_rows`` -- side, in frames, of the square super-tiles the 128 x 256
   tiles are grouped in (concurrent CTAs share those frames in L2);
 * ``pipe_chunks`` -- number of frame chunks the step is split into (more
   chunks overlap more of the copy and the packing with the Gram, fewer keep
-  each grouped launch long).
+  each grouped launch long);
+* ``kslab`` -- cap on the K columns of one tile item (0: none); narrower
+  slabs keep the rows the concurrent tiles read inside L2 at the price of
+  more epilogues.
 
 :func:`tune_dense` times every candidate pair on the caller's own stack and
 keeps the fastest for the key ``(nframes, pixels per bin)``; engines built
@@ -23,7 +26,7 @@ import threading
 
 import numpy as np
 
-DEFAULT_CANDIDATES = [(sr, pc) for sr in (1024, 2048, 4096) for pc in (4, 8, 12)]
+DEFAULT_CANDIDATES = [(sr, pc, ks) for sr in (2048, 4096) for pc in (6, 8) for ks in (0, 8192, 16384)]
 
 _lock = threading.Lock()
 _cache = {}
@@ -73,22 +76,29 @@ def store(key, value, path=None):
 
 def apply_cached(engine, path=None):
     """Set an engine's launch shapes from an earlier tuning of its key."""
+    with _lock:
+        _load(_cache_path(path))
+        if not _cache:
+            return None                  # nothing tuned in this process: skip the key
     v = lookup(key_of(engine.T, engine.qmask, engine.n_bins), path)
     if v is not None:
         engine.super_rows, engine.pipe_chunks = int(v[0]), int(v[1])
+        engine.kslab = int(v[2]) if len(v) > 2 else 0
     return v
 
 
 def tune_dense(correlator, frames, candidates=None, repeats=3, path=None):
     """Time ``correlate_device(frames)`` for every ``(super_rows,
-    pipe_chunks)`` candidate (CUDA events, after one warm-up call each), keep
-    the fastest for this stack's key and return ``(best, {candidate: ms})``.
-    ``frames`` must stay the same stack for all candidates."""
+    pipe_chunks[, kslab])`` candidate (CUDA events, after one warm-up call
+    each), keep the fastest for this stack's key and return
+    ``(best, {candidate: ms})``.  ``frames`` must stay the same stack for all
+    candidates."""
     import torch
     eng = correlator.engine
     times = {}
-    for sr, pc in (candidates or DEFAULT_CANDIDATES):
-        eng.super_rows, eng.pipe_chunks = int(sr), int(pc)
+    for cand in (candidates or DEFAULT_CANDIDATES):
+        cand = tuple(int(x) for x in cand) + ((0,) if len(cand) == 2 else ())
+        eng.super_rows, eng.pipe_chunks, eng.kslab = cand
         correlator.correlate_device(frames)
         stream = torch.cuda.current_stream(eng.dev)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -98,9 +108,9 @@ def tune_dense(correlator, frames, candidates=None, repeats=3, path=None):
             correlator.correlate_device(frames)
         e1.record(stream)
         e1.synchronize()
-        times[(int(sr), int(pc))] = e0.elapsed_time(e1) / repeats
+        times[cand] = e0.elapsed_time(e1) / repeats
     eng.check_error()
     best = min(times, key=times.get)
-    eng.super_rows, eng.pipe_chunks = best
+    eng.super_rows, eng.pipe_chunks, eng.kslab = best
     store(key_of(eng.T, eng.qmask, eng.n_bins), best, path)
     return best, times

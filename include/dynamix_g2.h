@@ -232,9 +232,12 @@ int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices
 
 /* Sub-blocked variants with packed event words (frames < 2^16, image rows up
  * to 29,000 pixels): the frames are cut into sub-blocks of 1024.
- * g2_csr_count_blocked writes sb_counts_dev[sb * H*W + p] (uint16, the
- * elements of pixel p in sub-block sb; ceil(nframes / 1024) * H*W entries)
- * and adds each pixel's total to counts_dev (caller zeroes).
+ * g2_csr_count_blocked writes row_bounds_dev[r * nframes + t] (uint32, the
+ * absolute index of row r's first element in frame t, r = 0..H; (H+1) *
+ * nframes entries, read again by the scatter), sb_counts_dev[sb * H*W + p]
+ * (uint16, the elements of pixel p in sub-block sb; ceil(nframes / 1024) *
+ * H*W entries) and adds each pixel's total to counts_dev (caller zeroes);
+ * fewer than 2^32 elements.
  * g2_csr_scatter_blocked writes each element as one word (t << 16) | v into
  * ev_words_dev[ev_offsets[p] ..) (ev_offsets: exclusive scan of the totals),
  * ordered by 32-frame window (t >> 5) and in any order inside a window;
@@ -246,12 +249,12 @@ int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices
  * width > 29,000. */
 int g2_csr_count_blocked(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
                          int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
-                         uint32_t* counts_dev, uint16_t* sb_counts_dev, int32_t* err_dev, void* stream);
+                         uint32_t* row_bounds_dev, uint32_t* counts_dev, uint16_t* sb_counts_dev, int32_t* err_dev,
+                         void* stream);
 int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
-                           const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
-                           int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
-                           const uint16_t* sb_counts_dev, uint32_t* ev_words_dev, int32_t* err_dev,
-                           void* stream);
+                           const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem, int32_t nframes,
+                           int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
+                           const uint16_t* sb_counts_dev, uint32_t* ev_words_dev, int32_t* err_dev, void* stream);
 int g2_events_sort_windows(uint32_t* ev_words_dev, const uint32_t* ev_offsets_dev, int64_t npix, void* stream);
 int g2_events_unpack(const uint32_t* ev_words_dev, int64_t n_events, int32_t elem_bytes, int32_t* ev_times_dev,
                      void* ev_data_dev, void* stream);

@@ -282,13 +282,16 @@ def test_autotuner_keeps_results_exact(built_lib, cuda_device):
     qm = annular_qmask(shape, 4, 2.0, 26.0)
     c = MatMulCorrelator(shape, T, qmask=qm)
     d = torch.from_numpy(fr).to(cuda_device)
-    best, times = tune.tune_dense(c, d, candidates=[(1024, 2), (2048, 4), (4096, 8)], repeats=1)
+    best, times = tune.tune_dense(c, d, candidates=[(1024, 2), (2048, 4, 256), (4096, 8, 512)], repeats=1)
     assert best in times and len(times) == 3
-    assert (c.engine.super_rows, c.engine.pipe_chunks) == best
+    assert (c.engine.super_rows, c.engine.pipe_chunks, c.engine.kslab) == best
     g = c.correlate(d)
     assert_exact(c, o.g2_exact(fr, qm), g)
+    for cand in times:                                   # every candidate gives the same exact sums
+        c.engine.super_rows, c.engine.pipe_chunks, c.engine.kslab = cand
+        assert_exact(c, o.g2_exact(fr, qm), c.correlate(d))
     c2 = MatMulCorrelator(shape, T, qmask=qm)            # same key: the choice is reused
-    assert (c2.engine.super_rows, c2.engine.pipe_chunks) == best
+    assert (c2.engine.super_rows, c2.engine.pipe_chunks, c2.engine.kslab) == best
 
 
 @pytest.mark.parametrize("bright", [False, True])

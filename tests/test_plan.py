@@ -219,3 +219,20 @@ def test_many_narrow_bins_share_a_chunk(mode):
         fr = fr * 300
     if mode != plan.MODE_E4M3:
         emulate_pack(fr, L)
+
+
+def test_kslab_caps_item_k_and_keeps_the_sums():
+    """A K-slab cap splits every Gram into pieces of at most that many columns
+    whose item sums still reproduce the oracle."""
+    z = golden("dense_small_u8")
+    fr, qm = z["frames"], z["qmask"]
+    T = fr.shape[0]
+    nb = int(qm.max())
+    L = plan.PackLayout(qm, nb, plan.MODE_FP16)
+    packed, emax = emulate_pack(fr, L)
+    grams = plan.chunk_grams(L, emax, kslab=128)
+    assert all(g[4] <= 128 for g in grams)
+    assert len(grams) > len(plan.chunk_grams(L, emax))
+    items = plan.gram_items(T, grams, kind="tc")
+    N = run_items(packed, items, nb, T, TC_BM, TC_BN)
+    assert np.array_equal(N, o.g2_exact(fr, qm)["numerator"])
