@@ -347,9 +347,12 @@ __global__ void __launch_bounds__(256)
         bad = true;
         continue;
       }
+      int64_t prev = -1;
 #pragma unroll 4
       for (int64_t k = s; k < e; ++k) {
         const int64_t col = static_cast<int64_t>(indices[k]);
+        bad |= col <= prev;  // repeated or descending column (sorted CSR expected)
+        prev = col;
         if (col < 0 || col >= W) {
           bad = true;
           continue;
@@ -405,52 +408,53 @@ __global__ void __launch_bounds__(SB_PER_CTA * 32)
   __syncwarp();
   const uint32_t n_total = ev_off[npix];
   const int64_t sb_end = sb0 + SUBBLOCK < T ? sb0 + SUBBLOCK : T;
+  // per batch of 32 frames, the lanes' segments (lane = frame) are walked as
+  // one flattened list, lane x taking element x: consecutive lanes read
+  // consecutive elements of a segment instead of 32 segments at once
+  uint32_t* pre = sm + static_cast<int64_t>(blockDim.x >> 5) * W + warp * 66;  // [33] exclusive prefix
+  uint32_t* beg = pre + 33;                                                    // [32] segment starts
   bool bad = false;
   for (int64_t t0 = sb0; t0 < sb_end; t0 += 32) {
     const int64_t t = t0 + lane;
-    if (t >= sb_end) continue;
-    const int64_t s = rb[static_cast<int64_t>(r) * T + t];
-    const int64_t e = rb[static_cast<int64_t>(r + 1) * T + t];
-    if (e < s || e > n_elem) {
-      bad = true;
-      continue;
-    }
-    const uint32_t tw = static_cast<uint32_t>(t) << 16;
-    int64_t prev = -1;
-    // four elements at a time without branches between them, so their loads,
-    // their shared-memory slot atomics and their stores overlap
-    for (int64_t k0 = s; k0 < e; k0 += 4) {
-      int64_t c[4];
-      uint32_t v[4];
-      bool in[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int64_t k = k0 + j;
-        in[j] = k < e;
-        c[j] = in[j] ? static_cast<int64_t>(indices[k]) : 0;
-        v[j] = in[j] ? static_cast<uint32_t>(data[k]) : 0u;
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (in[j]) {
-          bad |= c[j] <= prev || c[j] >= W;  // repeated, descending or out-of-range column
-          prev = c[j];
-          in[j] = c[j] >= 0 && c[j] < W;
-        }
-      }
-      uint32_t slot[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) slot[j] = in[j] ? atomicAdd(&cur[c[j]], 1u) : 0u;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (in[j]) {
-          if (slot[j] < n_total)
-            ev_words[slot[j]] = tw | v[j];
-          else
-            bad = true;
-        }
+    int64_t s = 0, e = 0;
+    if (t < sb_end) {
+      s = rb[static_cast<int64_t>(r) * T + t];
+      e = rb[static_cast<int64_t>(r + 1) * T + t];
+      if (e < s || e > n_elem) {
+        bad = true;
+        s = e = 0;
       }
     }
+    const uint32_t len = static_cast<uint32_t>(e - s);
+    uint32_t incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    pre[lane] = incl - len;
+    if (lane == 31) pre[32] = total;
+    beg[lane] = static_cast<uint32_t>(s);
+    __syncwarp();
+    for (uint32_t x = lane; x < total; x += 32) {
+      int f = 0;  // the last frame whose segment starts at or before x
+#pragma unroll
+      for (int step = 16; step; step >>= 1)
+        if (pre[f + step] <= x) f += step;
+      const int64_t k = static_cast<int64_t>(beg[f]) + (x - pre[f]);
+      const int64_t c = static_cast<int64_t>(indices[k]);
+      if (c < 0 || c >= W) {
+        bad = true;
+        continue;
+      }
+      const uint32_t slot = atomicAdd(&cur[c], 1u);
+      if (slot < n_total)
+        ev_words[slot] = (static_cast<uint32_t>(t0 + f) << 16) | static_cast<uint32_t>(data[k]);
+      else
+        bad = true;
+    }
+    __syncwarp();  // pre/beg are rewritten by the next batch
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
@@ -767,9 +771,9 @@ extern "C" int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, 
     return G2_ERR_ARG;
   if (nframes > 65536 || width > csr::ROW_MAX_W || n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
   // warps (sub-blocks) per CTA: up to 8, each holding one row of cursors
-  int warps = static_cast<int>((227 * 1024) / (static_cast<int64_t>(width) * 4));
+  int warps = static_cast<int>((227 * 1024) / (static_cast<int64_t>(width) * 4 + 66 * 4));
   warps = warps < 1 ? 1 : (warps > csr::SB_PER_CTA ? csr::SB_PER_CTA : warps);
-  const int64_t smem = static_cast<int64_t>(warps) * width * 4;
+  const int64_t smem = static_cast<int64_t>(warps) * (width + 66) * 4;
   const int64_t n_sb = (static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK;
   const dim3 grid(static_cast<unsigned>((n_sb + warps - 1) / warps), static_cast<unsigned>(height));
   cudaStream_t st = as_stream(stream);

@@ -37,7 +37,9 @@ __global__ void __launch_bounds__(THR)
   const int64_t tau0 = static_cast<int64_t>(blockIdx.x) * LAGS;
   const long long* row = S + r * T;
   unsigned long long acc[LPT] = {0, 0, 0, 0};
-  for (int64_t t0 = 0; t0 < T - tau0; t0 += WIN) {
+  // split z of gridDim.z takes every gridDim.z-th window of frames
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.z) * WIN; t0 < T - tau0;
+       t0 += static_cast<int64_t>(gridDim.z) * WIN) {
     bool wide = false;
     for (int i = threadIdx.x; i < WIN; i += THR) {
       const int64_t t = t0 + i;
@@ -76,8 +78,30 @@ __global__ void __launch_bounds__(THR)
 #pragma unroll
   for (int k = 0; k < LPT; ++k) {
     const int64_t tau = tau0 + threadIdx.x + k * THR;
-    if (tau < T) D[r * T + tau] = static_cast<long long>(acc[k]);
+    if (tau < T) {
+      if (gridDim.z == 1)
+        D[r * T + tau] = static_cast<long long>(acc[k]);
+      else if (acc[k])
+        atomicAdd(reinterpret_cast<unsigned long long*>(&D[r * T + tau]), acc[k]);  // D zeroed by the host
+    }
   }
+}
+
+// Launch G3 with enough blocks to fill the GPU: the frame windows are split
+// over gridDim.z and the partial sums added atomically (mod 2^64, exact).
+inline int launch_denominator(const long long* S, int32_t n_rows, int64_t T, long long* D, cudaStream_t st) {
+  const int64_t gx = (T + LAGS - 1) / LAGS;
+  if (gx > 0x7fffffff) return G2_ERR_TOO_LARGE;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  const int64_t windows = (T + WIN - 1) / WIN;
+  int64_t z = (4ll * sms + gx * n_rows - 1) / (gx * n_rows);
+  z = z < 1 ? 1 : (z > windows ? windows : (z > 32 ? 32 : z));
+  if (z > 1 && cudaMemsetAsync(D, 0, static_cast<size_t>(n_rows) * T * sizeof(long long), st) != cudaSuccess)
+    return G2_ERR_CUDA;
+  dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(n_rows), static_cast<unsigned>(z));
+  denom_kernel<<<grid, THR, 0, st>>>(S, T, D);
+  return launch_status();
 }
 
 __global__ void finalize_kernel(const long long* __restrict__ N, const long long* __restrict__ D,
@@ -137,12 +161,8 @@ extern "C" int g2_denominator(const int64_t* sums_dev, int32_t n_rows, int64_t n
   if (!sums_dev || !denom_dev || n_rows < 0 || nframes <= 0) return G2_ERR_ARG;
   if (n_rows == 0) return G2_OK;
   if (n_rows > 65535) return G2_ERR_TOO_LARGE;
-  const int64_t gx = (nframes + norm::LAGS - 1) / norm::LAGS;
-  if (gx > 0x7fffffff) return G2_ERR_TOO_LARGE;
-  dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(n_rows));
-  norm::denom_kernel<<<grid, norm::THR, 0, as_stream(stream)>>>(reinterpret_cast<const long long*>(sums_dev),
-                                                                 nframes, reinterpret_cast<long long*>(denom_dev));
-  return launch_status();
+  return norm::launch_denominator(reinterpret_cast<const long long*>(sums_dev), n_rows, nframes,
+                                  reinterpret_cast<long long*>(denom_dev), as_stream(stream));
 }
 
 extern "C" int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, const double* scale_dev,
