@@ -65,10 +65,8 @@ def parse():
 
 
 def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from dynamix_gb300.replicas import rank_info
+    return rank_info()
 
 
 def measured_peaks():
@@ -231,11 +229,8 @@ def run_ours(args):
             dist.barrier()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        from dynamix_gb300.replicas import max_over_ranks as mx
+        return mx(x, dist, dev)
 
     # ---- device-resident steps
     for _ in range(max(args.warmup, 3)):
@@ -260,7 +255,8 @@ def run_ours(args):
     clocks = sampler.stop()
     eng.check_error()
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    value = world * T / (ms / 1e3)
+    from dynamix_gb300.replicas import whole_job_rate
+    value = whole_job_rate(T, ms, world)
     info = dict(eng.last)
     chunks = int(info.get("pipeline_chunks", 1))
     # pack + one Gram per frame chunk, denominator, finalize
@@ -454,11 +450,8 @@ def run_sparse(args):
             dist.barrier()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        from dynamix_gb300.replicas import max_over_ranks as mx
+        return mx(x, dist, dev)
 
     for _ in range(max(args.warmup, 3)):
         corr.correlate_device(*inputs)
