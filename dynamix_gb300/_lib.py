@@ -64,9 +64,9 @@ SIGNATURES = {
     "g2_csr_count": (C.c_int, [_p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p]),
     "g2_exclusive_scan_u32": (C.c_int, [_p, _i64, _p, _p, _i64, _p]),
     "g2_csr_scatter": (C.c_int, [_p, _i32, _p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),
-    "g2_csr_count_blocked": (C.c_int, [_p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p]),
-    "g2_csr_scatter_blocked": (C.c_int, [_p, _i32, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p]),
-    "g2_events_sort_windows": (C.c_int, [_p, _p, _i64, _p]),
+    "g2_csr_count_blocked": (C.c_int, [_p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),
+    "g2_csr_stage_blocked": (C.c_int, [_p, _i32, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),
+    "g2_csr_gather_blocked": (C.c_int, [_p, _p, _p, _i32, _i64, _i64, _p, _i32, _p, _p, _p]),
     "g2_events_unpack": (C.c_int, [_p, _i64, _i32, _p, _p, _p]),
     "g2_denominator": (C.c_int, [_p, _i32, _i64, _p, _p]),
     "g2_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),

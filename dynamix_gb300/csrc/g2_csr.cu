@@ -229,61 +229,20 @@ __global__ void __launch_bounds__(256)
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
 
-// Frame order inside each pixel's list of packed words that is already ordered
-// by 32-frame window (t >> 5): a warp per pixel takes 32 words at a time and
-// ranks each word inside its window group by shuffles; a group that may run on
-// past the 32 words waits for the next round.
-__global__ void __launch_bounds__(256)
-    sort_windows_kernel(uint32_t* __restrict__ words, const uint32_t* __restrict__ ev_off, int64_t npix) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
-  for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x >> 5) + (threadIdx.x >> 5); p < npix;
-       p += warps) {
-    const int64_t s = ev_off[p];
-    const int64_t n = static_cast<int64_t>(ev_off[p + 1]) - s;
-    int64_t c0 = 0;
-    while (c0 + 1 < n) {
-      const bool has = c0 + lane < n;
-      const uint32_t w = has ? words[s + c0 + lane] : 0xFFFFFFFFu;
-      const uint32_t win = has ? (w >> 21) : 0xFFFFFFFFu;          // (t >> 5)
-      const uint32_t prev_win = __shfl_up_sync(0xffffffffu, win, 1);
-      const uint32_t heads = __ballot_sync(0xffffffffu, has && (lane == 0 || win != prev_win));
-      const int avail = static_cast<int>(n - c0 < 32 ? n - c0 : 32);
-      int commit = avail;
-      if (c0 + 32 < n) {                                            // the last group may continue
-        const int last_head = 31 - __clz(heads);
-        commit = last_head > 0 ? last_head : 32;
-      }
-      const uint32_t le = heads & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
-      const int start = le ? 31 - __clz(le) : 0;
-      const uint32_t gt = heads & ~(lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
-      const int gend = min(gt ? __ffs(gt) - 1 : 32, commit);
-      const uint32_t t = w >> 16;
-      int rank = 0;
-      for (int j = 0; j < 32; ++j) {
-        const uint32_t tj = __shfl_sync(0xffffffffu, t, j);
-        rank += (j >= start && j < gend && (tj < t || (tj == t && j < lane))) ? 1 : 0;
-      }
-      __syncwarp();
-      if (lane < commit) words[s + c0 + start + rank] = w;
-      __syncwarp();
-      c0 += commit;
-    }
-  }
-}
-
-// Sub-blocked transposition (frames < 2^16): the frames are cut into
-// sub-blocks of SUBBLOCK frames.  The count pass keeps, per image row (one
-// warp, lanes = 32 consecutive frames), the per-pixel counts of each
-// sub-block (uint16) instead of one total.  The scatter runs one CTA per (8
-// consecutive sub-blocks, image row), a warp per sub-block with its own slot
-// cursors (the pixel's offset plus the counts of the earlier sub-blocks), so
-// the CTA writes, for every pixel of its row, one contiguous stretch of that
-// pixel's list (8 x 1024 frames of events) while it runs: the sectors it
-// fills are complete before they leave L2.  Events come out ordered by
-// 32-frame window within a pixel, in any order inside a window.
+// Sub-blocked transposition (frames < 2^16, fewer than 2^32 elements): the
+// frames are cut into sub-blocks of SUBBLOCK frames.  The count pass keeps,
+// per image row (one warp, lanes = 32 consecutive frames), the per-pixel
+// counts of each sub-block (uint16) and the row's total per sub-block.  The
+// stage pass (one CTA per sub-block and row) writes the row's elements of the
+// sub-block into one contiguous stretch of a staging area, pixel by pixel; the
+// gather pass copies every pixel's runs, sub-block after sub-block, into the
+// pixel's list.  Each pass writes inside regions that stay in L2 until they
+// are complete (a single-pass scatter, whose every warp holds one partly
+// written sector per pixel of its row for 1024 frames, moves several times
+// its bytes through DRAM).
 constexpr int SUBBLOCK = 1024;
-constexpr int SB_PER_CTA = 8;
+constexpr int TILE_P = 64;  // pixels of one gather tile
+constexpr int UNROLL = 4;   // elements per lane with loads in flight together
 
 // Row bounds transposed to row-major: rb[r * T + t] = offsets[t] + indptr[t][r]
 // (absolute element index of the start of row r in frame t; r = H is the
@@ -322,51 +281,98 @@ __global__ void __launch_bounds__(256)
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
 
+// Count pass: one CTA per (sub-block, image row), the row's per-pixel counters
+// in shared memory.  Warps take 32-frame batches and walk each batch's
+// segments as one flattened list (lane x takes element x, so consecutive
+// lanes read consecutive indices); a column not above its predecessor in the
+// same segment is reported (sorted CSR expected).
 template <typename Ti>
 __global__ void __launch_bounds__(256)
     row_count_blocked_kernel(const Ti* __restrict__ indices, const uint32_t* __restrict__ rb, int64_t n_elem,
-                             int32_t T, int32_t H, int32_t W, int rows_per_cta, uint16_t* __restrict__ sb_counts,
-                             int32_t* __restrict__ err) {
+                             int32_t T, int32_t H, int32_t W, uint16_t* __restrict__ sb_counts,
+                             uint32_t* __restrict__ row_totals, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
+  __shared__ uint32_t s_tot[8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * rows_per_cta + warp;
-  if (warp >= rows_per_cta || r >= H) return;  // warp-uniform; no block barrier below
-  uint32_t* cnt = sm + static_cast<int64_t>(warp) * W;
-  for (int i = lane; i < W; i += 32) cnt[i] = 0;
-  __syncwarp();
-  const int64_t npix = static_cast<int64_t>(H) * W;
+  const int64_t sb = blockIdx.x;
+  const int r = blockIdx.y;
+  const int64_t sb0 = sb * SUBBLOCK;
+  const int64_t sb_end = sb0 + SUBBLOCK < T ? sb0 + SUBBLOCK : T;
+  uint32_t* cnt = sm;                  // [W] elements of each pixel of the row
+  uint32_t* pre = sm + W + warp * 66;  // [33] exclusive prefix of a batch's segments
+  uint32_t* beg = pre + 33;            // [32] segment starts
+  for (int i = threadIdx.x; i < W; i += 256) cnt[i] = 0;
+  __syncthreads();
   bool bad = false;
-  for (int64_t sb0 = 0; sb0 < T; sb0 += SUBBLOCK) {
-    const int64_t sb_end = sb0 + SUBBLOCK < T ? sb0 + SUBBLOCK : T;
-    for (int64_t t0 = sb0; t0 < sb_end; t0 += 32) {
-      const int64_t t = t0 + lane;
-      if (t >= sb_end) continue;
-      const int64_t s = rb[static_cast<int64_t>(r) * T + t];
-      const int64_t e = rb[static_cast<int64_t>(r + 1) * T + t];
-      if (e < s || e > n_elem) {
+  for (int64_t t0 = sb0 + warp * 32; t0 < sb_end; t0 += 8 * 32) {
+    const int64_t t = t0 + lane;
+    int64_t a = 0, b = 0;
+    if (t < sb_end) {
+      a = rb[static_cast<int64_t>(r) * T + t];
+      b = rb[static_cast<int64_t>(r + 1) * T + t];
+      if (b < a || b > n_elem) {
         bad = true;
-        continue;
+        a = b = 0;
       }
-      int64_t prev = -1;
-#pragma unroll 4
-      for (int64_t k = s; k < e; ++k) {
-        const int64_t col = static_cast<int64_t>(indices[k]);
-        bad |= col <= prev;  // repeated or descending column (sorted CSR expected)
-        prev = col;
-        if (col < 0 || col >= W) {
+    }
+    const uint32_t len = static_cast<uint32_t>(b - a);
+    uint32_t inc = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    pre[lane] = inc - len;
+    if (lane == 31) pre[32] = total;
+    beg[lane] = static_cast<uint32_t>(a);
+    __syncwarp();
+    for (uint32_t x0 = 0; x0 < total; x0 += 32 * UNROLL) {
+      int64_t c[UNROLL], prev[UNROLL];
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        const uint32_t x = x0 + u * 32 + lane;
+        c[u] = -1;
+        prev[u] = -2;
+        if (x < total) {
+          int f = 0;  // the last frame whose segment starts at or before x
+#pragma unroll
+          for (int step = 16; step; step >>= 1)
+            if (pre[f + step] <= x) f += step;
+          const int64_t k = static_cast<int64_t>(beg[f]) + (x - pre[f]);
+          c[u] = static_cast<int64_t>(indices[k]);
+          if (x > pre[f]) prev[u] = static_cast<int64_t>(indices[k - 1]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        if (x0 + u * 32 + lane >= total) continue;
+        bad |= c[u] <= prev[u];  // repeated or descending column
+        if (c[u] < 0 || c[u] >= W) {
           bad = true;
           continue;
         }
-        atomicAdd(&cnt[col], 1u);
+        atomicAdd(&cnt[c[u]], 1u);
       }
     }
-    __syncwarp();
-    uint16_t* out = sb_counts + (sb0 / SUBBLOCK) * npix + static_cast<int64_t>(r) * W;
-    for (int i = lane; i < W; i += 32) {
-      out[i] = static_cast<uint16_t>(cnt[i]);  // <= SUBBLOCK frames, one element each
-      cnt[i] = 0;
-    }
-    __syncwarp();
+    __syncwarp();  // pre/beg are rewritten by the next batch
+  }
+  __syncthreads();
+  uint16_t* out = sb_counts + sb * (static_cast<int64_t>(H) * W) + static_cast<int64_t>(r) * W;
+  uint32_t tot = 0;
+  for (int i = threadIdx.x; i < W; i += 256) {
+    const uint16_t v = static_cast<uint16_t>(cnt[i]);  // <= SUBBLOCK frames, one element each
+    out[i] = v;
+    tot += v;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if (lane == 0) s_tot[warp] = tot;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t sum = 0;
+    for (int w = 0; w < 8; ++w) sum += s_tot[w];
+    row_totals[sb * H + r] = sum;
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
@@ -383,78 +389,277 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Stage pass: one CTA per (sub-block, image row).  The row's elements of the
+// sub-block go to a staging area ordered sub-block by sub-block, row by row and
+// pixel by pixel; within a sub-block the staging area is therefore the
+// exclusive scan of sb_counts in pixel order.  The CTA assembles its region in
+// shared memory when it fits in buf_words and writes it out with coalesced
+// stores (no partly written sector leaves the SM); a larger region is written
+// in place.  Warps take 32-frame batches and walk each batch's segments as one
+// flattened list (lane x takes element x).  The start of every TILE_P-pixel
+// tile of the sub-block goes to tile_pos[sb * n_tiles + tile] for the gather.
 template <typename Tv, typename Ti>
-__global__ void __launch_bounds__(SB_PER_CTA * 32)
-    row_scatter_blocked_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices,
-                               const uint32_t* __restrict__ rb, int64_t n_elem, int32_t T, int32_t H, int32_t W,
-                               const uint32_t* __restrict__ ev_off, const uint16_t* __restrict__ sb_counts,
-                               uint32_t* __restrict__ ev_words, int32_t* __restrict__ err) {
+__global__ void __launch_bounds__(256)
+    row_stage_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices, const uint32_t* __restrict__ rb,
+                     int64_t n_elem, int32_t T, int32_t H, int32_t W, const uint16_t* __restrict__ sb_counts,
+                     const uint32_t* __restrict__ row_base, int64_t n_tiles, uint32_t* __restrict__ tile_pos,
+                     int buf_words, uint32_t* __restrict__ stage, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
+  __shared__ uint32_t s_tot[8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sb = blockIdx.x;
   const int r = blockIdx.y;
-  const int64_t sb = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
-  const int64_t sb0 = sb * SUBBLOCK;
-  if (r >= H || sb0 >= T) return;  // warp-uniform; no block barrier below
   const int64_t npix = static_cast<int64_t>(H) * W;
-  uint32_t* cur = sm + static_cast<int64_t>(warp) * W;
-  const int64_t row0 = static_cast<int64_t>(r) * W;
-  // the sub-block's first slot of each pixel: its offset plus the earlier sub-blocks
-  for (int i = lane; i < W; i += 32) {
-    uint32_t c = ev_off[row0 + i];
-#pragma unroll 8
-    for (int64_t b = 0; b < sb; ++b) c += sb_counts[b * npix + row0 + i];
-    cur[i] = c;
-  }
-  __syncwarp();
-  const uint32_t n_total = ev_off[npix];
+  const int64_t sb0 = sb * SUBBLOCK;
   const int64_t sb_end = sb0 + SUBBLOCK < T ? sb0 + SUBBLOCK : T;
-  // per batch of 32 frames, the lanes' segments (lane = frame) are walked as
-  // one flattened list, lane x taking element x: consecutive lanes read
-  // consecutive elements of a segment instead of 32 segments at once
-  uint32_t* pre = sm + static_cast<int64_t>(blockDim.x >> 5) * W + warp * 66;  // [33] exclusive prefix
-  uint32_t* beg = pre + 33;                                                    // [32] segment starts
-  bool bad = false;
-  for (int64_t t0 = sb0; t0 < sb_end; t0 += 32) {
+  uint32_t* cur = sm;                  // [W] next slot of each pixel, relative to the region
+  uint32_t* pre = sm + W + warp * 66;  // [33] exclusive prefix of a batch's segments
+  uint32_t* beg = pre + 33;            // [32] segment starts
+  uint32_t* buf = sm + W + 8 * 66;     // [buf_words] the region
+  const uint16_t* cnt = sb_counts + sb * npix + static_cast<int64_t>(r) * W;
+  // exclusive scan of the row's counts, each thread over a contiguous span
+  const int per = (W + 255) / 256;
+  const int i0 = threadIdx.x * per, i1 = min(W, i0 + per);
+  uint32_t own = 0;
+  for (int i = i0; i < i1; ++i) own += cnt[i];
+  uint32_t incl = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_tot[warp] = incl;
+  __syncthreads();
+  uint32_t run = incl - own, total = 0;
+  for (int w = 0; w < 8; ++w) {
+    run += w < warp ? s_tot[w] : 0u;
+    total += s_tot[w];
+  }
+  const int64_t base = row_base[sb * H + r];
+  const int64_t pix0 = static_cast<int64_t>(r) * W;
+  for (int i = i0; i < i1; ++i) {
+    cur[i] = run;
+    if ((pix0 + i) % TILE_P == 0) tile_pos[sb * n_tiles + (pix0 + i) / TILE_P] = static_cast<uint32_t>(base + run);
+    run += cnt[i];
+  }
+  __syncthreads();
+  const bool skip = base + total > n_elem;  // block-uniform
+  bool bad = skip;
+  const bool buffered = total <= static_cast<uint32_t>(buf_words);
+  for (int64_t t0 = sb0 + warp * 32; t0 < sb_end && !skip; t0 += 8 * 32) {
     const int64_t t = t0 + lane;
-    int64_t s = 0, e = 0;
+    int64_t a = 0, b = 0;
     if (t < sb_end) {
-      s = rb[static_cast<int64_t>(r) * T + t];
-      e = rb[static_cast<int64_t>(r + 1) * T + t];
-      if (e < s || e > n_elem) {
+      a = rb[static_cast<int64_t>(r) * T + t];
+      b = rb[static_cast<int64_t>(r + 1) * T + t];
+      if (b < a || b > n_elem) {
         bad = true;
-        s = e = 0;
+        a = b = 0;
       }
     }
-    const uint32_t len = static_cast<uint32_t>(e - s);
-    uint32_t incl = len;
+    const uint32_t len = static_cast<uint32_t>(b - a);
+    uint32_t inc = len;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
     }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    pre[lane] = incl - len;
-    if (lane == 31) pre[32] = total;
-    beg[lane] = static_cast<uint32_t>(s);
+    const uint32_t seg_total = __shfl_sync(0xffffffffu, inc, 31);
+    pre[lane] = inc - len;
+    if (lane == 31) pre[32] = seg_total;
+    beg[lane] = static_cast<uint32_t>(a);
     __syncwarp();
-    for (uint32_t x = lane; x < total; x += 32) {
-      int f = 0;  // the last frame whose segment starts at or before x
+    for (uint32_t x0 = 0; x0 < seg_total; x0 += 32 * UNROLL) {
+      // the loads of UNROLL elements are issued before their shared-memory
+      // atomics, so every lane keeps several global loads in flight
+      int64_t c[UNROLL];
+      uint32_t w[UNROLL];
 #pragma unroll
-      for (int step = 16; step; step >>= 1)
-        if (pre[f + step] <= x) f += step;
-      const int64_t k = static_cast<int64_t>(beg[f]) + (x - pre[f]);
-      const int64_t c = static_cast<int64_t>(indices[k]);
-      if (c < 0 || c >= W) {
+      for (int u = 0; u < UNROLL; ++u) {
+        const uint32_t x = x0 + u * 32 + lane;
+        c[u] = -1;
+        w[u] = 0;
+        if (x < seg_total) {
+          int f = 0;  // the last frame whose segment starts at or before x
+#pragma unroll
+          for (int step = 16; step; step >>= 1)
+            if (pre[f + step] <= x) f += step;
+          const int64_t k = static_cast<int64_t>(beg[f]) + (x - pre[f]);
+          c[u] = static_cast<int64_t>(indices[k]);
+          w[u] = (static_cast<uint32_t>(t0 + f) << 16) | static_cast<uint32_t>(data[k]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        if (x0 + u * 32 + lane >= seg_total) continue;
+        if (c[u] < 0 || c[u] >= W) {
+          bad = true;
+          continue;
+        }
+        const uint32_t slot = atomicAdd(&cur[c[u]], 1u);
+        if (slot >= total)
+          bad = true;
+        else if (buffered)
+          buf[slot] = w[u];
+        else
+          stage[base + slot] = w[u];
+      }
+    }
+    __syncwarp();  // pre/beg are rewritten by the next batch
+  }
+  if (buffered && !skip) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < total; i += 256) stage[base + i] = buf[i];
+  }
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// Gather pass: one CTA per tile of TILE_P consecutive pixels.  For every
+// sub-block the tile's runs are one contiguous chunk of the staging area
+// (starting at tile_pos); the CTA walks all chunks as one flattened list,
+// places each word at its pixel's list position in a shared-memory copy of the
+// tile's part of the event lists (when it fits in buf_words, else in place),
+// and writes that out with coalesced stores.  With `sort`, each run (one pixel,
+// one 1024-frame sub-block) is put in frame order by insertion, which gives
+// exactly the FramesCompressor layout.  Shared memory: 131 * n_sb + 1 words of
+// tables, then the buffer.
+__global__ void __launch_bounds__(256)
+    gather_tiles_kernel(const uint32_t* __restrict__ stage, const uint32_t* __restrict__ tile_pos,
+                        const uint16_t* __restrict__ sb_counts, int n_sb, int64_t npix, int64_t n_tiles,
+                        const uint32_t* __restrict__ ev_off, int64_t n_elem, int sort, int buf_words,
+                        uint32_t* __restrict__ ev_words, int32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  uint32_t* cp = sm;                       // [n_sb][TILE_P + 1] run starts within each chunk
+  uint32_t* dst = cp + n_sb * (TILE_P + 1);  // [n_sb][TILE_P] run starts within the tile's lists
+  uint32_t* cb = dst + n_sb * TILE_P;        // [n_sb + 1] chunk starts within the walk
+  uint32_t* tp = cb + n_sb + 1;              // [n_sb] chunk starts in the staging area
+  uint32_t* buf = tp + n_sb;                 // [buf_words]
+  __shared__ int s_bad;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tile = blockIdx.x;
+  const int64_t p0 = tile * TILE_P;
+  const int np = static_cast<int>(npix - p0 < TILE_P ? npix - p0 : TILE_P);
+  const int64_t base = ev_off[p0];
+  const int64_t tile_total = static_cast<int64_t>(ev_off[p0 + np]) - base;
+  if (threadIdx.x == 0) s_bad = (tile_total < 0 || base + tile_total > n_elem) ? 1 : 0;
+  for (int e = threadIdx.x; e < n_sb * TILE_P; e += 256) {
+    const int b = e / TILE_P, p = e % TILE_P;
+    cp[b * (TILE_P + 1) + p] = p < np ? sb_counts[b * npix + p0 + p] : 0u;
+  }
+  for (int b = threadIdx.x; b < n_sb; b += 256) tp[b] = tile_pos[b * n_tiles + tile];
+  __syncthreads();
+  // per sub-block: exclusive scan over the tile's pixels (a warp per sub-block)
+  for (int b = warp; b < n_sb; b += 8) {
+    uint32_t* c = cp + b * (TILE_P + 1);
+    const uint32_t a0 = c[lane], a1 = c[32 + lane];
+    uint32_t s0 = a0, s1 = a1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y0 = __shfl_up_sync(0xffffffffu, s0, o);
+      const uint32_t y1 = __shfl_up_sync(0xffffffffu, s1, o);
+      if (lane >= o) {
+        s0 += y0;
+        s1 += y1;
+      }
+    }
+    const uint32_t t0 = __shfl_sync(0xffffffffu, s0, 31);
+    __syncwarp();
+    c[lane] = s0 - a0;
+    c[32 + lane] = t0 + s1 - a1;
+    if (lane == 31) c[TILE_P] = t0 + s1;
+  }
+  __syncthreads();
+  if (threadIdx.x < TILE_P) {
+    // per pixel: where its run of each sub-block starts within the tile's lists
+    const int p = threadIdx.x;
+    if (p < np) {
+      int64_t run = static_cast<int64_t>(ev_off[p0 + p]) - base;
+      for (int b = 0; b < n_sb; ++b) {
+        dst[b * TILE_P + p] = static_cast<uint32_t>(run);
+        run += cp[b * (TILE_P + 1) + p + 1] - cp[b * (TILE_P + 1) + p];
+      }
+      if (run != static_cast<int64_t>(ev_off[p0 + p + 1]) - base) s_bad = 1;
+    } else {
+      for (int b = 0; b < n_sb; ++b) dst[b * TILE_P + p] = 0;
+    }
+  } else if (warp == 2) {
+    // chunk starts within the walk: exclusive scan of the chunk lengths
+    uint32_t carry = 0;
+    for (int b0 = 0; b0 < n_sb; b0 += 32) {
+      const int b = b0 + lane;
+      const uint32_t len = b < n_sb ? cp[b * (TILE_P + 1) + TILE_P] : 0u;
+      uint32_t s = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      if (b < n_sb) cb[b] = carry + s - len;
+      carry += __shfl_sync(0xffffffffu, s, 31);
+    }
+    if (lane == 0) cb[n_sb] = carry;
+  }
+  __syncthreads();
+  const uint32_t total = cb[n_sb];
+  if (s_bad || total != tile_total) {
+    if (threadIdx.x == 0) atomicOr(err, G2_DEVERR_BOUNDS);
+    return;  // block-uniform
+  }
+  const bool buffered = total <= static_cast<uint32_t>(buf_words);
+  uint32_t* out = buffered ? buf : ev_words + base;
+  bool bad = false;
+  for (uint32_t x0 = 0; x0 < total; x0 += 256 * UNROLL) {
+    uint32_t v[UNROLL], d[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const uint32_t x = x0 + u * 256 + threadIdx.x;
+      d[u] = 0xFFFFFFFFu;
+      v[u] = 0;
+      if (x >= total) continue;
+      int b = 0;  // the last chunk starting at or before x
+#pragma unroll
+      for (int step = 32; step; step >>= 1)
+        if (b + step < n_sb && cb[b + step] <= x) b += step;
+      const uint32_t y = x - cb[b];
+      const uint32_t* c = cp + b * (TILE_P + 1);
+      int p = 0;  // the pixel whose run holds y
+#pragma unroll
+      for (int step = 32; step; step >>= 1)
+        if (c[p + step] <= y) p += step;
+      const int64_t src = static_cast<int64_t>(tp[b]) + y;
+      const uint32_t dd = dst[b * TILE_P + p] + (y - c[p]);
+      if (src >= n_elem || dd >= total) {
         bad = true;
         continue;
       }
-      const uint32_t slot = atomicAdd(&cur[c], 1u);
-      if (slot < n_total)
-        ev_words[slot] = (static_cast<uint32_t>(t0 + f) << 16) | static_cast<uint32_t>(data[k]);
-      else
-        bad = true;
+      d[u] = dd;
+      v[u] = stage[src];
     }
-    __syncwarp();  // pre/beg are rewritten by the next batch
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u)
+      if (d[u] != 0xFFFFFFFFu) out[d[u]] = v[u];
+  }
+  if (sort) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < n_sb * TILE_P; e += 256) {
+      const int b = e / TILE_P, p = e % TILE_P;
+      if (p >= np) continue;
+      const uint32_t n = cp[b * (TILE_P + 1) + p + 1] - cp[b * (TILE_P + 1) + p];
+      uint32_t* run = out + dst[b * TILE_P + p];
+      for (uint32_t k = 1; k < n; ++k) {
+        const uint32_t w = run[k];
+        uint32_t j = k;
+        while (j > 0 && run[j - 1] > w) {
+          run[j] = run[j - 1];
+          --j;
+        }
+        run[j] = w;
+      }
+    }
+  }
+  if (buffered) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < total; i += 256) ev_words[base + i] = buf[i];
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
@@ -716,13 +921,15 @@ extern "C" int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const vo
 extern "C" int g2_csr_count_blocked(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
                                     int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height,
                                     int32_t width, uint32_t* row_bounds_dev, uint32_t* counts_dev,
-                                    uint16_t* sb_counts_dev, int32_t* err_dev, void* stream) {
+                                    uint16_t* sb_counts_dev, uint32_t* row_totals_dev, int32_t* err_dev,
+                                    void* stream) {
   using namespace g2;
-  if (!indices_dev || !indptr_dev || !offsets_dev || !row_bounds_dev || !counts_dev || !sb_counts_dev || !err_dev)
+  if (!indices_dev || !indptr_dev || !offsets_dev || !row_bounds_dev || !counts_dev || !sb_counts_dev ||
+      !row_totals_dev || !err_dev)
     return G2_ERR_ARG;
   if ((index_bytes != 4 && index_bytes != 8) || n_elem < 0 || nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
-  if (width > csr::ROW_MAX_W || n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
+  if (width > csr::ROW_MAX_W || height > 65535 || n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
   cudaStream_t st = as_stream(stream);
   const dim3 tgrid(static_cast<unsigned>((nframes + 31) / 32), static_cast<unsigned>((height + 1 + 31) / 32));
   if (index_bytes == 4)
@@ -733,19 +940,19 @@ extern "C" int g2_csr_count_blocked(const void* indices_dev, const void* indptr_
     csr::row_bounds_kernel<int64_t><<<tgrid, 256, 0, st>>>(reinterpret_cast<const int64_t*>(indptr_dev),
                                                             reinterpret_cast<const int64_t*>(offsets_dev), n_elem,
                                                             nframes, height, row_bounds_dev, err_dev);
-  const int rpc = rows_per_cta(width, 1);
-  const int64_t smem = static_cast<int64_t>(rpc) * width * 4;
-  const unsigned grid = static_cast<unsigned>((height + rpc - 1) / rpc);
+  const int64_t n_sb64 = (static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK;
+  const int64_t smem = (static_cast<int64_t>(width) + 8 * 66) * 4;
+  const dim3 grid(static_cast<unsigned>(n_sb64), static_cast<unsigned>(height));
   if (index_bytes == 4) {
     if (!allow_smem(csr::row_count_blocked_kernel<uint32_t>, smem)) return G2_ERR_CUDA;
-    csr::row_count_blocked_kernel<uint32_t><<<grid, rpc * 32, smem, st>>>(
-        reinterpret_cast<const uint32_t*>(indices_dev), row_bounds_dev, n_elem, nframes, height, width, rpc,
-        sb_counts_dev, err_dev);
+    csr::row_count_blocked_kernel<uint32_t><<<grid, 256, smem, st>>>(reinterpret_cast<const uint32_t*>(indices_dev),
+                                                                     row_bounds_dev, n_elem, nframes, height, width,
+                                                                     sb_counts_dev, row_totals_dev, err_dev);
   } else {
     if (!allow_smem(csr::row_count_blocked_kernel<int64_t>, smem)) return G2_ERR_CUDA;
-    csr::row_count_blocked_kernel<int64_t><<<grid, rpc * 32, smem, st>>>(
-        reinterpret_cast<const int64_t*>(indices_dev), row_bounds_dev, n_elem, nframes, height, width, rpc,
-        sb_counts_dev, err_dev);
+    csr::row_count_blocked_kernel<int64_t><<<grid, 256, smem, st>>>(reinterpret_cast<const int64_t*>(indices_dev),
+                                                                    row_bounds_dev, n_elem, nframes, height, width,
+                                                                    sb_counts_dev, row_totals_dev, err_dev);
   }
   const int64_t npix = static_cast<int64_t>(height) * width;
   const int n_sb = static_cast<int>((static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK);
@@ -757,51 +964,70 @@ extern "C" int g2_csr_count_blocked(const void* indices_dev, const void* indptr_
   return launch_status();
 }
 
-extern "C" int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
-                                      const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem,
-                                      int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
-                                      const uint16_t* sb_counts_dev, uint32_t* ev_words_dev, int32_t* err_dev,
-                                      void* stream) {
+namespace {
+// Words of the shared-memory buffer of a stage region or a gather tile: a
+// little above the mean (uniform data fits), between 1024 and 16384.
+int buffer_words(int64_t n_elem, int64_t units) {
+  const int64_t mean = units > 0 ? n_elem / units : n_elem;
+  const int64_t w = mean + mean / 16 + 512;
+  return static_cast<int>(w < 1024 ? 1024 : (w > 16384 ? 16384 : w));
+}
+}  // namespace
+
+extern "C" int g2_csr_stage_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                                    const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem,
+                                    int32_t nframes, int32_t height, int32_t width, const uint16_t* sb_counts_dev,
+                                    const uint32_t* row_base_dev, uint32_t* tile_pos_dev, uint32_t* stage_dev,
+                                    int32_t* err_dev, void* stream) {
   using namespace g2;
-  if (!data_dev || !indices_dev || !row_bounds_dev || !ev_offsets_dev || !sb_counts_dev || !ev_words_dev ||
-      !err_dev)
+  if (!data_dev || !indices_dev || !row_bounds_dev || !sb_counts_dev || !row_base_dev || !tile_pos_dev ||
+      !stage_dev || !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || (index_bytes != 4 && index_bytes != 8) || n_elem < 0 ||
       nframes <= 0 || height <= 0 || width <= 0)
     return G2_ERR_ARG;
-  if (nframes > 65536 || width > csr::ROW_MAX_W || n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
-  // warps (sub-blocks) per CTA: up to 8, each holding one row of cursors
-  int warps = static_cast<int>((227 * 1024) / (static_cast<int64_t>(width) * 4 + 66 * 4));
-  warps = warps < 1 ? 1 : (warps > csr::SB_PER_CTA ? csr::SB_PER_CTA : warps);
-  const int64_t smem = static_cast<int64_t>(warps) * (width + 66) * 4;
+  if (nframes > 65536 || width > csr::ROW_MAX_W || height > 65535 || n_elem >= (1ll << 32))
+    return G2_ERR_UNSUPPORTED;
   const int64_t n_sb = (static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK;
-  const dim3 grid(static_cast<unsigned>((n_sb + warps - 1) / warps), static_cast<unsigned>(height));
+  const int64_t npix = static_cast<int64_t>(height) * width;
+  const int64_t n_tiles = (npix + csr::TILE_P - 1) / csr::TILE_P;
+  const int buf = buffer_words(n_elem, n_sb * height);
+  const int64_t smem = (static_cast<int64_t>(width) + 8 * 66 + buf) * 4;
+  const dim3 grid(static_cast<unsigned>(n_sb), static_cast<unsigned>(height));
   cudaStream_t st = as_stream(stream);
-#define G2_BS(TV, TI)                                                                                           \
-  do {                                                                                                          \
-    if (!allow_smem(csr::row_scatter_blocked_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                         \
-    csr::row_scatter_blocked_kernel<TV, TI><<<grid, warps * 32, smem, st>>>(                                    \
-        reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev), row_bounds_dev, n_elem, \
-        nframes, height, width, ev_offsets_dev, sb_counts_dev, ev_words_dev, err_dev);                          \
+#define G2_ST(TV, TI)                                                                                              \
+  do {                                                                                                             \
+    if (!allow_smem(csr::row_stage_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                                      \
+    csr::row_stage_kernel<TV, TI><<<grid, 256, smem, st>>>(                                                        \
+        reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev), row_bounds_dev, n_elem,    \
+        nframes, height, width, sb_counts_dev, row_base_dev, n_tiles, tile_pos_dev, buf, stage_dev, err_dev);     \
   } while (0)
-  if (elem_bytes == 1 && index_bytes == 4) G2_BS(uint8_t, uint32_t);
-  else if (elem_bytes == 1) G2_BS(uint8_t, int64_t);
-  else if (index_bytes == 4) G2_BS(uint16_t, uint32_t);
-  else G2_BS(uint16_t, int64_t);
-#undef G2_BS
+  if (elem_bytes == 1 && index_bytes == 4) G2_ST(uint8_t, uint32_t);
+  else if (elem_bytes == 1) G2_ST(uint8_t, int64_t);
+  else if (index_bytes == 4) G2_ST(uint16_t, uint32_t);
+  else G2_ST(uint16_t, int64_t);
+#undef G2_ST
   return launch_status();
 }
 
-extern "C" int g2_events_sort_windows(uint32_t* ev_words_dev, const uint32_t* ev_offsets_dev, int64_t npix,
-                                      void* stream) {
+extern "C" int g2_csr_gather_blocked(const uint32_t* stage_dev, const uint32_t* tile_pos_dev,
+                                     const uint16_t* sb_counts_dev, int32_t nframes, int64_t npix, int64_t n_elem,
+                                     const uint32_t* ev_offsets_dev, int32_t sort, uint32_t* ev_words_dev,
+                                     int32_t* err_dev, void* stream) {
   using namespace g2;
-  if (!ev_words_dev || !ev_offsets_dev || npix <= 0) return G2_ERR_ARG;
-  const int sms = sm_count_current();
-  if (sms <= 0) return G2_ERR_CUDA;
-  int64_t blocks = (npix + 7) / 8;
-  if (blocks > static_cast<int64_t>(sms) * 16) blocks = static_cast<int64_t>(sms) * 16;
-  csr::sort_windows_kernel<<<static_cast<unsigned>(blocks), 256, 0, as_stream(stream)>>>(ev_words_dev,
-                                                                                       ev_offsets_dev, npix);
+  if (!stage_dev || !tile_pos_dev || !sb_counts_dev || !ev_offsets_dev || !ev_words_dev || !err_dev)
+    return G2_ERR_ARG;
+  if (nframes <= 0 || npix <= 0 || n_elem < 0) return G2_ERR_ARG;
+  if (nframes > 65536 || n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
+  const int n_sb = static_cast<int>((static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK);
+  const int64_t n_tiles = (npix + csr::TILE_P - 1) / csr::TILE_P;
+  if (n_tiles > 0x7fffffff) return G2_ERR_TOO_LARGE;
+  const int buf = buffer_words(n_elem * csr::TILE_P, npix);
+  const int64_t smem = (131ll * n_sb + 1 + buf) * 4;
+  if (!allow_smem(csr::gather_tiles_kernel, smem)) return G2_ERR_CUDA;
+  csr::gather_tiles_kernel<<<static_cast<unsigned>(n_tiles), 256, smem, as_stream(stream)>>>(
+      stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev, n_elem, sort ? 1 : 0, buf,
+      ev_words_dev, err_dev);
   return launch_status();
 }
 

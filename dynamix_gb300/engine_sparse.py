@@ -291,8 +291,9 @@ class SparseEngine:
 
     def packed_for(self, n):
         """Events travel as packed words (t << 16) | v: frames < 2^16, rows the
-        row-owned kernels take, fewer than 2^32 elements."""
-        return self.T <= 65535 and self.shape[1] <= self.ROW_MAX_W and n < 2 ** 32
+        row-owned kernels take (at most 29,000 pixels wide, 65,535 rows),
+        fewer than 2^32 elements."""
+        return self.T <= 65535 and self.shape[1] <= self.ROW_MAX_W and self.shape[0] <= 65535 and n < 2 ** 32
 
     def _counts_and_offsets(self, indices, indptr, offsets, ib, n):
         st = stream_handle(self.dev)
@@ -314,30 +315,45 @@ class SparseEngine:
         return buf
 
     SUBBLOCK = 1024
+    TILE_P = 64
 
-    def to_words(self, data, indices, indptr, offsets, ib, n):
-        """CSR on the device -> packed event words (ordered by 32-frame window
-        within a pixel) and event offsets (uint32 as int32) on the device;
-        requires :meth:`packed_for`.  Sub-blocked: per-(1024-frame block, pixel)
-        counts, their totals' scan, then the scatter."""
+    def to_words(self, data, indices, indptr, offsets, ib, n, sort=False):
+        """CSR on the device -> packed event words and event offsets (uint32
+        as int32) on the device; requires :meth:`packed_for`.  Counts per
+        (1024-frame sub-block, pixel) and per (sub-block, row), their scans,
+        the stage pass (runs grouped by sub-block, row and pixel) and the
+        gather pass (64-pixel tiles; each pixel's runs in sub-block order, in
+        frame order inside each run with ``sort``, so the whole list is in
+        frame order)."""
         torch = _torch()
         H, W = self.shape
         st = stream_handle(self.dev)
         self.events._mark("start_transpose")
         n_sb = -(-self.T // self.SUBBLOCK)
+        n_rows = n_sb * H
         sbc = self._buffer("sb_counts", n_sb * self.npix, torch.int16)
         rb = self._buffer("row_bounds", (H + 1) * self.T, torch.int32)
+        rt = self._buffer("row_totals", n_rows, torch.int32)
+        base = self._buffer("row_base", n_rows + 1, torch.int32)
+        rscr = self._buffer("row_scan_scratch", -(-n_rows // 8192), torch.int32)
         self.counts.zero_()
         _lib.check(self.lib.g2_csr_count_blocked(ptr(indices), ptr(indptr), ptr(offsets), ib, n, self.T, H, W,
-                                                 ptr(rb), ptr(self.counts), ptr(sbc), ptr(self.events.err), st),
-                   "g2_csr_count_blocked")
+                                                 ptr(rb), ptr(self.counts), ptr(sbc), ptr(rt),
+                                                 ptr(self.events.err), st), "g2_csr_count_blocked")
         _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
                                                   ptr(self.scan_scratch), self.scan_scratch.numel(), st),
                    "g2_exclusive_scan_u32")
+        _lib.check(self.lib.g2_exclusive_scan_u32(ptr(rt), n_rows, ptr(base), ptr(rscr), rscr.numel(), st),
+                   "g2_exclusive_scan_u32")
+        stage = self._buffer("stage_words", n, torch.int32)
+        tpos = self._buffer("tile_pos", n_sb * -(-self.npix // self.TILE_P), torch.int32)
+        _lib.check(self.lib.g2_csr_stage_blocked(ptr(data), data.element_size(), ptr(indices), ptr(rb), ib, n,
+                                                 self.T, H, W, ptr(sbc), ptr(base), ptr(tpos), ptr(stage),
+                                                 ptr(self.events.err), st), "g2_csr_stage_blocked")
         words = self._buffer("ev_words", n, torch.int32)
-        _lib.check(self.lib.g2_csr_scatter_blocked(ptr(data), data.element_size(), ptr(indices), ptr(rb), ib, n,
-                                                   self.T, H, W, ptr(self.ev_off), ptr(sbc), ptr(words),
-                                                   ptr(self.events.err), st), "g2_csr_scatter_blocked")
+        _lib.check(self.lib.g2_csr_gather_blocked(ptr(stage), ptr(tpos), ptr(sbc), self.T, self.npix, n,
+                                                  ptr(self.ev_off), 1 if sort else 0, ptr(words),
+                                                  ptr(self.events.err), st), "g2_csr_gather_blocked")
         self.events._mark("transpose")
         return words, self.ev_off
 
@@ -350,9 +366,7 @@ class SparseEngine:
         times = self._buffer("ev_times", n, torch.int32)
         evdata = self._buffer("ev_data", n, data.dtype)
         if self.packed_for(n):
-            words, off = self.to_words(data, indices, indptr, offsets, ib, n)
-            _lib.check(self.lib.g2_events_sort_windows(ptr(words), ptr(off), self.npix, stream_handle(self.dev)),
-                       "g2_events_sort_windows")
+            words, off = self.to_words(data, indices, indptr, offsets, ib, n, sort=True)
             _lib.check(self.lib.g2_events_unpack(ptr(words), n, data.element_size(), ptr(times), ptr(evdata),
                                                  stream_handle(self.dev)), "g2_events_unpack")
             return times, evdata, off

@@ -231,31 +231,39 @@ int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices
                    void* stream);
 
 /* Sub-blocked variants with packed event words (frames < 2^16, image rows up
- * to 29,000 pixels): the frames are cut into sub-blocks of 1024.
+ * to 29,000 pixels, fewer than 2^32 elements): the frames are cut into
+ * sub-blocks of 1024, n_sb = ceil(nframes / 1024).
  * g2_csr_count_blocked writes row_bounds_dev[r * nframes + t] (uint32, the
  * absolute index of row r's first element in frame t, r = 0..H; (H+1) *
- * nframes entries, read again by the scatter), sb_counts_dev[sb * H*W + p]
- * (uint16, the elements of pixel p in sub-block sb; ceil(nframes / 1024) *
- * H*W entries) and adds each pixel's total to counts_dev (caller zeroes);
- * fewer than 2^32 elements.
- * g2_csr_scatter_blocked writes each element as one word (t << 16) | v into
- * ev_words_dev[ev_offsets[p] ..) (ev_offsets: exclusive scan of the totals),
- * ordered by 32-frame window (t >> 5) and in any order inside a window;
- * column indices must increase strictly within a row (sorted CSR), else
- * G2_DEVERR_BOUNDS.  g2_events_sort_windows puts every pixel's words in frame
- * order; g2_events_unpack splits words into ev_times (int32) and ev_data
- * (elem_bytes 1 or 2) -- with the sort, the FramesCompressor layout
- * (event.py:267-284).  G2_ERR_UNSUPPORTED when nframes > 65536 (scatter) or
- * width > 29,000. */
+ * nframes entries), sb_counts_dev[sb * H*W + p] (uint16, the elements of
+ * pixel p in sub-block sb; n_sb * H*W entries), row_totals_dev[sb * H + r]
+ * (uint32, the elements of row r in sub-block sb; n_sb * H entries) and adds
+ * each pixel's total to counts_dev (caller zeroes).  Column indices must
+ * increase strictly within a row (sorted CSR), else G2_DEVERR_BOUNDS.
+ * g2_csr_stage_blocked takes row_base_dev (the exclusive scan of row_totals,
+ * n_sb * H + 1 entries) and writes every element as one word (t << 16) | v
+ * into stage_dev (n_elem words), grouped by sub-block, row and pixel, and the
+ * start of every 64-pixel tile's run of each sub-block into tile_pos_dev
+ * (n_sb * ceil(H*W / 64) entries).
+ * g2_csr_gather_blocked copies the runs into ev_words_dev[ev_offsets[p] ..)
+ * (ev_offsets: exclusive scan of the pixel totals, H*W + 1 entries; stage_dev
+ * and ev_words_dev hold n_elem words), in sub-block order, and with sort != 0
+ * in frame order inside each run -- then every pixel's list is in
+ * frame order.  g2_events_unpack splits words into ev_times (int32) and
+ * ev_data (elem_bytes 1 or 2): with the sort, the FramesCompressor layout
+ * (event.py:267-284).  G2_ERR_UNSUPPORTED when nframes > 65536 (stage,
+ * gather), height > 65535 or width > 29,000. */
 int g2_csr_count_blocked(const void* indices_dev, const void* indptr_dev, const void* offsets_dev,
                          int32_t index_bytes, int64_t n_elem, int32_t nframes, int32_t height, int32_t width,
-                         uint32_t* row_bounds_dev, uint32_t* counts_dev, uint16_t* sb_counts_dev, int32_t* err_dev,
-                         void* stream);
-int g2_csr_scatter_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
-                           const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem, int32_t nframes,
-                           int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
-                           const uint16_t* sb_counts_dev, uint32_t* ev_words_dev, int32_t* err_dev, void* stream);
-int g2_events_sort_windows(uint32_t* ev_words_dev, const uint32_t* ev_offsets_dev, int64_t npix, void* stream);
+                         uint32_t* row_bounds_dev, uint32_t* counts_dev, uint16_t* sb_counts_dev,
+                         uint32_t* row_totals_dev, int32_t* err_dev, void* stream);
+int g2_csr_stage_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                         const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem, int32_t nframes,
+                         int32_t height, int32_t width, const uint16_t* sb_counts_dev, const uint32_t* row_base_dev,
+                         uint32_t* tile_pos_dev, uint32_t* stage_dev, int32_t* err_dev, void* stream);
+int g2_csr_gather_blocked(const uint32_t* stage_dev, const uint32_t* tile_pos_dev, const uint16_t* sb_counts_dev,
+                          int32_t nframes, int64_t npix, int64_t n_elem, const uint32_t* ev_offsets_dev,
+                          int32_t sort, uint32_t* ev_words_dev, int32_t* err_dev, void* stream);
 int g2_events_unpack(const uint32_t* ev_words_dev, int64_t n_events, int32_t elem_bytes, int32_t* ev_times_dev,
                      void* ev_data_dev, void* stream);
 
