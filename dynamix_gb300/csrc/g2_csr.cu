@@ -516,10 +516,10 @@ __global__ void __launch_bounds__(256)
 
 // Gather pass: one CTA per tile of TILE_P consecutive pixels.  For every
 // sub-block the tile's runs are one contiguous chunk of the staging area
-// (starting at tile_pos); the CTA walks all chunks as one flattened list,
-// places each word at its pixel's list position in a shared-memory copy of the
-// tile's part of the event lists (when it fits in buf_words, else in place),
-// and writes that out with coalesced stores.  With `sort`, each run (one pixel,
+// (starting at tile_pos).  A thread per (sub-block, pixel) run copies the run
+// to its pixel's list position in a shared-memory copy of the tile's part of
+// the event lists (when it fits in buf_words, else in place), and the CTA
+// writes that out with coalesced stores.  With `sort`, each run (one pixel,
 // one 1024-frame sub-block) is put in frame order by insertion, which gives
 // exactly the FramesCompressor layout.  Shared memory: 131 * n_sb + 1 words of
 // tables, then the buffer.
@@ -608,47 +608,35 @@ __global__ void __launch_bounds__(256)
   const bool buffered = total <= static_cast<uint32_t>(buf_words);
   uint32_t* out = buffered ? buf : ev_words + base;
   bool bad = false;
-  for (uint32_t x0 = 0; x0 < total; x0 += 256 * UNROLL) {
-    uint32_t v[UNROLL], d[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const uint32_t x = x0 + u * 256 + threadIdx.x;
-      d[u] = 0xFFFFFFFFu;
-      v[u] = 0;
-      if (x >= total) continue;
-      int b = 0;  // the last chunk starting at or before x
-#pragma unroll
-      for (int step = 32; step; step >>= 1)
-        if (b + step < n_sb && cb[b + step] <= x) b += step;
-      const uint32_t y = x - cb[b];
-      const uint32_t* c = cp + b * (TILE_P + 1);
-      int p = 0;  // the pixel whose run holds y
-#pragma unroll
-      for (int step = 32; step; step >>= 1)
-        if (c[p + step] <= y) p += step;
-      const int64_t src = static_cast<int64_t>(tp[b]) + y;
-      const uint32_t dd = dst[b * TILE_P + p] + (y - c[p]);
-      if (src >= n_elem || dd >= total) {
-        bad = true;
-        continue;
-      }
-      d[u] = dd;
-      v[u] = stage[src];
+  // a thread per (sub-block, pixel) run: a warp takes 32 consecutive pixels
+  // of one sub-block, whose runs are adjacent in the staging area
+  for (int e = threadIdx.x; e < n_sb * TILE_P; e += 256) {
+    const int b = e / TILE_P, p = e % TILE_P;
+    if (p >= np) continue;
+    const uint32_t c0 = cp[b * (TILE_P + 1) + p];
+    const uint32_t n = cp[b * (TILE_P + 1) + p + 1] - c0;
+    if (n == 0) continue;
+    const int64_t src = static_cast<int64_t>(tp[b]) + c0;
+    const uint32_t d0 = dst[b * TILE_P + p];
+    if (src + n > n_elem || static_cast<int64_t>(d0) + n > total) {
+      bad = true;
+      continue;
     }
+    uint32_t* run = out + d0;
+    const uint32_t* in = stage + src;
+    uint32_t k = 0;
+    for (; k + UNROLL <= n; k += UNROLL) {
+      uint32_t v[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u)
-      if (d[u] != 0xFFFFFFFFu) out[d[u]] = v[u];
-  }
-  if (sort) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < n_sb * TILE_P; e += 256) {
-      const int b = e / TILE_P, p = e % TILE_P;
-      if (p >= np) continue;
-      const uint32_t n = cp[b * (TILE_P + 1) + p + 1] - cp[b * (TILE_P + 1) + p];
-      uint32_t* run = out + dst[b * TILE_P + p];
-      for (uint32_t k = 1; k < n; ++k) {
-        const uint32_t w = run[k];
-        uint32_t j = k;
+      for (int u = 0; u < UNROLL; ++u) v[u] = in[k + u];
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) run[k + u] = v[u];
+    }
+    for (; k < n; ++k) run[k] = in[k];
+    if (sort) {
+      for (uint32_t m = 1; m < n; ++m) {
+        const uint32_t w = run[m];
+        uint32_t j = m;
         while (j > 0 && run[j - 1] > w) {
           run[j] = run[j - 1];
           --j;
