@@ -68,6 +68,12 @@ SIGNATURES = {
     "g2_csr_stage_blocked": (C.c_int, [_p, _i32, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),
     "g2_csr_gather_blocked": (C.c_int, [_p, _p, _p, _i32, _i64, _i64, _p, _i32, _p, _p, _p]),
     "g2_events_unpack": (C.c_int, [_p, _i64, _i32, _p, _p, _p]),
+    "g2_compress_count": (C.c_int, [_p, _i32, _i32, _i64, _i32, _p, _p, _p, _p, _p, _p]),
+    "g2_compress_finish": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p, _p, _p]),
+    "g2_compress_stage": (C.c_int, [_p, _i32, _i32, _i64, _p, _p, _p, _p, _p, _i64, _p, _p]),
+    "g2_events_gather_rel": (C.c_int, [_p, _p, _p, _i32, _i64, _i64, _p, _i32, _p, _p, _p, _p, _p]),
+    "g2_stream_compress": (C.c_int, [_p, _i32, _i32, _i64, _i64, _i32, _i32, _p, _p, _p, _p, _p, _p, _p]),
+    "g2_stream_compact": (C.c_int, [_p, _p, _p, _i32, _i64, _i32, _p, _i64, _p, _p, _p, _p]),
     "g2_denominator": (C.c_int, [_p, _i32, _i64, _p, _p]),
     "g2_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
     "g2_normalize_static": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),

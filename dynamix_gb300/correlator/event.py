@@ -90,23 +90,45 @@ class FramesCompressor(object):
     int32, offsets uint32 of size H*W+1).
     """
 
-    def __init__(self, shape, nframes, max_nnz, dtype=np.int8):
+    def __init__(self, shape, nframes, max_nnz, dtype=np.int8, device=None, threshold=None):
         self.shape = shape
         self.nframes = nframes
         self.dtype = dtype
         self.max_nnz = max_nnz
         self.npix = int(np.prod(self.shape))
+        self.threshold = threshold
+        self._device = None
+        if device is not None:
+            # the event rows live on the GPU; frames go through g2_stream_compress
+            from ..compress import StreamCompressor
+            self._device = StreamCompressor(shape, nframes, max_nnz, dtype, threshold=threshold, device=device)
+            self.frames_counter = 0
+            return
         self._init_events_datastructure()
 
     def _init_events_datastructure(self):
         self.events_counter = np.zeros(self.npix, dtype=np.int32)
         self.events = np.zeros((self.npix, self.max_nnz), dtype=self.dtype)
         self.times = np.zeros((self.npix, self.max_nnz), dtype=np.int32)
+        self.mask = np.zeros(self.npix, dtype=bool)
         self.frames_counter = 0
 
     @staticmethod
-    def compress_all_stack(frames):
-        """Event structure of a whole (T, H, W) stack: (data, times, offsets)."""
+    def compress_all_stack(frames, device=None, threshold=None, mask=None, sum_frame=None):
+        """Event structure of a whole (T, H, W) stack: (data, times, offsets).
+
+        A CUDA tensor, or any stack with ``device`` given, is compressed on
+        the GPU (``dynamix_gb300.compress``; CUDA outputs for a CUDA input);
+        ``threshold``, ``mask`` and ``sum_frame`` (device tensors) select the
+        sticky hot-pixel mask and the sum frame there.  A numpy stack without
+        ``device`` is compressed on the host as the reference does."""
+        from ..engine import _torch
+        torch = _torch()
+        if device is not None or (isinstance(frames, torch.Tensor) and frames.is_cuda) \
+                or threshold is not None or mask is not None or sum_frame is not None:
+            from ..compress import compress_all_stack_device
+            return compress_all_stack_device(frames, device=device, threshold=threshold, mask=mask,
+                                             sum_frame=sum_frame)
         frames = np.asarray(frames)
         assert frames.ndim == 3
         ft = np.moveaxis(frames, 0, -1)
@@ -119,8 +141,17 @@ class FramesCompressor(object):
         return data, times, offsets
 
     def process_frame(self, frame):
-        """Append one frame's non-zero counts to the per-pixel lists."""
+        """Append one frame's non-zero counts to the per-pixel lists (on the
+        GPU when the compressor was built with a device)."""
+        if self._device is not None:
+            self._device.process_frames(frame)
+            self.frames_counter = self._device.frames_counter
+            return
         f = np.asarray(frame).ravel()
+        if self.threshold is not None:
+            # sticky hot-pixel mask (io/readdata.py:452-458)
+            self.mask |= f > self.threshold
+            f = np.where(self.mask, 0, f)
         mask = f > 0
         idx = np.flatnonzero(mask)
         if idx.size and np.any(self.events_counter[idx] >= self.max_nnz):
@@ -130,10 +161,22 @@ class FramesCompressor(object):
         self.events_counter[idx] += 1
         self.frames_counter += 1
 
+    def process_frames(self, frames):
+        """Append a batch of frames (B, H, W) -- one launch on the GPU."""
+        if self._device is not None:
+            self._device.process_frames(frames)
+            self.frames_counter = self._device.frames_counter
+            return
+        for f in frames:
+            self.process_frame(f)
+
     def get_compacted_events(self, wait_for_all_frames=True):
-        """(events, times, offsets) of the frames processed so far."""
+        """(events, times, offsets) of the frames processed so far (device
+        tensors, offsets int64, when the compressor runs on the GPU)."""
         if self.frames_counter < self.nframes - 1 and wait_for_all_frames:
             raise RuntimeError("Not all frames were compressed yet (%d/%d)" % (self.frames_counter, self.nframes))
+        if self._device is not None:
+            return self._device.get_compacted_events()
         offsets = np.zeros(self.events_counter.size + 1, dtype=np.uint32)
         offsets[1:] = np.cumsum(self.events_counter)
         keep = np.arange(self.max_nnz)[None, :] < self.events_counter[:, None]

@@ -523,17 +523,28 @@ __global__ void __launch_bounds__(256)
 // one 1024-frame sub-block) is put in frame order by insertion, which gives
 // exactly the FramesCompressor layout.  Shared memory: 131 * n_sb + 1 words of
 // tables, then the buffer.
+// Output modes of the gather: the staged words as they are (CSR path, absolute
+// frame numbers below 2^16), words whose frame field is relative to the
+// sub-block (frame compression) turned into absolute packed words, or split
+// into frame numbers (int32) and values (Tv).
+constexpr int GATHER_WORDS = 0;
+constexpr int GATHER_REL_WORDS = 1;
+constexpr int GATHER_REL_SPLIT = 2;
+
+template <int MODE, typename Tv>
 __global__ void __launch_bounds__(256)
     gather_tiles_kernel(const uint32_t* __restrict__ stage, const uint32_t* __restrict__ tile_pos,
                         const uint16_t* __restrict__ sb_counts, int n_sb, int64_t npix, int64_t n_tiles,
                         const uint32_t* __restrict__ ev_off, int64_t n_elem, int sort, int buf_words,
-                        uint32_t* __restrict__ ev_words, int32_t* __restrict__ err) {
+                        uint32_t* __restrict__ ev_words, int32_t* __restrict__ ev_times, Tv* __restrict__ ev_data,
+                        int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
   uint32_t* cp = sm;                       // [n_sb][TILE_P + 1] run starts within each chunk
   uint32_t* dst = cp + n_sb * (TILE_P + 1);  // [n_sb][TILE_P] run starts within the tile's lists
   uint32_t* cb = dst + n_sb * TILE_P;        // [n_sb + 1] chunk starts within the walk
   uint32_t* tp = cb + n_sb + 1;              // [n_sb] chunk starts in the staging area
-  uint32_t* buf = tp + n_sb;                 // [buf_words]
+  uint32_t* buf = tp + n_sb;                 // [buf_words] words, or frame numbers
+  uint16_t* bufd = reinterpret_cast<uint16_t*>(buf + buf_words);  // [buf_words] values (split mode)
   __shared__ int s_bad;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tile = blockIdx.x;
@@ -606,7 +617,7 @@ __global__ void __launch_bounds__(256)
     return;  // block-uniform
   }
   const bool buffered = total <= static_cast<uint32_t>(buf_words);
-  uint32_t* out = buffered ? buf : ev_words + base;
+  uint32_t* out = buffered ? buf : (MODE == GATHER_REL_SPLIT ? reinterpret_cast<uint32_t*>(ev_times) : ev_words) + base;
   bool bad = false;
   // a thread per (sub-block, pixel) run: a warp takes 32 consecutive pixels
   // of one sub-block, whose runs are adjacent in the staging area
@@ -624,16 +635,31 @@ __global__ void __launch_bounds__(256)
     }
     uint32_t* run = out + d0;
     const uint32_t* in = stage + src;
-    uint32_t k = 0;
-    for (; k + UNROLL <= n; k += UNROLL) {
-      uint32_t v[UNROLL];
+    if (MODE == GATHER_WORDS) {
+      uint32_t k = 0;
+      for (; k + UNROLL <= n; k += UNROLL) {
+        uint32_t v[UNROLL];
 #pragma unroll
-      for (int u = 0; u < UNROLL; ++u) v[u] = in[k + u];
+        for (int u = 0; u < UNROLL; ++u) v[u] = in[k + u];
 #pragma unroll
-      for (int u = 0; u < UNROLL; ++u) run[k + u] = v[u];
+        for (int u = 0; u < UNROLL; ++u) run[k + u] = v[u];
+      }
+      for (; k < n; ++k) run[k] = in[k];
+    } else if (MODE == GATHER_REL_WORDS) {
+      const uint32_t add = static_cast<uint32_t>(b) << 26;  // (b * 1024) << 16
+      for (uint32_t k = 0; k < n; ++k) run[k] = in[k] + add;
+    } else {
+      const uint32_t t_add = static_cast<uint32_t>(b) * SUBBLOCK;
+      for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t w = in[k];
+        run[k] = t_add + (w >> 16);  // frame number
+        if (buffered)
+          bufd[d0 + k] = static_cast<uint16_t>(w & 0xFFFFu);
+        else
+          ev_data[base + d0 + k] = static_cast<Tv>(w & 0xFFFFu);
+      }
     }
-    for (; k < n; ++k) run[k] = in[k];
-    if (sort) {
+    if (MODE == GATHER_WORDS && sort) {
       for (uint32_t m = 1; m < n; ++m) {
         const uint32_t w = run[m];
         uint32_t j = m;
@@ -647,7 +673,14 @@ __global__ void __launch_bounds__(256)
   }
   if (buffered) {
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < total; i += 256) ev_words[base + i] = buf[i];
+    if (MODE == GATHER_REL_SPLIT) {
+      for (uint32_t i = threadIdx.x; i < total; i += 256) {
+        ev_times[base + i] = static_cast<int32_t>(buf[i]);
+        ev_data[base + i] = static_cast<Tv>(bufd[i]);
+      }
+    } else {
+      for (uint32_t i = threadIdx.x; i < total; i += 256) ev_words[base + i] = buf[i];
+    }
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
@@ -1012,10 +1045,57 @@ extern "C" int g2_csr_gather_blocked(const uint32_t* stage_dev, const uint32_t* 
   if (n_tiles > 0x7fffffff) return G2_ERR_TOO_LARGE;
   const int buf = buffer_words(n_elem * csr::TILE_P, npix);
   const int64_t smem = (131ll * n_sb + 1 + buf) * 4;
-  if (!allow_smem(csr::gather_tiles_kernel, smem)) return G2_ERR_CUDA;
-  csr::gather_tiles_kernel<<<static_cast<unsigned>(n_tiles), 256, smem, as_stream(stream)>>>(
+  auto kernel = csr::gather_tiles_kernel<csr::GATHER_WORDS, uint8_t>;
+  if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
+  kernel<<<static_cast<unsigned>(n_tiles), 256, smem, as_stream(stream)>>>(
       stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev, n_elem, sort ? 1 : 0, buf,
-      ev_words_dev, err_dev);
+      ev_words_dev, nullptr, nullptr, err_dev);
+  return launch_status();
+}
+
+extern "C" int g2_events_gather_rel(const uint32_t* stage_dev, const uint32_t* tile_pos_dev,
+                                    const uint16_t* sb_counts_dev, int32_t nframes, int64_t npix, int64_t n_elem,
+                                    const uint32_t* ev_offsets_dev, int32_t elem_bytes, uint32_t* ev_words_dev,
+                                    int32_t* ev_times_dev, void* ev_data_dev, int32_t* err_dev, void* stream) {
+  using namespace g2;
+  if (!stage_dev || !tile_pos_dev || !sb_counts_dev || !ev_offsets_dev || !err_dev) return G2_ERR_ARG;
+  if (nframes <= 0 || npix <= 0 || n_elem < 0) return G2_ERR_ARG;
+  const bool words = ev_words_dev != nullptr;
+  if (words == (ev_times_dev != nullptr || ev_data_dev != nullptr)) return G2_ERR_ARG;  // one output form
+  if (!words && (!ev_times_dev || !ev_data_dev || (elem_bytes != 1 && elem_bytes != 2))) return G2_ERR_ARG;
+  if (words && nframes > 65536) return G2_ERR_UNSUPPORTED;
+  if (n_elem >= (1ll << 32)) return G2_ERR_UNSUPPORTED;
+  const int64_t n_sb64 = (static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK;
+  if (n_sb64 > 400) return G2_ERR_TOO_LARGE;  // the tile tables (131 words per sub-block) stay in shared memory
+  const int n_sb = static_cast<int>(n_sb64);
+  const int64_t n_tiles = (npix + csr::TILE_P - 1) / csr::TILE_P;
+  if (n_tiles > 0x7fffffff) return G2_ERR_TOO_LARGE;
+  const int64_t tables = (131ll * n_sb + 1) * 4, per_word = words ? 4 : 6;
+  int64_t buf = buffer_words(n_elem * csr::TILE_P, npix);
+  if (tables + buf * per_word > 227 * 1024) buf = (227 * 1024 - tables) / per_word;  // larger tiles go in place
+  const int64_t smem = tables + buf * per_word;
+  cudaStream_t st = as_stream(stream);
+  const unsigned grid = static_cast<unsigned>(n_tiles);
+  if (words) {
+    auto kernel = csr::gather_tiles_kernel<csr::GATHER_REL_WORDS, uint8_t>;
+    if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
+    kernel<<<grid, 256, smem, st>>>(stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev,
+                                    n_elem, 0, static_cast<int>(buf), ev_words_dev, nullptr, nullptr, err_dev);
+  } else if (elem_bytes == 1) {
+    auto kernel = csr::gather_tiles_kernel<csr::GATHER_REL_SPLIT, uint8_t>;
+    if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
+    kernel<<<grid, 256, smem, st>>>(stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev,
+                                    n_elem, 0, static_cast<int>(buf), nullptr, ev_times_dev,
+                                    reinterpret_cast<uint8_t*>(ev_data_dev),
+                                    err_dev);
+  } else {
+    auto kernel = csr::gather_tiles_kernel<csr::GATHER_REL_SPLIT, uint16_t>;
+    if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
+    kernel<<<grid, 256, smem, st>>>(stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev,
+                                    n_elem, 0, static_cast<int>(buf), nullptr, ev_times_dev,
+                                    reinterpret_cast<uint16_t*>(ev_data_dev),
+                                    err_dev);
+  }
   return launch_status();
 }
 

@@ -267,6 +267,65 @@ int g2_csr_gather_blocked(const uint32_t* stage_dev, const uint32_t* tile_pos_de
 int g2_events_unpack(const uint32_t* ev_words_dev, int64_t n_events, int32_t elem_bytes, int32_t* ev_times_dev,
                      void* ev_data_dev, void* stream);
 
+/* ---- frame compression: dense frames -> event lists ----------------------
+ * Device counterpart of FramesCompressor (event.py:207-321) with the
+ * hot-pixel threshold, sticky mask and sum frame of neigercompress
+ * (io/readdata.py:441-468).  frames_dev: (nframes, npix) values of kind
+ * elem_kind (1 u8, 2 u16, -1 i8, -2 i16); a value > 0 is an event, as in the
+ * reference's `frames > 0`.  n_sb = ceil(nframes / 1024), n_blk =
+ * ceil(npix / 1024) (at most 65535), n_tiles = ceil(npix / 64).
+ * g2_compress_count writes sb_counts_dev[sb * npix + p] (uint16, positives of
+ * pixel p in sub-block sb) and blk_totals_dev[sb * n_blk + b] (their sums over
+ * 1024-pixel blocks); threshold >= 0 also writes sb_first_dev (the first frame
+ * of the sub-block, counted from its start, with a value above the threshold;
+ * 0xFFFF for none) and sb_before_dev (positives before that frame);
+ * sum_frame_dev (int64 per pixel, nullable, caller zeroes) gets every raw
+ * value added.
+ * g2_compress_finish applies the sticky mask: mask_dev (uint8 per pixel,
+ * nullable, updated in place) drops every event of a masked pixel, and a
+ * value above the threshold masks its pixel from that frame on.  It corrects
+ * sb_counts and blk_totals and writes counts_dev (uint32 events per pixel)
+ * and t_cut_dev (int32 per pixel, nullable: the first dropped frame, nframes
+ * for none; needed by the stage pass when a threshold or a mask is used).
+ * Scan counts -> ev_offsets (npix + 1) and blk_totals -> blk_base
+ * (n_sb * n_blk + 1) with g2_exclusive_scan_u32; g2_compress_stage then
+ * writes stage_dev (n_stage words, at least the events) and tile_pos_dev
+ * (n_sb * n_tiles), and g2_events_gather_rel the event lists: packed words
+ * (t << 16) | v into ev_words_dev (nframes <= 65536; the input of
+ * g2_event_pairsum_packed), or ev_times_dev (int32) and ev_data_dev
+ * (elem_bytes 1 or 2) with ev_words_dev NULL (nframes up to 409,600).  Within
+ * a pixel the events come in frame order: exactly the compress_all_stack
+ * layout (event.py:267-284). */
+int g2_compress_count(const void* frames_dev, int32_t elem_kind, int32_t nframes, int64_t npix, int32_t threshold,
+                      uint16_t* sb_counts_dev, uint16_t* sb_first_dev, uint16_t* sb_before_dev,
+                      uint32_t* blk_totals_dev, int64_t* sum_frame_dev, void* stream);
+int g2_compress_finish(uint16_t* sb_counts_dev, const uint16_t* sb_first_dev, const uint16_t* sb_before_dev,
+                       int32_t nframes, int64_t npix, uint8_t* mask_dev, uint32_t* blk_totals_dev,
+                       uint32_t* counts_dev, int32_t* t_cut_dev, void* stream);
+int g2_compress_stage(const void* frames_dev, int32_t elem_kind, int32_t nframes, int64_t npix,
+                      const uint16_t* sb_counts_dev, const int32_t* t_cut_dev, const uint32_t* blk_base_dev,
+                      uint32_t* tile_pos_dev, uint32_t* stage_dev, int64_t n_stage, int32_t* err_dev, void* stream);
+int g2_events_gather_rel(const uint32_t* stage_dev, const uint32_t* tile_pos_dev, const uint16_t* sb_counts_dev,
+                         int32_t nframes, int64_t npix, int64_t n_elem, const uint32_t* ev_offsets_dev,
+                         int32_t elem_bytes, uint32_t* ev_words_dev, int32_t* ev_times_dev, void* ev_data_dev,
+                         int32_t* err_dev, void* stream);
+
+/* Streaming (process_frame and get_compacted_events, event.py:286-321): one
+ * call appends n_batch frames (frame numbers frame0, frame0 + 1, ...) to the
+ * per-pixel rows of events_dev (npix x max_nnz, the frames' type) and
+ * times_dev (int32); counter_dev (int32 per pixel) holds each row's length and
+ * stops at max_nnz, setting G2_DEVERR_RANGE; threshold >= 0 and mask_dev act
+ * as in g2_compress_finish (the mask persists across calls); sum_frame_dev
+ * (nullable) adds the raw values.  g2_stream_compact copies the rows to
+ * out_data_dev / out_times_dev at offsets_dev (the exclusive scan of
+ * counter_dev, npix + 1 entries); capacity is the outputs' length. */
+int g2_stream_compress(const void* frames_dev, int32_t elem_kind, int32_t n_batch, int64_t frame0, int64_t npix,
+                       int32_t max_nnz, int32_t threshold, uint8_t* mask_dev, int64_t* sum_frame_dev,
+                       void* events_dev, int32_t* times_dev, int32_t* counter_dev, int32_t* err_dev, void* stream);
+int g2_stream_compact(const void* events_dev, const int32_t* times_dev, const int32_t* counter_dev,
+                      int32_t elem_bytes, int64_t npix, int32_t max_nnz, const uint32_t* offsets_dev,
+                      int64_t capacity, void* out_data_dev, int32_t* out_times_dev, int32_t* err_dev, void* stream);
+
 /* ---- calc_std deviation (dense.py:58-66) ---------------------------------
  * g2_gram_std runs the Gram tiles of the items again (full K per item, fp32
  * accumulation: a float statistic, not an exact sum) and, for every pair

@@ -216,6 +216,30 @@ def compress_all_stack(frames):
     return data, times, offsets
 
 
+def compress_hot_pixels(frames, threshold=None, mask=None):
+    """Frame-by-frame compression with the sticky hot-pixel mask of the
+    streaming reader (``io/readdata.py:452-466``, ``neigercompress``).
+
+    Per frame ``i`` and pixel ``p``: the raw value is added to the sum frame; a
+    value above ``threshold`` sets the pixel's mask; a masked pixel's value is
+    zeroed; a value still > 0 is appended to the pixel's events with time
+    ``i``.  Returns ``(data, times, offsets, mask_after, sum_frame)`` in the
+    layout of :func:`compress_all_stack` (the mask and the sums per pixel)."""
+    assert frames.ndim == 3
+    T = frames.shape[0]
+    f = frames.reshape(T, -1).astype(np.int64)
+    m = np.zeros(f.shape[1], dtype=bool) if mask is None else np.asarray(mask).ravel().astype(bool).copy()
+    kept = np.zeros_like(f)
+    for i in range(T):
+        fr = f[i].copy()
+        if threshold is not None:
+            m |= fr > threshold
+        fr[m] = 0
+        kept[i] = fr
+    data, times, offsets = compress_all_stack(kept.reshape(frames.shape))
+    return data.astype(frames.dtype), times, offsets, m, f.sum(axis=0)
+
+
 def event_correlate_exact(vol_times, vol_data, offsets, qmask, shape, nframes, scale_factor=None):
     """Event-list correlation restated from ``evtcorrelator.cl:3-77``.
 

@@ -46,6 +46,13 @@ def test_argument_errors_are_caught_on_host(built_lib):
     assert built_lib.g2_pack_frames(None, 1, 1, 1, None, None, None, None, None, None, 1, 0, None, 128, None, 1,
                                     None, 0, None, None) == 1
     assert built_lib.g2_normalize_static(None, None, None, 1, 10, None, None, None) == 1
+    assert built_lib.g2_compress_count(None, 1, 10, 16, -1, None, None, None, None, None, None) == 1
+    assert built_lib.g2_compress_count(1, 3, 10, 16, -1, 1, None, None, 1, None, None) == 1   # bad kind
+    assert built_lib.g2_compress_count(1, 1, 10, 16, 5, 1, None, None, 1, None, None) == 1    # threshold, no outputs
+    assert built_lib.g2_compress_stage(None, 1, 10, 16, None, None, None, None, None, 0, None, None) == 1
+    assert built_lib.g2_events_gather_rel(1, 1, 1, 10, 16, 0, 1, 1, 1, 1, 1, 1, None) == 1  # both output forms
+    assert built_lib.g2_stream_compress(1, 1, 1, 0, 16, 0, -1, None, None, 1, 1, 1, 1, None) == 1  # max_nnz 0
+    assert built_lib.g2_stream_compact(None, None, None, 1, 16, 4, None, 0, None, None, None, None) == 1
 
 
 def test_item_layout_matches_c_struct():
