@@ -58,7 +58,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--frames", type=int, default=None, help="override T (testing only)")
-    p.add_argument("--workload", default="dense", choices=["dense", "u16", "sparse", "event", "serving"],
+    p.add_argument("--workload", default="dense", choices=["dense", "u16", "sparse", "event", "serving", "compress"],
                    help="dense: 514x1030x10k u8 Gram path (default); sparse / event: 2162x2068x20k CSR or "
                         "per-pixel event lists through the pair-sum path")
     return p.parse_args()
@@ -845,10 +845,182 @@ def run_u16(args):
     return 0
 
 
+COMPRESS_WORKLOAD = {
+    "workload": "compress_514x1030_u8_T10000",
+    "frame_shape": [514, 1030], "nframes": 10000, "dtype": "uint8", "rho": 0.99, "mean_photons": 0.1, "seed": 1,
+    "operation": "compress_all_stack (dense stack -> per-pixel event lists, times int32 + values u8 + offsets)",
+    "l2": "input stack (5.3 GB) larger than L2; no flush",
+}
+COMPRESS_CPU_FRAMES = 256
+
+
+def run_compress(args):
+    """Device frame compression of the dense headline stack (frames already in
+    HBM for ``value``; from pinned host memory, events copied back, for e2e)."""
+    import numpy as np
+    import torch
+
+    from dynamix_gb300 import build as b
+    from dynamix_gb300.compress import StackCompressor
+    from dynamix_gb300.speckle import speckle_torch
+
+    rank, world, local = dist_info()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    b.build(force=False)
+    T = args.frames
+    H, W = COMPRESS_WORKLOAD["frame_shape"]
+    npix = H * W
+    frames = speckle_torch(T, (H, W), COMPRESS_WORKLOAD["rho"], COMPRESS_WORKLOAD["mean_photons"],
+                           seed=COMPRESS_WORKLOAD["seed"], dtype="uint8", device=dev).reshape(T, npix)
+    comp = StackCompressor(T, npix, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        from dynamix_gb300.replicas import max_over_ranks as mx
+        return mx(x, dist, dev)
+
+    for _ in range(max(args.warmup, 3)):
+        comp.run(frames)
+    n_ev = comp.n_events
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    sampler = ClockSampler(uuid)
+    barrier()
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        comp.run(frames)
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    comp.profile = True
+    comp.run(frames)
+    st = comp.stage_times()
+    comp.profile = False
+    stack_bytes = T * npix
+    out_bytes = n_ev * 5 + (npix + 1) * 8
+    peaks, peak_kind = measured_peaks()
+    # dominant kernel: the count pass (reads the stack once); the stage pass reads it again
+    count_gbs = stack_bytes / (st["count"] / 1e3) / 1e9
+    stage_gbs = (stack_bytes + n_ev * 4) / (st["stage"] / 1e3) / 1e9
+    line = {
+        "metric": "compress_frames_per_s", "value": world * T / (ms / 1e3), "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": dict(COMPRESS_WORKLOAD, nframes=T, n_events=n_ev, parallelism="replicas" if world > 1 else "single"),
+        "hbm_GB_per_s_step": (stack_bytes + out_bytes) / (ms / 1e3) / 1e9,
+        "stages_ms": st,
+        "roofline": {"bound": "hbm", "achieved": count_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": count_gbs / peaks.get("hbm_gbs"), "traffic": None, "kernel": "g2_compress_count",
+                     "peak_source": "%s hbm_gbs" % peak_kind,
+                     "algorithmic_bytes_per_launch": stack_bytes, "launch_ms": st["count"],
+                     "stage_pass_GB_per_s": stage_gbs,
+                     "note": "two passes read the stack (count, stage); the algorithmic minimum reads it once"},
+        "clocks": clocks, "gpu_launches": 8 * args.steps,
+    }
+    if rank == 0 and not args.no_e2e:
+        host = torch.empty((T, npix), dtype=torch.uint8, pin_memory=True)
+        host.copy_(frames)
+        dfr = torch.empty_like(frames)
+        out_h = {}
+
+        def e2e_step():
+            dfr.copy_(host, non_blocking=True)
+            d, t, off = comp.run(dfr)
+            for k, x in (("d", d), ("t", t), ("o", off)):
+                buf = out_h.get(k)
+                if buf is None or buf.numel() < x.numel() or buf.dtype != x.dtype:
+                    buf = out_h[k] = torch.empty(x.numel() + 1024, dtype=x.dtype, pin_memory=True)
+                buf[:x.numel()].copy_(x, non_blocking=True)
+            torch.cuda.synchronize(dev)
+            return d.numel() * 5 + off.numel() * 8
+
+        for _ in range(2):
+            e2e_step()
+        t0 = time.perf_counter()
+        d2h = 0
+        for _ in range(args.steps):
+            d2h = e2e_step()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        line["e2e"] = {"value": T / (e2e_ms / 1e3), "unit": "frames/s", "ms_per_step": e2e_ms,
+                       "h2d_bytes_per_step": stack_bytes, "d2h_bytes_per_step": d2h,
+                       "path": "pinned host stack -> device -> StackCompressor.run -> pinned host events"}
+        del host, dfr
+    if rank == 0 and not args.no_cpu:
+        from oracle.g2_oracle import compress_all_stack
+        Ts = min(COMPRESS_CPU_FRAMES, T)
+        sample = frames[:Ts].reshape(Ts, H, W).cpu().numpy()
+        t0 = time.perf_counter()
+        compress_all_stack(sample)
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": Ts / sec, "unit": "frames/s", "cores": 1, "kind": "port",
+                                "sample": "numpy restatement of compress_all_stack on the first %d frames" % Ts}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def run_compress_reference(args):
+    """The reference's compress_all_stack is numpy on the host (event.py:267-284):
+    its restatement timed on a bounded sample of the same stack."""
+    import torch
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    from dynamix_gb300.speckle import speckle_torch
+    from oracle.g2_oracle import compress_all_stack
+    T = args.frames
+    H, W = COMPRESS_WORKLOAD["frame_shape"]
+    dev = torch.device("cuda", local)
+    Ts = min(COMPRESS_CPU_FRAMES, T)
+    sample = speckle_torch(T, (H, W), COMPRESS_WORKLOAD["rho"], COMPRESS_WORKLOAD["mean_photons"],
+                           seed=COMPRESS_WORKLOAD["seed"], dtype="uint8", device=dev)[:Ts].cpu().numpy()
+    for _ in range(args.warmup):
+        compress_all_stack(sample)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        compress_all_stack(sample)
+    sec = (time.perf_counter() - t0) / args.steps
+    v = Ts / sec
+    line = {
+        "metric": "compress_frames_per_s", "value": v, "unit": "frames/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": T / v * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": dict(COMPRESS_WORKLOAD, nframes=T),
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",
+                         "sample": "each step: numpy compress_all_stack on the first %d of %d frames" % (Ts, T)},
+        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "compress":
+        if args.frames is None:
+            args.frames = COMPRESS_WORKLOAD["nframes"]
+        if args.impl == "reference":
+            return run_compress_reference(args)
+        return run_compress(args)
     if args.workload == "u16":
         if args.frames is None:
             args.frames = U16_WORKLOAD["nframes"]

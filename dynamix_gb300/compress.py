@@ -101,6 +101,25 @@ class StackCompressor:
         self.err = torch.zeros(1, dtype=i32, device=dev)
         self.stage = None
         self.n_events = 0
+        self.profile = False
+        self.marks = []
+
+    def _mark(self, name):
+        if self.profile:
+            torch = _torch()
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(torch.cuda.current_stream(self.dev))
+            self.marks.append((name, e))
+
+    def stage_times(self):
+        """Milliseconds of each pass of the last profiled call (CUDA events)."""
+        torch = _torch()
+        torch.cuda.synchronize(self.dev)
+        out = {}
+        for (_, a), (name, b) in zip(self.marks, self.marks[1:]):
+            out[name] = out.get(name, 0.0) + a.elapsed_time(b)
+        self.marks = []
+        return out
 
     def _stage_buffer(self, n):
         torch = _torch()
@@ -126,14 +145,17 @@ class StackCompressor:
         kind = elem_kind(f.dtype)
         st = stream_handle(self.dev)
         self.err.zero_()
+        self._mark("start")
         self._cut = self.threshold >= 0 or mask is not None
         _lib.check(self.lib.g2_compress_count(ptr(f), kind, self.T, self.npix, self.threshold, ptr(self.sb_counts),
                                               _optr(self.sb_first), _optr(self.sb_before), ptr(self.blk_totals),
                                               _optr(sum_frame), st), "g2_compress_count")
+        self._mark("count")
         _lib.check(self.lib.g2_compress_finish(ptr(self.sb_counts), _optr(self.sb_first), _optr(self.sb_before),
                                                self.T, self.npix, _optr(mask), ptr(self.blk_totals),
                                                ptr(self.counts), ptr(self.t_cut) if self._cut else None, st),
                    "g2_compress_finish")
+        self._mark("finish")
         _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), self.npix, ptr(self.ev_off),
                                                   ptr(self.scan_scratch), self.scan_scratch.numel(), st),
                    "g2_exclusive_scan_u32")
@@ -141,6 +163,7 @@ class StackCompressor:
         _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.blk_totals), nb, ptr(self.blk_base),
                                                   ptr(self.blk_scratch), self.blk_scratch.numel(), st),
                    "g2_exclusive_scan_u32")
+        self._mark("scans")
         self.n_events = int(self.ev_off[-1].to(torch.int64).item()) & 0xFFFFFFFF
         return self.n_events
 
@@ -152,10 +175,12 @@ class StackCompressor:
         n = self.n_events
         st = stream_handle(self.dev)
         stage = self._stage_buffer(n)
+        self._mark("host_read")  # from the scans to here: the event count read and the output allocation
         _lib.check(self.lib.g2_compress_stage(ptr(frames), elem_kind(frames.dtype), self.T, self.npix,
                                               ptr(self.sb_counts), ptr(self.t_cut) if self._cut else None,
                                               ptr(self.blk_base), ptr(self.tile_pos), ptr(stage), stage.numel(),
                                               ptr(self.err), st), "g2_compress_stage")
+        self._mark("stage")
         if packed:
             if self.T > MAX_FRAMES_PACKED:
                 raise ValueError("packed event words hold at most %d frames" % MAX_FRAMES_PACKED)
@@ -163,6 +188,7 @@ class StackCompressor:
             _lib.check(self.lib.g2_events_gather_rel(ptr(stage), ptr(self.tile_pos), ptr(self.sb_counts), self.T,
                                                      self.npix, n, ptr(self.ev_off), 0, ptr(words), None, None,
                                                      ptr(self.err), st), "g2_events_gather_rel")
+            self._mark("gather")
             self.check_error()
             return words[:n], self.offsets()
         edt = torch.uint16 if frames.element_size() == 2 else torch.uint8
@@ -171,6 +197,7 @@ class StackCompressor:
         _lib.check(self.lib.g2_events_gather_rel(ptr(stage), ptr(self.tile_pos), ptr(self.sb_counts), self.T,
                                                  self.npix, n, ptr(self.ev_off), frames.element_size(), None,
                                                  ptr(times), ptr(data), ptr(self.err), st), "g2_events_gather_rel")
+        self._mark("gather")
         self.check_error()
         return data[:n].view(frames.dtype), times[:n], self.offsets()
 

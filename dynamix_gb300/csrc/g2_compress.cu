@@ -64,6 +64,69 @@ __device__ __forceinline__ void load4(const Tv* __restrict__ src, int64_t n_vali
   }
 }
 
+// Raw word holding 4 consecutive values (VEC loads) and its unpacking.
+template <typename Tv> struct Word4 { using type = uint32_t; };
+template <> struct Word4<uint16_t> { using type = uint2; };
+template <> struct Word4<int16_t> { using type = uint2; };
+
+template <typename Tv>
+__device__ __forceinline__ void unpack4(uint32_t w, int32_t v[PX]) {
+#pragma unroll
+  for (int j = 0; j < PX; ++j) {
+    const uint32_t b = (w >> (8 * j)) & 0xFFu;
+    v[j] = static_cast<Tv>(-1) < 0 ? static_cast<int32_t>(static_cast<int8_t>(b)) : static_cast<int32_t>(b);
+  }
+}
+template <typename Tv>
+__device__ __forceinline__ void unpack4(uint2 w, int32_t v[PX]) {
+  const uint32_t h[PX] = {w.x & 0xFFFFu, w.x >> 16, w.y & 0xFFFFu, w.y >> 16};
+#pragma unroll
+  for (int j = 0; j < PX; ++j)
+    v[j] = static_cast<Tv>(-1) < 0 ? static_cast<int32_t>(static_cast<int16_t>(h[j])) : static_cast<int32_t>(h[j]);
+}
+
+// frames whose loads are in flight together (VEC): 64 bytes per thread
+template <typename Tv> struct InFlight { static constexpr int frames = sizeof(Tv) == 1 ? 16 : 8; };
+
+// Walk frames [t, t1) of 4 pixels at src (frame stride npix), calling
+// f(v, t) per frame: with VEC, 64 bytes of loads per thread are issued
+// before they are used.
+// `more()` may stop the walk between groups of frames.
+template <typename Tv, bool VEC, typename F, typename M>
+__device__ __forceinline__ void walk_frames(const Tv* __restrict__ src, int64_t npix, int64_t t, int64_t t1,
+                                            int64_t n_valid, F&& f, M&& more) {
+  if (VEC) {
+    using W = typename Word4<Tv>::type;
+    constexpr int TU = InFlight<Tv>::frames;
+    for (; t + TU <= t1 && more(); t += TU) {
+      W raw[TU];
+#pragma unroll
+      for (int u = 0; u < TU; ++u) raw[u] = *reinterpret_cast<const W*>(src + u * npix);
+#pragma unroll
+      for (int u = 0; u < TU; ++u) {
+        int32_t v[PX];
+        unpack4<Tv>(raw[u], v);
+        f(v, t + u);
+      }
+      src += TU * npix;
+    }
+  }
+  for (; t + 4 <= t1 && more(); t += 4) {
+    int32_t v[4][PX];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) load4<Tv, VEC>(src + u * npix, n_valid, v[u]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) f(v[u], t + u);
+    src += 4 * npix;
+  }
+  for (; t < t1 && more(); ++t) {
+    int32_t v[PX];
+    load4<Tv, VEC>(src, n_valid, v);
+    f(v, t);
+    src += npix;
+  }
+}
+
 // Block-wide exclusive scan of one uint32 per thread; returns the prefix and
 // the block total.  s_warp: [THREADS / 32] shared words.
 __device__ __forceinline__ uint32_t block_scan(uint32_t x, uint32_t* s_warp, uint32_t& total) {
@@ -106,40 +169,20 @@ __global__ void __launch_bounds__(THREADS)
   uint32_t first[PX] = {NONE, NONE, NONE, NONE};
   long long sum[PX] = {0, 0, 0, 0};
   if (n_valid > 0) {
-    const Tv* src = frames + t0 * npix + p0;
-    int64_t t = t0;
-    for (; t + 4 <= t1; t += 4) {
-      int32_t v[4][PX];
+    walk_frames<Tv, VEC>(
+        frames + t0 * npix + p0, npix, t0, t1, n_valid,
+        [&](const int32_t v[PX], int64_t t) {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) load4<Tv, VEC>(src + u * npix, n_valid, v[u]);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-#pragma unroll
-        for (int j = 0; j < PX; ++j) {
-          if (THR && v[u][j] > thr && first[j] == NONE) {
-            first[j] = static_cast<uint32_t>(t + u - t0);
-            before[j] = cnt[j];
+          for (int j = 0; j < PX; ++j) {
+            if (THR && v[j] > thr && first[j] == NONE) {
+              first[j] = static_cast<uint32_t>(t - t0);
+              before[j] = cnt[j];
+            }
+            cnt[j] += v[j] > 0 ? 1u : 0u;
+            sum[j] += v[j];
           }
-          cnt[j] += v[u][j] > 0 ? 1u : 0u;
-          sum[j] += v[u][j];
-        }
-      }
-      src += 4 * npix;
-    }
-    for (; t < t1; ++t) {
-      int32_t v[PX];
-      load4<Tv, VEC>(src, n_valid, v);
-#pragma unroll
-      for (int j = 0; j < PX; ++j) {
-        if (THR && v[j] > thr && first[j] == NONE) {
-          first[j] = static_cast<uint32_t>(t - t0);
-          before[j] = cnt[j];
-        }
-        cnt[j] += v[j] > 0 ? 1u : 0u;
-        sum[j] += v[j];
-      }
-      src += npix;
-    }
+        },
+        [] { return true; });
 #pragma unroll
     for (int j = 0; j < PX; ++j) {
       if (j >= n_valid) break;
@@ -239,39 +282,28 @@ __global__ void __launch_bounds__(THREADS)
   }
   bool bad = skip;
   if (!skip && own > 0) {
-    const Tv* src = frames + t0 * npix + p0;
-    for (int64_t t = t0; t < t1 && cur[0] + cur[1] + cur[2] + cur[3] < end[0] + end[1] + end[2] + end[3];) {
-      const int nu = t + 4 <= t1 ? 4 : 1;
-      int32_t v[4][PX];
-      if (nu == 4) {
+    const uint32_t goal = end[0] + end[1] + end[2] + end[3];
+    walk_frames<Tv, VEC>(
+        frames + t0 * npix + p0, npix, t0, t1, n_valid,
+        [&](const int32_t v[PX], int64_t t) {
+          const uint32_t rel = static_cast<uint32_t>(t - t0);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) load4<Tv, VEC>(src + u * npix, n_valid, v[u]);
-      } else {
-        load4<Tv, VEC>(src, n_valid, v[0]);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (u >= nu) break;
-        const uint32_t rel = static_cast<uint32_t>(t + u - t0);
-#pragma unroll
-        for (int j = 0; j < PX; ++j) {
-          if (v[u][j] > 0 && t + u < cut[j]) {
-            if (cur[j] < end[j]) {
-              const uint32_t w = (rel << 16) | (static_cast<uint32_t>(v[u][j]) & 0xFFFFu);
-              if (buffered)
-                buf[cur[j]] = w;
-              else
-                stage[base + cur[j]] = w;
-              ++cur[j];
-            } else {
-              bad = true;
+          for (int j = 0; j < PX; ++j) {
+            if (v[j] > 0 && t < cut[j]) {
+              if (cur[j] < end[j]) {
+                const uint32_t w = (rel << 16) | (static_cast<uint32_t>(v[j]) & 0xFFFFu);
+                if (buffered)
+                  buf[cur[j]] = w;
+                else
+                  stage[base + cur[j]] = w;
+                ++cur[j];
+              } else {
+                bad = true;
+              }
             }
           }
-        }
-      }
-      t += nu;
-      src += nu * npix;
-    }
+        },
+        [&] { return cur[0] + cur[1] + cur[2] + cur[3] < goal; });  // every event placed: stop reading
   }
   if (buffered && !skip) {
     __syncthreads();

@@ -536,8 +536,8 @@ __global__ void __launch_bounds__(256)
     gather_tiles_kernel(const uint32_t* __restrict__ stage, const uint32_t* __restrict__ tile_pos,
                         const uint16_t* __restrict__ sb_counts, int n_sb, int64_t npix, int64_t n_tiles,
                         const uint32_t* __restrict__ ev_off, int64_t n_elem, int sort, int buf_words,
-                        uint32_t* __restrict__ ev_words, int32_t* __restrict__ ev_times, Tv* __restrict__ ev_data,
-                        int32_t* __restrict__ err) {
+                        int warp_runs, uint32_t* __restrict__ ev_words, int32_t* __restrict__ ev_times,
+                        Tv* __restrict__ ev_data, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
   uint32_t* cp = sm;                       // [n_sb][TILE_P + 1] run starts within each chunk
   uint32_t* dst = cp + n_sb * (TILE_P + 1);  // [n_sb][TILE_P] run starts within the tile's lists
@@ -619,9 +619,13 @@ __global__ void __launch_bounds__(256)
   const bool buffered = total <= static_cast<uint32_t>(buf_words);
   uint32_t* out = buffered ? buf : (MODE == GATHER_REL_SPLIT ? reinterpret_cast<uint32_t*>(ev_times) : ev_words) + base;
   bool bad = false;
-  // a thread per (sub-block, pixel) run: a warp takes 32 consecutive pixels
-  // of one sub-block, whose runs are adjacent in the staging area
-  for (int e = threadIdx.x; e < n_sb * TILE_P; e += 256) {
+  // a thread per (sub-block, pixel) run (a warp takes 32 consecutive pixels
+  // of one sub-block, whose runs are adjacent in the staging area), or, with
+  // warp_runs (long runs), a warp per run with its lanes on consecutive words
+  const int r_first = warp_runs ? (threadIdx.x >> 5) : threadIdx.x;
+  const int r_step = warp_runs ? 256 / 32 : 256;
+  const uint32_t k0 = warp_runs ? (threadIdx.x & 31) : 0u, k_step = warp_runs ? 32u : 1u;
+  for (int e = r_first; e < n_sb * TILE_P; e += r_step) {
     const int b = e / TILE_P, p = e % TILE_P;
     if (p >= np) continue;
     const uint32_t c0 = cp[b * (TILE_P + 1) + p];
@@ -636,21 +640,16 @@ __global__ void __launch_bounds__(256)
     uint32_t* run = out + d0;
     const uint32_t* in = stage + src;
     if (MODE == GATHER_WORDS) {
-      uint32_t k = 0;
-      for (; k + UNROLL <= n; k += UNROLL) {
-        uint32_t v[UNROLL];
-#pragma unroll
-        for (int u = 0; u < UNROLL; ++u) v[u] = in[k + u];
-#pragma unroll
-        for (int u = 0; u < UNROLL; ++u) run[k + u] = v[u];
-      }
-      for (; k < n; ++k) run[k] = in[k];
+#pragma unroll 4
+      for (uint32_t k = k0; k < n; k += k_step) run[k] = in[k];
     } else if (MODE == GATHER_REL_WORDS) {
       const uint32_t add = static_cast<uint32_t>(b) << 26;  // (b * 1024) << 16
-      for (uint32_t k = 0; k < n; ++k) run[k] = in[k] + add;
+#pragma unroll 4
+      for (uint32_t k = k0; k < n; k += k_step) run[k] = in[k] + add;
     } else {
       const uint32_t t_add = static_cast<uint32_t>(b) * SUBBLOCK;
-      for (uint32_t k = 0; k < n; ++k) {
+#pragma unroll 4
+      for (uint32_t k = k0; k < n; k += k_step) {
         const uint32_t w = in[k];
         run[k] = t_add + (w >> 16);  // frame number
         if (buffered)
@@ -660,15 +659,19 @@ __global__ void __launch_bounds__(256)
       }
     }
     if (MODE == GATHER_WORDS && sort) {
-      for (uint32_t m = 1; m < n; ++m) {
-        const uint32_t w = run[m];
-        uint32_t j = m;
-        while (j > 0 && run[j - 1] > w) {
-          run[j] = run[j - 1];
-          --j;
+      if (warp_runs) __syncwarp();
+      if (k0 == 0) {
+        for (uint32_t m = 1; m < n; ++m) {
+          const uint32_t w = run[m];
+          uint32_t j = m;
+          while (j > 0 && run[j - 1] > w) {
+            run[j] = run[j - 1];
+            --j;
+          }
+          run[j] = w;
         }
-        run[j] = w;
       }
+      if (warp_runs) __syncwarp();
     }
   }
   if (buffered) {
@@ -988,6 +991,9 @@ extern "C" int g2_csr_count_blocked(const void* indices_dev, const void* indptr_
 namespace {
 // Words of the shared-memory buffer of a stage region or a gather tile: a
 // little above the mean (uniform data fits), between 1024 and 16384.
+// Warp per (sub-block, pixel) run in the gather when runs average 16 words or more.
+int warp_runs(int64_t n_elem, int64_t n_sb, int64_t npix) { return n_elem >= 16 * n_sb * npix ? 1 : 0; }
+
 int buffer_words(int64_t n_elem, int64_t units) {
   const int64_t mean = units > 0 ? n_elem / units : n_elem;
   const int64_t w = mean + mean / 16 + 512;
@@ -1043,12 +1049,13 @@ extern "C" int g2_csr_gather_blocked(const uint32_t* stage_dev, const uint32_t* 
   const int n_sb = static_cast<int>((static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK);
   const int64_t n_tiles = (npix + csr::TILE_P - 1) / csr::TILE_P;
   if (n_tiles > 0x7fffffff) return G2_ERR_TOO_LARGE;
-  const int buf = buffer_words(n_elem * csr::TILE_P, npix);
+  const int wr = warp_runs(n_elem, n_sb, npix);
+  const int buf = wr ? 0 : buffer_words(n_elem * csr::TILE_P, npix);
   const int64_t smem = (131ll * n_sb + 1 + buf) * 4;
   auto kernel = csr::gather_tiles_kernel<csr::GATHER_WORDS, uint8_t>;
   if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
   kernel<<<static_cast<unsigned>(n_tiles), 256, smem, as_stream(stream)>>>(
-      stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev, n_elem, sort ? 1 : 0, buf,
+      stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev, n_elem, sort ? 1 : 0, buf, wr,
       ev_words_dev, nullptr, nullptr, err_dev);
   return launch_status();
 }
@@ -1071,7 +1078,9 @@ extern "C" int g2_events_gather_rel(const uint32_t* stage_dev, const uint32_t* t
   const int64_t n_tiles = (npix + csr::TILE_P - 1) / csr::TILE_P;
   if (n_tiles > 0x7fffffff) return G2_ERR_TOO_LARGE;
   const int64_t tables = (131ll * n_sb + 1) * 4, per_word = words ? 4 : 6;
-  int64_t buf = buffer_words(n_elem * csr::TILE_P, npix);
+  const int wr = warp_runs(n_elem, n_sb, npix);
+  // long runs are copied by whole warps (coalesced): no tile buffer, more CTAs per SM
+  int64_t buf = wr ? 0 : buffer_words(n_elem * csr::TILE_P, npix);
   if (tables + buf * per_word > 227 * 1024) buf = (227 * 1024 - tables) / per_word;  // larger tiles go in place
   const int64_t smem = tables + buf * per_word;
   cudaStream_t st = as_stream(stream);
@@ -1080,19 +1089,19 @@ extern "C" int g2_events_gather_rel(const uint32_t* stage_dev, const uint32_t* t
     auto kernel = csr::gather_tiles_kernel<csr::GATHER_REL_WORDS, uint8_t>;
     if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
     kernel<<<grid, 256, smem, st>>>(stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev,
-                                    n_elem, 0, static_cast<int>(buf), ev_words_dev, nullptr, nullptr, err_dev);
+                                    n_elem, 0, static_cast<int>(buf), wr, ev_words_dev, nullptr, nullptr, err_dev);
   } else if (elem_bytes == 1) {
     auto kernel = csr::gather_tiles_kernel<csr::GATHER_REL_SPLIT, uint8_t>;
     if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
     kernel<<<grid, 256, smem, st>>>(stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev,
-                                    n_elem, 0, static_cast<int>(buf), nullptr, ev_times_dev,
+                                    n_elem, 0, static_cast<int>(buf), wr, nullptr, ev_times_dev,
                                     reinterpret_cast<uint8_t*>(ev_data_dev),
                                     err_dev);
   } else {
     auto kernel = csr::gather_tiles_kernel<csr::GATHER_REL_SPLIT, uint16_t>;
     if (!allow_smem(kernel, smem)) return G2_ERR_CUDA;
     kernel<<<grid, 256, smem, st>>>(stage_dev, tile_pos_dev, sb_counts_dev, n_sb, npix, n_tiles, ev_offsets_dev,
-                                    n_elem, 0, static_cast<int>(buf), nullptr, ev_times_dev,
+                                    n_elem, 0, static_cast<int>(buf), wr, nullptr, ev_times_dev,
                                     reinterpret_cast<uint16_t*>(ev_data_dev),
                                     err_dev);
   }
