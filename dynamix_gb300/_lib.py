@@ -57,6 +57,8 @@ SIGNATURES = {
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
     "g2_gram_std": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p, _p, _p, _i64, _p, _i32, _p]),
     "g2_std_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
+    "g2_gram_ttcf": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _i64, _i32, _p, _i32, _p]),
+    "g2_ttcf_finish": (C.c_int, [_p, _i64, _i64, _p, _i32, _p]),
     "g2_event_pairsum": (C.c_int, [_p, _p, _i32, _i64, _p, _i64, _p, _p, _p, _i32, _p, _i32, _i32, _i32, _i32, _p,
                                    _p, _p, _p]),
     "g2_event_pairsum_packed": (C.c_int, [_p, _i64, _p, _i64, _p, _p, _p, _i32, _p, _i32, _i32, _i32, _i32, _p,

@@ -68,6 +68,16 @@ class _DenseBase(BaseCorrelator):
             return CorrelationResult(res, dev)
         return res
 
+    def two_time(self, q):
+        """Two-time correlation of q bin ``q`` (1-based, the ``ttcf_par`` of
+        event_y.py:104-161) for the last :meth:`correlate` call, float32
+        ``(nframes, nframes)``: P G(t,t') / (S(t) S(t')) off the diagonal,
+        the mean of the positive elements of the first upper diagonal on it
+        (event_y.py:148-157).  Computed on the tensor cores from the last
+        call's packed frames."""
+        out = self.engine.two_time(int(q) - 1).cpu().numpy()
+        return out
+
     # exact intermediate results of the last call (int64 / float64 numpy)
     @property
     def numerator(self):

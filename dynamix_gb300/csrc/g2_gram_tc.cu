@@ -58,13 +58,25 @@ constexpr int SMEM_BYTES_STD = 1024 + SMEM_BAR_OFF + 256 + 2 * STD_WORDS * 4;
 // t' >= t of one bin, r = P G(t,t') / (S(t) S(t')) and d = r - centre(tau);
 // the lag sums of d and d^2 (float per block, double in memory) and the count
 // of pairs with S(t) S(t') = 0.
+// The two-time mode (the TTCF of event_y.py:148-157) writes the same r for
+// every pair t' > t of one bin into a row-major matrix (row stride ld), and
+// its mirror (t', t) when `mirror` is set.
 struct StdOut {
   const long long* S;      // bin sums, indexed by item.s_off + t
   const float* centre;     // per lag, indexed by item.out_off + tau
   double* sum_d;           // indexed by item.out_off + tau
   double* sum_d2;
   unsigned int* zeros;
+  float* ttcf;             // two-time mode: [n][ld]
+  int64_t ld;
+  int64_t n;
+  int mirror;
 };
+
+// Epilogue modes of the Gram kernel.
+constexpr int MODE_NUMER = 0;  // lag sums of G (the numerator)
+constexpr int MODE_STD = 1;    // deviation of the per-pair ratio (calc_std)
+constexpr int MODE_TTCF = 2;   // per-pair ratio written as the two-time matrix
 
 struct MapsParam {
   CUtensorMap a[G2_MAX_JOBS];
@@ -93,9 +105,11 @@ __device__ __forceinline__ bool named_bar_any(uint32_t id, uint32_t n, bool v) {
 // them consistently (the epilogue records G2_DEVERR_BOUNDS).
 // In the deviation mode ``shift`` carries the bin's pixel count and ``s_off``
 // the offset of its sums.
-template <bool STD>
+template <int MODE>
 __device__ __forceinline__ bool item_ok(const g2_gram_item& w, const MapsParam& maps, int n_jobs,
-                                        int64_t numer_len, int64_t sums_len) {
+                                        int64_t numer_len, int64_t sums_len, int64_t max_frames) {
+  constexpr bool STD = MODE != MODE_NUMER;
+  if (MODE == MODE_TTCF && w.nframes > max_frames) return false;
   if (w.job < 0 || w.job >= n_jobs) return false;
   const int bk = stage_elems(maps.kind[w.job]);
   const bool shape = w.k_len > 0 && (w.k_len % bk) == 0 && (w.a_k0 % bk) == 0 && (w.b_k0 % bk) == 0 &&
@@ -105,7 +119,7 @@ __device__ __forceinline__ bool item_ok(const g2_gram_item& w, const MapsParam& 
          (w.s_off < 0 || (maps.ones[w.job] && w.shift == 0 && w.s_off + w.nframes <= sums_len));
 }
 
-template <bool STD>
+template <int MODE>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     gram_tc_kernel(const __grid_constant__ MapsParam maps, int n_jobs, const g2_gram_item* __restrict__ items,
                    int64_t n_items, unsigned long long* __restrict__ numer, int64_t numer_len,
@@ -140,6 +154,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     *abort_flag = 0;
     fence_mbar_init();
   }
+  constexpr bool STD = MODE != MODE_NUMER;
   for (int i = threadIdx.x; i < (STD ? 2 * STD_WORDS : 2 * NDIAG_PAD); i += NUM_THREADS) diag[i] = 0;
   if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
   tc_fence_before();
@@ -156,7 +171,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok<STD>(w, maps, n_jobs, numer_len, sums_len)) continue;
+        if (!item_ok<MODE>(w, maps, n_jobs, numer_len, sums_len, so.n)) continue;
         const CUtensorMap* ma = &maps.a[w.job];
         const CUtensorMap* mb = &maps.b[w.job];
         const int bk = stage_elems(maps.kind[w.job]);
@@ -194,7 +209,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
-        if (!item_ok<STD>(w, maps, n_jobs, numer_len, sums_len)) continue;
+        if (!item_ok<MODE>(w, maps, n_jobs, numer_len, sums_len, so.n)) continue;
         const bool fp8 = maps.kind[w.job] == G2_KIND_E4M3;
         const int buf = static_cast<int>(local & 1);
         const uint32_t ap = static_cast<uint32_t>((local >> 1) & 1);
@@ -244,7 +259,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     int64_t local = 0;
     for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x, ++local) {
       const g2_gram_item w = items[it];
-      if (!item_ok<STD>(w, maps, n_jobs, numer_len, sums_len)) {
+      if (!item_ok<MODE>(w, maps, n_jobs, numer_len, sums_len, so.n)) {
         if (etid == 0) atomicOr(err, G2_DEVERR_BOUNDS);
         --local;
         continue;
@@ -265,7 +280,34 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const bool row_live = w.i0 + row < w.nframes;
       const int col_end = min(BN, w.nframes - w.j0);                // columns < col_end are frames
       const int lag0 = w.j0 - w.i0 - (BM - 1);
-      if (STD) {
+      if (MODE == MODE_TTCF) {
+        // ---------------------------------------- two-time mode epilogue
+        const float P = static_cast<float>(w.shift);
+        const int64_t t = static_cast<int64_t>(w.i0) + row;
+        const float St = row_live ? static_cast<float>(so.S[w.s_off + t]) : 0.0f;
+#pragma unroll 1
+        for (int cc = 0; cc < BN / 32; ++cc) {
+          uint32_t v[32];
+          __syncwarp();
+          tmem_ld_32x32b_x32(tbase + static_cast<uint32_t>(cc * 32), v);
+          tmem_wait_ld();
+          if (!row_live) continue;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int c = cc * 32 + j;
+            const int64_t t2 = static_cast<int64_t>(w.j0) + c;
+            if (c >= col_end || t2 <= t) continue;  // t' >= T, or not above the diagonal
+            const float den = St * static_cast<float>(so.S[w.s_off + t2]);
+            const float r = P * (__uint_as_float(v[j]) * unscale) / den;  // 0/0 -> NaN as in the reference
+            so.ttcf[t * so.ld + t2] = r;
+            if (so.mirror) so.ttcf[t2 * so.ld + t] = r;
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&acce[buf]);
+        continue;
+      }
+      if (MODE == MODE_STD) {
         // ---------------------------------------- deviation mode epilogue
         float* cen = reinterpret_cast<float*>(diag) + (local & 1) * STD_WORDS;
         float* sd = cen + NDIAG_PAD;
@@ -364,7 +406,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 }  // namespace g2
 
 namespace {
-template <bool STD>
+template <int MODE>
 int launch_gram(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
                 uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len, int32_t* err_dev,
                 int32_t grid, void* stream, const g2::tc::StdOut& so) {
@@ -392,15 +434,15 @@ int launch_gram(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_de
     maps.kind[j] = jobs[j].elem_kind;
     maps.ones[j] = jobs[j].ones_row;
   }
-  const int smem = STD ? tc::SMEM_BYTES_STD : tc::SMEM_BYTES;
-  if (cudaFuncSetAttribute(tc::gram_tc_kernel<STD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+  const int smem = MODE != tc::MODE_NUMER ? tc::SMEM_BYTES_STD : tc::SMEM_BYTES;
+  if (cudaFuncSetAttribute(tc::gram_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
       cudaSuccess)
     return G2_ERR_CUDA;
   int sms = sm_count_current();
   if (sms <= 0) return G2_ERR_CUDA;
   int64_t g = grid > 0 ? grid : sms;
   if (g > n_items) g = n_items;
-  tc::gram_tc_kernel<STD><<<static_cast<unsigned>(g), tc::NUM_THREADS, smem, as_stream(stream)>>>(
+  tc::gram_tc_kernel<MODE><<<static_cast<unsigned>(g), tc::NUM_THREADS, smem, as_stream(stream)>>>(
       maps, n_jobs, items_dev, n_items, reinterpret_cast<unsigned long long*>(numer_dev), numer_len,
       reinterpret_cast<unsigned long long*>(sums_dev), sums_len, err_dev, so);
   return launch_status();
@@ -415,8 +457,8 @@ extern "C" int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item
       sums_len < 0 || (sums_len > 0 && !sums_dev))
     return G2_ERR_ARG;
   if (n_items > 0 && !items_dev) return G2_ERR_ARG;
-  const tc::StdOut none = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  return launch_gram<false>(jobs, n_jobs, items_dev, n_items, numer_dev, numer_len, sums_dev, sums_len, err_dev,
+  const tc::StdOut none = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0};
+  return launch_gram<tc::MODE_NUMER>(jobs, n_jobs, items_dev, n_items, numer_dev, numer_len, sums_dev, sums_len, err_dev,
                             grid, stream, none);
 }
 
@@ -430,10 +472,101 @@ extern "C" int g2_gram_std(const g2_job* jobs, int32_t n_jobs, const g2_gram_ite
     return G2_ERR_ARG;
   if (n_items > 0 && !items_dev) return G2_ERR_ARG;
   const tc::StdOut so = {reinterpret_cast<const long long*>(sums_dev), centre_dev, sum_d_dev, sum_d2_dev,
-                         zeros_dev};
+                         zeros_dev, nullptr, 0, 0, 0};
   // out_len bounds out_off + tau, sums_len bounds s_off + t; numer and sums
   // are not written in this mode
-  return launch_gram<true>(jobs, n_jobs, items_dev, n_items, reinterpret_cast<uint64_t*>(sum_d_dev), out_len,
+  return launch_gram<tc::MODE_STD>(jobs, n_jobs, items_dev, n_items, reinterpret_cast<uint64_t*>(sum_d_dev), out_len,
                            reinterpret_cast<uint64_t*>(const_cast<int64_t*>(sums_dev)), sums_len, err_dev, grid,
                            stream, so);
+}
+
+namespace g2 {
+namespace tc {
+// Below the diagonal when the matrix is not mirrored: 0 where S(t) S(t') != 0,
+// NaN where it is 0 (the reference's 0 * P / (S S) there).
+__global__ void __launch_bounds__(256)
+    ttcf_lower_kernel(float* __restrict__ out, int64_t n, int64_t ld, const long long* __restrict__ S) {
+  for (int64_t t = blockIdx.x; t < n; t += gridDim.x) {
+    const long long st = S[t];
+    for (int64_t t2 = threadIdx.x; t2 < t; t2 += blockDim.x)
+      out[t * ld + t2] = (st != 0 && S[t2] != 0) ? 0.0f : __int_as_float(0x7fc00000);
+  }
+}
+
+// The diagonal: every element but the last is the mean of the positive
+// elements of the first upper diagonal (NaN when there are none); the last is
+// 0, or NaN when S(T - 1) = 0.
+__global__ void __launch_bounds__(1024)
+    ttcf_diag_kernel(float* __restrict__ out, int64_t n, int64_t ld, const long long* __restrict__ S) {
+  __shared__ double s_sum[32];
+  __shared__ unsigned long long s_cnt[32];
+  double sum = 0.0;
+  unsigned long long cnt = 0;
+  for (int64_t j = threadIdx.x; j + 1 < n; j += blockDim.x) {
+    const float x = out[j * ld + j + 1];
+    if (x > 0.0f) {
+      sum += x;
+      ++cnt;
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    s_sum[warp] = sum;
+    s_cnt[warp] = cnt;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    sum = lane < (blockDim.x >> 5) ? s_sum[lane] : 0.0;
+    cnt = lane < (blockDim.x >> 5) ? s_cnt[lane] : 0ull;
+    for (int o = 16; o; o >>= 1) {
+      sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0) {
+      s_sum[0] = sum;
+      s_cnt[0] = cnt;
+    }
+  }
+  __syncthreads();
+  const float mean = s_cnt[0] ? static_cast<float>(s_sum[0] / static_cast<double>(s_cnt[0]))
+                              : __int_as_float(0x7fc00000);
+  for (int64_t j = threadIdx.x; j + 1 < n; j += blockDim.x) out[j * ld + j] = mean;
+  if (threadIdx.x == 0) out[(n - 1) * ld + (n - 1)] = S[n - 1] != 0 ? 0.0f : __int_as_float(0x7fc00000);
+}
+}  // namespace tc
+}  // namespace g2
+
+extern "C" int g2_gram_ttcf(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                            const int64_t* sums_dev, int64_t sums_len, float* ttcf_dev, int64_t nframes, int64_t ld,
+                            int32_t mirror, int32_t* err_dev, int32_t grid, void* stream) {
+  using namespace g2;
+  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !sums_dev || sums_len <= 0 || !ttcf_dev ||
+      nframes <= 0 || ld < nframes || !err_dev)
+    return G2_ERR_ARG;
+  if (n_items > 0 && !items_dev) return G2_ERR_ARG;
+  const tc::StdOut so = {reinterpret_cast<const long long*>(sums_dev), nullptr, nullptr, nullptr, nullptr,
+                         ttcf_dev, ld, nframes, mirror ? 1 : 0};
+  // items address S through s_off (bounded by sums_len) and may not have more
+  // frames than the matrix; numer is not written in this mode
+  return launch_gram<tc::MODE_TTCF>(jobs, n_jobs, items_dev, n_items, nullptr, sums_len,
+                                    reinterpret_cast<uint64_t*>(const_cast<int64_t*>(sums_dev)), sums_len, err_dev,
+                                    grid, stream, so);
+}
+
+extern "C" int g2_ttcf_finish(float* ttcf_dev, int64_t nframes, int64_t ld, const int64_t* bin_sums_dev,
+                              int32_t mirror, void* stream) {
+  using namespace g2;
+  if (!ttcf_dev || !bin_sums_dev || nframes <= 0 || ld < nframes) return G2_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  const long long* S = reinterpret_cast<const long long*>(bin_sums_dev);
+  if (!mirror) {
+    const int64_t blocks = nframes < 65536 ? nframes : 65536;
+    tc::ttcf_lower_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(ttcf_dev, nframes, ld, S);
+  }
+  tc::ttcf_diag_kernel<<<1, 1024, 0, st>>>(ttcf_dev, nframes, ld, S);
+  return launch_status();
 }

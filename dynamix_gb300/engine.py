@@ -554,6 +554,48 @@ class DenseEngine:
         self.dev_f64 = d64
         return d32[: self.n_bins]
 
+    def two_time(self, b):
+        """Two-time correlation of bin ``b`` (0-based) for the last run: the
+        TTCF of event_y.py:141-157, float32 device tensor ``(T, T)``:
+        P G(t,t') / (S(t) S(t')) off the diagonal (mirrored when the
+        reference mirrors it), the mean of the first upper diagonal's
+        positive elements on the diagonal.  One more tensor-core pass over the
+        bin's part of the last run's packed operand."""
+        torch = _torch()
+        if self.method != "tc":
+            raise NotImplementedError("the two-time correlation runs on the tensor-core path")
+        L = self._layouts.get(self._packed_mode)
+        if L is None or self.packed is None:
+            raise RuntimeError("two_time() needs a preceding run()")
+        if L.split:
+            raise NotImplementedError("the two-time correlation needs counts <= 2048 (no byte planes)")
+        if not 0 <= b < self.n_bins:
+            raise ValueError("bin %d outside [0, %d)" % (b, self.n_bins))
+        key = ("std", L.mode, self.T)
+        if key not in self._items_cache:
+            from .plan import std_items
+            npix = np.bincount(self.qmask.ravel()[self.qmask.ravel() > 0], minlength=self.n_bins + 1)[1:]
+            items = std_items(self.T, L, npix)
+            self._items_cache[key] = (items, torch.from_numpy(items.view(np.uint8).copy()).to(self.dev))
+        items = self._items_cache[key][0]
+        mine = items[items["out_off"] == b * self.T]
+        if mine.size == 0:
+            raise ValueError("bin %d has no pixels" % (b + 1))
+        items_dev = torch.from_numpy(mine.view(np.uint8).copy()).to(self.dev)
+        S = self.sums[b * self.T:(b + 1) * self.T] if self.sums.dim() == 1 else self.sums[b]
+        s_h = S.cpu().numpy().astype(np.float64)
+        # the reference mirrors when its diagonal k = -5 (0 or NaN = 0/0) sums below 1
+        mirror = 1 if self.T <= 5 or not np.any(s_h[:-5] * s_h[5:] == 0) else 0
+        out = torch.empty((self.T, self.T), dtype=torch.float32, device=self.dev)
+        st = stream_handle(self.dev)
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, L.ones_row)])
+        _lib.check(self.lib.g2_gram_ttcf(jobs, 1, ptr(items_dev), mine.size, ptr(self.sums), self.sums.numel(),
+                                         ptr(out), self.T, self.T, mirror, ptr(self.err), self.grid, st),
+                   "g2_gram_ttcf")
+        _lib.check(self.lib.g2_ttcf_finish(ptr(out), self.T, self.T, ptr(S), mirror, st), "g2_ttcf_finish")
+        self.check_error()
+        return out
+
     def check_denominator_range(self):
         """Raise if int64 D could have overflowed (checked from S on the host)."""
         S = self.sums[: self.n_bins].cpu().numpy()

@@ -343,6 +343,24 @@ int g2_gram_std(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_de
 int g2_std_finalize(const double* sum_d_dev, const double* sum_d2_dev, const uint32_t* zeros_dev, int32_t n_rows,
                     int64_t nframes, float* dev_f32, double* dev_f64, void* stream);
 
+/* ---- two-time correlation (the TTCF of event_y.py:141-157) ---------------
+ * g2_gram_ttcf runs the Gram tiles of one bin's items (built as for
+ * g2_gram_std: whole K, shift = the bin's pixel count P, s_off = the offset of
+ * its sums) and writes r = P G(t,t') / (S(t) S(t')) for every pair t' > t as
+ * float32 into ttcf_dev[t * ld + t'] and, with mirror != 0, into
+ * ttcf_dev[t' * ld + t] (0/0 gives NaN, as in the reference); items with more
+ * frames than nframes are skipped (G2_DEVERR_BOUNDS).  g2_ttcf_finish
+ * completes the matrix as the reference does: without mirror, 0 below the
+ * diagonal (NaN where S(t) S(t') = 0); on the diagonal the mean of the
+ * positive elements of the first upper diagonal (NaN when there are none),
+ * except the last element: 0, or NaN when S(T-1) = 0.  The reference mirrors
+ * when its diagonal k = -5 sums below 1: when no S(t) S(t+5) is 0, or T <= 5. */
+int g2_gram_ttcf(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                 const int64_t* sums_dev, int64_t sums_len, float* ttcf_dev, int64_t nframes, int64_t ld,
+                 int32_t mirror, int32_t* err_dev, int32_t grid, void* stream);
+int g2_ttcf_finish(float* ttcf_dev, int64_t nframes, int64_t ld, const int64_t* bin_sums_dev, int32_t mirror,
+                   void* stream);
+
 /* ---- G3: denominator ----------------------------------------------------
  * Replaces correlate_1D (dynamix/resources/opencl/densecorrelator.cl:156-176),
  * the denominator loop of normalize_correlation (evtcorrelator.cl:70-73) and

@@ -380,3 +380,28 @@ def reference_event_correlate(vol_times, vol_data, offsets, qmask, shape, nframe
     if rc:
         raise ValueError("g2r_event_correlate failed with status %d" % rc)
     return {"res_int": res_int, "sums": sums, "g2": res}
+
+
+def ttcf_exact(frames, qmask, q):
+    """Two-time correlation of bin ``q`` (1-based) restated from
+    ``correlator/event_y.py:141-157`` (with ``ncorrelatepm``, :72-98, for the
+    pair sums): cc(t, t') = sum over the bin's pixels of I(t) I(t') for
+    t' > t, s(t) the bin's frame sums, trc = (cc P / T) / (s s^T / T);
+    mirrored (trc + trc^T) when its diagonal k = -5 sums below 1; the diagonal
+    set to the mean of the positive elements of the first upper diagonal,
+    except its last element.  float64."""
+    T = frames.shape[0]
+    x = frames.reshape(T, -1)[:, np.asarray(qmask).ravel() == q].astype(np.float64)
+    P = x.shape[1]
+    cc = np.triu(x @ x.T, 1)
+    s = x.sum(axis=1).reshape(T, 1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        norm = (s @ s.T) / T
+        trc = (cc * P / T) / norm
+        if np.sum(np.diag(trc, k=-5)) < 1:
+            trc = trc + trc.T
+        tmp = np.diag(trc, k=1)
+        tmp = np.mean(tmp[tmp > 0]) if np.any(tmp > 0) else np.nan
+    for j in range(T - 1):
+        trc[j, j] = tmp
+    return trc
