@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--frames", type=int, default=None, help="override T (testing only)")
+    p.add_argument("--shape", default=None, help="H,W of the sparse/event frames (profiling only)")
     p.add_argument("--workload", default="dense", choices=["dense", "u16", "sparse", "event", "serving", "compress"],
                    help="dense: 514x1030x10k u8 Gram path (default); sparse / event: 2162x2068x20k CSR or "
                         "per-pixel event lists through the pair-sum path")
@@ -77,13 +78,14 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profile_traffic(name):
+def profile_traffic(name, key="traffic_bytes_per_launch"):
     """Per-launch DRAM bytes of a kernel from a committed ncu summary (or None)."""
     path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
-            if line.strip().startswith("traffic_bytes_per_launch"):
-                return float(line.split("=")[1].split()[0])
+            parts = line.split("=")
+            if len(parts) >= 2 and parts[0].strip() == key:
+                return float(parts[1].split()[0])
     except OSError:
         pass
     return None
@@ -376,10 +378,22 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------- sparse / event
-def make_sparse_workload(dev, T):
+def sparse_shape(args):
+    """Frame shape of the sparse/event workloads: the headline shape, or a
+    smaller one given with --shape (profiling at the same density)."""
+    if getattr(args, "shape", None):
+        h, w = (int(x) for x in args.shape.split(","))
+        return h, w
+    return tuple(SPARSE_WORKLOAD["frame_shape"])
+
+
+def make_sparse_workload(dev, T, shape=None):
     from dynamix_gb300.speckle import annular_qmask, speckle_csr_torch
-    H, W = SPARSE_WORKLOAD["frame_shape"]
-    qmask = annular_qmask((H, W), SPARSE_WORKLOAD["n_bins"], 20.0, 1000.0, center=(1081, 1034))
+    H, W = shape or SPARSE_WORKLOAD["frame_shape"]
+    if (H, W) == tuple(SPARSE_WORKLOAD["frame_shape"]):
+        qmask = annular_qmask((H, W), SPARSE_WORKLOAD["n_bins"], 20.0, 1000.0, center=(1081, 1034))
+    else:  # the same number of annuli over the smaller frame
+        qmask = annular_qmask((H, W), SPARSE_WORKLOAD["n_bins"], 10.0, min(H, W) / 2 - 2, center=(H // 2, W // 2))
     csr = speckle_csr_torch(T, (H, W), SPARSE_WORKLOAD["rho"], SPARSE_WORKLOAD["mean_photons"],
                             seed=SPARSE_WORKLOAD["seed"], device=dev)
     return csr, qmask
@@ -423,8 +437,8 @@ def run_sparse(args):
         dist.init_process_group("nccl", device_id=dev)
     b.build(force=False)
     T = args.frames
-    H, W = SPARSE_WORKLOAD["frame_shape"]
-    (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T)
+    H, W = sparse_shape(args)
+    (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T, (H, W))
     offsets = offsets.to(torch.int32)              # one index type (int32) for the whole CSR stack
     sc = SparseCorrelator((H, W), T, qmask=qmask)
     ev_times, ev_data, ev_off = (x.clone() for x in sc.engine.to_events(data, indices, indptr, offsets, 4,
@@ -505,7 +519,7 @@ def run_sparse(args):
         stage_report["transpose"] = {"ms": tms, "GB_per_s": transpose_bytes / (tms / 1e3) / 1e9,
                                      "bytes": transpose_bytes, "kernels": "count, scan (3), scatter"}
         launches += 5
-    cfg = dict(SPARSE_WORKLOAD, nframes=T, workload=SPARSE_WORKLOAD["workload"].replace(
+    cfg = dict(SPARSE_WORKLOAD, nframes=T, frame_shape=[H, W], workload=SPARSE_WORKLOAD["workload"].replace(
         "sparse", "sparse_csr" if args.workload == "sparse" else "event_lists"),
         parallelism="replicas" if world > 1 else "single", n_elements=n_elem,
         binned_pixels=P_b, binned_events=n_binned_events, pair_ops=pairs)
@@ -515,7 +529,10 @@ def run_sparse(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
         "hbm_GB_per_s_step": step_bytes / (ms / 1e3) / 1e9,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": profile_traffic("event_pairsum_2162x2068_T20000.md"), "kernel": "g2_event_pairsum",
+                     "traffic": profile_traffic("event_pairsum_2162x2068_T20000.md",
+                                                "traffic_bytes_per_launch" if args.workload == "event"
+                                                else "traffic_bytes_per_launch_packed"),
+                     "kernel": "g2_event_pairsum",
                      "peak_source": "%s hbm_gbs" % peak_kind, "algorithmic_bytes_per_launch": pair_bytes,
                      "launch_ms": pair_ms,
                      "note": "bound by shared-memory atomics (one per event pair), not by HBM"},
@@ -565,13 +582,13 @@ def run_sparse_reference(args):
     if rank != 0:
         return 0
     T = args.frames
-    H, W = SPARSE_WORKLOAD["frame_shape"]
+    H, W = sparse_shape(args)
     dev = torch.device("cuda", local)
     from dynamix_gb300 import build as b
     from dynamix_gb300.correlator import SparseCorrelator
     b.build(force=False)
     # the CSR stack is generated on the device and turned into event lists there
-    (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T)
+    (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T, (H, W))
     offsets = offsets.to(torch.int32)
     sc = SparseCorrelator((H, W), T, qmask=qmask)
     t_h, d_h, o_h = (x.cpu().numpy() for x in sc.engine.to_events(data, indices, indptr, offsets, 4,
