@@ -29,6 +29,7 @@ namespace ev {
 constexpr int THREADS = 768;
 constexpr int WARPS = THREADS / 32;
 constexpr int EV = 128;                    // events of one pixel staged per block of pairs
+constexpr int ROWS = 8;                    // rows of the pair block walked together
 constexpr uint32_t DRAIN = 1u << 31;
 constexpr int SMEM_FIXED = WARPS * 2 * EV * 4;
 constexpr int SMEM_STATIC = WARPS * 8;    // block-reduction slots
@@ -95,19 +96,35 @@ __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, c
         __syncwarp();
         B = bufB;
       }
-      for (int i = 0; i < na; ++i) {
-        const uint32_t wi = bufA[i];
-        const uint32_t vi = wi & 0xFFFFu;
-        if (vi == 0) continue;  // warp-uniform
-        const int ti = static_cast<int>(wi >> 16);
-        for (int j = (jb == ib ? i : 0) + lane; j < nb; j += 32) {
+      // ROWS rows (i .. i + ROWS - 1) per pass: each partner word read from
+      // shared memory serves ROWS pairs, and the row overhead is paid once
+      // per ROWS rows.  Absent rows and pairs below the diagonal get a zero
+      // product, whose unconditional add changes nothing.
+      const bool tri = jb == ib;
+      for (int i = 0; i < na; i += ROWS) {
+        uint32_t vi[ROWS];
+        int ti[ROWS];
+        uint32_t any = 0;
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+          const uint32_t w = i + r < na ? bufA[i + r] : 0u;
+          vi[r] = w & 0xFFFFu;
+          ti[r] = static_cast<int>(w >> 16);
+          any |= vi[r];
+        }
+        if (any == 0) continue;  // warp-uniform
+        for (int j = (tri ? i : 0) + lane; j < nb; j += 32) {
           const uint32_t wj = B[j];
-          const int lag = abs(static_cast<int>(wj >> 16) - ti);
-          const uint32_t prod = vi * (wj & 0xFFFFu);
-          if (FAST) {
-            atomicAdd(&hist[lag], prod);  // a zero product (invalid event) adds nothing
-          } else if (prod) {
-            add_counter(&hist[lag], &gN[lag], prod);
+          const int tj = static_cast<int>(wj >> 16);
+          const uint32_t vj = wj & 0xFFFFu;
+#pragma unroll
+          for (int r = 0; r < ROWS; ++r) {
+            const uint32_t prod = (!tri || j >= i + r) ? vi[r] * vj : 0u;  // the diagonal block takes j >= i + r
+            const int lag = abs(tj - ti[r]);
+            if (FAST)
+              atomicAdd(&hist[lag], prod);
+            else if (prod)
+              add_counter(&hist[lag], &gN[lag], prod);
           }
         }
       }
