@@ -1,10 +1,11 @@
 // G3 (denominator) and G4 (finalize).
 //
 // G3: D[r][tau] = sum_t S[r][t] * S[r][t+tau] in int64 for every row r (one row
-// per (job, bin)).  A block owns 1024 lags of one row (4 per thread, strided by
-// the block size so the shared loads stay conflict-free) and walks t in
-// shared-memory windows of 1024 frames; the shifted window is padded with
-// zeros beyond T, so no per-term bounds test is needed.
+// per (job, bin)).  A block owns 1024 lags of one row (4 consecutive per
+// thread) and walks t in shared-memory windows of 1024 frames; the shifted
+// window is padded with zeros beyond T, so no per-term bounds test is needed,
+// and stored with one pad word per 32 so the threads' 4-word stride stays
+// free of bank conflicts.
 // Replaces correlate_1D (densecorrelator.cl:156-176), the sum loop of
 // normalize_correlation (evtcorrelator.cl:70-73) and the mean outer product
 // of py_dense_correlator (dense.py:55, :63).
@@ -24,44 +25,82 @@ constexpr int LPT = 4;               // lags per thread, strided by THR
 constexpr int LAGS = THR * LPT;      // lags per block
 constexpr int WIN = 1024;            // frames per shared window
 
-// S values are split into 32-bit halves in shared memory.  Windows whose
+// S values are split into 32-bit halves in shared memory.  A window whose
+// largest value m gives m^2 * (terms) < 2^32 accumulates in 32 bits (one
+// 64-bit add per lag at its end).  Otherwise, windows whose
 // values all fit in 32 bits (the usual case: a bin sum is at most
 // pixels x max count) take one 32 x 32 -> 64-bit multiply-add per term;
 // others add the cross terms too (arithmetic mod 2^64, exact while D < 2^63,
 // which the host checks).
+// Padded index of the shifted window: one pad word per 32, so lanes 4 words
+// apart (a thread's 4 consecutive lags) fall on distinct banks.
+__device__ __forceinline__ int pad32(int x) { return x + (x >> 5); }
+constexpr int WIN2_PAD = WIN + LAGS + (WIN + LAGS) / 32;
+
 __global__ void __launch_bounds__(THR)
     denom_kernel(const long long* __restrict__ S, int64_t T, long long* __restrict__ D) {
   __shared__ uint32_t lo1[WIN], hi1[WIN];
-  __shared__ uint32_t lo2[WIN + LAGS], hi2[WIN + LAGS];
+  __shared__ uint32_t lo2[WIN2_PAD], hi2[WIN2_PAD];
+  __shared__ uint32_t s_wmax[THR / 32];
   const int64_t r = blockIdx.y;
   const int64_t tau0 = static_cast<int64_t>(blockIdx.x) * LAGS;
   const long long* row = S + r * T;
+  const int l0 = LPT * threadIdx.x;  // this thread's lags: tau0 + l0 + k
   unsigned long long acc[LPT] = {0, 0, 0, 0};
   // split z of gridDim.z takes every gridDim.z-th window of frames
   for (int64_t t0 = static_cast<int64_t>(blockIdx.z) * WIN; t0 < T - tau0;
        t0 += static_cast<int64_t>(gridDim.z) * WIN) {
     bool wide = false;
+    uint32_t vmax = 0;
     for (int i = threadIdx.x; i < WIN; i += THR) {
       const int64_t t = t0 + i;
       const unsigned long long v = t < T ? static_cast<unsigned long long>(row[t]) : 0ull;
       lo1[i] = static_cast<uint32_t>(v);
       hi1[i] = static_cast<uint32_t>(v >> 32);
       wide |= (v >> 32) != 0;
+      vmax = max(vmax, static_cast<uint32_t>(v));
     }
     for (int i = threadIdx.x; i < WIN + LAGS; i += THR) {
       const int64_t t = t0 + tau0 + i;
       const unsigned long long v = t < T ? static_cast<unsigned long long>(row[t]) : 0ull;
-      lo2[i] = static_cast<uint32_t>(v);
-      hi2[i] = static_cast<uint32_t>(v >> 32);
+      lo2[pad32(i)] = static_cast<uint32_t>(v);
+      hi2[pad32(i)] = static_cast<uint32_t>(v >> 32);
       wide |= (v >> 32) != 0;
+      vmax = max(vmax, static_cast<uint32_t>(v));
     }
+    vmax = __reduce_max_sync(0xffffffffu, vmax);
+    if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = vmax;  // read after the barrier below
     const int n = static_cast<int>(T - tau0 - t0 < WIN ? T - tau0 - t0 : WIN);  // terms with t + tau0 < T
-    if (__syncthreads_or(wide)) {
+    const bool any_wide = __syncthreads_or(wide);
+    uint32_t wmax = 0;
+#pragma unroll
+    for (int w = 0; w < THR / 32; ++w) wmax = max(wmax, s_wmax[w]);
+    if (!any_wide && static_cast<unsigned long long>(wmax) * wmax * static_cast<unsigned long long>(n) < (1ull << 32)) {
+      // every term of the window and their sum fit 32 bits: 32-bit
+      // multiply-adds, one 64-bit add per lag at the end of the window; the
+      // shifted values b[k] = S(t + tau0 + l0 + k) slide along in registers,
+      // one shared load per four multiply-adds
+      uint32_t part[LPT] = {0, 0, 0, 0};
+      uint32_t bv[LPT];
+#pragma unroll
+      for (int k = 0; k < LPT - 1; ++k) bv[k + 1] = lo2[pad32(l0 + k)];
+#pragma unroll 4
+      for (int i = 0; i < n; ++i) {
+        const uint32_t a = lo1[i];
+#pragma unroll
+        for (int k = 0; k < LPT - 1; ++k) bv[k] = bv[k + 1];
+        bv[LPT - 1] = lo2[pad32(i + l0 + LPT - 1)];
+#pragma unroll
+        for (int k = 0; k < LPT; ++k) part[k] += a * bv[k];
+      }
+#pragma unroll
+      for (int k = 0; k < LPT; ++k) acc[k] += part[k];
+    } else if (any_wide) {
       for (int i = 0; i < n; ++i) {
         const unsigned long long a_lo = lo1[i], a_hi = hi1[i];
 #pragma unroll
         for (int k = 0; k < LPT; ++k) {
-          const int j = i + threadIdx.x + k * THR;
+          const int j = pad32(i + l0 + k);
           acc[k] += a_lo * lo2[j] + ((a_hi * lo2[j] + a_lo * hi2[j]) << 32);
         }
       }
@@ -70,14 +109,14 @@ __global__ void __launch_bounds__(THR)
       for (int i = 0; i < n; ++i) {
         const uint32_t a = lo1[i];
 #pragma unroll
-        for (int k = 0; k < LPT; ++k) acc[k] += static_cast<unsigned long long>(a) * lo2[i + threadIdx.x + k * THR];
+        for (int k = 0; k < LPT; ++k) acc[k] += static_cast<unsigned long long>(a) * lo2[pad32(i + l0 + k)];
       }
     }
     __syncthreads();
   }
 #pragma unroll
   for (int k = 0; k < LPT; ++k) {
-    const int64_t tau = tau0 + threadIdx.x + k * THR;
+    const int64_t tau = tau0 + l0 + k;
     if (tau < T) {
       if (gridDim.z == 1)
         D[r * T + tau] = static_cast<long long>(acc[k]);
