@@ -26,8 +26,8 @@ constexpr int LAGS = THR * LPT;      // lags per block
 constexpr int WIN = 1024;            // frames per shared window
 
 // S values are split into 32-bit halves in shared memory.  A window whose
-// largest value m gives m^2 * (terms) < 2^32 accumulates in 32 bits (one
-// 64-bit add per lag at its end).  Otherwise, windows whose
+// largest value m is below 2^16 accumulates in 32 bits, added to the 64-bit
+// sums every (2^32 - 1) / m^2 frames.  Otherwise, windows whose
 // values all fit in 32 bits (the usual case: a bin sum is at most
 // pixels x max count) take one 32 x 32 -> 64-bit multiply-add per term;
 // others add the cross terms too (arithmetic mod 2^64, exact while D < 2^63,
@@ -75,26 +75,32 @@ __global__ void __launch_bounds__(THR)
     uint32_t wmax = 0;
 #pragma unroll
     for (int w = 0; w < THR / 32; ++w) wmax = max(wmax, s_wmax[w]);
-    if (!any_wide && static_cast<unsigned long long>(wmax) * wmax * static_cast<unsigned long long>(n) < (1ull << 32)) {
-      // every term of the window and their sum fit 32 bits: 32-bit
-      // multiply-adds, one 64-bit add per lag at the end of the window; the
+    // frames whose products sum below 2^32: (2^32 - 1) / max^2 (0 when one
+    // product may not fit 32 bits)
+    const unsigned long long m2 = static_cast<unsigned long long>(wmax) * wmax;
+    const int run32 = m2 == 0 ? n : static_cast<int>(min(0xFFFFFFFFull / m2, static_cast<unsigned long long>(n)));
+    if (!any_wide && run32 > 0) {
+      // 32-bit multiply-adds, added to the 64-bit sums every run32 frames; the
       // shifted values b[k] = S(t + tau0 + l0 + k) slide along in registers,
       // one shared load per four multiply-adds
-      uint32_t part[LPT] = {0, 0, 0, 0};
       uint32_t bv[LPT];
 #pragma unroll
       for (int k = 0; k < LPT - 1; ++k) bv[k + 1] = lo2[pad32(l0 + k)];
+      for (int i0 = 0; i0 < n; i0 += run32) {
+        const int i1 = min(n, i0 + run32);
+        uint32_t part[LPT] = {0, 0, 0, 0};
 #pragma unroll 4
-      for (int i = 0; i < n; ++i) {
-        const uint32_t a = lo1[i];
+        for (int i = i0; i < i1; ++i) {
+          const uint32_t a = lo1[i];
 #pragma unroll
-        for (int k = 0; k < LPT - 1; ++k) bv[k] = bv[k + 1];
-        bv[LPT - 1] = lo2[pad32(i + l0 + LPT - 1)];
+          for (int k = 0; k < LPT - 1; ++k) bv[k] = bv[k + 1];
+          bv[LPT - 1] = lo2[pad32(i + l0 + LPT - 1)];
 #pragma unroll
-        for (int k = 0; k < LPT; ++k) part[k] += a * bv[k];
+          for (int k = 0; k < LPT; ++k) part[k] += a * bv[k];
+        }
+#pragma unroll
+        for (int k = 0; k < LPT; ++k) acc[k] += part[k];
       }
-#pragma unroll
-      for (int k = 0; k < LPT; ++k) acc[k] += part[k];
     } else if (any_wide) {
       for (int i = 0; i < n; ++i) {
         const unsigned long long a_lo = lo1[i], a_hi = hi1[i];

@@ -31,3 +31,22 @@ def test_denominator_exact(built_lib, cuda_device, T):
     with np.errstate(over="ignore"):
         ref = _corr(S)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("vmax", [200, 3000, 65535, 70000])
+def test_denominator_value_ranges(built_lib, cuda_device, vmax):
+    # 32-bit runs of a whole window (200), of a few hundred frames (3000), of
+    # one frame (65535), and the 64-bit path (70000)
+    import torch
+    from dynamix_gb300 import _lib
+    from dynamix_gb300.engine import ptr, stream_handle
+    T = 3000
+    rng = np.random.default_rng(vmax)
+    S = rng.integers(0, vmax + 1, (4, T)).astype(np.int64)
+    S[:, rng.integers(0, T, 4)] = vmax                               # the maximum occurs
+    S[3, :1500] = 0                                                  # dark frames in one row
+    lib = _lib.load()
+    s = torch.from_numpy(S).to(cuda_device)
+    d = torch.zeros_like(s)
+    _lib.check(lib.g2_denominator(ptr(s), 4, T, ptr(d), stream_handle(cuda_device)), "g2_denominator")
+    assert np.array_equal(d.cpu().numpy(), _corr(S))
