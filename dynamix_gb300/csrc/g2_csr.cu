@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(256)
 // its bytes through DRAM).
 constexpr int SUBBLOCK = 1024;
 constexpr int TILE_P = 64;  // pixels of one gather tile
+constexpr int STAGE_THREADS = 512;  // threads of a stage CTA (the shared region limits CTAs per SM)
 constexpr int UNROLL = 4;   // elements per lane with loads in flight together
 
 // Row bounds transposed to row-major: rb[r * T + t] = offsets[t] + indptr[t][r]
@@ -399,13 +400,13 @@ __global__ void __launch_bounds__(256)
 // flattened list (lane x takes element x).  The start of every TILE_P-pixel
 // tile of the sub-block goes to tile_pos[sb * n_tiles + tile] for the gather.
 template <typename Tv, typename Ti>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(STAGE_THREADS)
     row_stage_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices, const uint32_t* __restrict__ rb,
                      int64_t n_elem, int32_t T, int32_t H, int32_t W, const uint16_t* __restrict__ sb_counts,
                      const uint32_t* __restrict__ row_base, int64_t n_tiles, uint32_t* __restrict__ tile_pos,
                      int buf_words, uint32_t* __restrict__ stage, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
-  __shared__ uint32_t s_tot[8];
+  __shared__ uint32_t s_tot[STAGE_THREADS / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t sb = blockIdx.x;
   const int r = blockIdx.y;
@@ -415,10 +416,10 @@ __global__ void __launch_bounds__(256)
   uint32_t* cur = sm;                  // [W] next slot of each pixel, relative to the region
   uint32_t* pre = sm + W + warp * 66;  // [33] exclusive prefix of a batch's segments
   uint32_t* beg = pre + 33;            // [32] segment starts
-  uint32_t* buf = sm + W + 8 * 66;     // [buf_words] the region
+  uint32_t* buf = sm + W + (STAGE_THREADS / 32) * 66;  // [buf_words] the region
   const uint16_t* cnt = sb_counts + sb * npix + static_cast<int64_t>(r) * W;
   // exclusive scan of the row's counts, each thread over a contiguous span
-  const int per = (W + 255) / 256;
+  const int per = (W + STAGE_THREADS - 1) / STAGE_THREADS;
   const int i0 = threadIdx.x * per, i1 = min(W, i0 + per);
   uint32_t own = 0;
   for (int i = i0; i < i1; ++i) own += cnt[i];
@@ -431,7 +432,7 @@ __global__ void __launch_bounds__(256)
   if (lane == 31) s_tot[warp] = incl;
   __syncthreads();
   uint32_t run = incl - own, total = 0;
-  for (int w = 0; w < 8; ++w) {
+  for (int w = 0; w < STAGE_THREADS / 32; ++w) {
     run += w < warp ? s_tot[w] : 0u;
     total += s_tot[w];
   }
@@ -446,7 +447,7 @@ __global__ void __launch_bounds__(256)
   const bool skip = base + total > n_elem;  // block-uniform
   bool bad = skip;
   const bool buffered = total <= static_cast<uint32_t>(buf_words);
-  for (int64_t t0 = sb0 + warp * 32; t0 < sb_end && !skip; t0 += 8 * 32) {
+  for (int64_t t0 = sb0 + warp * 32; t0 < sb_end && !skip; t0 += STAGE_THREADS) {
     const int64_t t = t0 + lane;
     int64_t a = 0, b = 0;
     if (t < sb_end) {
@@ -509,7 +510,7 @@ __global__ void __launch_bounds__(256)
   }
   if (buffered && !skip) {
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < total; i += 256) stage[base + i] = buf[i];
+    for (uint32_t i = threadIdx.x; i < total; i += STAGE_THREADS) stage[base + i] = buf[i];
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
 }
@@ -1019,13 +1020,13 @@ extern "C" int g2_csr_stage_blocked(const void* data_dev, int32_t elem_bytes, co
   const int64_t npix = static_cast<int64_t>(height) * width;
   const int64_t n_tiles = (npix + csr::TILE_P - 1) / csr::TILE_P;
   const int buf = buffer_words(n_elem, n_sb * height);
-  const int64_t smem = (static_cast<int64_t>(width) + 8 * 66 + buf) * 4;
+  const int64_t smem = (static_cast<int64_t>(width) + (csr::STAGE_THREADS / 32) * 66 + buf) * 4;
   const dim3 grid(static_cast<unsigned>(n_sb), static_cast<unsigned>(height));
   cudaStream_t st = as_stream(stream);
 #define G2_ST(TV, TI)                                                                                              \
   do {                                                                                                             \
     if (!allow_smem(csr::row_stage_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                                      \
-    csr::row_stage_kernel<TV, TI><<<grid, 256, smem, st>>>(                                                        \
+    csr::row_stage_kernel<TV, TI><<<grid, csr::STAGE_THREADS, smem, st>>>(                                                        \
         reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev), row_bounds_dev, n_elem,    \
         nframes, height, width, sb_counts_dev, row_base_dev, n_tiles, tile_pos_dev, buf, stage_dev, err_dev);     \
   } while (0)
