@@ -226,9 +226,112 @@ class EventEngine:
         return d(range_off), d(range_bin), d(cta_range_off), int(range_bin.size), int(cta_range_off.size - 1)
 
     def run(self, vol_times, vol_data, offsets):
+        if self.host_pipeline_ok(vol_times, vol_data, offsets):
+            return self.run_host_pipelined(vol_times, vol_data, offsets)
         times, counts, offs, n_ev, mx = events_to_device(vol_times, vol_data, offsets, self.npix, self.T,
                                                          self.dev)
         return self.run_device(times, counts, offs, n_ev, mx)
+
+    HOST_CHUNKS = 4
+
+    def host_pipeline_ok(self, vol_times, vol_data, offsets):
+        """Pinned host tensors (times int32, counts uint8/uint16, offsets
+        int32/int64 of npix + 1) go through the chunked host pipeline."""
+        torch = _torch()
+        ts = (vol_times, vol_data, offsets)
+        if not all(isinstance(x, torch.Tensor) and not x.is_cuda and x.is_pinned() and x.is_contiguous()
+                   and x.dim() == 1 for x in ts):
+            return False
+        return (vol_times.dtype == torch.int32 and vol_data.dtype in (torch.uint8, torch.uint16)
+                and offsets.dtype in (torch.int32, torch.int64) and offsets.numel() == self.npix + 1
+                and vol_times.numel() == vol_data.numel() and self.n_bins > 0)
+
+    def _chunk_plans(self):
+        """Per pixel chunk (raster order, equal pixel counts): its binned
+        pixels bin by bin and their CTA ranges, for both pair kernels."""
+        plans = getattr(self, "_host_plans", None)
+        if plans is None:
+            torch = _torch()
+            sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
+            K = self.HOST_CHUNKS
+            bounds = [self.npix * c // K for c in range(K + 1)]
+            plans = []
+            for c in range(K):
+                keep = (self.binned >= bounds[c]) & (self.binned < bounds[c + 1])
+                pix, bins = self.binned[keep], self.binned_bin[keep]
+                d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.dev)
+                per = {}
+                for k, n in (("smem", self.SMEM_CTAS_PER_SM), ("global", self.GLOBAL_CTAS_PER_SM)):
+                    ro, rb, cro = cta_ranges(bins, sms * n)
+                    per[k] = (d(ro), d(rb), d(cro), int(rb.size), int(cro.size - 1))
+                plans.append((bounds[c], bounds[c + 1], d(pix.astype(np.int32)), per))
+            self._host_plans = plans
+        return plans
+
+    def run_host_pipelined(self, vol_times, vol_data, offsets):
+        """Events in pinned host memory: offsets and counts are copied and
+        checked first (one synchronisation: offsets start at 0 and never
+        decrease, counts give the kernel choice), then the frame times in
+        pixel chunks, each chunk's pair sums running while the next chunk is
+        copied; times outside [0, nframes) are found by the pair kernel and
+        raise ValueError after the call."""
+        torch = _torch()
+        cur = torch.cuda.current_stream(self.dev)
+        copy_s = getattr(self, "_copy_stream", None)
+        if copy_s is None:
+            copy_s = self._copy_stream = torch.cuda.Stream(self.dev)
+        offs64 = offsets.to(self.dev, non_blocking=True).to(torch.int64)
+        counts = vol_data.to(self.dev, non_blocking=True)
+        n_ev = int(offs64[-1].item())                     # synchronises the two copies
+        bad = bool(offs64[0].item() != 0) or bool(torch.any(offs64[1:] < offs64[:-1]).item())
+        if bad:
+            raise ValueError("offsets must start at 0 and be non-decreasing")
+        if n_ev >= 2 ** 32:
+            raise ValueError("too many events for uint32 offsets")
+        if vol_times.numel() < n_ev:
+            raise ValueError("offsets reference %d events but only %d are given" % (n_ev, vol_times.numel()))
+        mx = int(counts[:n_ev].to(torch.int32).max().item()) if n_ev else 0
+        offs = offs64.to(torch.int32)                     # uint32 bit pattern (n_ev < 2^32)
+        times = getattr(self, "_times_buf", None)
+        if times is None or times.numel() < max(n_ev, 1):
+            self._times_buf = None
+            times = self._times_buf = torch.empty(max(n_ev, 1), dtype=torch.int32, device=self.dev)
+        self.numer.zero_()
+        self.sums.zero_()
+        self.err.zero_()
+        use_smem = self.T * 8 + 24576 + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
+        kind = "smem" if use_smem else "global"
+        host_off = offsets                                 # pinned host offsets for the chunk bounds
+        st = stream_handle(self.dev)
+        start = torch.cuda.Event()
+        start.record(cur)
+        copy_s.wait_event(start)
+        self._mark("start_pairs")
+        for p0, p1, pix, per in self._chunk_plans():
+            e0 = int(host_off[p0]) & 0xFFFFFFFF
+            e1 = int(host_off[p1]) & 0xFFFFFFFF
+            if e1 > e0:
+                with torch.cuda.stream(copy_s):
+                    times[e0:e1].copy_(vol_times[e0:e1], non_blocking=True)
+                    done = torch.cuda.Event()
+                    done.record(copy_s)
+                cur.wait_event(done)
+            ro, rb, cro, n_ranges, n_ctas = per[kind]
+            if n_ranges and e1 > e0:
+                _lib.check(self.lib.g2_event_pairsum(
+                    ptr(times), ptr(counts), counts.element_size(), n_ev, ptr(offs), self.npix, ptr(pix),
+                    ptr(ro), ptr(rb), n_ranges, ptr(cro), n_ctas, self.T, self.n_bins, mx, ptr(self.numer),
+                    ptr(self.sums), ptr(self.err), st), "g2_event_pairsum")
+        self._mark("pairsum")
+        _lib.check(self.lib.g2_denominator(ptr(self.sums), self.n_bins, self.T, ptr(self.denom), st),
+                   "g2_denominator")
+        _lib.check(self.lib.g2_finalize(ptr(self.numer), ptr(self.denom), ptr(self.scale), self.n_bins,
+                                        self.T, ptr(self.g2_f32), ptr(self.g2_f64), st), "g2_finalize")
+        self._mark("normalize")
+        self._host_refs = (vol_times, offsets)            # alive until the copies have run
+        self._times_checked = True
+        self.last = {"n_events": n_ev, "max_count": mx, "kernel": kind, "host_chunks": self.HOST_CHUNKS}
+        return self.g2_f32[: self.n_bins]
 
     def run_device(self, times, counts, offs, n_ev, mx, reset_error=True):
         """G6 + G3 + G4 on validated device events: ``times`` int32 with
@@ -268,6 +371,10 @@ class EventEngine:
 
     def check_error(self):
         code = int(self.err.item())
+        if code and getattr(self, "_times_checked", False) and code == _lib.DEVERR_BOUNDS:
+            self._times_checked = False
+            raise ValueError("event times must lie in [0, nframes)")
+        self._times_checked = False
         if code:
             raise DeviceError(_lib.device_error_message(code))
 

@@ -126,3 +126,34 @@ def test_against_reference_event_kernel(built_lib, cuda_device, name):
     ok = np.isfinite(rg)
     assert np.array_equal(ok, np.isfinite(g))
     assert np.all(np.abs(g[ok] - rg[ok]) <= 1e-5 * np.abs(rg[ok]))
+
+
+def test_pinned_host_events_pipeline(built_lib, cuda_device):
+    # pinned host event arrays take the chunked copy/pair-sum pipeline; the
+    # result equals the oracle, and bad inputs raise as on the other paths
+    import torch
+    from dynamix_gb300.correlator import EventCorrelator
+    z = golden("dense_cfg1_u8")
+    fr, qm = z["frames"], z["qmask"]
+    T = fr.shape[0]
+    ref = o.g2_exact(fr, qm)
+    t = torch.from_numpy(z["ev_times"]).pin_memory()
+    d = torch.from_numpy(z["ev_data"]).pin_memory()
+    off = torch.from_numpy(z["ev_offsets"].astype(np.int64)).pin_memory()
+    c = EventCorrelator(fr.shape[1:], T, 1, qmask=qm)
+    assert c.engine.host_pipeline_ok(t, d, off)
+    g = c.correlate(t, d, off)
+    check(c, ref, g)
+    assert c.engine.last.get("host_chunks") == c.engine.HOST_CHUNKS
+    g2 = c.correlate(t, d, off)                      # a second call gives the same result
+    assert np.array_equal(g, g2)
+    bad_t = t.clone().pin_memory()
+    bad_t[len(bad_t) // 2] = T                       # a frame outside [0, T)
+    with pytest.raises(ValueError):
+        c.correlate(bad_t, d, off)
+    bad_off = off.clone().pin_memory()
+    bad_off[5] = bad_off[6] + 1                      # decreasing offsets
+    with pytest.raises(ValueError):
+        c.correlate(t, d, bad_off)
+    g3 = c.correlate(t, d, off)                      # and the correlator still works
+    assert np.array_equal(g, g3)
