@@ -232,7 +232,7 @@ class EventEngine:
                                                          self.dev)
         return self.run_device(times, counts, offs, n_ev, mx)
 
-    HOST_CHUNKS = 4
+    HOST_CHUNKS = 8
 
     def host_pipeline_ok(self, vol_times, vol_data, offsets):
         """Pinned host tensors (times int32, counts uint8/uint16, offsets
