@@ -69,6 +69,9 @@ SIGNATURES = {
     "g2_csr_count_blocked": (C.c_int, [_p, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),
     "g2_csr_stage_blocked": (C.c_int, [_p, _i32, _p, _p, _i32, _i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p]),
     "g2_csr_gather_blocked": (C.c_int, [_p, _p, _p, _i32, _i64, _i64, _p, _i32, _p, _p, _p]),
+    "g2_csr_stage_frames": (C.c_int, [_p, _i32, _p, _p, _i32, _i64, _i32, _i32, _i64, _i32, _i32, _p, _p, _p, _p,
+                                      _p, _p]),
+    "g2_add_carry_u32": (C.c_int, [_p, _i64, _p, _p]),
     "g2_events_unpack": (C.c_int, [_p, _i64, _i32, _p, _p, _p]),
     "g2_compress_count": (C.c_int, [_p, _i32, _i32, _i64, _i32, _p, _p, _p, _p, _p, _p]),
     "g2_compress_finish": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p, _p, _p]),

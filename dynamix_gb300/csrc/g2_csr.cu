@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(STAGE_THREADS)
     row_stage_kernel(const Tv* __restrict__ data, const Ti* __restrict__ indices, const uint32_t* __restrict__ rb,
                      int64_t n_elem, int32_t T, int32_t H, int32_t W, const uint16_t* __restrict__ sb_counts,
                      const uint32_t* __restrict__ row_base, int64_t n_tiles, uint32_t* __restrict__ tile_pos,
-                     int buf_words, uint32_t* __restrict__ stage, int32_t* __restrict__ err) {
+                     int buf_words, uint32_t* __restrict__ stage, int32_t frame0, int32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint32_t sm[];
   __shared__ uint32_t s_tot[STAGE_THREADS / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(STAGE_THREADS)
             if (pre[f + step] <= x) f += step;
           const int64_t k = static_cast<int64_t>(beg[f]) + (x - pre[f]);
           c[u] = static_cast<int64_t>(indices[k]);
-          w[u] = (static_cast<uint32_t>(t0 + f) << 16) | static_cast<uint32_t>(data[k]);
+          w[u] = (static_cast<uint32_t>(frame0 + t0 + f) << 16) | static_cast<uint32_t>(data[k]);
         }
       }
 #pragma unroll
@@ -687,6 +687,17 @@ __global__ void __launch_bounds__(256)
     }
   }
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+}
+
+// values[0 .. n] += carry, then carry = values[n] (one block: a running
+// exclusive scan continued across calls).
+__global__ void __launch_bounds__(1024)
+    add_carry_kernel(uint32_t* __restrict__ values, int64_t n, uint32_t* __restrict__ carry) {
+  const uint32_t c = *carry;
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i <= n; i += blockDim.x) values[i] += c;
+  __syncthreads();
+  if (threadIdx.x == 0) *carry = values[n];
 }
 
 // Packed words -> (times int32, data) arrays.
@@ -913,6 +924,13 @@ extern "C" int g2_exclusive_scan_u32(const uint32_t* in_dev, int64_t n, uint32_t
   return launch_status();
 }
 
+extern "C" int g2_add_carry_u32(uint32_t* values_dev, int64_t n, uint32_t* carry_dev, void* stream) {
+  using namespace g2;
+  if (!values_dev || !carry_dev || n < 0) return G2_ERR_ARG;
+  csr::add_carry_kernel<<<1, 1024, 0, as_stream(stream)>>>(values_dev, n, carry_dev);
+  return launch_status();
+}
+
 extern "C" int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
                               const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
                               int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
@@ -1002,33 +1020,35 @@ int buffer_words(int64_t n_elem, int64_t units) {
 }
 }  // namespace
 
-extern "C" int g2_csr_stage_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
-                                    const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem,
-                                    int32_t nframes, int32_t height, int32_t width, const uint16_t* sb_counts_dev,
-                                    const uint32_t* row_base_dev, uint32_t* tile_pos_dev, uint32_t* stage_dev,
-                                    int32_t* err_dev, void* stream) {
+namespace {
+int stage_frames(const void* data_dev, int32_t elem_bytes, const void* indices_dev, const uint32_t* row_bounds_dev,
+                 int32_t index_bytes, int64_t n_elem, int32_t frame0, int32_t nframes, int64_t frame_elems,
+                 int32_t height, int32_t width, const uint16_t* sb_counts_dev, const uint32_t* row_base_dev,
+                 uint32_t* tile_pos_dev, uint32_t* stage_dev, int32_t* err_dev, void* stream) {
   using namespace g2;
   if (!data_dev || !indices_dev || !row_bounds_dev || !sb_counts_dev || !row_base_dev || !tile_pos_dev ||
       !stage_dev || !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || (index_bytes != 4 && index_bytes != 8) || n_elem < 0 ||
-      nframes <= 0 || height <= 0 || width <= 0)
+      nframes <= 0 || height <= 0 || width <= 0 || frame0 < 0 || frame0 % csr::SUBBLOCK != 0 || frame_elems < 0)
     return G2_ERR_ARG;
-  if (nframes > 65536 || width > csr::ROW_MAX_W || height > 65535 || n_elem >= (1ll << 32))
+  if (static_cast<int64_t>(frame0) + nframes > 65536 || width > csr::ROW_MAX_W || height > 65535 ||
+      n_elem >= (1ll << 32))
     return G2_ERR_UNSUPPORTED;
   const int64_t n_sb = (static_cast<int64_t>(nframes) + csr::SUBBLOCK - 1) / csr::SUBBLOCK;
   const int64_t npix = static_cast<int64_t>(height) * width;
   const int64_t n_tiles = (npix + csr::TILE_P - 1) / csr::TILE_P;
-  const int buf = buffer_words(n_elem, n_sb * height);
+  const int buf = buffer_words(frame_elems, n_sb * height);
   const int64_t smem = (static_cast<int64_t>(width) + (csr::STAGE_THREADS / 32) * 66 + buf) * 4;
   const dim3 grid(static_cast<unsigned>(n_sb), static_cast<unsigned>(height));
   cudaStream_t st = as_stream(stream);
 #define G2_ST(TV, TI)                                                                                              \
   do {                                                                                                             \
     if (!allow_smem(csr::row_stage_kernel<TV, TI>, smem)) return G2_ERR_CUDA;                                      \
-    csr::row_stage_kernel<TV, TI><<<grid, csr::STAGE_THREADS, smem, st>>>(                                                        \
+    csr::row_stage_kernel<TV, TI><<<grid, csr::STAGE_THREADS, smem, st>>>(                                         \
         reinterpret_cast<const TV*>(data_dev), reinterpret_cast<const TI*>(indices_dev), row_bounds_dev, n_elem,    \
-        nframes, height, width, sb_counts_dev, row_base_dev, n_tiles, tile_pos_dev, buf, stage_dev, err_dev);     \
+        nframes, height, width, sb_counts_dev, row_base_dev, n_tiles, tile_pos_dev, buf, stage_dev, frame0,        \
+        err_dev);                                                                                                  \
   } while (0)
   if (elem_bytes == 1 && index_bytes == 4) G2_ST(uint8_t, uint32_t);
   else if (elem_bytes == 1) G2_ST(uint8_t, int64_t);
@@ -1036,6 +1056,26 @@ extern "C" int g2_csr_stage_blocked(const void* data_dev, int32_t elem_bytes, co
   else G2_ST(uint16_t, int64_t);
 #undef G2_ST
   return launch_status();
+}
+}  // namespace
+
+extern "C" int g2_csr_stage_blocked(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                                    const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem,
+                                    int32_t nframes, int32_t height, int32_t width, const uint16_t* sb_counts_dev,
+                                    const uint32_t* row_base_dev, uint32_t* tile_pos_dev, uint32_t* stage_dev,
+                                    int32_t* err_dev, void* stream) {
+  return stage_frames(data_dev, elem_bytes, indices_dev, row_bounds_dev, index_bytes, n_elem, 0, nframes, n_elem,
+                      height, width, sb_counts_dev, row_base_dev, tile_pos_dev, stage_dev, err_dev, stream);
+}
+
+extern "C" int g2_csr_stage_frames(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                                   const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem,
+                                   int32_t frame0, int32_t nframes, int64_t frame_elems, int32_t height,
+                                   int32_t width, const uint16_t* sb_counts_dev, const uint32_t* row_base_dev,
+                                   uint32_t* tile_pos_dev, uint32_t* stage_dev, int32_t* err_dev, void* stream) {
+  return stage_frames(data_dev, elem_bytes, indices_dev, row_bounds_dev, index_bytes, n_elem, frame0, nframes,
+                      frame_elems, height, width, sb_counts_dev, row_base_dev, tile_pos_dev, stage_dev, err_dev,
+                      stream);
 }
 
 extern "C" int g2_csr_gather_blocked(const uint32_t* stage_dev, const uint32_t* tile_pos_dev,

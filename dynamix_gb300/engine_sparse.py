@@ -14,6 +14,8 @@ numpy inputs are validated on the host before the copy.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 
 from . import _lib
@@ -371,10 +373,13 @@ class EventEngine:
 
     def check_error(self):
         code = int(self.err.item())
-        if code and getattr(self, "_times_checked", False) and code == _lib.DEVERR_BOUNDS:
-            self._times_checked = False
+        times_checked, csr_checked = getattr(self, "_times_checked", False), getattr(self, "_csr_checked", False)
+        self._times_checked = self._csr_checked = False
+        if code == _lib.DEVERR_BOUNDS and times_checked:
             raise ValueError("event times must lie in [0, nframes)")
-        self._times_checked = False
+        if code == _lib.DEVERR_BOUNDS and csr_checked:
+            raise ValueError("malformed CSR stack: row pointers, or column indices outside [0, width) or not "
+                             "increasing within a row")
         if code:
             raise DeviceError(_lib.device_error_message(code))
 
@@ -488,7 +493,118 @@ class SparseEngine:
         self.events._mark("transpose")
         return times, evdata, self.ev_off
 
+    HOST_SB_PER_CHUNK = 4   # 1024-frame sub-blocks per copied frame group
+
+    def host_pipeline_ok(self, data, indices, indptr, offsets):
+        """Pinned host tensors (counts uint8/uint16; indices, row pointers and
+        frame offsets all int32 or all int64) of a stack the packed
+        transposition takes go through the frame-group pipeline."""
+        torch = _torch()
+        ts = (data, indices, indptr, offsets)
+        if not all(isinstance(x, torch.Tensor) and not x.is_cuda and x.is_pinned() and x.is_contiguous()
+                   and x.dim() == 1 for x in ts):
+            return False
+        H, W = self.shape
+        return (data.dtype in (torch.uint8, torch.uint16) and indices.dtype in (torch.int32, torch.int64)
+                and indptr.dtype == indices.dtype and offsets.dtype == indices.dtype
+                and data.numel() == indices.numel() and indptr.numel() == (H + 1) * self.T
+                and offsets.numel() == self.T + 1 and self.packed_for(data.numel()) and self.events.n_bins > 0)
+
+    def _dev_buffer(self, name, like, n):
+        torch = _torch()
+        buf = getattr(self, name, None)
+        if buf is None or buf.numel() < max(n, 1) or buf.dtype != like:
+            setattr(self, name, None)
+            buf = torch.empty(max(n, 1), dtype=like, device=self.dev)
+            setattr(self, name, buf)
+        return buf
+
+    def run_host_pipelined(self, data, indices, indptr, offsets):
+        """A CSR stack in pinned host memory, frame group by frame group: the
+        copy of group g + 1 runs while group g is counted and staged (the
+        staging bases continue across groups through a running carry); the
+        gather, the pair sums and the normalisation follow.  Frame offsets are
+        checked on the host; malformed rows or columns found by the kernels
+        raise ValueError after the call."""
+        torch = _torch()
+        H, W = self.shape
+        T, npix = self.T, self.npix
+        n = int(data.numel())
+        off_h = offsets.to(torch.int64)
+        if int(off_h[0]) != 0 or bool(torch.any(off_h[1:] < off_h[:-1])) or int(off_h[-1]) > n:
+            raise ValueError("frame offsets must start at 0, never decrease and stay within the elements")
+        ib = indices.element_size()
+        eb = data.element_size()
+        cur = torch.cuda.current_stream(self.dev)
+        copy_s = getattr(self, "_copy_stream", None)
+        if copy_s is None:
+            copy_s = self._copy_stream = torch.cuda.Stream(self.dev)
+        d_data = self._dev_buffer("_h_data", data.dtype, n)
+        d_ind = self._dev_buffer("_h_ind", indices.dtype, n)
+        d_ip = self._dev_buffer("_h_ip", indptr.dtype, indptr.numel())
+        d_off = self._dev_buffer("_h_off", offsets.dtype, offsets.numel())
+        n_sb = -(-T // self.SUBBLOCK)
+        n_tiles = -(-npix // self.TILE_P)
+        G = self.HOST_SB_PER_CHUNK
+        sbc = self._buffer("sb_counts", n_sb * npix, torch.int16)
+        rt = self._buffer("row_totals", n_sb * H + 1, torch.int32)
+        base = self._buffer("row_base", n_sb * H + 1, torch.int32)
+        rscr = self._buffer("row_scan_scratch", -(-(G * H) // 8192) + 1, torch.int32)
+        carry = self._buffer("row_carry", 1, torch.int32)
+        rb = self._buffer("row_bounds_group", (H + 1) * min(T, G * self.SUBBLOCK), torch.int32)
+        tpos = self._buffer("tile_pos", n_sb * n_tiles, torch.int32)
+        stage = self._buffer("stage_words", n, torch.int32)
+        err = self.events.err
+        self.counts.zero_()
+        carry.zero_()
+        err.zero_()
+        st = stream_handle(self.dev)
+        start = torch.cuda.Event()
+        start.record(cur)
+        copy_s.wait_event(start)
+        with torch.cuda.stream(copy_s):
+            d_off.copy_(offsets, non_blocking=True)
+        self.events._mark("start_transpose")
+        addr = lambda t, k: C.c_void_p(t.data_ptr() + k * t.element_size())
+        for sb0 in range(0, n_sb, G):
+            f0, f1 = sb0 * self.SUBBLOCK, min(T, (sb0 + G) * self.SUBBLOCK)
+            e0, e1 = int(off_h[f0]), int(off_h[f1])
+            with torch.cuda.stream(copy_s):
+                if e1 > e0:
+                    d_ind[e0:e1].copy_(indices[e0:e1], non_blocking=True)
+                    d_data[e0:e1].copy_(data[e0:e1], non_blocking=True)
+                d_ip[f0 * (H + 1):f1 * (H + 1)].copy_(indptr[f0 * (H + 1):f1 * (H + 1)], non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(copy_s)
+            cur.wait_event(done)
+            k = -(-(f1 - f0) // self.SUBBLOCK)
+            _lib.check(self.lib.g2_csr_count_blocked(ptr(d_ind), addr(d_ip, f0 * (H + 1)), addr(d_off, f0), ib, n,
+                                                     f1 - f0, H, W, ptr(rb), ptr(self.counts),
+                                                     addr(sbc, sb0 * npix), addr(rt, sb0 * H), ptr(err), st),
+                       "g2_csr_count_blocked")
+            _lib.check(self.lib.g2_exclusive_scan_u32(addr(rt, sb0 * H), k * H, addr(base, sb0 * H), ptr(rscr),
+                                                      rscr.numel(), st), "g2_exclusive_scan_u32")
+            _lib.check(self.lib.g2_add_carry_u32(addr(base, sb0 * H), k * H, ptr(carry), st), "g2_add_carry_u32")
+            _lib.check(self.lib.g2_csr_stage_frames(ptr(d_data), eb, ptr(d_ind), ptr(rb), ib, n, f0, f1 - f0,
+                                                    e1 - e0, H, W, addr(sbc, sb0 * npix), addr(base, sb0 * H),
+                                                    addr(tpos, sb0 * n_tiles), ptr(stage), ptr(err), st),
+                       "g2_csr_stage_frames")
+        _lib.check(self.lib.g2_exclusive_scan_u32(ptr(self.counts), npix, ptr(self.ev_off), ptr(self.scan_scratch),
+                                                  self.scan_scratch.numel(), st), "g2_exclusive_scan_u32")
+        words = self._buffer("ev_words", n, torch.int32)
+        _lib.check(self.lib.g2_csr_gather_blocked(ptr(stage), ptr(tpos), ptr(sbc), T, npix, n, ptr(self.ev_off), 0,
+                                                  ptr(words), ptr(err), st), "g2_csr_gather_blocked")
+        self.events._mark("transpose")
+        mx = int(d_data[:n].to(torch.int32).max().item()) if n else 0
+        self._host_refs = (data, indices, indptr, offsets)
+        out = self.events.run_device(words, None, self.ev_off, n, mx, reset_error=False)
+        self.events._csr_checked = True
+        self.last = dict(self.events.last, n_elements=n, packed=True, host_sb_per_chunk=G)
+        return out
+
     def run(self, data, indices, indptr, offsets):
+        if self.host_pipeline_ok(data, indices, indptr, offsets):
+            return self.run_host_pipelined(data, indices, indptr, offsets)
         counts, ind, ip, off, ib, n, mx = csr_to_device(data, indices, indptr, offsets, self.shape, self.T,
                                                         self.dev)
         packed = self.packed_for(n)

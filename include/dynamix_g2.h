@@ -224,6 +224,10 @@ int g2_csr_count(const void* indices_dev, const void* indptr_dev, const void* of
                  uint32_t* counts_dev, int32_t* err_dev, void* stream);
 int g2_exclusive_scan_u32(const uint32_t* in_dev, int64_t n, uint32_t* out_dev, uint32_t* scratch_dev,
                           int64_t scratch_len, void* stream);
+/* values_dev[0 .. n] += *carry_dev, then *carry_dev = values_dev[n]: continues
+ * an exclusive scan (g2_exclusive_scan_u32 writes n + 1 values) across pieces
+ * scanned one after another on the same stream. */
+int g2_add_carry_u32(uint32_t* values_dev, int64_t n, uint32_t* carry_dev, void* stream);
 int g2_csr_scatter(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
                    const void* indptr_dev, const void* offsets_dev, int32_t index_bytes, int64_t n_elem,
                    int32_t nframes, int32_t height, int32_t width, const uint32_t* ev_offsets_dev,
@@ -261,6 +265,17 @@ int g2_csr_stage_blocked(const void* data_dev, int32_t elem_bytes, const void* i
                          const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem, int32_t nframes,
                          int32_t height, int32_t width, const uint16_t* sb_counts_dev, const uint32_t* row_base_dev,
                          uint32_t* tile_pos_dev, uint32_t* stage_dev, int32_t* err_dev, void* stream);
+/* g2_csr_stage_blocked for the frames frame0 .. frame0 + nframes - 1 only
+ * (frame0 a multiple of 1024; row_bounds_dev as written by
+ * g2_csr_count_blocked for those frames, sb_counts_dev, row_base_dev and
+ * tile_pos_dev pointing at their first sub-block; frame_elems, the elements of
+ * those frames, sizes the shared-memory buffer): a stack arriving frame group
+ * by frame group is staged while the next group is copied. */
+int g2_csr_stage_frames(const void* data_dev, int32_t elem_bytes, const void* indices_dev,
+                        const uint32_t* row_bounds_dev, int32_t index_bytes, int64_t n_elem, int32_t frame0,
+                        int32_t nframes, int64_t frame_elems, int32_t height, int32_t width,
+                        const uint16_t* sb_counts_dev, const uint32_t* row_base_dev, uint32_t* tile_pos_dev,
+                        uint32_t* stage_dev, int32_t* err_dev, void* stream);
 int g2_csr_gather_blocked(const uint32_t* stage_dev, const uint32_t* tile_pos_dev, const uint16_t* sb_counts_dev,
                           int32_t nframes, int64_t npix, int64_t n_elem, const uint32_t* ev_offsets_dev,
                           int32_t sort, uint32_t* ev_words_dev, int32_t* err_dev, void* stream);

@@ -116,3 +116,44 @@ def test_wide_rows_take_the_walk_kernels(built_lib, cuda_device):
     assert np.array_equal(c.numerator, ref["numerator"])
     assert np.array_equal(c.sums, ref["sums"])
     assert np.array_equal(g, ref["g2"].astype(np.float32), equal_nan=True)
+
+
+@pytest.mark.parametrize("name,index_dtype", [("dense_cfg1_u8", np.int32), ("dense_u16", np.int64),
+                                              ("synthetic", np.int32)])
+def test_pinned_host_csr_pipeline(built_lib, cuda_device, name, index_dtype):
+    # pinned host CSR tensors take the frame-group pipeline (count and stage of
+    # a group while the next one is copied); equal to the oracle, and malformed
+    # stacks still raise
+    import torch
+    from dynamix_gb300.correlator import SparseCorrelator
+    if name == "synthetic":                        # 2600 frames: three frame groups of one sub-block
+        from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+        fr = speckle_numpy(2600, (40, 56), 0.98, 0.2, seed=17)
+        qm = annular_qmask((40, 56), 4, 2.0, 20.0)
+    else:
+        z = golden(name)
+        fr, qm = z["frames"], z["qmask"]
+    T, H, W = fr.shape
+    data, indices, indptr, offsets = o.frames_to_csr(fr)
+    ref = o.csr_correlate_exact(data, indices, indptr, offsets, (H, W), T, qmask=qm)
+    pin = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a).astype(dt)).pin_memory()
+    d = pin(data, data.dtype)
+    ind, ip, off = (pin(a, index_dtype) for a in (indices, indptr, offsets))
+    c = SparseCorrelator((H, W), T, qmask=qm)
+    c.engine.HOST_SB_PER_CHUNK = 1                 # several frame groups even for short stacks
+    assert c.engine.host_pipeline_ok(d, ind, ip, off)
+    g = c.correlate(d, ind, ip, off)
+    assert c.engine.last.get("host_sb_per_chunk") == 1
+    assert np.array_equal(c.numerator, ref["numerator"])
+    assert np.array_equal(c.sums, ref["sums"])
+    assert np.array_equal(c.denominator, ref["denominator"])
+    assert np.array_equal(g, ref["g2"].astype(np.float32), equal_nan=True)
+    bad = ind.clone().pin_memory()
+    bad[len(bad) // 3] = W + 5                     # a column outside the row
+    with pytest.raises(ValueError):
+        c.correlate(d, bad, ip, off)
+    bad_off = off.clone().pin_memory()
+    bad_off[3] = bad_off[4] + 1
+    with pytest.raises(ValueError):
+        c.correlate(d, ind, ip, bad_off)
+    assert np.array_equal(c.correlate(d, ind, ip, off), g)
