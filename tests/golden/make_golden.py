@@ -56,7 +56,7 @@ CASES = [
     # name, T, shape, rho, mu, dtype, n_bins, r_min, r_max, seed
     ("dense_small_u8", 200, (48, 40), 0.98, 0.5, np.uint8, 5, 2.0, 22.0, 11),
     ("dense_bright_u8", 120, (32, 32), 0.95, 20.0, np.uint8, 3, 0.0, 16.0, 12),
-    ("dense_cfg1_u8", 1000, (128, 128), 0.98, 0.05, np.uint8, 8, 0.0, 64.0, 0),
+    ("dense_128x128_u8", 1000, (128, 128), 0.98, 0.05, np.uint8, 8, 0.0, 64.0, 0),
     ("dense_u16", 150, (40, 36), 0.99, 60.0, np.uint16, 4, 1.0, 20.0, 13),
 ]
 

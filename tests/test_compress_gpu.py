@@ -21,7 +21,7 @@ def _check_layout(got, ref):
     assert np.array_equal(_to_np(d).astype(np.int64), rd.astype(np.int64))
 
 
-@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_cfg1_u8", "dense_u16"])
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_128x128_u8", "dense_u16"])
 def test_golden_layout(built_lib, cuda_device, name):
     import torch
     from dynamix_gb300.correlator import FramesCompressor

@@ -42,7 +42,7 @@ def assert_exact(c, ref, g32=None):
 
 
 @pytest.mark.parametrize("method", ["tc", "plain"])
-@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_cfg1_u8", "dense_u16"])
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_128x128_u8", "dense_u16"])
 def test_golden_cases(built_lib, cuda_device, name, method):
     z = golden(name)
     ref = o.g2_exact(z["frames"], z["qmask"])
@@ -236,7 +236,7 @@ def test_chunked_pipeline_matches_single_pass(built_lib, cuda_device, T):
     assert np.array_equal(g, gb, equal_nan=True)
 
 
-@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_cfg1_u8", "dense_u16"])
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_128x128_u8", "dense_u16"])
 def test_calc_std(built_lib, cuda_device, name):
     """calc_std (dense.py:58-66): against the float64 oracle to 1e-4 relative
     (float products and ratios on the tensor cores, float64 reduction) and

@@ -15,7 +15,7 @@ def check(c, ref, g):
     assert np.array_equal(g, ref["g2"].astype(np.float32), equal_nan=True)
 
 
-@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_cfg1_u8", "dense_u16"])
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_128x128_u8", "dense_u16"])
 def test_reference_event_layout(built_lib, cuda_device, name):
     from dynamix_gb300.correlator import EventCorrelator
     z = golden(name)
@@ -133,7 +133,7 @@ def test_pinned_host_events_pipeline(built_lib, cuda_device):
     # result equals the oracle, and bad inputs raise as on the other paths
     import torch
     from dynamix_gb300.correlator import EventCorrelator
-    z = golden("dense_cfg1_u8")
+    z = golden("dense_128x128_u8")
     fr, qm = z["frames"], z["qmask"]
     T = fr.shape[0]
     ref = o.g2_exact(fr, qm)

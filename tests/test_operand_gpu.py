@@ -49,7 +49,7 @@ def test_fp32_accumulation_exact(built_lib, cuda_device, operand, k):
     assert np.array_equal(c.numerator, ref["numerator"])
 
 
-@pytest.mark.parametrize("name", ["dense_small_u8", "dense_cfg1_u8", "dense_edge"])
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_128x128_u8", "dense_edge"])
 def test_e4m3_golden(built_lib, cuda_device, name):
     from dynamix_gb300.correlator import MatMulCorrelator
     z = golden(name)

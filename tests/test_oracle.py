@@ -11,7 +11,7 @@ import pytest
 from conftest import golden
 from oracle import g2_oracle as o
 
-CASES = ["dense_small_u8", "dense_bright_u8", "dense_cfg1_u8", "dense_u16"]
+CASES = ["dense_small_u8", "dense_bright_u8", "dense_128x128_u8", "dense_u16"]
 
 
 @pytest.mark.parametrize("name", CASES)

@@ -57,7 +57,7 @@ def test_csr_layout_errors(built_lib, cuda_device):
 
 
 @pytest.mark.parametrize("name,index_dtype", [("dense_small_u8", np.uint32), ("dense_u16", np.int64),
-                                              ("dense_cfg1_u8", np.uint32)])
+                                              ("dense_128x128_u8", np.uint32)])
 def test_csr_to_events_is_frames_compressor_layout(built_lib, cuda_device, name, index_dtype):
     """The device transposition yields exactly FramesCompressor's layout:
     pixel-major, frames ascending within a pixel (event.py:267-284)."""
@@ -118,7 +118,7 @@ def test_wide_rows_take_the_walk_kernels(built_lib, cuda_device):
     assert np.array_equal(g, ref["g2"].astype(np.float32), equal_nan=True)
 
 
-@pytest.mark.parametrize("name,index_dtype", [("dense_cfg1_u8", np.int32), ("dense_u16", np.int64),
+@pytest.mark.parametrize("name,index_dtype", [("dense_128x128_u8", np.int32), ("dense_u16", np.int64),
                                               ("synthetic", np.int32)])
 def test_pinned_host_csr_pipeline(built_lib, cuda_device, name, index_dtype):
     # pinned host CSR tensors take the frame-group pipeline (count and stage of

@@ -19,7 +19,7 @@ def _same(got, ref, rtol=2e-6):
     assert np.all(np.abs(got[ok] - ref[ok]) <= rtol * np.abs(ref[ok]) + 1e-30)
 
 
-@pytest.mark.parametrize("name,q", [("dense_small_u8", 1), ("dense_small_u8", 3), ("dense_cfg1_u8", 2),
+@pytest.mark.parametrize("name,q", [("dense_small_u8", 1), ("dense_small_u8", 3), ("dense_128x128_u8", 2),
                                     ("dense_u16", 4)])
 def test_ttcf_golden_frames(built_lib, cuda_device, name, q):
     from dynamix_gb300.correlator import MatMulCorrelator
