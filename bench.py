@@ -379,8 +379,8 @@ def run_ours(args):
 
 # ---------------------------------------------------------------- sparse / event
 def sparse_shape(args):
-    """Frame shape of the sparse/event workloads: the headline shape, or a
-    smaller one given with --shape (profiling at the same density)."""
+    """Frame shape of the sparse/event workloads: 2162 x 2068, or a smaller
+    one given with --shape (profiling at the same density)."""
     if getattr(args, "shape", None):
         h, w = (int(x) for x in args.shape.split(","))
         return h, w
@@ -872,7 +872,7 @@ COMPRESS_CPU_FRAMES = 256
 
 
 def run_compress(args):
-    """Device frame compression of the dense headline stack (frames already in
+    """Device frame compression of the 514 x 1030 x 10,000 u8 stack (frames already in
     HBM for ``value``; from pinned host memory, events copied back, for e2e)."""
     import numpy as np
     import torch
