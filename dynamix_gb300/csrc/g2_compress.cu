@@ -36,6 +36,7 @@ constexpr int THREADS = 256;
 constexpr int BLK_PX = THREADS * PX;  // pixels of one CTA
 constexpr int TILE_P = 64;           // pixels of one gather tile (as in the CSR path)
 constexpr int STAGE_BUF = 8192;      // words of a CTA region assembled in shared memory
+constexpr int WCAP = STAGE_BUF / (2 * (THREADS / 32));  // words of one warp's chunk (words + positions)
 constexpr uint16_t NONE = 0xFFFFu;
 
 // Four consecutive values of one frame as int32 (sign-extended for signed
@@ -83,6 +84,18 @@ __device__ __forceinline__ void unpack4(uint2 w, int32_t v[PX]) {
 #pragma unroll
   for (int j = 0; j < PX; ++j)
     v[j] = static_cast<Tv>(-1) < 0 ? static_cast<int32_t>(static_cast<int16_t>(h[j])) : static_cast<int32_t>(h[j]);
+}
+
+// Value j of the 4 in a raw word.
+template <typename Tv>
+__device__ __forceinline__ int32_t lane_value(uint32_t w, int j) {
+  const uint32_t b = (w >> (8 * j)) & 0xFFu;
+  return static_cast<Tv>(-1) < 0 ? static_cast<int32_t>(static_cast<int8_t>(b)) : static_cast<int32_t>(b);
+}
+template <typename Tv>
+__device__ __forceinline__ int32_t lane_value(uint2 w, int j) {
+  const uint32_t h = ((j < 2 ? w.x : w.y) >> (16 * (j & 1))) & 0xFFFFu;
+  return static_cast<Tv>(-1) < 0 ? static_cast<int32_t>(static_cast<int16_t>(h)) : static_cast<int32_t>(h);
 }
 
 // frames whose loads are in flight together (VEC): 64 bytes per thread
@@ -242,7 +255,8 @@ __global__ void __launch_bounds__(THREADS)
 
 // Pass 4 (after the scans).  A thread's 4 pixels get their run starts from a
 // block scan of the sub-block counts; the region of the CTA is assembled in
-// shared memory when it fits (coalesced write-out), else written in place.
+// shared memory when it fits (coalesced write-out), else each warp assembles
+// chunks of frames in its shared slice (coalesced within each pixel's piece).
 template <typename Tv, bool VEC, bool CUT>
 __global__ void __launch_bounds__(THREADS)
     stage_kernel(const Tv* __restrict__ frames, int32_t T, int64_t npix, const uint16_t* __restrict__ sb_counts,
@@ -281,15 +295,94 @@ __global__ void __launch_bounds__(THREADS)
     if (j < n_valid && p % TILE_P == 0) tile_pos[sb * n_tiles + p / TILE_P] = static_cast<uint32_t>(base + cur[j]);
   }
   bool bad = skip;
-  if (!skip && own > 0) {
-    const uint32_t goal = end[0] + end[1] + end[2] + end[3];
-    walk_frames<Tv, VEC>(
-        frames + t0 * npix + p0, npix, t0, t1, n_valid,
-        [&](const int32_t v[PX], int64_t t) {
-          const uint32_t rel = static_cast<uint32_t>(t - t0);
+  const uint32_t goal = end[0] + end[1] + end[2] + end[3];
+  int64_t t = t0;
+  if (VEC && !skip && !buffered) {
+    // Region too large for shared memory: each warp takes CHUNK frames of its
+    // 128 pixels at a time, counts them from registers, scans the counts
+    // across the warp and assembles the chunk's words pixel-major in its own
+    // shared slice, then writes them out with consecutive lanes on
+    // consecutive words (each pixel's words of the chunk are one contiguous
+    // piece of its run).  A chunk with more than WCAP words, or with more
+    // values than a pixel's run has room for, is written word by word.
+    using W = typename Word4<Tv>::type;
+    constexpr int CHUNK = 2 * InFlight<Tv>::frames;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t* wb = buf + (threadIdx.x >> 5) * (2 * WCAP);
+    uint32_t* wd = wb + WCAP;
+    const Tv* src = frames + t0 * npix + p0;
+    for (; t + CHUNK <= t1; t += CHUNK, src += CHUNK * npix) {
+      const bool mine = own > 0 && cur[0] + cur[1] + cur[2] + cur[3] < goal;
+      if (!__any_sync(0xffffffffu, mine)) break;
+      W raw[CHUNK];
+#pragma unroll
+      for (int u = 0; u < CHUNK; ++u) raw[u] = mine ? *reinterpret_cast<const W*>(src + u * npix) : W{};
+      uint32_t c[PX] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (int u = 0; u < CHUNK; ++u) {
+        int32_t v[PX];
+        unpack4<Tv>(raw[u], v);
+#pragma unroll
+        for (int j = 0; j < PX; ++j) c[j] += v[j] > 0 && (!CUT || t + u < cut[j]) ? 1u : 0u;
+      }
+      bool over = false;
+#pragma unroll
+      for (int j = 0; j < PX; ++j) over |= cur[j] + c[j] > end[j];
+      const uint32_t n = c[0] + c[1] + c[2] + c[3];
+      uint32_t incl = n;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += y;
+      }
+      const uint32_t wtotal = __shfl_sync(0xffffffffu, incl, 31);
+      const uint32_t rel0 = static_cast<uint32_t>(t - t0);
+      if (__any_sync(0xffffffffu, over) || wtotal > static_cast<uint32_t>(WCAP)) {
+#pragma unroll
+        for (int u = 0; u < CHUNK; ++u) {
+          int32_t v[PX];
+          unpack4<Tv>(raw[u], v);
 #pragma unroll
           for (int j = 0; j < PX; ++j) {
-            if (v[j] > 0 && t < cut[j]) {
+            if (v[j] > 0 && (!CUT || t + u < cut[j])) {
+              if (cur[j] < end[j]) {
+                stage[base + cur[j]] = ((rel0 + u) << 16) | (static_cast<uint32_t>(v[j]) & 0xFFFFu);
+                ++cur[j];
+              } else {
+                bad = true;
+              }
+            }
+          }
+        }
+      } else {
+        uint32_t pos = incl - n;
+#pragma unroll
+        for (int j = 0; j < PX; ++j) {
+#pragma unroll
+          for (int u = 0; u < CHUNK; ++u) {
+            const int32_t v = lane_value<Tv>(raw[u], j);
+            if (v > 0 && (!CUT || t + u < cut[j])) {
+              wb[pos] = ((rel0 + u) << 16) | (static_cast<uint32_t>(v) & 0xFFFFu);
+              wd[pos] = cur[j];
+              ++pos;
+              ++cur[j];
+            }
+          }
+        }
+        __syncwarp();
+        for (uint32_t i = lane; i < wtotal; i += 32) stage[base + wd[i]] = wb[i];
+        __syncwarp();
+      }
+    }
+  }
+  if (!skip && own > 0 && t < t1) {
+    walk_frames<Tv, VEC>(
+        frames + t * npix + p0, npix, t, t1, n_valid,
+        [&](const int32_t v[PX], int64_t tf) {
+          const uint32_t rel = static_cast<uint32_t>(tf - t0);
+#pragma unroll
+          for (int j = 0; j < PX; ++j) {
+            if (v[j] > 0 && tf < cut[j]) {
               if (cur[j] < end[j]) {
                 const uint32_t w = (rel << 16) | (static_cast<uint32_t>(v[j]) & 0xFFFFu);
                 if (buffered)

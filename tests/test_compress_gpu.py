@@ -116,6 +116,34 @@ def test_hot_pixel_threshold_and_mask(built_lib, cuda_device, threshold, with_ma
     assert np.array_equal(_to_np(s), rsum)
 
 
+@pytest.mark.parametrize("dtype,density,threshold", [
+    (np.uint8, 0.05, None),     # warp chunks of 32 frames assembled in shared memory
+    (np.uint8, 0.05, 40),       # the same with the cut frame of the threshold
+    (np.uint8, 0.6, None),      # chunks beyond the warp's shared slice: written word by word
+    (np.uint16, 0.1, None),     # chunks of 16 frames
+    (np.int16, 0.1, 40),
+    (np.int8, 0.08, None),
+])
+def test_chunked_stage(built_lib, cuda_device, dtype, density, threshold):
+    # CTA regions (1024 pixels x 1024 frames) far beyond the shared buffer; T leaves a
+    # partial last sub-block with a tail shorter than one chunk
+    import torch
+    from dynamix_gb300.compress import compress_all_stack_device
+    rng = np.random.default_rng(int(density * 1000) + (threshold or 0))
+    T, shape = 2100, (32, 64)
+    info = np.iinfo(dtype)
+    vals = rng.integers(1, min(info.max, 60) + 1, size=(T,) + shape)
+    fr = np.where(rng.random((T,) + shape) < density, vals, 0).astype(dtype)
+    if info.min < 0:
+        fr[rng.random((T,) + shape) < 0.05] = -3               # negatives are not events
+    mask0 = (rng.random(shape) < 0.03).astype(np.uint8)
+    rd, rt, ro, rmask, rsum = o.compress_hot_pixels(fr, threshold, mask0)
+    m = torch.from_numpy(mask0.ravel().copy()).to(cuda_device)
+    got = compress_all_stack_device(torch.from_numpy(fr).to(cuda_device), threshold=threshold, mask=m)
+    _check_layout(got, (rd, rt, ro))
+    assert np.array_equal(_to_np(m).astype(bool), rmask)
+
+
 @pytest.mark.parametrize("threshold", [None, 30])
 def test_streaming_equals_whole_stack(built_lib, cuda_device, threshold):
     # the reference's test_progressive_compression (correlator/test/test_event.py:62-73), on the GPU,
