@@ -35,7 +35,7 @@ constexpr int PX = 4;                // consecutive pixels of one thread
 constexpr int THREADS = 256;
 constexpr int BLK_PX = THREADS * PX;  // pixels of one CTA
 constexpr int TILE_P = 64;           // pixels of one gather tile (as in the CSR path)
-constexpr int STAGE_BUF = 8192;      // words of a CTA region assembled in shared memory
+constexpr int STAGE_BUF = 16384;     // words of a CTA region assembled in shared memory (dynamic, 64 KB)
 constexpr int WCAP = STAGE_BUF / (2 * (THREADS / 32));  // words of one warp's chunk (words + positions)
 constexpr uint16_t NONE = 0xFFFFu;
 
@@ -98,6 +98,45 @@ __device__ __forceinline__ int32_t lane_value(uint2 w, int j) {
   return static_cast<Tv>(-1) < 0 ? static_cast<int32_t>(static_cast<int16_t>(h)) : static_cast<int32_t>(h);
 }
 
+// Positive-value flags of a 32-bit word of packed values, all lanes at once:
+// the top bit of each 8-bit (u8/i8) or 16-bit (u16/i16) lane is set when the
+// lane's value is > 0.  Adding the low bits to all-ones-but-top carries into
+// the top bit when any low bit is set (never across lanes); unsigned values
+// are positive when any bit is set, signed ones when in addition the sign bit
+// is clear.
+template <typename Tv>
+__device__ __forceinline__ uint32_t positive_flags(uint32_t w) {
+  constexpr uint32_t low = sizeof(Tv) == 1 ? 0x7F7F7F7Fu : 0x7FFF7FFFu;
+  const uint32_t any_low = (w & low) + low;
+  return (static_cast<Tv>(-1) < 0 ? (any_low & ~w) : (any_low | w)) & ~low;
+}
+
+// Lane counters of positive values: a0 holds 4 byte counters (8-bit values,
+// at most 255 frames between flushes) or, with a1, 4 16-bit counters.
+template <typename Tv>
+__device__ __forceinline__ void add_positive(uint32_t w, uint32_t& a0, uint32_t&) {
+  a0 += positive_flags<Tv>(w) >> 7;
+}
+template <typename Tv>
+__device__ __forceinline__ void add_positive(uint2 w, uint32_t& a0, uint32_t& a1) {
+  a0 += positive_flags<Tv>(w.x) >> 15;
+  a1 += positive_flags<Tv>(w.y) >> 15;
+}
+template <typename Tv>
+__device__ __forceinline__ void flush_positive(uint32_t& a0, uint32_t& a1, uint32_t c[PX]) {
+  if (sizeof(Tv) == 1) {
+#pragma unroll
+    for (int j = 0; j < PX; ++j) c[j] += (a0 >> (8 * j)) & 0xFFu;
+  } else {
+    c[0] += a0 & 0xFFFFu;
+    c[1] += a0 >> 16;
+    c[2] += a1 & 0xFFFFu;
+    c[3] += a1 >> 16;
+  }
+  a0 = 0;
+  a1 = 0;
+}
+
 // frames whose loads are in flight together (VEC): 64 bytes per thread
 template <typename Tv> struct InFlight { static constexpr int frames = sizeof(Tv) == 1 ? 16 : 8; };
 
@@ -140,6 +179,27 @@ __device__ __forceinline__ void walk_frames(const Tv* __restrict__ src, int64_t 
   }
 }
 
+// Positive values of frames [0, n) of 4 pixels at src (VEC loads), added to
+// cnt: lane counters flushed every 128 frames.
+template <typename Tv>
+__device__ __forceinline__ void count_positive(const Tv* __restrict__ src, int64_t npix, int64_t n,
+                                               uint32_t cnt[PX]) {
+  using W = typename Word4<Tv>::type;
+  constexpr int TU = InFlight<Tv>::frames;
+  uint32_t a0 = 0, a1 = 0;
+  int64_t t = 0;
+  for (int g = 1; t + TU <= n; t += TU, ++g) {
+    W raw[TU];
+#pragma unroll
+    for (int u = 0; u < TU; ++u) raw[u] = *reinterpret_cast<const W*>(src + (t + u) * npix);
+#pragma unroll
+    for (int u = 0; u < TU; ++u) add_positive<Tv>(raw[u], a0, a1);
+    if (g % (128 / TU) == 0) flush_positive<Tv>(a0, a1, cnt);
+  }
+  for (; t < n; ++t) add_positive<Tv>(*reinterpret_cast<const W*>(src + t * npix), a0, a1);
+  flush_positive<Tv>(a0, a1, cnt);
+}
+
 // Block-wide exclusive scan of one uint32 per thread; returns the prefix and
 // the block total.  s_warp: [THREADS / 32] shared words.
 __device__ __forceinline__ uint32_t block_scan(uint32_t x, uint32_t* s_warp, uint32_t& total) {
@@ -164,8 +224,9 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t x, uint32_t* s_warp, uin
   return before + inc - x;
 }
 
-// Pass 1.  sb_first / sb_before are written only with THR.
-template <typename Tv, bool VEC, bool THR>
+// Pass 1.  sb_first / sb_before are written only with THR, sum_frame only
+// with SUM.
+template <typename Tv, bool VEC, bool THR, bool SUM>
 __global__ void __launch_bounds__(THREADS)
     count_kernel(const Tv* __restrict__ frames, int32_t T, int64_t npix, int32_t thr,
                  uint16_t* __restrict__ sb_counts, uint16_t* __restrict__ sb_first, uint16_t* __restrict__ sb_before,
@@ -182,20 +243,24 @@ __global__ void __launch_bounds__(THREADS)
   uint32_t first[PX] = {NONE, NONE, NONE, NONE};
   long long sum[PX] = {0, 0, 0, 0};
   if (n_valid > 0) {
-    walk_frames<Tv, VEC>(
-        frames + t0 * npix + p0, npix, t0, t1, n_valid,
-        [&](const int32_t v[PX], int64_t t) {
+    if (VEC && !THR && !SUM) {
+      count_positive<Tv>(frames + t0 * npix + p0, npix, t1 - t0, cnt);
+    } else {
+      walk_frames<Tv, VEC>(
+          frames + t0 * npix + p0, npix, t0, t1, n_valid,
+          [&](const int32_t v[PX], int64_t t) {
 #pragma unroll
-          for (int j = 0; j < PX; ++j) {
-            if (THR && v[j] > thr && first[j] == NONE) {
-              first[j] = static_cast<uint32_t>(t - t0);
-              before[j] = cnt[j];
+            for (int j = 0; j < PX; ++j) {
+              if (THR && v[j] > thr && first[j] == NONE) {
+                first[j] = static_cast<uint32_t>(t - t0);
+                before[j] = cnt[j];
+              }
+              cnt[j] += v[j] > 0 ? 1u : 0u;
+              if (SUM) sum[j] += v[j];
             }
-            cnt[j] += v[j] > 0 ? 1u : 0u;
-            sum[j] += v[j];
-          }
-        },
-        [] { return true; });
+          },
+          [] { return true; });
+    }
 #pragma unroll
     for (int j = 0; j < PX; ++j) {
       if (j >= n_valid) break;
@@ -205,7 +270,7 @@ __global__ void __launch_bounds__(THREADS)
         sb_first[sb * npix + p] = static_cast<uint16_t>(first[j]);
         sb_before[sb * npix + p] = static_cast<uint16_t>(before[j]);
       }
-      if (sum_frame && sum[j] != 0)
+      if (SUM && sum[j] != 0)
         atomicAdd(reinterpret_cast<unsigned long long*>(&sum_frame[p]), static_cast<unsigned long long>(sum[j]));
     }
   }
@@ -264,7 +329,7 @@ __global__ void __launch_bounds__(THREADS)
                  uint32_t* __restrict__ tile_pos, uint32_t* __restrict__ stage, int64_t n_stage,
                  int32_t* __restrict__ err) {
   __shared__ uint32_t s_warp[THREADS / 32];
-  __shared__ uint32_t buf[STAGE_BUF];
+  extern __shared__ uint32_t buf[];  // STAGE_BUF words
   const int64_t sb = blockIdx.x;
   const int64_t n_blk = gridDim.y;
   const int64_t p0 = static_cast<int64_t>(blockIdx.y) * BLK_PX + static_cast<int64_t>(threadIdx.x) * PX;
@@ -318,12 +383,19 @@ __global__ void __launch_bounds__(THREADS)
 #pragma unroll
       for (int u = 0; u < CHUNK; ++u) raw[u] = mine ? *reinterpret_cast<const W*>(src + u * npix) : W{};
       uint32_t c[PX] = {0u, 0u, 0u, 0u};
+      if (CUT) {
 #pragma unroll
-      for (int u = 0; u < CHUNK; ++u) {
-        int32_t v[PX];
-        unpack4<Tv>(raw[u], v);
+        for (int u = 0; u < CHUNK; ++u) {
+          int32_t v[PX];
+          unpack4<Tv>(raw[u], v);
 #pragma unroll
-        for (int j = 0; j < PX; ++j) c[j] += v[j] > 0 && (!CUT || t + u < cut[j]) ? 1u : 0u;
+          for (int j = 0; j < PX; ++j) c[j] += v[j] > 0 && t + u < cut[j] ? 1u : 0u;
+        }
+      } else {
+        uint32_t a0 = 0, a1 = 0;  // CHUNK < 256 frames: no flush before the end
+#pragma unroll
+        for (int u = 0; u < CHUNK; ++u) add_positive<Tv>(raw[u], a0, a1);
+        flush_positive<Tv>(a0, a1, c);
       }
       bool over = false;
 #pragma unroll
@@ -488,37 +560,55 @@ int n_blocks(int64_t n, int64_t per, int sms, int waves) {
 bool kind_ok(int32_t k) { return k == 1 || k == 2 || k == -1 || k == -2; }
 int64_t kind_bytes(int32_t k) { return k < 0 ? -k : k; }
 
+template <typename Tv, bool SUM>
+void launch_count_sum(const Tv* f, bool vec, bool thr_on, dim3 grid, cudaStream_t st, int32_t T, int64_t npix,
+                      int32_t thr, uint16_t* sbc, uint16_t* sbf, uint16_t* sbb, uint32_t* blk, long long* sum) {
+  if (vec && thr_on)
+    cmp::count_kernel<Tv, true, true, SUM><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk, sum);
+  else if (vec)
+    cmp::count_kernel<Tv, true, false, SUM><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk, sum);
+  else if (thr_on)
+    cmp::count_kernel<Tv, false, true, SUM><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk, sum);
+  else
+    cmp::count_kernel<Tv, false, false, SUM><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk,
+                                                                           sum);
+}
+
 template <typename Tv>
 void launch_count(const void* frames, bool vec, bool thr_on, dim3 grid, cudaStream_t st, int32_t T, int64_t npix,
                   int32_t thr, uint16_t* sbc, uint16_t* sbf, uint16_t* sbb, uint32_t* blk, long long* sum) {
   const Tv* f = reinterpret_cast<const Tv*>(frames);
-  if (vec && thr_on)
-    cmp::count_kernel<Tv, true, true><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk, sum);
-  else if (vec)
-    cmp::count_kernel<Tv, true, false><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk, sum);
-  else if (thr_on)
-    cmp::count_kernel<Tv, false, true><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk, sum);
+  if (sum)
+    launch_count_sum<Tv, true>(f, vec, thr_on, grid, st, T, npix, thr, sbc, sbf, sbb, blk, sum);
   else
-    cmp::count_kernel<Tv, false, false><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, thr, sbc, sbf, sbb, blk, sum);
+    launch_count_sum<Tv, false>(f, vec, thr_on, grid, st, T, npix, thr, sbc, sbf, sbb, blk, sum);
+}
+
+template <typename Tv, bool VEC, bool CUT>
+int launch_stage_as(const Tv* f, dim3 grid, cudaStream_t st, int32_t T, int64_t npix, const uint16_t* sbc,
+                    const int32_t* cut, const uint32_t* base, int64_t n_tiles, uint32_t* tpos, uint32_t* stage,
+                    int64_t n_stage, int32_t* err) {
+  constexpr int smem = cmp::STAGE_BUF * 4;
+  if (cudaFuncSetAttribute(cmp::stage_kernel<Tv, VEC, CUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+      cudaSuccess)
+    return G2_ERR_CUDA;
+  cmp::stage_kernel<Tv, VEC, CUT><<<grid, cmp::THREADS, smem, st>>>(f, T, npix, sbc, cut, base, n_tiles, tpos, stage,
+                                                                    n_stage, err);
+  return G2_OK;
 }
 
 template <typename Tv>
-void launch_stage(const void* frames, bool vec, bool cut_on, dim3 grid, cudaStream_t st, int32_t T, int64_t npix,
-                  const uint16_t* sbc, const int32_t* cut, const uint32_t* base, int64_t n_tiles, uint32_t* tpos,
-                  uint32_t* stage, int64_t n_stage, int32_t* err) {
+int launch_stage(const void* frames, bool vec, bool cut_on, dim3 grid, cudaStream_t st, int32_t T, int64_t npix,
+                 const uint16_t* sbc, const int32_t* cut, const uint32_t* base, int64_t n_tiles, uint32_t* tpos,
+                 uint32_t* stage, int64_t n_stage, int32_t* err) {
   const Tv* f = reinterpret_cast<const Tv*>(frames);
   if (vec && cut_on)
-    cmp::stage_kernel<Tv, true, true><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, sbc, cut, base, n_tiles, tpos,
-                                                                     stage, n_stage, err);
-  else if (vec)
-    cmp::stage_kernel<Tv, true, false><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, sbc, cut, base, n_tiles, tpos,
-                                                                      stage, n_stage, err);
-  else if (cut_on)
-    cmp::stage_kernel<Tv, false, true><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, sbc, cut, base, n_tiles, tpos,
-                                                                      stage, n_stage, err);
-  else
-    cmp::stage_kernel<Tv, false, false><<<grid, cmp::THREADS, 0, st>>>(f, T, npix, sbc, cut, base, n_tiles, tpos,
-                                                                       stage, n_stage, err);
+    return launch_stage_as<Tv, true, true>(f, grid, st, T, npix, sbc, cut, base, n_tiles, tpos, stage, n_stage, err);
+  if (vec)
+    return launch_stage_as<Tv, true, false>(f, grid, st, T, npix, sbc, cut, base, n_tiles, tpos, stage, n_stage, err);
+  if (cut_on)
+    return launch_stage_as<Tv, false, true>(f, grid, st, T, npix, sbc, cut, base, n_tiles, tpos, stage, n_stage, err);
+  return launch_stage_as<Tv, false, false>(f, grid, st, T, npix, sbc, cut, base, n_tiles, tpos, stage, n_stage, err);
 }
 
 // Grid of the count and stage passes: (sub-blocks, 1024-pixel blocks).
@@ -604,24 +694,25 @@ extern "C" int g2_compress_stage(const void* frames_dev, int32_t elem_kind, int3
   const bool vec = npix % cmp::PX == 0 && aligned(frames_dev, static_cast<uintptr_t>(eb * cmp::PX));
   const bool cut_on = t_cut_dev != nullptr;
   cudaStream_t st = as_stream(stream);
+  int lrc;
   switch (elem_kind) {
     case 1:
-      launch_stage<uint8_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev, blk_base_dev,
-                            n_tiles, tile_pos_dev, stage_dev, n_stage, err_dev);
+      lrc = launch_stage<uint8_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev,
+                             blk_base_dev, n_tiles, tile_pos_dev, stage_dev, n_stage, err_dev);
       break;
     case -1:
-      launch_stage<int8_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev, blk_base_dev,
-                           n_tiles, tile_pos_dev, stage_dev, n_stage, err_dev);
+      lrc = launch_stage<int8_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev,
+                             blk_base_dev, n_tiles, tile_pos_dev, stage_dev, n_stage, err_dev);
       break;
     case 2:
-      launch_stage<uint16_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev,
+      lrc = launch_stage<uint16_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev,
                              blk_base_dev, n_tiles, tile_pos_dev, stage_dev, n_stage, err_dev);
       break;
     default:
-      launch_stage<int16_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev, blk_base_dev,
-                            n_tiles, tile_pos_dev, stage_dev, n_stage, err_dev);
+      lrc = launch_stage<int16_t>(frames_dev, vec, cut_on, grid, st, nframes, npix, sb_counts_dev, t_cut_dev,
+                             blk_base_dev, n_tiles, tile_pos_dev, stage_dev, n_stage, err_dev);
   }
-  return launch_status();
+  return lrc != G2_OK ? lrc : launch_status();
 }
 
 extern "C" int g2_stream_compress(const void* frames_dev, int32_t elem_kind, int32_t n_batch, int64_t frame0,
