@@ -868,6 +868,16 @@ COMPRESS_WORKLOAD = {
     "operation": "compress_all_stack (dense stack -> per-pixel event lists, times int32 + values u8 + offsets)",
     "l2": "input stack (5.3 GB) larger than L2; no flush",
 }
+
+
+def compress_config(T, **extra):
+    """The compression workload's config for a stack of T frames."""
+    H, W = COMPRESS_WORKLOAD["frame_shape"]
+    cfg = dict(COMPRESS_WORKLOAD, nframes=T, workload="compress_%dx%d_u8_T%d" % (H, W, T),
+               l2="input stack (%.2f GB) %s than L2; no flush" % (T * H * W / 1e9,
+                                                                 "larger" if T * H * W > 129e6 else "smaller"))
+    cfg.update(extra)
+    return cfg
 COMPRESS_CPU_FRAMES = 256
 
 
@@ -919,35 +929,39 @@ def run_compress(args):
     sampler.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    comp.profile = True  # CUDA events between the passes of every timed call
     e0.record(stream)
     for _ in range(args.steps):
         comp.run(frames)
     e1.record(stream)
     barrier()
     clocks = sampler.stop()
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    comp.profile = True
-    comp.run(frames)
-    st = comp.stage_times()
     comp.profile = False
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    st = comp.stage_times(calls=args.steps)
     stack_bytes = T * npix
     out_bytes = n_ev * 5 + (npix + 1) * 8
     peaks, peak_kind = measured_peaks()
-    # dominant kernel: the count pass (reads the stack once); the stage pass reads it again
+    # dominant kernel: the stage pass (reads the stack, writes a 4-byte word per event);
+    # the count pass reads the stack once more, the gather moves the words to the lists
     count_gbs = stack_bytes / (st["count"] / 1e3) / 1e9
-    stage_gbs = (stack_bytes + n_ev * 4) / (st["stage"] / 1e3) / 1e9
+    stage_bytes = stack_bytes + n_ev * 4
+    stage_gbs = stage_bytes / (st["stage"] / 1e3) / 1e9
+    traffic = profile_traffic("launches_compress_514x1030_T10000.md")
+    if traffic is not None:
+        traffic *= T / COMPRESS_WORKLOAD["nframes"]
     line = {
         "metric": "compress_frames_per_s", "value": world * T / (ms / 1e3), "unit": "frames/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": dict(COMPRESS_WORKLOAD, nframes=T, n_events=n_ev, parallelism="replicas" if world > 1 else "single"),
+        "config": compress_config(T, n_events=n_ev, parallelism="replicas" if world > 1 else "single"),
         "hbm_GB_per_s_step": (stack_bytes + out_bytes) / (ms / 1e3) / 1e9,
         "stages_ms": st,
-        "roofline": {"bound": "hbm", "achieved": count_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": count_gbs / peaks.get("hbm_gbs"), "traffic": None, "kernel": "g2_compress_count",
+        "roofline": {"bound": "hbm", "achieved": stage_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": stage_gbs / peaks.get("hbm_gbs"), "traffic": traffic, "kernel": "g2_compress_stage",
                      "peak_source": "%s hbm_gbs" % peak_kind,
-                     "algorithmic_bytes_per_launch": stack_bytes, "launch_ms": st["count"],
-                     "stage_pass_GB_per_s": stage_gbs,
+                     "algorithmic_bytes_per_launch": stage_bytes, "launch_ms": st["stage"],
+                     "count_pass_GB_per_s": count_gbs,
                      "note": "two passes read the stack (count, stage); the algorithmic minimum reads it once"},
         "clocks": clocks, "gpu_launches": 8 * args.steps,
     }
@@ -1019,7 +1033,7 @@ def run_compress_reference(args):
         "metric": "compress_frames_per_s", "value": v, "unit": "frames/s", "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": T / v * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": dict(COMPRESS_WORKLOAD, nframes=T),
+        "config": compress_config(T),
         "cpu_baseline": {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",
                          "sample": "each step: numpy compress_all_stack on the first %d of %d frames" % (Ts, T)},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

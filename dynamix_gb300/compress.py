@@ -111,13 +111,15 @@ class StackCompressor:
             e.record(torch.cuda.current_stream(self.dev))
             self.marks.append((name, e))
 
-    def stage_times(self):
-        """Milliseconds of each pass of the last profiled call (CUDA events)."""
+    def stage_times(self, calls=1):
+        """Milliseconds of each pass (CUDA events), averaged over the ``calls``
+        profiled calls since the last reading."""
         torch = _torch()
         torch.cuda.synchronize(self.dev)
         out = {}
         for (_, a), (name, b) in zip(self.marks, self.marks[1:]):
-            out[name] = out.get(name, 0.0) + a.elapsed_time(b)
+            if name != "start":  # "start" closes the gap between two calls
+                out[name] = out.get(name, 0.0) + a.elapsed_time(b) / calls
         self.marks = []
         return out
 
