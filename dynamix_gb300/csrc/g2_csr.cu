@@ -620,10 +620,66 @@ __global__ void __launch_bounds__(256)
   const bool buffered = total <= static_cast<uint32_t>(buf_words);
   uint32_t* out = buffered ? buf : (MODE == GATHER_REL_SPLIT ? reinterpret_cast<uint32_t*>(ev_times) : ev_words) + base;
   bool bad = false;
+  if (warp_runs && !(MODE == GATHER_WORDS && sort)) {
+    // long runs: a warp takes RUNS consecutive runs at a time (adjacent in the
+    // staging area) with its lanes on consecutive words, one load of each run
+    // in flight per lane before the stores
+    constexpr int RUNS = 4;
+    for (int e0 = warp * RUNS; e0 < n_sb * TILE_P; e0 += (256 / 32) * RUNS) {
+      uint32_t n[RUNS], d0[RUNS], t_add[RUNS];
+      const uint32_t* in[RUNS];
+      uint32_t nmax = 0;
+#pragma unroll
+      for (int r = 0; r < RUNS; ++r) {
+        const int e = e0 + r;
+        const int b = e / TILE_P, p = e % TILE_P;
+        n[r] = 0;
+        d0[r] = 0;
+        in[r] = stage;
+        t_add[r] = MODE == GATHER_REL_WORDS ? static_cast<uint32_t>(b) << 26 : static_cast<uint32_t>(b) * SUBBLOCK;
+        if (e >= n_sb * TILE_P || p >= np) continue;
+        const uint32_t c0 = cp[b * (TILE_P + 1) + p];
+        const uint32_t cnt = cp[b * (TILE_P + 1) + p + 1] - c0;
+        const int64_t src = static_cast<int64_t>(tp[b]) + c0;
+        const uint32_t d = dst[b * TILE_P + p];
+        if (src + cnt > n_elem || static_cast<int64_t>(d) + cnt > total) {
+          bad = true;
+          continue;
+        }
+        n[r] = cnt;
+        d0[r] = d;
+        in[r] = stage + src;
+        nmax = cnt > nmax ? cnt : nmax;
+      }
+      for (uint32_t k = lane; k < nmax; k += 32) {
+        uint32_t w[RUNS];
+#pragma unroll
+        for (int r = 0; r < RUNS; ++r) w[r] = k < n[r] ? in[r][k] : 0u;
+#pragma unroll
+        for (int r = 0; r < RUNS; ++r) {
+          if (k >= n[r]) continue;
+          uint32_t* run = out + d0[r];
+          if (MODE == GATHER_WORDS) {
+            run[k] = w[r];
+          } else if (MODE == GATHER_REL_WORDS) {
+            run[k] = w[r] + t_add[r];
+          } else {
+            run[k] = t_add[r] + (w[r] >> 16);  // frame number
+            if (buffered)
+              bufd[d0[r] + k] = static_cast<uint16_t>(w[r] & 0xFFFFu);
+            else
+              ev_data[base + d0[r] + k] = static_cast<Tv>(w[r] & 0xFFFFu);
+          }
+        }
+      }
+    }
+  }
   // a thread per (sub-block, pixel) run (a warp takes 32 consecutive pixels
   // of one sub-block, whose runs are adjacent in the staging area), or, with
-  // warp_runs (long runs), a warp per run with its lanes on consecutive words
-  const int r_first = warp_runs ? (threadIdx.x >> 5) : threadIdx.x;
+  // warp_runs (long runs) and sorting, a warp per run with its lanes on
+  // consecutive words
+  const int r_first = warp_runs ? ((MODE == GATHER_WORDS && sort) ? (threadIdx.x >> 5) : n_sb * TILE_P)
+                                : threadIdx.x;
   const int r_step = warp_runs ? 256 / 32 : 256;
   const uint32_t k0 = warp_runs ? (threadIdx.x & 31) : 0u, k_step = warp_runs ? 32u : 1u;
   for (int e = r_first; e < n_sb * TILE_P; e += r_step) {
