@@ -41,7 +41,7 @@ struct Cfg {
   static_assert(BUF % 16 == 0, "staging rows must keep 16-byte cp.async destinations aligned");
 };
 
-template <typename Tin, int MODE>
+template <typename Tin, int MODE, bool SUMS>
 __global__ void __launch_bounds__(THREADS, 3)
     pack_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix, const int32_t* __restrict__ chunk_entry_off,
                 const int32_t* __restrict__ entry_dst, const uint32_t* __restrict__ entry_meta,
@@ -200,8 +200,10 @@ __global__ void __launch_bounds__(THREADS, 3)
               range_bad |= 2u;
           }
         }
-        const uint32_t vs = __reduce_add_sync(gslot[k], v);
-        if (lead_s && vs) atomicAdd(&s_sum[f][sl], vs);
+        if (SUMS) {
+          const uint32_t vs = __reduce_add_sync(gslot[k], v);
+          if (lead_s && vs) atomicAdd(&s_sum[f][sl], vs);
+        }
         if (MODE == 1) {
           const uint32_t h = v >> 8, l = v & 255u;
           const uint32_t eh = __reduce_add_sync(gpiece[k], h * h);
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(THREADS, 3)
     __syncthreads();
 
     // ---- flush bin sums, fold piece energies into running maxima
-    for (int i = tid; i < F * MAX_SLOTS; i += THREADS) {
+    for (int i = tid; SUMS && i < F * MAX_SLOTS; i += THREADS) {
       const int f = i / MAX_SLOTS, sl = i - f * MAX_SLOTS;
       const uint32_t s = s_sum[f][sl];
       if (s) {
@@ -432,10 +434,15 @@ template <typename Tin, int MODE>
 void launch(dim3 grid, cudaStream_t st, const void* frames, int64_t T, int64_t npix, const int32_t* ceo,
             const int32_t* ed, const uint32_t* em, const int32_t* csb, const int32_t* cpo, const int32_t* bk,
             void* packed, int64_t cols, int64_t* sums, int n_bins, uint32_t* pe, int64_t n_pieces, int32_t* err) {
-  pack_kernel<Tin, MODE><<<grid, THREADS, 0, st>>>(reinterpret_cast<const Tin*>(frames), T, npix, ceo, ed, em, csb,
-                                                   cpo, bk, reinterpret_cast<uint8_t*>(packed), cols,
-                                                   reinterpret_cast<unsigned long long*>(sums), n_bins, pe, n_pieces,
-                                                   err);
+  auto* s = reinterpret_cast<unsigned long long*>(sums);
+  if (sums)
+    pack_kernel<Tin, MODE, true><<<grid, THREADS, 0, st>>>(reinterpret_cast<const Tin*>(frames), T, npix, ceo, ed,
+                                                           em, csb, cpo, bk, reinterpret_cast<uint8_t*>(packed),
+                                                           cols, s, n_bins, pe, n_pieces, err);
+  else
+    pack_kernel<Tin, MODE, false><<<grid, THREADS, 0, st>>>(reinterpret_cast<const Tin*>(frames), T, npix, ceo, ed,
+                                                            em, csb, cpo, bk, reinterpret_cast<uint8_t*>(packed),
+                                                            cols, s, n_bins, pe, n_pieces, err);
 }
 
 }  // namespace pack
@@ -449,7 +456,7 @@ extern "C" int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_
                               uint32_t* piece_emax_dev, int64_t n_pieces, int32_t* err_dev, void* stream) {
   using namespace g2;
   if (!frames_dev || !chunk_entry_off_dev || !entry_dst_dev || !entry_meta_dev || !chunk_slot_bin_dev ||
-      !chunk_piece_off_dev || !packed_dev || !sums_dev || !piece_emax_dev || !err_dev)
+      !chunk_piece_off_dev || !packed_dev || !piece_emax_dev || !err_dev)
     return G2_ERR_ARG;
   if ((elem_bytes != 1 && elem_bytes != 2) || nframes <= 0 || npix <= 0 || n_chunks < 0 ||
       n_chunks != (npix + G2_PACK_CHUNK - 1) / G2_PACK_CHUNK || mode < 0 || mode > 2 ||

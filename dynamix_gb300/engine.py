@@ -233,12 +233,23 @@ class DenseEngine:
             bufs[L.mode] = torch.zeros(n, dtype=torch.int32, device=self.dev)
         return bufs[L.mode]
 
+    def ones(self, L):
+        """Whether the packed operand of layout L carries the row of ones after
+        the frames, from which the tensor-core Gram takes the bin sums: e4m3
+        operands always, fp16 operands on the tensor-core path (the fp16 bit
+        pattern 1 is 2^-24, the scale of the counts; the pack then skips its
+        sum reduction).  Byte planes and the plain kernel get the sums from
+        the pack."""
+        return bool(L.ones_row or (L.mode == MODE_FP16 and self.method == "tc"))
+
     def _packed_buffer(self, L):
         """The packed operand buffer, [T (+1)][packed_cols]; zeroed whenever its
         layout changes, since the pack kernels write only the binned columns
-        (padding stays 0).  e4m3 layouts get the row of ones after the frames."""
+        (padding stays 0).  Layouts with :meth:`ones` get the row of ones after
+        the frames."""
         torch = _torch()
-        rows = self.T + (1 if L.ones_row else 0)
+        ones = self.ones(L)
+        rows = self.T + (1 if ones else 0)
         nbytes = rows * L.packed_bytes_per_frame
         fresh = False
         if self.packed is None or self.packed.numel() < nbytes:
@@ -250,7 +261,7 @@ class DenseEngine:
             fresh = True
         if fresh:
             self._packed_mode = L.mode
-            if L.ones_row:
+            if ones:
                 row = torch.from_numpy(L.ones_row_values().view(np.uint8)).to(self.dev)
                 off = self.T * L.packed_bytes_per_frame
                 self.packed[off:off + row.numel()].copy_(row)
@@ -289,8 +300,8 @@ class DenseEngine:
         _lib.check(self.lib.g2_pack_frames(
             ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_entry_off),
             ptr(L.d_entry_dst), ptr(L.d_entry_meta), ptr(L.d_chunk_slot_bin), ptr(L.d_chunk_piece_off),
-            ptr(L.d_bin_kpad), L.n_chunks, mode, ptr(packed), L.packed_cols, ptr(self.sums), self.n_bins,
-            ptr(emax), L.n_pieces, ptr(self.err), st), "g2_pack_frames")
+            ptr(L.d_bin_kpad), L.n_chunks, mode, ptr(packed), L.packed_cols, None if self.ones(L) else ptr(self.sums),
+            self.n_bins, ptr(emax), L.n_pieces, ptr(self.err), st), "g2_pack_frames")
         return L
 
     def items_for(self, L, grams):
@@ -298,7 +309,7 @@ class DenseEngine:
         if key not in self._items_cache:
             torch = _torch()
             items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method,
-                               s_base=0 if (L.ones_row and self.method == "tc") else None,
+                               s_base=0 if (self.ones(L) and self.method == "tc") else None,
                                super_rows=self.super_rows)
             dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
             if len(self._items_cache) > 8:
@@ -308,7 +319,7 @@ class DenseEngine:
 
     def numerator(self, L, items_dev, n_items):
         self.numer.zero_()
-        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, L.ones_row)])
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, self.ones(L))])
         st = stream_handle(self.dev)
         if self.method == "tc":
             _lib.check(self.lib.g2_gram_tc(jobs, 1, ptr(items_dev), n_items, ptr(self.numer), self.numer.numel(),
@@ -386,7 +397,7 @@ class DenseEngine:
         if key not in self._items_cache:
             torch = _torch()
             grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit, self.kslab)
-            items = gram_items(self.T, grams, job=0, out_base=0, kind="tc", s_base=0 if L.ones_row else None,
+            items = gram_items(self.T, grams, job=0, out_base=0, kind="tc", s_base=0 if self.ones(L) else None,
                                super_rows=self.super_rows)
             T = self.T
             n = max(1, min(self.pipe_chunks, T // 256))
@@ -451,7 +462,7 @@ class DenseEngine:
         copy_s.wait_event(start)
         pack_s.wait_event(start)
         npix, pc = self.npix, L.packed_cols
-        jobs = _lib.jobs_array([(packed.data_ptr(), self.T, pc, L.kind, L.ones_row)])
+        jobs = _lib.jobs_array([(packed.data_ptr(), self.T, pc, L.kind, self.ones(L))])
         item_bytes = _lib.ITEM_DTYPE.itemsize
         for c in range(bounds.size - 1):
             t0, t1 = int(bounds[c]), int(bounds[c + 1])
@@ -544,7 +555,7 @@ class DenseEngine:
         sd2.zero_()
         zeros.zero_()
         st = stream_handle(self.dev)
-        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, L.ones_row)])
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, self.ones(L))])
         if items.size:
             _lib.check(self.lib.g2_gram_std(jobs, 1, ptr(dev_items), items.size, ptr(self.sums), self.sums.numel(),
                                             ptr(self.g2_f32), ptr(sd), ptr(sd2), ptr(zeros), sd.numel(),
@@ -588,7 +599,7 @@ class DenseEngine:
         mirror = 1 if self.T <= 5 or not np.any(s_h[:-5] * s_h[5:] == 0) else 0
         out = torch.empty((self.T, self.T), dtype=torch.float32, device=self.dev)
         st = stream_handle(self.dev)
-        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, L.ones_row)])
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, self.ones(L))])
         _lib.check(self.lib.g2_gram_ttcf(jobs, 1, ptr(items_dev), mine.size, ptr(self.sums), self.sums.numel(),
                                          ptr(out), self.T, self.T, mirror, ptr(self.err), self.grid, st),
                    "g2_gram_ttcf")

@@ -473,7 +473,7 @@ class G2Server:
                     continue
                 off = job.arena_off
                 items = gram_items(job.T, grams, job=0, out_base=off, kind=self.method,
-                                   s_base=off if (L.ones_row and self.method == "tc") else None)
+                                   s_base=off if (eng.ones(L) and self.method == "tc") else None)
             except Exception as e:
                 self._release(job)
                 self._fail(job.req, e)
@@ -523,7 +523,7 @@ class G2Server:
             it["job"] = len(jobs)
             parts.append(it)
             L = job.layout
-            jobs.append((job.engine.packed.data_ptr(), job.T, L.packed_cols, L.kind, L.ones_row))
+            jobs.append((job.engine.packed.data_ptr(), job.T, L.packed_cols, L.kind, job.engine.ones(L)))
             taken.append((job, k, ops))
         if not parts:
             return False

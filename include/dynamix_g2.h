@@ -119,7 +119,8 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
  *   bin_kpad[bin] (the low-byte plane of the bin).
  * mode 2: the count as a byte at entry_dst (counts <= 16).
  * A count that does not fit the mode sets G2_DEVERR_RANGE in err_dev.
- * Adds S_b(t) into sums_dev[b * nframes + t] (caller zeroes it) and raises
+ * Adds S_b(t) into sums_dev[b * nframes + t] (caller zeroes it; null: no bin
+ * sums, for operands whose Gram takes them from a row of ones) and raises
  * piece_emax_dev[plane * n_pieces + piece] (caller zeroes it) to the max over
  * frames of the sum of squared packed values of the piece (plane 1 = low bytes).
  * Packed columns that no entry maps to (bin padding) are not written.
