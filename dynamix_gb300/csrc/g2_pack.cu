@@ -7,13 +7,15 @@
 // once, coalesced), then every thread moves its binned pixels -- up to 8 per
 // thread, their destinations kept in registers for the whole kernel -- to the
 // packed matrix.  Within a chunk the pixels of one bin are consecutive packed
-// columns, so the stores of a warp are contiguous.  Bin sums and the
-// squared-count energies used for the Gram's exact K split are reduced per warp
-// (match_any + reduce_add), then per block in shared memory; S gets one int64
-// atomic per (chunk, bin, frame).  Energies are kept per "piece" = (64-column
-// output segment) x (chunk): piece_emax[p] = max over frames of the piece's
-// sum of squares; the host sums the pieces of a segment, which bounds the
-// segment's energy in every frame.
+// columns, so the stores of a warp are contiguous.  Bin sums (when asked for:
+// a Gram with a row of ones gives them otherwise) and the squared-count
+// energies used for the Gram's exact K split are reduced per warp (match_any +
+// reduce_add), then per block in shared memory; S gets one int64 atomic per
+// (chunk, bin, frame).  Energies are kept per "piece" = (64-column output
+// segment) x (chunk): per step of F frames each entry takes its largest
+// square, and piece_emax[p] = max over steps of the piece's sum of those,
+// which bounds the piece's sum of squares in every frame; the host sums the
+// pieces of a segment, which bounds the segment's energy in every frame.
 // Replaces compute_sums_dense (densecorrelator.cl:65-150) and the gather /
 // float32 cast of py_dense_correlator (dense.py:48-50).
 #include "g2_ptx.cuh"
@@ -34,7 +36,7 @@ constexpr int PPT = MAX_PIECES / THREADS;  // pieces per thread for the running 
 // the unaligned start).
 template <typename Tin>
 struct Cfg {
-  static constexpr int F = sizeof(Tin) == 1 ? 4 : 2;
+  static constexpr int F = 4;
   static constexpr int CHUNK_BYTES = CH * static_cast<int>(sizeof(Tin));
   static constexpr int BUF = CHUNK_BYTES + 16;
   static constexpr int WORDS = CHUNK_BYTES / 16 + 1;  // 16-byte words covering one unaligned chunk
@@ -51,11 +53,11 @@ __global__ void __launch_bounds__(THREADS, 3)
                 int64_t n_pieces, int32_t* __restrict__ err) {
   using C = Cfg<Tin>;
   constexpr int F = C::F;
-  constexpr int PL = MODE == 1 ? 2 : 1;  // energy planes
+  constexpr int PL = MODE == 1 ? 2 : 1;  // energy planes (mode 1: high and low bytes)
   __shared__ __align__(16) uint8_t s_buf[2][F][C::BUF];  // double buffer: cp.async fills one while
                                                           // the other is consumed
   __shared__ uint32_t s_sum[F][MAX_SLOTS];
-  __shared__ uint32_t s_e[PL][F][MAX_PIECES];
+  __shared__ uint32_t s_e[PL][MAX_PIECES];
   __shared__ int s_bin[MAX_SLOTS];
   __shared__ int s_kpad[MAX_SLOTS];
 
@@ -100,7 +102,7 @@ __global__ void __launch_bounds__(THREADS, 3)
     s_kpad[tid] = (b >= 0 && MODE == 1) ? bin_kpad[b] : 0;
   }
   for (int i = tid; i < F * MAX_SLOTS; i += THREADS) (&s_sum[0][0])[i] = 0;
-  for (int i = tid; i < PL * F * MAX_PIECES; i += THREADS) (&s_e[0][0][0])[i] = 0;
+  for (int i = tid; i < PL * MAX_PIECES; i += THREADS) (&s_e[0][0])[i] = 0;
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
   uint32_t run_max[PL][PPT];
 #pragma unroll
@@ -108,6 +110,7 @@ __global__ void __launch_bounds__(THREADS, 3)
 #pragma unroll
     for (int j = 0; j < PPT; ++j) run_max[q][j] = 0;
   uint32_t range_bad = 0;
+  uint32_t sq_max = 0;  // largest squared count this thread moved (modes 0 and 2)
   const int64_t total_bytes = T * npix * static_cast<int64_t>(sizeof(Tin));
   const uint8_t* fbytes = reinterpret_cast<const uint8_t*>(frames);
   const int64_t row_bytes = packed_cols * (MODE == 2 ? 1 : 2);
@@ -176,6 +179,7 @@ __global__ void __launch_bounds__(THREADS, 3)
       const int pc = static_cast<int>(meta[k] >> 18);
       const bool lead_s = (__ffs(gslot[k]) - 1) == lane;
       const bool lead_p = (__ffs(gpiece[k]) - 1) == lane;
+      uint32_t e0 = 0, e1 = 0;  // the entry's largest squared value(s) over the step's frames
 #pragma unroll
       for (int f = 0; f < F; ++f) {
         const int64_t t = t0 + f;
@@ -206,16 +210,23 @@ __global__ void __launch_bounds__(THREADS, 3)
         }
         if (MODE == 1) {
           const uint32_t h = v >> 8, l = v & 255u;
-          const uint32_t eh = __reduce_add_sync(gpiece[k], h * h);
-          const uint32_t el = __reduce_add_sync(gpiece[k], l * l);
-          if (lead_p && eh) atomicAdd(&s_e[0][f][pc], eh);
-          if (lead_p && el) atomicAdd(&s_e[PL - 1][f][pc], el);
+          e0 = max(e0, h * h);
+          e1 = max(e1, l * l);
         } else {
           // counts above the mode's range are flagged; keep the energy finite
-          const uint32_t vv = v <= 2048u ? v * v : 4194304u;
-          const uint32_t e = __reduce_add_sync(gpiece[k], vv);
-          if (lead_p && e) atomicAdd(&s_e[0][f][pc], e);
+          e0 = max(e0, v <= 2048u ? v * v : 4194304u);
         }
+      }
+      // The piece's sum over its entries of each entry's largest square over
+      // the step's frames bounds the piece's sum of squares in each of them:
+      // one reduction per step instead of one per frame.
+      const uint32_t ea = __reduce_add_sync(gpiece[k], e0);
+      if (lead_p && ea) atomicAdd(&s_e[0][pc], ea);
+      if (MODE == 1) {
+        const uint32_t eb = __reduce_add_sync(gpiece[k], e1);
+        if (lead_p && eb) atomicAdd(&s_e[1][pc], eb);
+      } else {
+        sq_max = max(sq_max, e0);
       }
     }
     __syncthreads();
@@ -237,11 +248,8 @@ __global__ void __launch_bounds__(THREADS, 3)
       for (int j = 0; j < PPT; ++j) {
         const int pc = tid + j * THREADS;
         if (pc < np) {
-#pragma unroll
-          for (int f = 0; f < F; ++f) {
-            run_max[q][j] = max(run_max[q][j], s_e[q][f][pc]);
-            s_e[q][f][pc] = 0;
-          }
+          run_max[q][j] = max(run_max[q][j], s_e[q][pc]);
+          s_e[q][pc] = 0;
         }
       }
     // the accumulators are reused and the buffer just read is refilled by the
@@ -257,6 +265,11 @@ __global__ void __launch_bounds__(THREADS, 3)
       if (pc < np && g0 + pc < n_pieces && run_max[q][j])
         atomicMax(&piece_emax[q * n_pieces + g0 + pc], run_max[q][j]);
     }
+  if (MODE != 1) {
+    // the chunk's largest squared count, in plane 1 at its first piece
+    const uint32_t m = __reduce_max_sync(0xffffffffu, sq_max);
+    if (lane == 0 && m && np > 0 && g0 < n_pieces) atomicMax(&piece_emax[n_pieces + g0], m);
+  }
   if (range_bad & 1u) atomicOr(err, G2_DEVERR_RANGE);
   if (range_bad & 2u) atomicOr(err, G2_DEVERR_BOUNDS);
 }

@@ -228,7 +228,7 @@ class DenseEngine:
         layout itself may be shared by other engines)."""
         torch = _torch()
         bufs = self.__dict__.setdefault("_emax_bufs", {})
-        n = max(1, L.n_pieces * L.n_planes)
+        n = max(1, L.n_pieces * 2)  # two planes (g2_pack_frames)
         if L.mode not in bufs or bufs[L.mode].numel() < n:
             bufs[L.mode] = torch.zeros(n, dtype=torch.int32, device=self.dev)
         return bufs[L.mode]
@@ -351,7 +351,8 @@ class DenseEngine:
             if mode == MODE_E4M3:
                 seg_emax = e4m3_segment_bound(L)          # counts <= 16 bound every sum
             else:
-                seg_emax = L.segment_emax(self._piece_emax(L).cpu().numpy().view(np.uint32))
+                pe = self._piece_emax(L).cpu().numpy().view(np.uint32)
+                seg_emax = L.segment_emax(pe)
             code = int(self.err.item())
             wide = frames_dev.element_size() == 2
             if code & _lib.DEVERR_RANGE and mode == MODE_E4M3 and self.operand == "auto":
@@ -375,9 +376,9 @@ class DenseEngine:
                     mode = MODE_BYTES
                     continue
                 raise
-            if (mode == MODE_FP16 and self.method == "tc" and self.operand == "auto" and seg_emax.size
-                    and int(seg_emax.max()) < 17 * 17):
-                # every count <= 16: the next call can use e4m3
+            if (mode == MODE_FP16 and self.method == "tc" and self.operand == "auto" and L.n_pieces
+                    and int(pe[L.n_pieces: 2 * L.n_pieces].max()) <= 16 * 16):
+                # every count <= 16 (the chunks' largest squares): the next call can use e4m3
                 if frames_dev.element_size() == 1:
                     self._u8_hint = MODE_E4M3
                 else:

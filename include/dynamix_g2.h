@@ -121,8 +121,12 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
  * A count that does not fit the mode sets G2_DEVERR_RANGE in err_dev.
  * Adds S_b(t) into sums_dev[b * nframes + t] (caller zeroes it; null: no bin
  * sums, for operands whose Gram takes them from a row of ones) and raises
- * piece_emax_dev[plane * n_pieces + piece] (caller zeroes it) to the max over
- * frames of the sum of squared packed values of the piece (plane 1 = low bytes).
+ * piece_emax_dev[plane * n_pieces + piece] (2 * n_pieces words; caller zeroes
+ * them): plane 0 (and, in mode 1, plane 1 for the low bytes) bounds the sum of
+ * squared packed values of the piece in every frame (the max over groups of 4
+ * frames of the sum over entries of each entry's largest square in the
+ * group); in modes 0 and 2 plane 1 holds, at each chunk's first piece, the
+ * largest squared value of the chunk (0 elsewhere).
  * Packed columns that no entry maps to (bin padding) are not written.
  */
 int g2_pack_frames(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
