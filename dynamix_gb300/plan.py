@@ -147,8 +147,9 @@ class PackLayout:
 
     def segment_emax(self, piece_emax):
         """Per 64-column output segment, the sum over its pieces of the pieces'
-        max-over-frames energies: an upper bound of the segment's energy in
-        every frame (indexed by packed column // 64)."""
+        energy bounds (each bounds its piece's sum of squares in every frame):
+        an upper bound of the segment's energy in every frame (indexed by
+        packed column // 64)."""
         pe = np.asarray(piece_emax, dtype=np.float64)
         nseg = self.packed_cols // BK
         out = np.bincount(self.piece_seg, weights=pe[: self.n_pieces], minlength=nseg)
