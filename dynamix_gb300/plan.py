@@ -209,18 +209,17 @@ def k_chunks(emax_a, emax_b, limit=EXACT_LIMIT):
         raise OverflowError("a packed unit exceeds the exact fp32 bound")
     if n and ea.sum() * eb.sum() <= lim2:
         return [(0, n)]
+    # greedy: each chunk takes units while the product of its sums fits (the
+    # sums are integers below 2^53, so prefix-sum differences are exact)
+    sa = np.concatenate(([0.0], np.cumsum(ea)))
+    sb = np.concatenate(([0.0], np.cumsum(eb)))
     chunks = []
     u0 = 0
-    sa = sb = 0.0
-    for u in range(n):
-        na, nb = sa + ea[u], sb + eb[u]
-        if na * nb > lim2:
-            chunks.append((u0, u))
-            u0, sa, sb = u, ea[u], eb[u]
-        else:
-            sa, sb = na, nb
-    if n:
-        chunks.append((u0, n))
+    while u0 < n:
+        over = np.flatnonzero((sa[u0 + 1:] - sa[u0]) * (sb[u0 + 1:] - sb[u0]) > lim2)
+        u1 = n if over.size == 0 else u0 + int(over[0])
+        chunks.append((u0, u1))
+        u0 = u1
     return chunks
 
 
