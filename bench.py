@@ -11,9 +11,10 @@ with the frames in pinned host memory (``MatMulCorrelator.correlate``: H2D copy,
 pipeline, g2 back to the host).  The stack (5.3 GB) is larger than L2, so no
 flush is needed between steps.
 
-``--impl reference`` times the CPU baseline instead: the float32 restatement
-of the reference's MatMulCorrelator (numpy BLAS on all host cores) on the
-first 2048 frames of the same stack, scaled to 10,000 frames by its O(T^2) cost.
+``--impl reference`` times the CPU reference instead: the reference's own
+MatMulCorrelator (numpy BLAS on all host cores; its float32 restatement when
+the reference package is not installed) on all 10,000 frames of the same
+stack, one full-size call.
 
 Multi-GPU (torchrun): independent replicas, one stack per GPU ("weak" scaling).
 """
@@ -92,7 +93,10 @@ def profile_traffic(name, key="traffic_bytes_per_launch"):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons every 100 ms during the timed region,
+    for this process's GPU only (matched by UUID); when no sample matches the
+    UUID the clocks are reported as unavailable rather than taken from the
+    other GPUs of the machine."""
 
     FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -124,8 +128,10 @@ class ClockSampler:
         rows = [[x.strip() for x in line.split(",")] for line in self.out.read().splitlines()]
         os.unlink(self.out.name)
         rows = [r for r in rows if len(r) >= 8]
-        mine = [r for r in rows if self.uuid and self.uuid in r[0].lower()]
-        rows = mine or rows
+        rows = [r for r in rows if self.uuid and self.uuid in r[0].lower()]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None,
+                    "reasons": ["unavailable: no nvidia-smi sample matched this GPU's UUID"]}
         sm, smax, power, reasons = [], [], [], set()
         for r in rows:
             try:
@@ -142,6 +148,37 @@ class ClockSampler:
                 "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
 
 
+def tc_rate(dev, kind, iters=40000, reps=5):
+    """Dense MMA rate (TFLOP/s, 2 ops per MAC) of this GPU for the Gram's
+    operand kind, from the library's own tcgen05 probe (M128 N256, operands
+    resident in shared memory, one CTA per SM; best of ``reps`` launches timed
+    with CUDA events on the launching stream)."""
+    import ctypes
+    import torch
+    from dynamix_gb300 import _lib
+    lib = _lib.load()
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    h = ctypes.c_void_p(stream.cuda_stream)
+    _lib.check(lib.g2_tc_rate_probe(kind, 2000, 0, ctypes.c_void_p(err.data_ptr()), h), "g2_tc_rate_probe")
+    best = float("inf")
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(lib.g2_tc_rate_probe(kind, iters, 0, ctypes.c_void_p(err.data_ptr()), h), "g2_tc_rate_probe")
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    if int(err.item()):
+        raise RuntimeError("tensor-core probe: " + _lib.device_error_message(int(err.item())))
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    k = 32 if kind == _lib.KIND_E4M3 else 16
+    macs = sms * iters * 4 * 128 * 256 * k
+    return 2.0 * macs / (best / 1e3) / 1e12, {"launch_ms": best, "ctas": sms, "iters": iters,
+                                              "mma": "tcgen05 M128 N256 K%d x4 per iteration" % k}
+
+
 def make_workload(dev, T):
     from dynamix_gb300.speckle import annular_qmask, speckle_torch
     H, W = WORKLOAD["frame_shape"]
@@ -151,15 +188,43 @@ def make_workload(dev, T):
     return frames, qmask
 
 
+def reference_matmul():
+    """(correlate(frames, qmask) callable, kind, label) of the CPU MatMul
+    correlator: the reference's own ``MatMulCorrelator`` (dense.py:118-142,
+    imported from the installed reference package behind inert OpenCL stubs)
+    when the package is present, else its float32 restatement."""
+    try:
+        from oracle.ref_import import import_module
+        dense = import_module("dynamix.correlator.dense")
+
+        def run(frames, qmask):
+            return dense.MatMulCorrelator(frames.shape[1:], frames.shape[0], qmask=qmask).correlate(frames)
+        return run, "reference", "the reference's own MatMulCorrelator.correlate (numpy float32 BLAS)"
+    except ImportError:
+        from oracle.g2_oracle import matmul_correlator_port
+
+        def run(frames, qmask):
+            return matmul_correlator_port(frames, qmask)
+        return run, "port", "float32 restatement of MatMulCorrelator (numpy BLAS)"
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
+
+
 def cpu_port_time(frames_host, qmask, repeats=1):
-    """Seconds per call of the float32 MatMulCorrelator restatement (all host threads)."""
-    from oracle.g2_oracle import matmul_correlator_port
+    """Seconds per call of the CPU MatMul correlator (all host threads), with its kind and label."""
+    run, kind, label = reference_matmul()
     ts = []
     for _ in range(repeats):
         t0 = time.perf_counter()
-        matmul_correlator_port(frames_host, qmask)
+        with __import__("numpy").errstate(all="ignore"):
+            run(frames_host, qmask)
         ts.append(time.perf_counter() - t0)
-    return ts
+    return ts, kind, label
 
 
 def cpu_scale(T_full, t_sample, T_sample):
@@ -167,33 +232,41 @@ def cpu_scale(T_full, t_sample, T_sample):
     return T_full / (t_sample * (T_full / T_sample) ** 2)
 
 
+REF_WARMUP_FRAMES = 256
+
+
 def run_reference(args):
+    """The CPU reference on the whole workload: one call of the MatMul
+    correlator on all 10,000 frames (all host cores), after a warm-up call on
+    the first frames.  One full-size call takes minutes, so the run measures
+    exactly one step whatever --steps asks for, and says so."""
     import numpy as np
     import torch
     rank, world, local = dist_info()
     if rank != 0:
         return 0
     T_full = args.frames
-    Ts = min(CPU_SAMPLE_FRAMES, T_full)
     dev = torch.device("cuda", local) if torch.cuda.is_available() else torch.device("cpu")
-    frames, qmask = make_workload(dev, Ts)
+    frames, qmask = make_workload(dev, T_full)
     host = frames.cpu().numpy()
     del frames
-    for _ in range(args.warmup):
-        cpu_port_time(host, qmask)
-    ts = cpu_port_time(host, qmask, repeats=args.steps)
-    t = sum(ts) / len(ts)
-    v = cpu_scale(T_full, t, Ts)
-    ncores = os.cpu_count()
+    Tw = min(REF_WARMUP_FRAMES, T_full)
+    cpu_port_time(np.ascontiguousarray(host[:Tw]), qmask)
+    ts, kind, label = cpu_port_time(host, qmask, repeats=1)
+    t = ts[0]
+    v = T_full / t
+    ncores = host_cores()
     line = {
         "metric": "g2_frames_per_s", "value": v, "unit": "frames/s", "impl": "reference", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "steps": 1, "warmup": 1, "steps_requested": args.steps, "warmup_requested": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(WORKLOAD, nframes=T_full),
-        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": ncores, "kind": "port",
-                         "sample": "first %d of the %d frames, all 16 bins; float32 MatMulCorrelator restatement "
-                                   "(numpy BLAS, %d threads); O(T^2) cost scaled to %d frames"
-                                   % (Ts, T_full, ncores, T_full)},
+        "config": dict(WORKLOAD, nframes=T_full, parallelism="single"),
+        "note": "one full-size call (all %d frames, all 16 bins) timed; a warm-up call on the first %d frames "
+                "before it; more steps would take minutes each" % (T_full, Tw),
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": ncores, "kind": kind,
+                         "sample": "the whole workload: %s on all %d frames, %d host threads, %.1f s"
+                                   % (label, T_full, ncores, t)},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -284,14 +357,17 @@ def run_ours(args):
     peaks, peak_kind = measured_peaks()
     gram_avg = sum(gram_ms) / len(gram_ms)
     achieved = 2.0 * macs / (gram_avg / 1e3) / 1e12
-    # Denominator of the Gram roofline: the measured dense bf16 burst rate (the
-    # kernel runs at full clock, below the power cap), doubled for e4m3
-    # operands (dense fp8 = 2 x dense bf16 on this part; derived, not measured).
-    bf16 = peaks.get("bf16_tflops")
-    if info.get("mode") == "e4m3":
-        peak, peak_src = 2.0 * bf16, "%s bf16_tflops x 2 (dense e4m3 rate, derived)" % peak_kind
-    else:
-        peak, peak_src = bf16, "%s bf16_tflops (dense f16 rate)" % peak_kind
+    # Denominator of the Gram roofline: the dense rate of the MMA kind the Gram
+    # ran on, measured in this run by the library's own tcgen05 probe (the
+    # kernel runs at full clock, below the power cap, like the probe).
+    from dynamix_gb300 import _lib as L
+    kind = L.KIND_E4M3 if info.get("mode") == "e4m3" else L.KIND_FP16
+    peak, probe = tc_rate(dev, kind)
+    peak_f16, _ = tc_rate(dev, L.KIND_FP16) if kind == L.KIND_E4M3 else (peak, None)
+    peak_src = ("tcgen05 kind::%s rate measured in this run (g2_tc_rate_probe: %d CTAs x %d iterations of "
+                "4 x M128 N256 MMAs on shared-memory operands, best of 5, %.3f ms)"
+                % ("f8f6f4 e4m3" if kind == L.KIND_E4M3 else "f16", probe["ctas"], probe["iters"],
+                   probe["launch_ms"]))
     pack_bytes = T * H * W + T * info["packed_cols"] * (1 if info.get("mode") == "e4m3" else 2)
     pack_avg = sum(pack_ms) / len(pack_ms)
     traffic = profile_traffic("gram_tc_dense_514x1030_%s.md" % info.get("mode"))
@@ -309,7 +385,9 @@ def run_ours(args):
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic, "kernel": "g2_gram_tc",
                      "peak_source": peak_src,
-                     "algorithmic_ops_per_launch": 2 * macs, "launch_ms": gram_avg},
+                     "algorithmic_ops_per_launch": 2 * macs, "launch_ms": gram_avg,
+                     "other_peaks": {"tcgen05_f16_probe": peak_f16, "bf16_cublas_" + peak_kind: peaks.get(
+                         "bf16_tflops")}},
         "stages_ms": {"pack": pack_avg, "gram_tc": gram_avg,
                       "note": "stage times from %d steps run unpipelined (one pack, one Gram launch); the timed "
                               "steps overlap the pack of frame chunk c+1 with the Gram tiles chunk c completes "
@@ -343,33 +421,46 @@ def run_ours(args):
                        "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
         del host
 
-    # ---- same-GPU plain (CUDA-core) comparator
+    # ---- same-GPU plain (CUDA-core) comparators: the u8 __dp4a kernel (four
+    # byte products per instruction) and the 32-bit IMAD kernel on fp16-packed
+    # counts; the speed-up is stated against the faster of the two
     if not args.no_plain:
-        pc = MatMulCorrelator((H, W), T, qmask=qmask, extra_options={"method": "plain"})
-        pc.correlate_device(frames)
-        barrier()
-        e0.record(stream)
-        nplain = 2
-        for _ in range(nplain):
+        plain = {}
+        for method in ("dp4a", "plain"):
+            pc = MatMulCorrelator((H, W), T, qmask=qmask, extra_options={"method": method})
             pc.correlate_device(frames)
-        e1.record(stream)
-        barrier()
-        pms = max_over_ranks(e0.elapsed_time(e1) / nplain)
-        same = bool(torch.equal(pc.engine.numer, eng.numer) and torch.equal(pc.engine.denom, eng.denom))
-        line["plain"] = {"ms_per_step": pms, "value": world * T / (pms / 1e3), "unit": "frames/s",
-                         "speedup_tc_vs_plain": pms / ms, "bit_identical_N_D": same}
-        del pc
+            barrier()
+            e0.record(stream)
+            nplain = 2
+            for _ in range(nplain):
+                pc.correlate_device(frames)
+            e1.record(stream)
+            barrier()
+            pc.engine.check_error()
+            pms = max_over_ranks(e0.elapsed_time(e1) / nplain)
+            same = bool(torch.equal(pc.engine.numer, eng.numer) and torch.equal(pc.engine.denom, eng.denom)
+                        and torch.equal(pc.engine.sums, eng.sums))
+            plain[method] = {"ms_per_step": pms, "value": world * T / (pms / 1e3), "unit": "frames/s",
+                             "bit_identical_N_S_D": same,
+                             "kernel": {"dp4a": "g2_plain_dp4a (u8 counts, __dp4a, 128x128 blocks)",
+                                        "plain": "g2_plain_direct (fp16-packed counts, 32-bit IMAD)"}[method],
+                             "int_tops": 2.0 * macs / (pms / 1e3) / 1e12}
+            del pc
+        best = min(plain, key=lambda m: plain[m]["ms_per_step"])
+        line["plain"] = dict(plain[best], method=best, speedup_tc_vs_plain=plain[best]["ms_per_step"] / ms,
+                             bit_identical_N_D=plain[best]["bit_identical_N_S_D"], comparators=plain)
 
     # ---- CPU baseline (rank 0, bounded sample)
     if not args.no_cpu and rank == 0:
         Ts = min(CPU_SAMPLE_FRAMES, T)
         host = frames[:Ts].cpu().numpy()
-        ts = cpu_port_time(host, qmask)
-        ncores = os.cpu_count()
+        ts, kind, label = cpu_port_time(host, qmask)
+        ncores = host_cores()
         line["cpu_baseline"] = {
-            "value": cpu_scale(T, ts[0], Ts), "unit": "frames/s", "cores": ncores, "kind": "port",
-            "sample": "first %d of the %d frames, all 16 bins; float32 MatMulCorrelator restatement (numpy BLAS, "
-                      "%d threads) took %.2f s; O(T^2) cost scaled to %d frames" % (Ts, T, ncores, ts[0], T)}
+            "value": cpu_scale(T, ts[0], Ts), "unit": "frames/s", "cores": ncores, "kind": kind,
+            "sample": "first %d of the %d frames, all 16 bins; %s, %d threads, took %.2f s; O(T^2) cost scaled "
+                      "to %d frames (the reference arm times all %d frames)" % (Ts, T, label, ncores, ts[0], T,
+                                                                               T)}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

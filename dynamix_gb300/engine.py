@@ -153,12 +153,14 @@ class DenseEngine:
         self.npix = self.shape[0] * self.shape[1]
         self.qmask = np.ascontiguousarray(qmask, dtype=np.int32)
         self.n_bins = int(n_bins)
-        if method not in ("tc", "plain"):
-            raise ValueError("method must be 'tc' or 'plain'")
+        if method not in ("tc", "plain", "dp4a"):
+            raise ValueError("method must be 'tc', 'plain' or 'dp4a'")
         if operand != "auto" and operand not in self.MODES:
             raise ValueError("operand must be 'auto', 'e4m3', 'fp16' or 'bytes'")
         if method == "plain" and operand == "e4m3":
             raise ValueError("the plain kernel reads fp16 operands")
+        if method == "dp4a" and operand not in ("auto", "e4m3"):
+            raise ValueError("the dp4a kernel reads the raw u8 counts (the e4m3 packing)")
         self.method = method
         self.operand = operand
         self.exact_limit = int(exact_limit)
@@ -309,7 +311,7 @@ class DenseEngine:
         if key not in self._items_cache:
             torch = _torch()
             items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method,
-                               s_base=0 if (self.ones(L) and self.method == "tc") else None,
+                               s_base=0 if (self.ones(L) and self.method in ("tc", "dp4a")) else None,
                                super_rows=self.super_rows)
             dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
             if len(self._items_cache) > 8:
@@ -325,6 +327,10 @@ class DenseEngine:
             _lib.check(self.lib.g2_gram_tc(jobs, 1, ptr(items_dev), n_items, ptr(self.numer), self.numer.numel(),
                                            ptr(self.sums), self.sums.numel(), ptr(self.err), self.grid, st),
                        "g2_gram_tc")
+        elif self.method == "dp4a":
+            _lib.check(self.lib.g2_plain_dp4a(jobs, 1, ptr(items_dev), n_items, ptr(self.numer),
+                                              self.numer.numel(), ptr(self.sums), self.sums.numel(), ptr(self.err),
+                                              st), "g2_plain_dp4a")
         else:
             _lib.check(self.lib.g2_plain_direct(jobs, 1, ptr(items_dev), n_items, ptr(self.numer),
                                                 self.numer.numel(), ptr(self.err), st), "g2_plain_direct")
@@ -515,6 +521,8 @@ class DenseEngine:
             frames_dev = frames_to_device(frames_dev, self.dev)
         self._events = []
         self._mark("split")
+        if self.method == "dp4a":
+            return self._run_dp4a(frames_dev)
         mode = self.choose_mode(frames_dev)
         self._mark("pack")
         L, grams = self._pack_and_plan(frames_dev, mode)
@@ -526,6 +534,31 @@ class DenseEngine:
         self._mark("end")
         self.last = {"mode": ["fp16", "bytes", "e4m3"][L.mode], "split": int(L.split), "n_items": int(items.size),
                      "n_grams": n_chunks, "packed_cols": L.packed_cols}
+        return self.g2_f32[: self.n_bins]
+
+    def _run_dp4a(self, frames_dev):
+        """The u8 plain comparator: the e4m3 pack (a byte permutation, so the
+        packed matrix holds the raw u8 counts whatever their range), then the
+        __dp4a direct kernel over 128 x 128 blocks of at most 65,536 columns
+        (exact uint32 entries for any u8 counts), bin sums from the row of
+        ones, G3, G4."""
+        if frames_dev.element_size() != 1:
+            raise ValueError("the dp4a kernel reads u8 counts")
+        self._mark("pack")
+        L = self.pack(frames_dev, MODE_E4M3)
+        code = int(self.err.item()) & ~_lib.DEVERR_RANGE      # counts > 16 are fine here
+        if code:
+            raise DeviceError(_lib.device_error_message(code))
+        self.err.zero_()
+        grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit, self.kslab)
+        items, items_dev, n_chunks = self.items_for(L, grams)
+        self._mark("gram_dp4a")
+        self.numerator(L, items_dev, items.size)
+        self._mark("normalise")
+        self.normalise()
+        self._mark("end")
+        self.last = {"mode": "u8", "split": 0, "n_items": int(items.size), "n_grams": n_chunks,
+                     "packed_cols": L.packed_cols}
         return self.g2_f32[: self.n_bins]
 
     def deviation(self):

@@ -2,7 +2,10 @@
  * dynamix_g2.h -- C ABI of the GB300 (sm_103a) g2 correlator kernels.
  *
  * All pointers named *_dev are device pointers owned by the caller; the
- * library allocates no device memory.  Every entry point is asynchronous on
+ * library allocates no device memory at run time.  The one device buffer it
+ * holds itself is the file-scope array of g2_normalize_static
+ * (G2_STATIC_DENOM_MAX int64, 4 MiB), which every GPU that loads the library
+ * keeps until the process exits.  Every entry point is asynchronous on
  * the given CUDA stream (a cudaStream_t passed as void*; NULL = legacy default
  * stream), returns a status code (G2_OK = 0) and never throws.  Argument
  * errors are detected on the host before anything is launched.
@@ -181,6 +184,27 @@ int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev
 int g2_plain_direct(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev,
                     int64_t n_items, uint64_t* numer_dev, int64_t numer_len, int32_t* err_dev,
                     void* stream);
+
+/* The same direct integer sums on the raw u8 counts, four byte products per
+ * __dp4a (the fastest CUDA-core form of correlator_multiQ_dense,
+ * dynamix/resources/opencl/densecorrelator.cl:6-56, for 8-bit frames).
+ * Packed operand: the e4m3 packing of g2_pack_e4m3, read as raw u8 bytes
+ * (elem_kind G2_KIND_E4M3, any count 0..255).  Items: 128 x 128 blocks with
+ * k_len a multiple of 64 and <= 65,536 (uint32 entries exact for any u8);
+ * with the job's row of ones and s_off >= 0 the bin sums are added to
+ * sums_dev as in g2_gram_tc. */
+int g2_plain_dp4a(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev,
+                  int64_t n_items, uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev,
+                  int64_t sums_len, int32_t* err_dev, void* stream);
+
+/* ---- tensor-core rate probe ---------------------------------------------
+ * No counterpart in the reference: a measurement utility.  One CTA per SM
+ * (grid <= 0) or `grid` CTAs each issue `iters` x 4 tcgen05.mma M128 N256
+ * (K = 32 for kind G2_KIND_E4M3, 16 for G2_KIND_FP16) on shared-memory
+ * resident count-like operands, no global memory traffic: the dense rate of
+ * the MMA kind the Gram uses, for its roofline.  MACs per launch =
+ * grid * iters * 4 * 128 * 256 * K. */
+int g2_tc_rate_probe(int32_t kind, int64_t iters, int32_t grid, int32_t* err_dev, void* stream);
 
 /* ---- G6: event-list pair sums -------------------------------------------
  * Replaces event_correlator (dynamix/resources/opencl/evtcorrelator.cl:3-47)
@@ -408,7 +432,11 @@ int g2_finalize(const int64_t* numer_dev, const int64_t* denom_dev, const double
  * library holds until the process exits; n_rows * nframes above that maximum
  * returns G2_ERR_TOO_LARGE.  The caller passes N, S, scale and the outputs.
  * The first call on a device looks up that array's device address (with the
- * device current) -- make that first call before any stream capture.  All
+ * device current) -- make that first call before any stream capture.  The
+ * address is cached per device ordinal for the life of the process: after a
+ * cudaDeviceReset (or any teardown of the device's primary context) the
+ * cached address is stale, so do not call this entry point again in that
+ * process after such a reset.  All
  * calls share the one array and it keeps the last call's contents (every
  * element a call reads is written by the same call first, so nothing needs
  * clearing); calls whose work overlaps on the GPU race on it.  This entry

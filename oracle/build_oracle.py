@@ -43,7 +43,18 @@ def load():
 
 # ---- the reference's own event kernels, compiled as C (only where the
 # reference sources are present; the outputs stay in oracle/_ref/)
-REF_ROOT = "/root/reference"
+
+
+def reference_root():
+    """Where the dynamix sources are: ``$DYNAMIX_REFERENCE_ROOT`` when set, else
+    a directory ``reference`` beside this repository's root."""
+    env = os.environ.get("DYNAMIX_REFERENCE_ROOT")
+    if env:
+        return env
+    return os.path.abspath(os.path.join(HERE, "..", "..", "reference"))
+
+
+REF_ROOT = reference_root()
 REF_CL = os.path.join(REF_ROOT, "dynamix", "resources", "opencl", "evtcorrelator.cl")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_MAX_EVT_COUNT = 4096

@@ -146,4 +146,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, os.path.abspath(os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..")))
+    from oracle.build_oracle import reference_root
+    main(sys.argv[1] if len(sys.argv) > 1 else reference_root())

@@ -309,3 +309,48 @@ def test_64_narrow_bins(built_lib, cuda_device, bright):
     g = c.correlate(fr)
     assert c.engine.last["mode"] == ("bytes" if bright else "fp16")
     assert_exact(c, o.g2_exact(fr, qm), g)
+
+
+# ---- the u8 __dp4a plain comparator -----------------------------------------
+@pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_128x128_u8"])
+def test_dp4a_golden_cases(built_lib, cuda_device, name):
+    z = golden(name)
+    ref = o.g2_exact(z["frames"], z["qmask"])
+    c, g = run(z["frames"], z["qmask"], "dp4a")
+    assert c.engine.last["mode"] == "u8"
+    assert_exact(c, ref, g)
+
+
+def test_dp4a_edges_and_ragged(built_lib, cuda_device):
+    z = golden("dense_edge")
+    fr = z["frames"]
+    for qm in (None, z["qmask_gap"]):
+        c, g = run(fr, qm, "dp4a")
+        assert_exact(c, o.g2_exact(fr, qm), g)
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    for T in (1, 127, 129, 257):
+        fr = speckle_numpy(T, (20, 26), 0.95, 3.0, seed=T)
+        qm = annular_qmask((20, 26), 3, 1.0, 12.0)
+        c, g = run(fr, qm, "dp4a")
+        assert_exact(c, o.g2_exact(fr, qm), g)
+
+
+def test_dp4a_saturated_wide_bin(built_lib, cuda_device):
+    """Counts of 255 over a 70,000-pixel bin: one Gram entry is 70,000 * 255^2
+    > 2^32, so the K split at 65,536 columns is what keeps the uint32
+    accumulators exact."""
+    T, shape = 40, (1, 70000)
+    rng = np.random.default_rng(3)
+    fr = np.where(rng.random((T,) + shape) < 0.95, 255, rng.integers(0, 255, (T,) + shape)).astype(np.uint8)
+    qm = np.ones(shape, np.int32)
+    qm[0, :100] = 2
+    ref = o.g2_exact(fr, qm)
+    c, g = run(fr, qm, "dp4a")
+    assert c.engine.last["n_grams"] >= 3
+    assert_exact(c, ref, g)
+
+
+def test_dp4a_rejects_u16(built_lib, cuda_device):
+    fr = np.full((8, 4, 4), 300, dtype=np.uint16)
+    with pytest.raises(ValueError):
+        run(fr, None, "dp4a")

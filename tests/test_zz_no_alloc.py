@@ -39,7 +39,11 @@ def test_normalize_static_matches_two_step(built_lib, cuda_device):
     lib = built_lib
     dev = cuda_device
     stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
-    for call, (n_rows, T, seed) in enumerate([(16, 3000, 1), (5, 777, 2)]):
+    from dynamix_gb300 import _lib
+    # the last case fills the array exactly (8 x 65536 = G2_STATIC_DENOM_MAX elements): its last element and
+    # the boundary of the size check are exercised
+    cases = [(16, 3000, 1), (5, 777, 2), (8, _lib.STATIC_DENOM_MAX // 8, 3)]
+    for call, (n_rows, T, seed) in enumerate(cases):
         S, N, scale = _inputs(torch, dev, n_rows, T, seed)
         # existing entry points, caller-owned denominator
         D = torch.empty((n_rows, T), dtype=torch.int64, device=dev)
