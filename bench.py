@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--frames", type=int, default=None, help="override T (testing only)")
     p.add_argument("--shape", default=None, help="H,W of the sparse/event frames (profiling only)")
+    p.add_argument("--tile", default=None, choices=["pair", "single"],
+                   help="tensor-core block of the dense Gram (default: the engine's)")
     p.add_argument("--workload", default="dense", choices=["dense", "u16", "sparse", "event", "serving", "compress"],
                    help="dense: 514x1030x10k u8 Gram path (default); sparse / event: 2162x2068x20k CSR or "
                         "per-pixel event lists through the pair-sum path")
@@ -293,7 +295,7 @@ def run_ours(args):
     T = args.frames
     frames, qmask = make_workload(dev, T)
     H, W = WORKLOAD["frame_shape"]
-    corr = MatMulCorrelator((H, W), T, qmask=qmask)
+    corr = MatMulCorrelator((H, W), T, qmask=qmask, extra_options={"tile": args.tile} if args.tile else {})
     eng = corr.engine
     npix = np.bincount(qmask.ravel(), minlength=17)[1:]
     macs = gram_macs(T, npix)
@@ -341,15 +343,23 @@ def run_ours(args):
     # with CUDA events on the launching stream around each stage
     eng.profile = True
     eng.pipeline = False
-    gram_ms, pack_ms = [], []
     n_attr = max(3, min(args.steps, 10))
-    corr.correlate_device(frames)
-    eng.take_events()
-    for _ in range(n_attr):
+    tile0 = eng.tile
+    by_tile = {}
+    for tile in (tile0, "single" if tile0 == "pair" else "pair"):
+        eng.tile = tile
+        g_ms, p_ms = [], []
         corr.correlate_device(frames)
-        st = eng.stage_times(eng.take_events())
-        gram_ms.append(st.get("gram_tc", float("nan")))
-        pack_ms.append(st.get("pack", float("nan")))
+        eng.take_events()
+        for _ in range(n_attr):
+            corr.correlate_device(frames)
+            st = eng.stage_times(eng.take_events())
+            g_ms.append(st.get("gram_tc", float("nan")))
+            p_ms.append(st.get("pack", float("nan")))
+        eng.check_error()
+        by_tile[tile] = (g_ms, p_ms)
+    eng.tile = tile0
+    gram_ms, pack_ms = by_tile[tile0]
     eng.profile = False
     eng.pipeline = True
     serial_info = dict(eng.last)
@@ -388,7 +398,8 @@ def run_ours(args):
                      "algorithmic_ops_per_launch": 2 * macs, "launch_ms": gram_avg,
                      "other_peaks": {"tcgen05_f16_probe": peak_f16, "bf16_cublas_" + peak_kind: peaks.get(
                          "bf16_tflops")}},
-        "stages_ms": {"pack": pack_avg, "gram_tc": gram_avg,
+        "gram_ms_by_tile": {t: sum(v[0]) / len(v[0]) for t, v in by_tile.items()},
+        "stages_ms": {"pack": pack_avg, "gram_tc": gram_avg, "tile": tile0,
                       "note": "stage times from %d steps run unpipelined (one pack, one Gram launch); the timed "
                               "steps overlap the pack of frame chunk c+1 with the Gram tiles chunk c completes "
                               "(%d chunks)" % (n_attr, chunks)},

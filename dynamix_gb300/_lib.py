@@ -54,6 +54,7 @@ SIGNATURES = {
     "g2_pack_e4m3": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _p, _p]),
     "g2_binned_max": (C.c_int, [_p, _i32, _i64, _i64, _p, _i64, _p, _p]),
     "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
+    "g2_gram_tc_pair": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
     "g2_plain_dp4a": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _p]),
     "g2_tc_rate_probe": (C.c_int, [_i32, _i64, _i32, _p, _p]),

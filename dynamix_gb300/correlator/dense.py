@@ -37,7 +37,7 @@ class _DenseBase(BaseCorrelator):
         self.engine = DenseEngine(self.shape, self.nframes, self.qmask, self.n_bins, scale,
                                   device=opts.get("device"), method=opts.get("method", "tc"),
                                   exact_limit=opts.get("exact_limit", 1 << 24), grid=opts.get("grid", 0),
-                                  operand=opts.get("operand", "auto"))
+                                  operand=opts.get("operand", "auto"), tile=opts.get("tile"))
 
     def correlate_device(self, frames):
         """Run on the device and return the float32 g2 device tensor (no copy back).

@@ -23,7 +23,7 @@ import threading
 import numpy as np
 
 from . import _lib
-from .plan import (E4M3_MAX_EXACT, EXACT_LIMIT, FP16_MAX_EXACT, MODE_BYTES, MODE_E4M3, MODE_FP16, TC_BN,
+from .plan import (E4M3_MAX_EXACT, EXACT_LIMIT, FP16_MAX_EXACT, MODE_BYTES, MODE_E4M3, MODE_FP16, TILE_SHAPES,
                    PackLayout, chunk_grams, e4m3_segment_bound, gram_items)
 
 
@@ -138,13 +138,17 @@ class DenseEngine:
     ``operand`` selects the packed element type of the tensor-core Gram:
     ``"auto"`` (e4m3 when every binned count is <= 16, else fp16 counts when
     <= 2048, else fp16 byte planes), or one of ``"e4m3"``, ``"fp16"``,
-    ``"bytes"``.  The plain comparator always uses fp16."""
+    ``"bytes"``.  The plain comparator always uses fp16.
+
+    ``tile`` selects the tensor-core kernel: ``"pair"`` (256 x 256 blocks on
+    CTA pairs, g2_gram_tc_pair) or ``"single"`` (128 x 256 blocks, one CTA
+    each, g2_gram_tc)."""
 
     MODES = {"fp16": MODE_FP16, "bytes": MODE_BYTES, "e4m3": MODE_E4M3}
 
     def __init__(self, shape, nframes, qmask, n_bins, scale, device=None, method="tc",
                  exact_limit=EXACT_LIMIT, grid=0, operand="auto", numer=None, sums=None, layouts=None,
-                 qmask_digest=None):
+                 qmask_digest=None, tile=None):
         torch = _torch()
         self.lib = _lib.load()
         self.dev = require_cuda(device)
@@ -163,6 +167,10 @@ class DenseEngine:
             raise ValueError("the dp4a kernel reads the raw u8 counts (the e4m3 packing)")
         self.method = method
         self.operand = operand
+        tile = self.TILE if tile is None else tile
+        if tile not in ("pair", "single"):
+            raise ValueError("tile must be 'pair' or 'single'")
+        self.tile = tile
         self.exact_limit = int(exact_limit)
         self.grid = int(grid)
         self.scale = torch.as_tensor(np.asarray(scale, dtype=np.float64), device=self.dev)
@@ -306,11 +314,18 @@ class DenseEngine:
             self.n_bins, ptr(emax), L.n_pieces, ptr(self.err), st), "g2_pack_frames")
         return L
 
+    @property
+    def item_kind(self):
+        """The planner's block kind of this engine's numerator kernel."""
+        if self.method == "tc":
+            return "pair" if self.tile == "pair" else "tc"
+        return self.method
+
     def items_for(self, L, grams):
-        key = (L.mode, self.method, tuple(grams), self.super_rows)
+        key = (L.mode, self.item_kind, tuple(grams), self.super_rows)
         if key not in self._items_cache:
             torch = _torch()
-            items = gram_items(self.T, grams, job=0, out_base=0, kind=self.method,
+            items = gram_items(self.T, grams, job=0, out_base=0, kind=self.item_kind,
                                s_base=0 if (self.ones(L) and self.method in ("tc", "dp4a")) else None,
                                super_rows=self.super_rows)
             dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
@@ -324,9 +339,7 @@ class DenseEngine:
         jobs = _lib.jobs_array([(self.packed.data_ptr(), self.T, L.packed_cols, L.kind, self.ones(L))])
         st = stream_handle(self.dev)
         if self.method == "tc":
-            _lib.check(self.lib.g2_gram_tc(jobs, 1, ptr(items_dev), n_items, ptr(self.numer), self.numer.numel(),
-                                           ptr(self.sums), self.sums.numel(), ptr(self.err), self.grid, st),
-                       "g2_gram_tc")
+            self.gram_launch(jobs, items_dev.data_ptr(), n_items, st)
         elif self.method == "dp4a":
             _lib.check(self.lib.g2_plain_dp4a(jobs, 1, ptr(items_dev), n_items, ptr(self.numer),
                                               self.numer.numel(), ptr(self.sums), self.sums.numel(), ptr(self.err),
@@ -334,6 +347,14 @@ class DenseEngine:
         else:
             _lib.check(self.lib.g2_plain_direct(jobs, 1, ptr(items_dev), n_items, ptr(self.numer),
                                                 self.numer.numel(), ptr(self.err), st), "g2_plain_direct")
+
+    def gram_launch(self, jobs, items_ptr, n_items, stream):
+        """One launch of the tensor-core Gram kernel this engine's tile selects."""
+        fn, name = ((self.lib.g2_gram_tc_pair, "g2_gram_tc_pair") if self.tile == "pair"
+                    else (self.lib.g2_gram_tc, "g2_gram_tc"))
+        _lib.check(fn(jobs, 1, C.c_void_p(items_ptr), n_items, ptr(self.numer), self.numer.numel(), ptr(self.sums),
+                      self.sums.numel(), ptr(self.err), self.grid,
+                      stream if isinstance(stream, C.c_void_p) else C.c_void_p(stream)), name)
 
     def normalise(self):
         st = stream_handle(self.dev)
@@ -392,6 +413,7 @@ class DenseEngine:
             return L, grams
 
     # -- chunked pipeline (e4m3) ---------------------------------------------
+    TILE = "single"
     PIPE_CHUNKS = 8
     SUPER_ROWS = 2048
     KSLAB = 0                 # no cap on the K columns of one tile item
@@ -400,17 +422,18 @@ class DenseEngine:
         """Items of the e4m3 Gram grouped by the frame chunk whose packing
         makes them ready (a tile needs frames up to its last column), LPT order
         inside a group; cached per layout."""
-        key = ("pipe", L.mode, self.T, self.exact_limit, self.grid, self.pipe_chunks, self.super_rows, self.kslab)
+        key = ("pipe", L.mode, self.T, self.exact_limit, self.grid, self.pipe_chunks, self.super_rows, self.kslab,
+               self.item_kind)
         if key not in self._items_cache:
             torch = _torch()
             grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit, self.kslab)
-            items = gram_items(self.T, grams, job=0, out_base=0, kind="tc", s_base=0 if self.ones(L) else None,
-                               super_rows=self.super_rows)
+            items = gram_items(self.T, grams, job=0, out_base=0, kind=self.item_kind,
+                               s_base=0 if self.ones(L) else None, super_rows=self.super_rows)
             T = self.T
             n = max(1, min(self.pipe_chunks, T // 256))
             step = -(-(-(-T // n)) // 128) * 128               # chunk of frames, a multiple of 128
             bounds = np.array(list(range(0, T, step)) + [T], dtype=np.int64)
-            need = np.minimum(items["j0"].astype(np.int64) + TC_BN, T)
+            need = np.minimum(items["j0"].astype(np.int64) + TILE_SHAPES[self.item_kind][1], T)
             grp = np.searchsorted(bounds[1:], need, side="left")
             order = np.argsort(grp, kind="stable")
             items, grp = items[order], grp[order]
@@ -488,10 +511,7 @@ class DenseEngine:
             cur.wait_event(e)
             k0, k1 = int(starts[c]), int(starts[c + 1])
             if k1 > k0:
-                _lib.check(self.lib.g2_gram_tc(jobs, 1, dev_items.data_ptr() + k0 * item_bytes, k1 - k0,
-                                               ptr(self.numer), self.numer.numel(), ptr(self.sums),
-                                               self.sums.numel(), ptr(self.err), self.grid, cur.cuda_stream),
-                           "g2_gram_tc")
+                self.gram_launch(jobs, dev_items.data_ptr() + k0 * item_bytes, k1 - k0, cur.cuda_stream)
         self._mark("normalise")
         self.normalise()
         self._mark("end")
@@ -502,7 +522,7 @@ class DenseEngine:
             self._u8_hint = MODE_FP16                 # counts above 16: rerun on fp16 operands
             return self.run(frames_dev, pipelined=False)
         self.last = {"mode": "e4m3", "split": int(L.split), "n_items": int(items.size), "n_grams": n_grams,
-                     "packed_cols": L.packed_cols, "pipeline_chunks": int(bounds.size - 1)}
+                     "packed_cols": L.packed_cols, "pipeline_chunks": int(bounds.size - 1), "tile": self.tile}
         return self.g2_f32[: self.n_bins]
 
     # -- whole pipeline ----------------------------------------------------
@@ -533,7 +553,8 @@ class DenseEngine:
         self.normalise()
         self._mark("end")
         self.last = {"mode": ["fp16", "bytes", "e4m3"][L.mode], "split": int(L.split), "n_items": int(items.size),
-                     "n_grams": n_chunks, "packed_cols": L.packed_cols}
+                     "n_grams": n_chunks, "packed_cols": L.packed_cols,
+                     "tile": self.tile if self.method == "tc" else self.method}
         return self.g2_f32[: self.n_bins]
 
     def _run_dp4a(self, frames_dev):

@@ -31,6 +31,13 @@ SUPER_ROWS = 2048       # frames per side of a super-tile
 
 MODE_FP16, MODE_BYTES, MODE_E4M3 = 0, 1, 2
 
+# (rows, columns) of one Gram item per kernel: the single-CTA tensor-core
+# block (g2_gram_tc), the CTA-pair block (g2_gram_tc_pair: 256 rows over two
+# SMs), and the CUDA-core comparators' blocks
+PAIR_BM, PAIR_BN = 256, 256
+TILE_SHAPES = {"tc": (TC_BM, TC_BN), "pair": (PAIR_BM, PAIR_BN), "plain": (PLAIN_BM, PLAIN_BN),
+               "dp4a": (PLAIN_BM, PLAIN_BN)}
+
 
 def _roundup(x, m):
     return (x + m - 1) // m * m
@@ -251,14 +258,15 @@ def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc", s_base=None, supe
 
     ``chunked_grams``: iterable of ``(bin, a_off, b_off, k0, k_len, shift)`` with
     columns relative to the job's packed matrix.  ``kind`` selects the block
-    shape (tensor-core 128x256 or plain 128x128).  Items are sorted by k_len
+    shape (:data:`TILE_SHAPES`: single-CTA tensor-core 128x256, CTA-pair
+    256x256, CUDA-core 128x128).  Items are sorted by k_len
     (descending, stable) so that the persistent kernel's static round-robin
     schedule starts with the longest items.  ``s_base`` (tensor-core items of a
     job whose packed matrix carries the row of ones): element offset of the
     job's bin sums; the blocks then also cover that row and add S_b(t) at
     ``s_base + b * T + t``.
     """
-    bm, bn = (TC_BM, TC_BN) if kind == "tc" else (PLAIN_BM, PLAIN_BN)
+    bm, bn = TILE_SHAPES[kind]
     i0, j0 = _tiles(int(T), bm, bn, super_rows=int(super_rows), extra_col=s_base is not None)
     parts = []
     for (b, a_off, b_off, k0, klen, shift) in chunked_grams:

@@ -177,6 +177,18 @@ int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev
                uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
                int32_t* err_dev, int32_t grid, void* stream);
 
+/* The same Gram on CTA pairs (replaces the same reference code as
+ * g2_gram_tc): an item covers a 256 x n block, rows [i0, i0+256) against rows
+ * [j0, j0+n), n = min(256, frames (and row of ones) left from j0, rounded up
+ * to 32).  Two CTAs on two SMs share one tcgen05.mma.cta_group::2 M256: each
+ * loads its own 128 rows of A and n/2 rows of B per stage (32 KB), so each SM
+ * streams a third less from L2 per MMA cycle than g2_gram_tc.  Same item
+ * fields, exactness contract and outputs.  grid <= 0: as many CTA pairs as
+ * can be resident; otherwise about grid CTAs (rounded up to pairs). */
+int g2_gram_tc_pair(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                    uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
+                    int32_t* err_dev, int32_t grid, void* stream);
+
 /* ---- G5: plain direct kernel (CUDA cores, integer) ----------------------
  * The same-GPU non-tensor-core comparator: the direct integer numerator of
  * correlator_multiQ_dense (dynamix/resources/opencl/densecorrelator.cl:6-56),

@@ -47,15 +47,15 @@ def load():
 
 def reference_root():
     """Where the dynamix sources are: ``$DYNAMIX_REFERENCE_ROOT`` when set, else
-    a directory ``reference`` beside this repository's root."""
-    env = os.environ.get("DYNAMIX_REFERENCE_ROOT")
-    if env:
-        return env
-    return os.path.abspath(os.path.join(HERE, "..", "..", "reference"))
+    a ``reference`` checkout beside this repository, else the package
+    installed under ``baseline/_ref`` (see ``oracle/ref_import.py``)."""
+    from oracle.ref_import import candidate_roots, find_root
+    return find_root() or candidate_roots()[0]
 
 
 REF_ROOT = reference_root()
-REF_CL = os.path.join(REF_ROOT, "dynamix", "resources", "opencl", "evtcorrelator.cl")
+REF_OPENCL = os.path.join(REF_ROOT, "dynamix", "resources", "opencl")
+REF_CL = os.path.join(REF_OPENCL, "evtcorrelator.cl")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_MAX_EVT_COUNT = 4096
 REF_DTYPES = {"u8": "uchar", "u16": "ushort"}
@@ -105,3 +105,50 @@ def load_ref(tag):
         lib.g2r_max_evt_count.restype = i
         _ref[tag] = lib
     return _ref[tag]
+
+
+# ---- the reference's dense and CSR kernels (work-group barriers and local
+# memory), compiled as C with opencl_wg_shim.h and run by ref_wg_driver.c
+REF_WG_FILES = {"dense": "densecorrelator.cl", "csr": "correlator.cl"}
+
+
+def build_ref_wg(kind, defines, force=False):
+    """Compile the reference's ``densecorrelator.cl`` (kind "dense") or
+    ``correlator.cl`` (kind "csr") with the compile-time parameters the
+    reference passes to the OpenCL compiler (``defines``: name -> value, e.g.
+    IMAGE_WIDTH, NUM_BINS, DTYPE), into ``oracle/_ref/``.  Returns the library
+    path, or None when the reference sources are absent."""
+    cl = os.path.join(REF_OPENCL, REF_WG_FILES[kind])
+    if not os.path.exists(cl):
+        return None
+    os.makedirs(REF_DIR, exist_ok=True)
+    shim = os.path.join(HERE, "opencl_wg_shim.h")
+    drv = os.path.join(HERE, "ref_wg_driver.c")
+    tag = "_".join("%s%s" % (k, str(v).replace(" ", "")) for k, v in sorted(defines.items()))
+    lib = os.path.join(REF_DIR, "lib%s_%s.so" % (kind, tag))
+    newest = max(os.path.getmtime(p) for p in (cl, shim, drv))
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < newest:
+        defs = ["-D%s=%s" % (k, v) for k, v in sorted(defines.items())]
+        defs.append("-DG2W_DENSE" if kind == "dense" else "-DG2W_CSR")
+        tmp = lib + ".%d.tmp" % os.getpid()
+        subprocess.run(["gcc", "-O1", "-std=gnu11", "-w", "-fPIC", "-shared", "-pthread", "-fsigned-char", "-I", HERE]
+                       + defs + ["-include", shim, "-x", "c", cl, "-x", "none", drv, "-o", tmp], check=True)
+        os.replace(tmp, lib)
+    return lib
+
+
+def load_ref_wg(kind, defines):
+    """ctypes handle of :func:`build_ref_wg`'s library, or None."""
+    path = build_ref_wg(kind, defines)
+    if path is None:
+        return None
+    lib = ctypes.CDLL(path)
+    p, i = ctypes.c_void_p, ctypes.c_int
+    if kind == "dense":
+        lib.g2w_dense_sums.argtypes = [p, p, p, i, i]
+        lib.g2w_dense_corr1d.argtypes = [p, p, i, i]
+        lib.g2w_dense_numerator.argtypes = [p, p, p, p, i, i, i]
+    else:
+        lib.g2w_csr_sums.argtypes = [p, p, p, i]
+        lib.g2w_csr_correlate.argtypes = [p, p, p, p, p, p, p, i, i]
+    return lib

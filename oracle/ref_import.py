@@ -96,6 +96,13 @@ def install_stubs():
     for name in ("h5py", "hdf5plugin", "fabio"):
         if missing(name):
             _mod(name, File=_Inert, open=_Inert)
+    if missing("psutil"):
+        _mod("psutil", cpu_count=lambda logical=True: os.cpu_count())
+    # the Fortran extension (setup.py builds it with numpy.distutils; no
+    # Fortran compiler here): only referenced at import time on these paths
+    if "dynamix.correlator.WXPCS" not in sys.modules:
+        _mod("dynamix.correlator.WXPCS", fecorrt=_Inert, fecorr=_Inert, dropimgood=_Inert, eigerpix=_Inert,
+             droplet3=_Inert)
 
 
 def import_module(name, root=None):

@@ -187,3 +187,29 @@ def test_compressed_stack_feeds_event_correlator(built_lib, cuda_device):
     ref = o.g2_exact(fr, qm)
     assert np.array_equal(c.numerator, ref["numerator"])
     assert np.array_equal(g, ref["g2"].astype(np.float32), equal_nan=True)
+
+
+@pytest.mark.parametrize("name", ["neiger_thr40", "neiger_thr0", "neiger_nomask"])
+def test_hot_pixel_matches_reference_reader(built_lib, cuda_device, name):
+    """Threshold, sticky mask, sum frame and trace against the buffers of the
+    reference's own neigercompress (io/readdata.py:441-457) called frame by
+    frame (tests/golden/make_eventy_golden.py): bit-exact."""
+    import torch
+    from dynamix_gb300.compress import compress_all_stack_device
+    z = golden(name)
+    fr = z["frames"]
+    cnt = z["cnt"].astype(np.int64)
+    rd = np.concatenate([z["evs"][p, 1:c + 1] for p, c in enumerate(cnt)]).astype(np.int64)
+    rt = np.concatenate([z["tms"][p, 1:c + 1] for p, c in enumerate(cnt)]).astype(np.int64)
+    ro = np.concatenate([[0], np.cumsum(cnt)])
+    m = torch.from_numpy(z["mask0"].astype(np.uint8).copy()).to(cuda_device)
+    s = torch.zeros(fr[0].size, dtype=torch.int64, device=cuda_device)
+    d, t, off = compress_all_stack_device(torch.from_numpy(fr).to(cuda_device), threshold=int(z["threshold"]),
+                                          mask=m, sum_frame=s)
+    assert np.array_equal(_to_np(off).astype(np.int64), ro)
+    assert np.array_equal(_to_np(t).astype(np.int64), rt)
+    assert np.array_equal(_to_np(d).astype(np.int64), rd)
+    assert np.array_equal(_to_np(m).astype(bool), z["mask_after"].astype(bool))
+    assert np.array_equal(_to_np(s), z["afr"].astype(np.int64))
+    trace = np.bincount(_to_np(t).astype(np.int64), weights=_to_np(d).astype(np.float64), minlength=fr.shape[0])
+    assert np.array_equal(trace.astype(np.int64), z["trace"].astype(np.int64))

@@ -67,3 +67,24 @@ def test_ttcf_rejects_bad_bin(built_lib, cuda_device):
     c.correlate(fr)
     with pytest.raises(ValueError):
         c.two_time(int(qm.max()) + 1)
+
+
+@pytest.mark.parametrize("name", ["eventy_ttcf_small", "eventy_ttcf_dark", "eventy_ttcf_tiles"])
+def test_matches_reference_event_engine(built_lib, cuda_device, name):
+    """The two-time matrix, g2 and deviation against the outputs of the
+    reference's own nbecorrts_q (event_y.py:104-165, run by
+    tests/golden/make_eventy_golden.py): the reference computes in float32,
+    so the float32 results agree to 2e-6 relative (TTCF, g2) and the
+    deviation to 1e-3 (float statistics on both sides); NaN positions equal."""
+    from dynamix_gb300.correlator import MatMulCorrelator
+    z = golden(name)
+    fr, qm, q = z["frames"], z["qmask"], int(z["ttcf_par"])
+    c = MatMulCorrelator(fr.shape[1:], fr.shape[0], qmask=qm)
+    res, dev = c.correlate(fr, calc_std=True)
+    _same(c.two_time(q), z["trc"].astype(np.float64))
+    _same(res[:, 1:], z["res"].astype(np.float64))
+    want = z["dev"].astype(np.float64)
+    got = c.engine.dev_f64[: c.n_bins].cpu().numpy()[:, 1:]
+    assert np.array_equal(np.isfinite(got), np.isfinite(want))
+    ok = np.isfinite(want) & (np.abs(want) > 1e-6)
+    assert np.all(np.abs(got[ok] - want[ok]) <= 1e-3 * np.abs(want[ok]))
