@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libdynamix_g2.so")
 G2_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "unsupported device or feature",
           4: "size exceeds a kernel limit"}
-DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE = 1, 2, 4
+DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_RANGE, DEVERR_RANGE_CHECK = 1, 2, 4, 8
 
 BK = 64          # source segment width (pixels)
 PAD = 128        # packed bins and packed_cols are multiples of this
@@ -26,6 +26,7 @@ PACK_CHUNK, PACK_MAX_SLOTS, PACK_MAX_PIECES, PACK_WORDS_PER_CHUNK = 2048, 128, 5
 TC_BM, TC_BN = 128, 256
 PLAIN_BM, PLAIN_BN = 128, 128
 MAX_JOBS = 32
+ITEM_EMPTY = -1
 KIND_FP16, KIND_E4M3 = 0, 1
 
 # numpy mirror of g2_gram_item (48 bytes, 8-byte aligned)
@@ -53,8 +54,10 @@ SIGNATURES = {
                                  _i64, _p, _p]),
     "g2_pack_e4m3": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _p, _p]),
     "g2_binned_max": (C.c_int, [_p, _i32, _i64, _i64, _p, _i64, _p, _p]),
+    "g2_pack_e4m3_units": (C.c_int, [_p, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p]),
     "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_gram_tc_pair": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
+    "g2_gram_workers": (C.c_int, [_i32, _p]),
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
     "g2_plain_dp4a": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _p]),
     "g2_tc_rate_probe": (C.c_int, [_i32, _i64, _i32, _p, _p]),
@@ -143,4 +146,6 @@ def device_error_message(code):
         msgs.append("an out-of-range index was skipped")
     if code & DEVERR_RANGE:
         msgs.append("a count does not fit the packing")
+    if code & DEVERR_RANGE_CHECK:
+        msgs.append("a count may not fit the packing (unchecked)")
     return "; ".join(msgs) or "device error %d" % code

@@ -145,6 +145,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = cluster; it < n_items && ok; it += n_clusters) {
         const g2_gram_item w = items[it];
+        if (w.job == G2_ITEM_EMPTY) continue;
         if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) continue;
         const CUtensorMap* m = &maps.map[w.job];
         const int bk = stage_elems(maps.kind[w.job]);
@@ -189,6 +190,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = cluster; it < n_items && ok; it += n_clusters) {
         const g2_gram_item w = items[it];
+        if (w.job == G2_ITEM_EMPTY) continue;
         if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) continue;
         const bool fp8 = maps.kind[w.job] == G2_KIND_E4M3;
         const int n = item_n(w, maps);
@@ -240,6 +242,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NUM_THREADS, 1)
     int64_t local = 0;
     for (int64_t it = cluster; it < n_items; it += n_clusters, ++local) {
       const g2_gram_item w = items[it];
+      if (w.job == G2_ITEM_EMPTY) {
+        --local;
+        continue;
+      }
       if (!item_ok(w, maps, n_jobs, numer_len, sums_len)) {
         if (etid == 0 && rank == 0) atomicOr(err, G2_DEVERR_BOUNDS);
         --local;
@@ -315,6 +321,41 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NUM_THREADS, 1)
 }  // namespace pair
 }  // namespace g2
 
+namespace {
+int pair_max_clusters(int* out) {
+  using namespace g2;
+  if (cudaFuncSetAttribute(pair::gram_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pair::SMEM_BYTES) !=
+      cudaSuccess)
+    return G2_ERR_CUDA;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(sms & ~1), 1, 1);
+  cfg.blockDim = dim3(pair::NUM_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = pair::SMEM_BYTES;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, pair::gram_pair_kernel, &cfg) != cudaSuccess || n < 1) return G2_ERR_CUDA;
+  *out = n;
+  return G2_OK;
+}
+}  // namespace
+
+extern "C" int g2_gram_workers(int32_t pair, int32_t* workers) {
+  using namespace g2;
+  if (!workers) return G2_ERR_ARG;
+  if (pair) {
+    int n = 0;
+    const int st = pair_max_clusters(&n);
+    if (st != G2_OK) return st;
+    *workers = n;
+    return G2_OK;
+  }
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  *workers = sms;
+  return G2_OK;
+}
+
 extern "C" int g2_gram_tc_pair(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
                                uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
                                int32_t* err_dev, int32_t grid, void* stream) {
@@ -344,21 +385,10 @@ extern "C" int g2_gram_tc_pair(const g2_job* jobs, int32_t n_jobs, const g2_gram
     maps.kind[j] = jobs[j].elem_kind;
     maps.ones[j] = jobs[j].ones_row;
   }
-  if (cudaFuncSetAttribute(pair::gram_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pair::SMEM_BYTES) !=
-      cudaSuccess)
-    return G2_ERR_CUDA;
-  const int sms = sm_count_current();
-  if (sms <= 0) return G2_ERR_CUDA;
   // clusters that can be resident at once (one CTA per SM)
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(static_cast<unsigned>(sms & ~1), 1, 1);
-  cfg.blockDim = dim3(pair::NUM_THREADS, 1, 1);
-  cfg.dynamicSmemBytes = pair::SMEM_BYTES;
-  cfg.stream = as_stream(stream);
   int max_clusters = 0;
-  if (cudaOccupancyMaxActiveClusters(&max_clusters, pair::gram_pair_kernel, &cfg) != cudaSuccess ||
-      max_clusters < 1)
-    return G2_ERR_CUDA;
+  const int st = pair_max_clusters(&max_clusters);
+  if (st != G2_OK) return st;
   int64_t clusters = grid > 0 ? (grid + 1) / 2 : max_clusters;
   if (clusters > max_clusters) clusters = max_clusters;
   if (clusters > n_items) clusters = n_items;

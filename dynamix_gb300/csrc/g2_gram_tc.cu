@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
+        if (w.job == G2_ITEM_EMPTY) continue;
         if (!item_ok<MODE>(w, maps, n_jobs, numer_len, sums_len, so.n)) continue;
         const CUtensorMap* ma = &maps.a[w.job];
         const CUtensorMap* mb = &maps.b[w.job];
@@ -209,6 +210,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
         const g2_gram_item w = items[it];
+        if (w.job == G2_ITEM_EMPTY) continue;
         if (!item_ok<MODE>(w, maps, n_jobs, numer_len, sums_len, so.n)) continue;
         const bool fp8 = maps.kind[w.job] == G2_KIND_E4M3;
         const int buf = static_cast<int>(local & 1);
@@ -259,6 +261,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     int64_t local = 0;
     for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x, ++local) {
       const g2_gram_item w = items[it];
+      if (w.job == G2_ITEM_EMPTY) {
+        --local;
+        continue;
+      }
       if (!item_ok<MODE>(w, maps, n_jobs, numer_len, sums_len, so.n)) {
         if (etid == 0) atomicOr(err, G2_DEVERR_BOUNDS);
         --local;

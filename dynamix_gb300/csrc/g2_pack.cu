@@ -427,6 +427,152 @@ __global__ void __launch_bounds__(THREADS, 4)
   if (range_bad) atomicOr(err, G2_DEVERR_RANGE);
 }
 
+// ---- e4m3 from u8 counts, by work units -----------------------------------
+// The same byte permutation as pack_e4m3_kernel, organised so that a warp
+// never diverges: the host cuts each chunk's destination bytes into units
+// of four classes -- 16 bytes from 16 consecutive source bytes (one 16-byte
+// store), 4 from 4 consecutive (one 32-bit funnel shift), 4 gathered from 4
+// arbitrary source bytes, single bytes (words shared with a neighbouring
+// chunk or bin padding) -- and groups them in blocks of 32 units of one
+// class; warp w of a block takes blocks w, w + 8, ... of its chunk and runs
+// each over the step's F frames.  Units are uint4 {destination (in units of
+// the class's size), source(s), source(s), class}, read from L1 each step.
+// The range check ORs every moved byte into one word per thread: with counts
+// <= 15 every byte of it stays <= 15, and only a count of 16 or more can make
+// one exceed 16, in which case G2_DEVERR_RANGE_CHECK asks the caller for the
+// exact maximum (g2_binned_max) -- one instruction per word instead of four.
+constexpr uint32_t UNIT_NONE = 0, UNIT_VEC = 1, UNIT_WORD = 2, UNIT_GATHER = 3, UNIT_BYTE = 4;
+
+__global__ void __launch_bounds__(THREADS, 4)
+    pack_e4m3_units_kernel(const uint8_t* __restrict__ frames, int64_t T, int64_t npix,
+                           const int32_t* __restrict__ block_off, const uint4* __restrict__ units,
+                           uint8_t* __restrict__ packed, int64_t packed_cols, int32_t* __restrict__ err) {
+  using C = Cfg<uint8_t>;
+  constexpr int F = C::F;
+  constexpr int ROW = C::BUF + 16;  // staging row: the chunk, its unaligned start, spare words
+  __shared__ __align__(16) uint8_t s_buf[2][F][ROW];
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int lane = tid & 31;
+  const int64_t c = blockIdx.x;
+  const int64_t p0 = c * CH;
+  const int b0 = block_off[c];
+  const int nb = block_off[c + 1] - b0;
+  const int64_t total_bytes = T * npix;
+  const int64_t n_vec = packed_cols / 16, n_word = packed_cols / 4;
+  uint32_t seen = 0;  // OR of every moved byte
+  bool bad = false;
+
+  auto issue = [&](int64_t t0, int buf) {
+    for (int w = tid; w < F * C::WORDS; w += THREADS) {
+      const int f = w / C::WORDS;
+      const int wi = w - f * C::WORDS;
+      const int64_t t = t0 + f;
+      const int64_t a = ((t * npix + p0) & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
+      const int64_t avail = t < T ? total_bytes - a : 0;
+      const int nbytes = avail <= 0 ? 0 : (avail >= 16 ? 16 : static_cast<int>(avail));
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(&s_buf[buf][f][wi * 16])),
+                   "l"(nbytes ? frames + a : frames), "r"(nbytes)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  const int64_t stride = static_cast<int64_t>(gridDim.y) * F;
+  int64_t t0 = static_cast<int64_t>(blockIdx.y) * F;
+  if (t0 < T) issue(t0, 0);
+  for (int step = 0; t0 < T; ++step, t0 += stride) {
+    const int buf = step & 1;
+    if (t0 + stride < T) {
+      issue(t0 + stride, buf ^ 1);
+    } else {
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncthreads();
+    const int nf = static_cast<int>(T - t0 < F ? T - t0 : F);
+    uint32_t delta[F];
+    uint8_t* row[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      delta[f] = static_cast<uint32_t>(((t0 + f) * npix + p0) & 15) + f * ROW;
+      row[f] = packed + (t0 + f) * packed_cols;
+    }
+    const uint8_t* base = &s_buf[buf][0][0];
+    for (int blk = warp; blk < nb; blk += THREADS / 32) {
+      const uint4 u = units[static_cast<int64_t>(b0 + blk) * 32 + lane];
+      if (u.w == UNIT_VEC) {
+        if (u.x >= n_vec || u.y > CH - 16) {
+          bad = true;
+          continue;
+        }
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          if (f >= nf) break;
+          const uint32_t o = delta[f] + u.y;
+          const uint32_t* p = reinterpret_cast<const uint32_t*>(base + (o & ~3u));
+          const uint32_t sh = 8 * (o & 3u);
+          uint4 v;
+          v.x = __funnelshift_r(p[0], p[1], sh);
+          v.y = __funnelshift_r(p[1], p[2], sh);
+          v.z = __funnelshift_r(p[2], p[3], sh);
+          v.w = __funnelshift_r(p[3], p[4], sh);
+          seen |= v.x | v.y | v.z | v.w;
+          *reinterpret_cast<uint4*>(row[f] + 16 * static_cast<int64_t>(u.x)) = v;
+        }
+      } else if (u.w == UNIT_WORD) {
+        if (u.x >= n_word || u.y > CH - 4) {
+          bad = true;
+          continue;
+        }
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          if (f >= nf) break;
+          const uint32_t o = delta[f] + u.y;
+          const uint32_t* p = reinterpret_cast<const uint32_t*>(base + (o & ~3u));
+          const uint32_t v = __funnelshift_r(p[0], p[1], 8 * (o & 3u));
+          seen |= v;
+          *reinterpret_cast<uint32_t*>(row[f] + 4 * static_cast<int64_t>(u.x)) = v;
+        }
+      } else if (u.w == UNIT_GATHER) {
+        const uint32_t s0 = u.y & 0xFFFFu, s1 = u.y >> 16, s2 = u.z & 0xFFFFu, s3 = u.z >> 16;
+        if (u.x >= n_word || s0 >= CH || s1 >= CH || s2 >= CH || s3 >= CH) {
+          bad = true;
+          continue;
+        }
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          if (f >= nf) break;
+          const uint8_t* q = base + delta[f];
+          const uint32_t v = static_cast<uint32_t>(q[s0]) | (static_cast<uint32_t>(q[s1]) << 8) |
+                             (static_cast<uint32_t>(q[s2]) << 16) | (static_cast<uint32_t>(q[s3]) << 24);
+          seen |= v;
+          *reinterpret_cast<uint32_t*>(row[f] + 4 * static_cast<int64_t>(u.x)) = v;
+        }
+      } else if (u.w == UNIT_BYTE) {
+        if (u.x >= packed_cols || u.y >= CH) {
+          bad = true;
+          continue;
+        }
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          if (f >= nf) break;
+          const uint8_t v = base[delta[f] + u.y];
+          seen |= v;
+          row[f][u.x] = v;
+        }
+      }
+    }
+    // the buffer just read is refilled by the copies issued at the next step
+    __syncthreads();
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
+  // a byte of the OR above 16 means some count may exceed 16
+  if (((seen & 0x7F7F7F7Fu) + 0x6F6F6F6Fu | seen) & 0x80808080u) atomicOr(err, G2_DEVERR_RANGE_CHECK);
+}
+
 template <typename Tin>
 __global__ void binned_max_kernel(const Tin* __restrict__ frames, int64_t T, int64_t npix,
                                   const int32_t* __restrict__ col_src, int64_t n_cols, uint32_t* __restrict__ out) {
@@ -536,6 +682,32 @@ extern "C" int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t 
     pack::pack_e4m3_kernel<uint16_t><<<grid, pack::THREADS, 0, as_stream(stream)>>>(
         reinterpret_cast<const uint16_t*>(frames_dev), nframes, npix, chunk_word_off_dev, word_dst_dev, ws, out,
         packed_cols, err_dev);
+  return launch_status();
+}
+
+extern "C" int g2_pack_e4m3_units(const void* frames_dev, int64_t nframes, int64_t npix,
+                                  const int32_t* unit_block_off_dev, const uint32_t* units_dev, int64_t n_chunks,
+                                  void* packed_dev, int64_t packed_cols, int32_t* err_dev, void* stream) {
+  using namespace g2;
+  if (!frames_dev || !unit_block_off_dev || !units_dev || !packed_dev || !err_dev) return G2_ERR_ARG;
+  if (nframes <= 0 || npix <= 0 || n_chunks != (npix + G2_PACK_CHUNK - 1) / G2_PACK_CHUNK || packed_cols <= 0 ||
+      packed_cols % G2_PAD != 0)
+    return G2_ERR_ARG;
+  if (!aligned(packed_dev, 16) || !aligned(frames_dev, 16) || !aligned(units_dev, 16)) return G2_ERR_ARG;
+  if (n_chunks == 0) return G2_OK;
+  if (n_chunks > 0x7fffffff) return G2_ERR_TOO_LARGE;
+  const int sms = sm_count_current();
+  if (sms <= 0) return G2_ERR_CUDA;
+  const int F = pack::Cfg<uint8_t>::F;
+  int64_t gy = (static_cast<int64_t>(sms) * 16 + n_chunks - 1) / n_chunks;
+  const int64_t max_gy = (nframes + F - 1) / F;
+  if (gy > max_gy) gy = max_gy;
+  if (gy > 65535) gy = 65535;
+  if (gy < 1) gy = 1;
+  dim3 grid(static_cast<unsigned>(n_chunks), static_cast<unsigned>(gy));
+  pack::pack_e4m3_units_kernel<<<grid, pack::THREADS, 0, as_stream(stream)>>>(
+      reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, unit_block_off_dev,
+      reinterpret_cast<const uint4*>(units_dev), reinterpret_cast<uint8_t*>(packed_dev), packed_cols, err_dev);
   return launch_status();
 }
 

@@ -24,7 +24,7 @@ import numpy as np
 
 from . import _lib
 from .plan import (E4M3_MAX_EXACT, EXACT_LIMIT, FP16_MAX_EXACT, MODE_BYTES, MODE_E4M3, MODE_FP16, TILE_SHAPES,
-                   PackLayout, chunk_grams, e4m3_segment_bound, gram_items)
+                   PackLayout, balance_items, chunk_grams, e4m3_segment_bound, gram_items)
 
 
 def _torch():
@@ -89,6 +89,7 @@ def frames_to_device(frames, dev):
     return torch.from_numpy(np.ascontiguousarray(a.astype(tgt))).to(dev)
 
 
+_WORKERS = {}
 _LAYOUTS = collections.OrderedDict()
 _LAYOUTS_LOCK = threading.Lock()
 _LAYOUTS_MAX = 48
@@ -125,6 +126,8 @@ def device_layout(qmask, n_bins, mode, dev, digest=None):
         L.d_chunk_word_off = d(L.chunk_word_off)
         L.d_word_dst = d(L.word_dst)
         L.d_word_src = d(L.word_src.view(np.int32))
+        L.d_unit_block_off = d(L.unit_block_off)
+        L.d_units = d(L.units.view(np.int32))
     with _LAYOUTS_LOCK:
         _LAYOUTS[key] = L
         while len(_LAYOUTS) > _LAYOUTS_MAX:
@@ -192,6 +195,7 @@ class DenseEngine:
         self.last = {}
         self._u8_hint = MODE_E4M3 if method == "tc" else MODE_FP16
         self._u16_hint = MODE_E4M3 if method == "tc" else MODE_FP16
+        self.operand_hint = "auto"
         self._packed_mode = None
         self.pipeline = True      # chunked copy/pack/Gram overlap where it applies
         self.pipe_chunks = self.PIPE_CHUNKS
@@ -202,6 +206,19 @@ class DenseEngine:
         self.profile = False      # record CUDA events around every stage
         self.stage_ms = {}
         self._events = []
+
+    def set_operand_hint(self, operand):
+        """The packed operand kind the next call tries first (tensor-core
+        path, ``operand="auto"``): "e4m3", "fp16", "bytes" or "auto" (the
+        narrowest)."""
+        if operand not in ("auto", "e4m3", "fp16", "bytes"):
+            raise ValueError("operand hint must be 'auto', 'e4m3', 'fp16' or 'bytes'")
+        self.operand_hint = operand
+        if self.method != "tc" or self.operand != "auto":
+            return
+        mode = MODE_E4M3 if operand == "auto" else self.MODES[operand]
+        self._u8_hint = mode if mode != MODE_BYTES else MODE_FP16
+        self._u16_hint = mode
 
     def _mark(self, name):
         if self.profile:
@@ -302,10 +319,7 @@ class DenseEngine:
         self.err.zero_()
         st = stream_handle(self.dev)
         if mode == MODE_E4M3:
-            _lib.check(self.lib.g2_pack_e4m3(
-                ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_word_off),
-                ptr(L.d_word_dst), ptr(L.d_word_src), L.n_chunks, ptr(packed), L.packed_cols, ptr(self.err), st),
-                "g2_pack_e4m3")
+            self.pack_e4m3(frames_dev.data_ptr(), frames_dev.element_size(), self.T, L, packed.data_ptr(), st)
             return L
         _lib.check(self.lib.g2_pack_frames(
             ptr(frames_dev), frames_dev.element_size(), self.T, self.npix, ptr(L.d_chunk_entry_off),
@@ -321,13 +335,63 @@ class DenseEngine:
             return "pair" if self.tile == "pair" else "tc"
         return self.method
 
+    def workers(self):
+        """Persistent workers of a tensor-core Gram launch (CTAs, or CTA pairs
+        for the pair tile), as the kernel will use them."""
+        pair = self.tile == "pair"
+        if self.grid > 0:
+            return (self.grid + 1) // 2 if pair else self.grid
+        key = (str(self.dev), pair)
+        if key not in _WORKERS:
+            n = C.c_int32(0)
+            _lib.check(self.lib.g2_gram_workers(1 if pair else 0, C.byref(n)), "g2_gram_workers")
+            _WORKERS[key] = int(n.value)
+        return _WORKERS[key]
+
+    def balanced(self, items, L):
+        """``items`` laid out for the kernel's workers, longest-first balanced
+        (tensor-core launches only)."""
+        if self.method != "tc" or items.size == 0:
+            return items
+        return balance_items(items, self.workers(), 128 if L.kind == _lib.KIND_E4M3 else 64, self.item_kind,
+                             ones=self.ones(L))
+
+    pack_units = True         # u8 e4m3 packing by work units (g2_pack_e4m3_units)
+
+    def pack_e4m3(self, frames_ptr, elem_bytes, nframes, L, packed_ptr, stream):
+        """One launch of the e4m3 pack over ``nframes`` frames at ``frames_ptr``
+        into the packed rows at ``packed_ptr``."""
+        st = stream if isinstance(stream, C.c_void_p) else C.c_void_p(stream)
+        if elem_bytes == 1 and self.pack_units:
+            _lib.check(self.lib.g2_pack_e4m3_units(
+                C.c_void_p(frames_ptr), nframes, self.npix, ptr(L.d_unit_block_off), ptr(L.d_units), L.n_chunks,
+                C.c_void_p(packed_ptr), L.packed_cols, ptr(self.err), st), "g2_pack_e4m3_units")
+        else:
+            _lib.check(self.lib.g2_pack_e4m3(
+                C.c_void_p(frames_ptr), elem_bytes, nframes, self.npix, ptr(L.d_chunk_word_off), ptr(L.d_word_dst),
+                ptr(L.d_word_src), L.n_chunks, C.c_void_p(packed_ptr), L.packed_cols, ptr(self.err), st),
+                "g2_pack_e4m3")
+
+    def resolve_range_check(self, code, frames_dev):
+        """An e4m3 pack that could not tell whether every count fits sets
+        DEVERR_RANGE_CHECK: the exact binned maximum of ``frames_dev`` decides
+        (DEVERR_RANGE when a count exceeds 16).  Returns the resolved code."""
+        if not code & _lib.DEVERR_RANGE_CHECK:
+            return code
+        code &= ~_lib.DEVERR_RANGE_CHECK
+        if self._binned_max(frames_dev) > E4M3_MAX_EXACT:
+            code |= _lib.DEVERR_RANGE
+        self.err.fill_(code)
+        return code
+
     def items_for(self, L, grams):
-        key = (L.mode, self.item_kind, tuple(grams), self.super_rows)
+        key = (L.mode, self.item_kind, tuple(grams), self.super_rows, self.grid)
         if key not in self._items_cache:
             torch = _torch()
             items = gram_items(self.T, grams, job=0, out_base=0, kind=self.item_kind,
                                s_base=0 if (self.ones(L) and self.method in ("tc", "dp4a")) else None,
                                super_rows=self.super_rows)
+            items = self.balanced(items, L)
             dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
             if len(self._items_cache) > 8:
                 self._items_cache.clear()
@@ -381,6 +445,8 @@ class DenseEngine:
                 pe = self._piece_emax(L).cpu().numpy().view(np.uint32)
                 seg_emax = L.segment_emax(pe)
             code = int(self.err.item())
+            if mode == MODE_E4M3:
+                code = self.resolve_range_check(code, frames_dev)
             wide = frames_dev.element_size() == 2
             if code & _lib.DEVERR_RANGE and mode == MODE_E4M3 and self.operand == "auto":
                 mode = MODE_FP16
@@ -413,7 +479,7 @@ class DenseEngine:
             return L, grams
 
     # -- chunked pipeline (e4m3) ---------------------------------------------
-    TILE = "single"
+    TILE = "pair"
     PIPE_CHUNKS = 8
     SUPER_ROWS = 2048
     KSLAB = 0                 # no cap on the K columns of one tile item
@@ -435,9 +501,10 @@ class DenseEngine:
             bounds = np.array(list(range(0, T, step)) + [T], dtype=np.int64)
             need = np.minimum(items["j0"].astype(np.int64) + TILE_SHAPES[self.item_kind][1], T)
             grp = np.searchsorted(bounds[1:], need, side="left")
-            order = np.argsort(grp, kind="stable")
-            items, grp = items[order], grp[order]
-            starts = np.searchsorted(grp, np.arange(bounds.size), side="left")
+            # each chunk's launch balanced over the kernel's workers
+            parts = [self.balanced(items[grp == g], L) for g in range(bounds.size - 1)]
+            starts = np.concatenate([[0], np.cumsum([p.size for p in parts])]).astype(np.int64)
+            items = np.concatenate(parts) if parts else items[:0]
             dev_items = torch.from_numpy(items.view(np.uint8).copy()).to(self.dev)
             if len(self._items_cache) > 8:
                 self._items_cache.clear()
@@ -502,10 +569,8 @@ class DenseEngine:
                     e = torch.cuda.Event()
                     e.record(copy_s)
                 pack_s.wait_event(e)
-            _lib.check(self.lib.g2_pack_e4m3(
-                frames_dev.data_ptr() + t0 * npix, 1, t1 - t0, npix, ptr(L.d_chunk_word_off), ptr(L.d_word_dst),
-                ptr(L.d_word_src), L.n_chunks, packed.data_ptr() + t0 * pc, pc, ptr(self.err),
-                pack_s.cuda_stream), "g2_pack_e4m3")
+            self.pack_e4m3(frames_dev.data_ptr() + t0 * npix, 1, t1 - t0, L, packed.data_ptr() + t0 * pc,
+                           pack_s.cuda_stream)
             e = torch.cuda.Event()
             e.record(pack_s)
             cur.wait_event(e)
@@ -517,7 +582,7 @@ class DenseEngine:
         self._mark("end")
         if host:
             self._frames_host_ref = frames            # alive until the copies are done
-        code = int(self.err.item())
+        code = self.resolve_range_check(int(self.err.item()), frames_dev)
         if code & _lib.DEVERR_RANGE and self.operand == "auto":
             self._u8_hint = MODE_FP16                 # counts above 16: rerun on fp16 operands
             return self.run(frames_dev, pipelined=False)
@@ -567,7 +632,7 @@ class DenseEngine:
             raise ValueError("the dp4a kernel reads u8 counts")
         self._mark("pack")
         L = self.pack(frames_dev, MODE_E4M3)
-        code = int(self.err.item()) & ~_lib.DEVERR_RANGE      # counts > 16 are fine here
+        code = int(self.err.item()) & ~(_lib.DEVERR_RANGE | _lib.DEVERR_RANGE_CHECK)   # counts > 16 are fine here
         if code:
             raise DeviceError(_lib.device_error_message(code))
         self.err.zero_()

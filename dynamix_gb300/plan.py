@@ -21,7 +21,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._lib import (BK, ITEM_DTYPE, KIND_E4M3, KIND_FP16, PACK_CHUNK, PACK_MAX_PIECES, PACK_MAX_SLOTS,
+from ._lib import (BK, ITEM_DTYPE, ITEM_EMPTY, KIND_E4M3, KIND_FP16, PACK_CHUNK, PACK_MAX_PIECES, PACK_MAX_SLOTS,
                    PACK_WORDS_PER_CHUNK, PAD, PLAIN_BM, PLAIN_BN, TC_BM, TC_BN)
 
 EXACT_LIMIT = 1 << 24   # fp32 represents every integer up to 2^24 exactly
@@ -30,6 +30,7 @@ E4M3_MAX_EXACT = 16     # e4m3 represents every integer up to 2^4 exactly
 SUPER_ROWS = 2048       # frames per side of a super-tile
 
 MODE_FP16, MODE_BYTES, MODE_E4M3 = 0, 1, 2
+UNIT_NONE, UNIT_VEC, UNIT_WORD, UNIT_GATHER, UNIT_BYTE = 0, 1, 2, 3, 4   # classes of the e4m3 pack's units
 
 # (rows, columns) of one Gram item per kernel: the single-CTA tensor-core
 # block (g2_gram_tc), the CTA-pair block (g2_gram_tc_pair: 256 rows over two
@@ -151,6 +152,63 @@ class PackLayout:
             ws[:, 0] = (srcs[:, 0] | (srcs[:, 1] << 12) | ((srcs[:, 2] & 0xFF) << 24)).astype(np.uint32)
             ws[:, 1] = ((srcs[:, 2] >> 8) | (srcs[:, 3] << 4) | (wslot << 16)).astype(np.uint32)
             self.word_src = ws
+            self._build_units(dst, pix, chunk)
+
+    def _build_units(self, dst, pix, chunk):
+        """Work units of the u8 e4m3 pack (``g2_pack_e4m3_units``), per chunk
+        in blocks of 32 of one class (a warp runs a block without diverging):
+        UNIT_VEC 16 destination bytes from 16 consecutive source bytes (one
+        16-byte store), UNIT_WORD 4 from 4 consecutive, UNIT_GATHER 4 from 4
+        arbitrary source bytes of the chunk, UNIT_BYTE one byte (destination
+        words shared with another chunk or with bin padding).  A unit is four
+        uint32: destination (in units of its size), source offset(s) in the
+        chunk, class."""
+        n = self.packed_cols
+        dchunk = np.full(n, -1, dtype=np.int64)
+        dsrc = np.full(n, -1, dtype=np.int64)
+        dchunk[dst] = chunk
+        dsrc[dst] = pix - chunk * PACK_CHUNK
+        nv, nw = n // 16, n // 4
+        vc, vs = dchunk.reshape(nv, 16), dsrc.reshape(nv, 16)
+        vec = (vc[:, 0] >= 0) & (vc == vc[:, :1]).all(1) & (np.diff(vs, axis=1) == 1).all(1)
+        wc, ws = dchunk.reshape(nw, 4), dsrc.reshape(nw, 4)
+        owned = (wc[:, 0] >= 0) & (wc == wc[:, :1]).all(1) & ~np.repeat(vec, 4)
+        run = owned & (np.diff(ws, axis=1) == 1).all(1)
+        gat = owned & ~run
+        byte = (dchunk >= 0) & ~np.repeat(vec, 16) & ~np.repeat(owned, 4)
+        classes = []
+        iv = np.flatnonzero(vec)
+        classes.append((vc[iv, 0], np.stack([iv, vs[iv, 0], np.zeros_like(iv), np.full_like(iv, UNIT_VEC)], 1)))
+        iw = np.flatnonzero(run)
+        classes.append((wc[iw, 0], np.stack([iw, ws[iw, 0], np.zeros_like(iw), np.full_like(iw, UNIT_WORD)], 1)))
+        ig = np.flatnonzero(gat)
+        g = ws[ig]
+        classes.append((wc[ig, 0], np.stack([ig, g[:, 0] | (g[:, 1] << 16), g[:, 2] | (g[:, 3] << 16),
+                                             np.full_like(ig, UNIT_GATHER)], 1)))
+        ib = np.flatnonzero(byte)
+        classes.append((dchunk[ib], np.stack([ib, dsrc[ib], np.zeros_like(ib), np.full_like(ib, UNIT_BYTE)], 1)))
+        # blocks: per chunk, per class, groups of 32 units (the last one padded with UNIT_NONE)
+        blocks_per_chunk = np.zeros(self.n_chunks, dtype=np.int64)
+        per_class = []
+        for ch, u in classes:
+            order = np.argsort(ch, kind="stable")
+            ch, u = ch[order], u[order]
+            cnt = np.bincount(ch, minlength=self.n_chunks)
+            nb = -(-cnt // 32)
+            blocks_per_chunk += nb
+            per_class.append((ch, u, cnt, nb))
+        off = np.concatenate([[0], np.cumsum(blocks_per_chunk)])
+        units = np.zeros((int(off[-1]) * 32, 4), dtype=np.uint32)
+        units[:, 3] = UNIT_NONE
+        nxt = off[:-1].copy()                      # next free block of each chunk
+        for ch, u, cnt, nb in per_class:
+            first = np.concatenate([[0], np.cumsum(cnt)])[:-1]
+            rank = np.arange(ch.size) - first[ch]  # position of a unit inside its chunk's class list
+            slot = (nxt[ch] * 32 + rank).astype(np.int64)
+            units[slot] = u.astype(np.uint32)
+            nxt += nb
+        self.unit_block_off = off.astype(np.int32)
+        self.units = units.reshape(-1)
 
     def segment_emax(self, piece_emax):
         """Per 64-column output segment, the sum over its pieces of the pieces'
@@ -287,6 +345,54 @@ def gram_items(T, chunked_grams, job=0, out_base=0, kind="tc", s_base=None, supe
     items = np.concatenate(parts)
     order = np.argsort(-items["k_len"].astype(np.int64), kind="stable")
     return items[order]
+
+
+ITEM_OVERHEAD_STAGES = 4   # fixed cost of an item (descriptor, epilogue hand-off), in full-width stages
+
+
+def item_costs(items, stage_elems, kind, ones=True):
+    """Relative tensor-core time of each item: its K stages times the share
+    of a full-width MMA its columns take, plus a fixed per-item cost.  Pair
+    items use n = min(256, frames (+ row of ones) left from j0, rounded up to
+    32) columns (g2_gram_tc_pair); single-CTA items always 256."""
+    bn = TILE_SHAPES[kind][1]
+    stages = items["k_len"].astype(np.float64) / float(stage_elems)
+    if kind == "pair":
+        live = items["nframes"].astype(np.int64) - items["j0"].astype(np.int64)
+        if ones:
+            live = live + (items["s_off"] >= 0)
+        n = np.clip((live + 31) // 32 * 32, 32, bn)
+        stages = stages * (n / float(bn))
+    return stages + ITEM_OVERHEAD_STAGES
+
+
+def balance_items(items, workers, stage_elems, kind, ones=True):
+    """Static longest-first list schedule of one launch's items over
+    ``workers`` persistent workers (CTAs, or CTA pairs for "pair" items):
+    each item, largest cost first, goes to the least-loaded worker, and the
+    list is laid out so that worker w reads slots w, w + workers, ... (the
+    kernels' pattern), unused slots holding ``job = G2_ITEM_EMPTY``.  Items
+    keep their relative order within a worker (bins and super-tiles stay
+    together in time)."""
+    import heapq
+    n = items.size
+    if workers <= 1 or n <= workers:
+        return items
+    cost = item_costs(items, stage_elems, kind, ones)
+    order = np.argsort(-cost, kind="stable")
+    heap = [(0.0, w) for w in range(workers)]
+    lists = [[] for _ in range(workers)]
+    for i in order:
+        load, w = heapq.heappop(heap)
+        lists[w].append(i)
+        heapq.heappush(heap, (load + cost[i], w))
+    m = max(len(lst) for lst in lists)
+    out = np.zeros(m * workers, dtype=ITEM_DTYPE)
+    out["job"] = ITEM_EMPTY
+    for w, lst in enumerate(lists):
+        if lst:
+            out[w + workers * np.arange(len(lst))] = items[np.sort(np.asarray(lst))]
+    return out
 
 
 def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT, kslab=0):

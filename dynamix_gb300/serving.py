@@ -416,6 +416,9 @@ class G2Server:
             job.frames_dev = frames_dev
             job.engine = DenseEngine(job.shape, job.T, job.qmask, job.n_bins, job.scale, device=self.dev,
                                      method=self.method, numer=numer, sums=sums, qmask_digest=job.qdigest)
+            # the pack's error word is read after the frames are released: the
+            # kernel that checks every count exactly is the one that fits
+            job.engine.pack_units = False
         req.frames = None                           # the server keeps no reference to the input
         if job.n_bins == 0:
             self._promote(job, np.empty(0, dtype=_lib.ITEM_DTYPE))

@@ -10,13 +10,20 @@ free parameters that change speed but never results:
   each grouped launch long);
 * ``kslab`` -- cap on the K columns of one tile item (0: none); narrower
   slabs keep the rows the concurrent tiles read inside L2 at the price of
-  more epilogues.
+  more epilogues;
+* ``tile`` -- the tensor-core block: ``"pair"`` (256 x 256 on CTA pairs,
+  tcgen05 cta_group::2) or ``"single"`` (128 x 256 on one CTA);
+* ``operand`` -- the packed operand kind tried first: ``"e4m3"`` (kind::f8f6f4,
+  counts <= 16), ``"fp16"`` (kind::f16, counts <= 2048) or ``"bytes"``
+  (kind::f16 on byte planes); a stack whose counts do not fit falls back to a
+  wider kind, so a narrow choice only wins when the counts allow it.
 
-:func:`tune_dense` times every candidate pair on the caller's own stack and
-keeps the fastest for the key ``(nframes, pixels per bin)``; engines built
-later for the same key pick it up (:func:`apply_cached`).  Choices are kept in
-memory and, when ``path`` is given (or ``DYNAMIX_G2_TUNE_CACHE`` is set), in
-a JSON file.
+:func:`tune_dense` times every candidate on the caller's own stack and keeps
+the fastest for the key ``(nframes, pixels per bin)``; engines built later for
+the same key pick it up (:func:`apply_cached`).  Choices are kept in memory
+and, when ``path`` is given (or ``DYNAMIX_G2_TUNE_CACHE`` is set), in a JSON
+file.  A candidate is ``(super_rows, pipe_chunks[, kslab[, tile[,
+operand]]])``; missing trailing entries take the engine's current values.
 """
 from __future__ import annotations
 
@@ -26,7 +33,9 @@ import threading
 
 import numpy as np
 
-DEFAULT_CANDIDATES = [(sr, pc, ks) for sr in (2048, 4096) for pc in (6, 8) for ks in (0, 8192, 16384)]
+DEFAULT_CANDIDATES = [(2048, pc, 0, tile, op) for tile in ("pair", "single") for pc in (6, 8, 12)
+                      for op in ("e4m3", "fp16")]
+FIELDS = ("super_rows", "pipe_chunks", "kslab", "tile", "operand")
 
 _lock = threading.Lock()
 _cache = {}
@@ -74,6 +83,27 @@ def store(key, value, path=None):
             os.replace(tmp, p)
 
 
+def current(engine):
+    """The engine's values of :data:`FIELDS`."""
+    return (int(engine.super_rows), int(engine.pipe_chunks), int(getattr(engine, "kslab", 0)),
+            getattr(engine, "tile", "single"), getattr(engine, "operand_hint", "auto"))
+
+
+def complete(cand, engine):
+    """A candidate with its missing trailing entries taken from the engine."""
+    cand = tuple(cand)
+    return cand + current(engine)[len(cand):]
+
+
+def set_choice(engine, v):
+    engine.super_rows, engine.pipe_chunks = int(v[0]), int(v[1])
+    engine.kslab = int(v[2]) if len(v) > 2 else 0
+    if len(v) > 3 and v[3] in ("pair", "single"):
+        engine.tile = v[3]
+    if len(v) > 4 and hasattr(engine, "set_operand_hint"):
+        engine.set_operand_hint(v[4])
+
+
 def apply_cached(engine, path=None):
     """Set an engine's launch shapes from an earlier tuning of its key."""
     with _lock:
@@ -82,23 +112,23 @@ def apply_cached(engine, path=None):
             return None                  # nothing tuned in this process: skip the key
     v = lookup(key_of(engine.T, engine.qmask, engine.n_bins), path)
     if v is not None:
-        engine.super_rows, engine.pipe_chunks = int(v[0]), int(v[1])
-        engine.kslab = int(v[2]) if len(v) > 2 else 0
+        set_choice(engine, v)
     return v
 
 
 def tune_dense(correlator, frames, candidates=None, repeats=3, path=None):
-    """Time ``correlate_device(frames)`` for every ``(super_rows,
-    pipe_chunks[, kslab])`` candidate (CUDA events, after one warm-up call
-    each), keep the fastest for this stack's key and return
-    ``(best, {candidate: ms})``.  ``frames`` must stay the same stack for all
-    candidates."""
+    """Time ``correlate_device(frames)`` for every candidate (CUDA events,
+    after one warm-up call each), keep the fastest for this stack's key and
+    return ``(best, {candidate: ms})`` with complete 5-entry candidates.
+    ``frames`` must stay the same stack for all candidates."""
     import torch
     eng = correlator.engine
+    start = current(eng)
     times = {}
     for cand in (candidates or DEFAULT_CANDIDATES):
-        cand = tuple(int(x) for x in cand) + ((0,) if len(cand) == 2 else ())
-        eng.super_rows, eng.pipe_chunks, eng.kslab = cand
+        cand = tuple(cand) + start[len(cand):]     # missing entries: the engine's values at the start
+        set_choice(eng, start)
+        set_choice(eng, cand)
         correlator.correlate_device(frames)
         stream = torch.cuda.current_stream(eng.dev)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -111,6 +141,7 @@ def tune_dense(correlator, frames, candidates=None, repeats=3, path=None):
         times[cand] = e0.elapsed_time(e1) / repeats
     eng.check_error()
     best = min(times, key=times.get)
-    eng.super_rows, eng.pipe_chunks, eng.kslab = best
+    set_choice(eng, start)
+    set_choice(eng, best)
     store(key_of(eng.T, eng.qmask, eng.n_bins), best, path)
     return best, times

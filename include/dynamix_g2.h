@@ -38,6 +38,7 @@ extern "C" {
 #define G2_DEVERR_TIMEOUT   1  /* a bounded wait expired; the kernel bailed out */
 #define G2_DEVERR_BOUNDS    2  /* an index was out of range and was skipped */
 #define G2_DEVERR_RANGE     4  /* a count does not fit the requested packing */
+#define G2_DEVERR_RANGE_CHECK 8 /* a count may not fit the packing: check the exact maximum */
 
 #define G2_ABI_VERSION      1
 
@@ -67,9 +68,15 @@ extern "C" {
  * and columns >= nframes never enter them.  When the job's packed matrix has a
  * row of ones at row nframes (g2_job.ones_row) and s_off >= 0, the column of
  * that row holds the bin sums: G(t, nframes) = sum_k A(t, k) = S(t), added to
- * sums[s_off + t] for t < nframes. */
+ * sums[s_off + t] for t < nframes.
+ * The persistent Gram kernels give worker w (a CTA, or a CTA pair for
+ * g2_gram_tc_pair) the items w, w + W, w + 2W, ... of the list (W workers, see
+ * g2_gram_workers); a caller that balances the work per worker fills the
+ * unused slots of that pattern with G2_ITEM_EMPTY. */
+#define G2_ITEM_EMPTY (-1)  /* g2_gram_item.job of an empty slot: skipped by every role */
+
 typedef struct g2_gram_item {
-    int32_t job;       /* index into the jobs array of the launch */
+    int32_t job;       /* index into the jobs array of the launch, or G2_ITEM_EMPTY */
     int32_t i0;        /* first frame of the A rows */
     int32_t j0;        /* first frame of the B rows */
     int32_t a_k0;      /* first packed column of A (multiple of the stage width) */
@@ -157,6 +164,22 @@ int g2_pack_e4m3(const void* frames_dev, int32_t elem_bytes, int64_t nframes, in
                  const uint32_t* word_src_dev, int64_t n_chunks, void* packed_dev, int64_t packed_cols,
                  int32_t* err_dev, void* stream);
 
+/* The same packed result as g2_pack_e4m3 for u8 frames, by work units: the
+ * destination bytes of chunk c are the units of blocks [unit_block_off[c],
+ * unit_block_off[c+1]), 32 units per block (units_dev: 4 uint32 per unit,
+ * 16-byte aligned): {destination, source, source, class} with class 1 = 16
+ * bytes from 16 consecutive source bytes at source (destination in 16-byte
+ * units), 2 = 4 bytes from 4 consecutive (destination in 4-byte units), 3 = 4
+ * bytes from sources src0 | src1 << 16, src2 | src3 << 16 (4-byte units),
+ * 4 = one byte (destination in bytes), 0 = none; sources are offsets in the
+ * chunk.  A block holds one class.  Instead of checking every count, the
+ * kernel sets G2_DEVERR_RANGE_CHECK when a count above 15 may be present (an
+ * OR of the moved bytes exceeds 16); the caller then checks the exact maximum
+ * (g2_binned_max) before using the e4m3 operand. */
+int g2_pack_e4m3_units(const void* frames_dev, int64_t nframes, int64_t npix,
+                       const int32_t* unit_block_off_dev, const uint32_t* units_dev, int64_t n_chunks,
+                       void* packed_dev, int64_t packed_cols, int32_t* err_dev, void* stream);
+
 /* Largest count over the binned pixels (col_src >= 0): picks split 0/1.
  * No reference counterpart (the reference never checks its dtype range). */
 int g2_binned_max(const void* frames_dev, int32_t elem_bytes, int64_t nframes, int64_t npix,
@@ -188,6 +211,12 @@ int g2_gram_tc(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev
 int g2_gram_tc_pair(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
                     uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
                     int32_t* err_dev, int32_t grid, void* stream);
+
+/* Number of persistent workers W a Gram launch with grid <= 0 uses on the
+ * current device: CTAs for g2_gram_tc (pair = 0), CTA pairs resident at once
+ * for g2_gram_tc_pair (pair = 1).  No reference counterpart (the reference's
+ * work-group shapes are fixed, dense.py:184-188). */
+int g2_gram_workers(int32_t pair, int32_t* workers);
 
 /* ---- G5: plain direct kernel (CUDA cores, integer) ----------------------
  * The same-GPU non-tensor-core comparator: the direct integer numerator of

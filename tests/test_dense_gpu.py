@@ -282,16 +282,18 @@ def test_autotuner_keeps_results_exact(built_lib, cuda_device):
     qm = annular_qmask(shape, 4, 2.0, 26.0)
     c = MatMulCorrelator(shape, T, qmask=qm)
     d = torch.from_numpy(fr).to(cuda_device)
-    best, times = tune.tune_dense(c, d, candidates=[(1024, 2), (2048, 4, 256), (4096, 8, 512)], repeats=1)
-    assert best in times and len(times) == 3
-    assert (c.engine.super_rows, c.engine.pipe_chunks, c.engine.kslab) == best
+    cands = [(1024, 2), (2048, 4, 256, "single"), (4096, 8, 512, "pair", "fp16"), (2048, 6, 0, "pair", "e4m3")]
+    best, times = tune.tune_dense(c, d, candidates=cands, repeats=1)
+    assert best in times and len(times) == 4 and all(len(k) == 5 for k in times)
+    assert tune.current(c.engine)[:4] == best[:4]
     g = c.correlate(d)
     assert_exact(c, o.g2_exact(fr, qm), g)
     for cand in times:                                   # every candidate gives the same exact sums
-        c.engine.super_rows, c.engine.pipe_chunks, c.engine.kslab = cand
+        tune.set_choice(c.engine, cand)
         assert_exact(c, o.g2_exact(fr, qm), c.correlate(d))
+        assert c.engine.last["tile"] == cand[3]
     c2 = MatMulCorrelator(shape, T, qmask=qm)            # same key: the choice is reused
-    assert (c2.engine.super_rows, c2.engine.pipe_chunks, c2.engine.kslab) == best
+    assert tune.current(c2.engine)[:4] == best[:4]
 
 
 @pytest.mark.parametrize("bright", [False, True])
@@ -354,3 +356,21 @@ def test_dp4a_rejects_u16(built_lib, cuda_device):
     fr = np.full((8, 4, 4), 300, dtype=np.uint16)
     with pytest.raises(ValueError):
         run(fr, None, "dp4a")
+
+
+@pytest.mark.parametrize("tile", ["pair", "single"])
+@pytest.mark.parametrize("name", ["refcl_dense_u8", "refcl_dense_wide"])
+def test_matches_reference_dense_kernel(built_lib, cuda_device, name, tile):
+    """N and S bit-exact against the reference's own densecorrelator.cl
+    (correlator_multiQ_dense + compute_sums_dense, run as C by
+    tests/golden/make_wg_golden.py); DenseCorrelator's float32 g2 within 2e-6
+    of the reference kernel's float32 g2."""
+    z = golden(name)
+    fr, qm = z["frames"], z["qmask"]
+    c, g = run(fr, qm, "tc", cls="DenseCorrelator", tile=tile)
+    assert np.array_equal(c.numerator, z["numer_f"].astype(np.int64))
+    assert np.array_equal(c.sums, z["sums"].astype(np.int64))
+    ref = z["g2"].astype(np.float64)
+    ok = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(g), ok)
+    assert np.all(np.abs(g[ok] - ref[ok]) <= 2e-6 * np.abs(ref[ok]))

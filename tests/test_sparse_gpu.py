@@ -157,3 +157,19 @@ def test_pinned_host_csr_pipeline(built_lib, cuda_device, name, index_dtype):
     with pytest.raises(ValueError):
         c.correlate(d, ind, ip, bad_off)
     assert np.array_equal(c.correlate(d, ind, ip, off), g)
+
+
+@pytest.mark.parametrize("name", ["refcl_csr_u8", "refcl_csr_dense_rows"])
+def test_matches_reference_csr_kernel(built_lib, cuda_device, name):
+    """N and S bit-exact against the reference's own correlator.cl (compute_sums +
+    correlator_oneQ_Nt run as C by tests/golden/make_wg_golden.py); float32 g2
+    within 2e-6 of the reference's float32 g2."""
+    from dynamix_gb300.correlator import SparseCorrelator
+    z = golden(name)
+    T, H, W = z["frames"].shape
+    c = SparseCorrelator((H, W), T)
+    g = c.correlate(z["data"], z["indices"], z["indptr"], z["offsets"])
+    assert np.array_equal(c.numerator[0], z["numer"])
+    assert np.array_equal(c.sums[0], z["sums"].astype(np.int64))
+    ref = z["g2"].astype(np.float64)
+    assert np.all(np.abs(g.astype(np.float64) - ref) <= 2e-6 * np.abs(ref))
