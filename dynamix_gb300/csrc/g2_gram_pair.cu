@@ -13,8 +13,10 @@
 // per MMA cycle, and the ring holds six stages.  The arithmetic and the
 // exactness argument are those of the single-CTA kernel (g2_gram_tc.cu):
 // e4m3 bytes 0..16 = count * 2^-9 or fp16 words 0..2048 = count * 2^-24,
-// fp32 sums kept below 2^24 by the caller's K split, lag sums in uint32
-// shared counters, int64 atomics to the numerator.
+// fp32 sums kept below 2^24 by the caller's K split, int64 atomics to the
+// numerator.  The epilogue sums each 32 x 32 block's lag diagonals in
+// registers (g2_epilogue.cuh: a rotation by lane and warp reductions), then
+// adds one value per lane and lag group to uint32 shared counters.
 //
 // Roles per CTA (192 threads): warp 0 lane 0 TMA producer (both CTAs), warp 1
 // lane 0 MMA issuer (leader only; warp 1 of both CTAs allocates TMEM), warps
@@ -27,6 +29,7 @@
 // cuda.py:67-116, densecorrelator.cl:6-56.
 #include <cstring>
 #include <mutex>
+#include "g2_epilogue.cuh"
 #include "g2_ptx.cuh"
 #include "g2_host.h"
 
@@ -262,28 +265,40 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       const int i0 = w.i0 + static_cast<int>(rank) * HALF;  // first frame of this CTA's rows
       const bool row_live = i0 + row < w.nframes;
       const int n = item_n(w, maps);
-      const int col_end = min(n, w.nframes - w.j0);            // columns < col_end are frames
       const int lag0 = w.j0 - i0 - (HALF - 1);
       const int ones_col = w.s_off >= 0 ? w.nframes - w.j0 : -1;  // -1 or >= n: not in this block
+      // rows past the frames (the row of ones among them) contribute nothing;
+      // columns past the frames are TMA zero fill, except the row of ones,
+      // whose column goes to the bin sums
+      const float us = row_live ? unscale : 0.0f;
+      const int dwarp = (HALF - 1) - q * 32 + lane;  // lag index of offset `lane` in chunk 0
+      uint32_t carry = 0;
 #pragma unroll 1
       for (int cc = 0; cc < n / 32; ++cc) {
         uint32_t v[32];
         __syncwarp();  // tcgen05.ld is warp-collective
         tmem_ld_32x32b_x32(tbase + static_cast<uint32_t>(cc * 32), v);
         tmem_wait_ld();
-        if (!row_live) continue;
-        const int dbase = cc * 32 - row + (HALF - 1);
-        const int jx = ones_col - cc * 32;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const uint32_t x = __float2uint_rn(__uint_as_float(v[j]) * unscale);
-          if (j == jx) {
-            if (x) atomicAdd(&sums[w.s_off + i0 + row], static_cast<unsigned long long>(x));
-          } else if (x && cc * 32 + j < col_end) {
-            atomicAdd(&dacc[dbase + j], x);
-          }
+        for (int j = 0; j < 32; ++j) v[j] = __float2uint_rn(__uint_as_float(v[j]) * us);
+        const int jx = ones_col - cc * 32;
+        if (jx >= 0 && jx < 32) {  // warp-uniform
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (j == jx) {
+              if (v[j]) atomicAdd(&sums[w.s_off + i0 + row], static_cast<unsigned long long>(v[j]));
+              v[j] = 0;
+            }
         }
+        uint32_t hi, lo;
+        block_lag_sums(v, static_cast<uint32_t>(lane), hi, lo);
+        // lag group cc - 1 is complete: this chunk's lo and the previous chunk's hi
+        const uint32_t val = carry + lo;
+        const int d = (cc - 1) * 32 + dwarp;
+        if (val && d >= 0) atomicAdd(&dacc[d], val);
+        carry = hi;
       }
+      if (carry) atomicAdd(&dacc[(n / 32 - 1) * 32 + dwarp], carry);
       // this warp's TMEM reads are done: release the buffer to the leader's MMA
       tc_fence_before();
       __syncwarp();

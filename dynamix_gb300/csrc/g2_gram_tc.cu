@@ -12,21 +12,23 @@
 // first binades); read as fp16, the 16-bit values 0..2048 are exactly
 // count * 2^-24.  Products are exact in fp32 and the caller splits K so that
 // every partial sum is an integer below 2^24 times that power of two; the
-// epilogue rescales (exact), converts each element to uint32 and sums the
-// lag diagonals in uint32 shared-memory counters (<= 128 * 2^24 < 2^32), which
-// are then added to the int64 numerator.
+// epilogue rescales (exact), converts each element to uint32, sums the lag
+// diagonals of each 32 x 32 block in registers and then in uint32 shared
+// counters (<= 128 * 2^24 < 2^32), which are added to the int64 numerator.
 //
 // Roles (192 threads, one CTA per SM, persistent over a static item schedule):
 //   warp 0 lane 0  TMA producer: A (128 x 64) and B (256 x 64) fp16 tiles per
 //                  stage, 4-stage ring, 128-byte swizzle
 //   warp 1 lane 0  MMA issuer: 4 x (M128 N256 K16) per stage into one of two
 //                  TMEM accumulators (2 x 256 columns)
-//   warps 2..5     epilogue: tcgen05.ld 32 columns at a time, skewed lag sums
-//                  in shared memory, int64 atomics to the numerator
+//   warps 2..5     epilogue: tcgen05.ld 32 columns at a time, lag sums by
+//                  lane rotation and warp reductions, int64 atomics to the
+//                  numerator
 // Replaces dense.py:54,61-64 (numpy sgemm + diagonal loop), cuda.py:67-116
 // (cuBLAS sgemm + extract_upper_diags) and densecorrelator.cl:6-56.
 #include <cstring>
 #include <mutex>
+#include "g2_epilogue.cuh"
 #include "g2_ptx.cuh"
 #include "g2_host.h"
 
@@ -366,25 +368,38 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         continue;
       }
       const int ones_col = w.s_off >= 0 ? w.nframes - w.j0 : -1;  // -1 or >= BN: not in this block
+      // rows past the frames (the row of ones among them) contribute nothing;
+      // columns past the frames are TMA zero fill, except the row of ones,
+      // whose column goes to the bin sums.  Lag sums of each 32 x 32 block in
+      // registers (g2_epilogue.cuh), one shared add per lane and lag group.
+      const float us = row_live ? unscale : 0.0f;
+      const int dwarp = (BM - 1) - q * 32 + lane;  // lag index of offset `lane` in chunk 0
+      uint32_t carry = 0;
 #pragma unroll 1
       for (int cc = 0; cc < BN / 32; ++cc) {
         uint32_t v[32];
         __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the previous chunk
         tmem_ld_32x32b_x32(tbase + static_cast<uint32_t>(cc * 32), v);
         tmem_wait_ld();
-        if (!row_live) continue;
-        const int dbase = cc * 32 - row + (BM - 1);
-        const int jx = ones_col - cc * 32;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const uint32_t x = __float2uint_rn(__uint_as_float(v[j]) * unscale);
-          if (j == jx) {
-            if (x) atomicAdd(&sums[w.s_off + w.i0 + row], static_cast<unsigned long long>(x));
-          } else if (x && cc * 32 + j < col_end) {
-            atomicAdd(&dacc[dbase + j], x);
-          }
+        for (int j = 0; j < 32; ++j) v[j] = __float2uint_rn(__uint_as_float(v[j]) * us);
+        const int jx = ones_col - cc * 32;
+        if (jx >= 0 && jx < 32) {  // warp-uniform
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (j == jx) {
+              if (v[j]) atomicAdd(&sums[w.s_off + w.i0 + row], static_cast<unsigned long long>(v[j]));
+              v[j] = 0;
+            }
         }
+        uint32_t hi, lo;
+        block_lag_sums(v, static_cast<uint32_t>(lane), hi, lo);
+        const uint32_t val = carry + lo;  // lag group cc - 1 is complete
+        const int d = (cc - 1) * 32 + dwarp;
+        if (val && d >= 0) atomicAdd(&dacc[d], val);
+        carry = hi;
       }
+      if (carry) atomicAdd(&dacc[(BN / 32 - 1) * 32 + dwarp], carry);
       tc_fence_before();
       mbar_arrive(&acce[buf]);
       named_bar_sync(1, EPI_THREADS);
