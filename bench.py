@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparator")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extra", action="store_true",
+                   help="dense line only: skip the u16 / sparse / event sub-lines (configurations 3 and 4)")
     p.add_argument("--frames", type=int, default=None, help="override T (testing only)")
     p.add_argument("--shape", default=None, help="H,W of the sparse/event frames (profiling only)")
     p.add_argument("--tile", default=None, choices=["pair", "single"],
@@ -472,6 +474,17 @@ def run_ours(args):
             "sample": "first %d of the %d frames, all 16 bins; %s, %d threads, took %.2f s; O(T^2) cost scaled "
                       "to %d frames (the reference arm times all %d frames)" % (Ts, T, label, ncores, ts[0], T,
                                                                                T)}
+    # ---- configurations 3 (u16 precision stress) and 4 (CSR and event lists),
+    # measured in the same run so that every configuration has a line
+    if not args.no_extra:
+        del frames
+        torch.cuda.empty_cache()
+        extra_steps = max(3, min(args.steps, 10))
+        configs = {"u16": measure_u16(args, dev, U16_WORKLOAD["nframes"], extra_steps, args.warmup,
+                                      cpu=not args.no_cpu and rank == 0, e2e=not args.no_e2e)}
+        configs.update(measure_sparse(args, dev, SPARSE_WORKLOAD["nframes"], extra_steps, args.warmup, dist=dist,
+                                      world=world, rank=rank, cpu=not args.no_cpu, e2e=not args.no_e2e))
+        line["configs"] = configs
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -523,23 +536,71 @@ def cpu_event_sample(times, data, offs, qmask, shape, T, stride):
     return time.perf_counter() - t0, pairs
 
 
-def run_sparse(args):
+def event_rows_sample(ev_times, ev_data, ev_off, qmask, shape, row_stride):
+    """The event lists of every ``row_stride``-th image row (rows below the
+    frame width: the rows the reference's event launch reaches, event.py:183)
+    as a smaller image on the host: (times, data, offsets, qmask, shape, pair
+    operations).  A row's events are one contiguous slice of the lists."""
     import numpy as np
     import torch
+    H, W = shape
+    rows = np.arange(0, min(H, W), row_stride)
+    off = ev_off.to(torch.int64).cpu().numpy()
+    sl = [(int(off[y * W]), int(off[(y + 1) * W])) for y in rows]
+    times = torch.cat([ev_times[a:b] for a, b in sl]).cpu().numpy()
+    data = torch.cat([ev_data[a:b] for a, b in sl]).cpu().numpy()
+    counts = np.concatenate([np.diff(off[y * W:(y + 1) * W + 1]) for y in rows])
+    offs = np.zeros(counts.size + 1, dtype=np.uint32)
+    offs[1:] = np.cumsum(counts)
+    qm = np.ascontiguousarray(qmask[rows])
+    binned = qm.ravel() > 0
+    pairs = int((counts[binned] * (counts[binned] + 1) // 2).sum())
+    return times, data, offs, qm, (rows.size, W), pairs
 
-    from dynamix_gb300 import build as b
+
+CPU_EVENT_ROW_STRIDE = 16
+
+
+def cpu_event_baseline(ev_times, ev_data, ev_off, qmask, shape, T, all_pairs):
+    """frames/s of the CPU pair sums on a sample of rows, scaled by pair
+    operations to the whole stack: the reference's own evtcorrelator.cl
+    (event_correlator + normalize_correlation compiled as C, all host threads;
+    the OpenCL runtime is not available) when its sources are installed, else
+    the C restatement."""
+    from oracle.g2_oracle import event_pairsum_c, reference_event_correlate
+    ncores = host_cores()
+    t_h, d_h, o_h, qm, sub_shape, sp = event_rows_sample(ev_times, ev_data, ev_off, qmask, shape,
+                                                         CPU_EVENT_ROW_STRIDE)
+    kind, label = "reference", ("the reference's own evtcorrelator.cl (event_correlator + normalize_correlation, "
+                                "compiled as C through the OpenCL shim, %d threads)" % ncores)
+    t0 = time.perf_counter()
+    try:
+        ok = reference_event_correlate(t_h, d_h, o_h, qm, sub_shape, T, n_threads=ncores) is not None
+    except ValueError:
+        ok = False
+    secs = time.perf_counter() - t0
+    if not ok:
+        kind, label = "port", "the C restatement of evtcorrelator.cl:3-47 (int64, %d threads)" % ncores
+        t0 = time.perf_counter()
+        event_pairsum_c(t_h, d_h, o_h, qm, sub_shape, T)
+        secs = time.perf_counter() - t0
+    full = secs * all_pairs / max(sp, 1)
+    return {"value": T / full, "unit": "frames/s", "cores": ncores, "kind": kind,
+            "sample": "event pair sums of every %dth image row (%d pair ops of %d) by %s in %.2f s, scaled by pair "
+                      "ops to all %d frames; the CSR-to-event step is not included" % (
+                          CPU_EVENT_ROW_STRIDE, sp, all_pairs, label, secs, T)}
+
+
+def measure_sparse(args, dev, T, steps, warmup, which=("sparse", "event"), shape=None, dist=None, world=1,
+                   rank=0, cpu=True, e2e=True):
+    """Lines of the CSR workload (SparseCorrelator: CSR -> event lists on the
+    device, pair sums, normalisation) and of the event-list workload
+    (EventCorrelator on the same stack's lists), from one generated stack.
+    Returns {kind: line} for the kinds in ``which``."""
+    import torch
     from dynamix_gb300.correlator import EventCorrelator, SparseCorrelator
 
-    rank, world, local = dist_info()
-    dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
-    b.build(force=False)
-    T = args.frames
-    H, W = sparse_shape(args)
+    H, W = shape or tuple(SPARSE_WORKLOAD["frame_shape"])
     (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T, (H, W))
     offsets = offsets.to(torch.int32)              # one index type (int32) for the whole CSR stack
     sc = SparseCorrelator((H, W), T, qmask=qmask)
@@ -548,17 +609,12 @@ def run_sparse(args):
     torch.cuda.synchronize(dev)
     n_elem = int(data.numel())
     n_binned_events, pairs = event_stats(ev_off, qmask)
-    if args.workload == "event":
-        corr = EventCorrelator((H, W), T, 1, qmask=qmask)
-        inputs = (ev_times, ev_data, ev_off)
-        events_engine = corr.engine
-        del data, indices, indptr, offsets
-    else:
-        corr = sc
-        inputs = (data, indices, indptr, offsets)
-        events_engine = sc.engine.events
-        del ev_times, ev_data
     stream = torch.cuda.current_stream(dev)
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -569,116 +625,128 @@ def run_sparse(args):
         from dynamix_gb300.replicas import max_over_ranks as mx
         return mx(x, dist, dev)
 
-    for _ in range(max(args.warmup, 3)):
-        corr.correlate_device(*inputs)
-    corr.engine.check_error()
-    uuid = None
-    try:
-        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
-    except Exception:
-        pass
-    sampler = ClockSampler(uuid)
-    events_engine.profile = True
-    barrier()
-    sampler.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    step_events = []
-    for _ in range(args.steps):
-        corr.correlate_device(*inputs)
-        step_events.append(events_engine.take_events())
-    e1.record(stream)
-    barrier()
-    clocks = sampler.stop()
-    events_engine.profile = False
-    corr.engine.check_error()
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    stages = {}
-    for ev in step_events:
-        for k, v in events_engine.stage_times(ev).items():
-            stages[k] = stages.get(k, 0.0) + v / args.steps
-    info = dict(events_engine.last)
-
-    # algorithmic bytes per step (each array read or written once)
     npix = H * W
     P_b = int((qmask > 0).sum())
     n_bins = SPARSE_WORKLOAD["n_bins"]
     transpose_bytes = 14 * n_elem + 8 * (H + 1) * T + 16 * npix
     pair_bytes = 5 * n_binned_events + 12 * P_b + 16 * n_bins * T
     norm_bytes = 6 * 8 * n_bins * T
-    step_bytes = pair_bytes + norm_bytes + (transpose_bytes if args.workload == "sparse" else 0)
     peaks, peak_kind = measured_peaks()
     hbm = peaks.get("hbm_gbs")
-    pair_ms = stages.get("pairsum", float("nan"))
-    achieved = pair_bytes / (pair_ms / 1e3) / 1e9
-    stage_report = {"pairsum": {"ms": pair_ms, "GB_per_s": achieved, "bytes": pair_bytes,
-                                "pair_ops_per_s": pairs / (pair_ms / 1e3)},
-                    "normalize": {"ms": stages.get("normalize", float("nan")), "bytes": norm_bytes}}
-    launches = 3   # pair sums, denominator, finalize
-    if args.workload == "sparse":
-        tms = stages.get("transpose", float("nan"))
-        stage_report["transpose"] = {"ms": tms, "GB_per_s": transpose_bytes / (tms / 1e3) / 1e9,
-                                     "bytes": transpose_bytes, "kernels": "count, scan (3), scatter"}
-        launches += 5
-    cfg = dict(SPARSE_WORKLOAD, nframes=T, frame_shape=[H, W], workload=SPARSE_WORKLOAD["workload"].replace(
-        "sparse", "sparse_csr" if args.workload == "sparse" else "event_lists"),
-        parallelism="replicas" if world > 1 else "single", n_elements=n_elem,
-        binned_pixels=P_b, binned_events=n_binned_events, pair_ops=pairs)
-    line = {
-        "metric": "g2_frames_per_s", "value": world * T / (ms / 1e3), "unit": "frames/s", "n_gpus": world,
-        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
-        "hbm_GB_per_s_step": step_bytes / (ms / 1e3) / 1e9,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": profile_traffic("event_pairsum_2162x2068_T20000.md",
-                                                "traffic_bytes_per_launch" if args.workload == "event"
-                                                else "traffic_bytes_per_launch_packed"),
-                     "kernel": "g2_event_pairsum",
-                     "peak_source": "%s hbm_gbs" % peak_kind, "algorithmic_bytes_per_launch": pair_bytes,
-                     "launch_ms": pair_ms,
-                     "note": "bound by shared-memory atomics (one per event pair), not by HBM"},
-        "stages": stage_report, "clocks": clocks, "gpu_launches": launches * args.steps, "plan": info,
-    }
-
-    if not args.no_e2e:
-        host = [x.cpu().pin_memory() for x in inputs]
-        corr.correlate(*host)
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            corr.correlate(*host)
-        barrier()
-        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
-        line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
-                       "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in host)),
-                       "d2h_bytes_per_step": int(n_bins * T * 4 + 4), "ms_per_step": e2e_ms}
-        del host
-
-    if not args.no_cpu and rank == 0:
-        if args.workload == "event":
-            t_h, d_h, o_h = (x.cpu().numpy() for x in inputs)
+    cpu_line = cpu_event_baseline(ev_times, ev_data, ev_off, qmask, (H, W), T, pairs) if cpu and rank == 0 else None
+    out = {}
+    for kind in which:
+        if kind == "event":
+            corr = EventCorrelator((H, W), T, 1, qmask=qmask)
+            inputs = (ev_times, ev_data, ev_off)
+            events_engine = corr.engine
         else:
-            t_h, d_h, o_h = (x.cpu().numpy() for x in sc.engine.to_events(*inputs, 4, n_elem))
-        o_h = o_h.view(np.uint32)
-        secs, sample_pairs = cpu_event_sample(t_h, d_h, o_h, qmask, (H, W), T, CPU_SAMPLE_PIXEL_STRIDE)
-        ncores = os.cpu_count()
-        full = secs * pairs / max(sample_pairs, 1)
-        line["cpu_baseline"] = {
-            "value": T / full, "unit": "frames/s", "cores": ncores, "kind": "port",
-            "sample": "event pair sums (C restatement of evtcorrelator.cl:3-47, int64, %d threads) over every "
-                      "%dth binned pixel: %d pair ops in %.2f s, scaled by pair ops to the %d of all %d frames; "
-                      "the CSR-to-event step is not included" % (ncores, CPU_SAMPLE_PIXEL_STRIDE, sample_pairs,
-                                                                secs, pairs, T)}
+            corr = sc
+            inputs = (data, indices, indptr, offsets)
+            events_engine = sc.engine.events
+        for _ in range(max(warmup, 3)):
+            corr.correlate_device(*inputs)
+        corr.engine.check_error()
+        sampler = ClockSampler(uuid)
+        events_engine.profile = True
+        barrier()
+        sampler.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step_events = []
+        for _ in range(steps):
+            corr.correlate_device(*inputs)
+            step_events.append(events_engine.take_events())
+        e1.record(stream)
+        barrier()
+        clocks = sampler.stop()
+        events_engine.profile = False
+        corr.engine.check_error()
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps)
+        stages = {}
+        for ev in step_events:
+            for k, v in events_engine.stage_times(ev).items():
+                stages[k] = stages.get(k, 0.0) + v / steps
+        info = dict(events_engine.last)
+        step_bytes = pair_bytes + norm_bytes + (transpose_bytes if kind == "sparse" else 0)
+        pair_ms = stages.get("pairsum", float("nan"))
+        achieved = pair_bytes / (pair_ms / 1e3) / 1e9
+        stage_report = {"pairsum": {"ms": pair_ms, "GB_per_s": achieved, "bytes": pair_bytes,
+                                    "pair_ops_per_s": pairs / (pair_ms / 1e3)},
+                        "normalize": {"ms": stages.get("normalize", float("nan")), "bytes": norm_bytes}}
+        launches = 3   # pair sums, denominator, finalize
+        if kind == "sparse":
+            tms = stages.get("transpose", float("nan"))
+            stage_report["transpose"] = {"ms": tms, "GB_per_s": transpose_bytes / (tms / 1e3) / 1e9,
+                                         "bytes": transpose_bytes,
+                                         "kernels": "row bounds, row counts, sub-block sums, two scans (3 each), "
+                                                    "stage, gather"}
+            launches += 11
+        cfg = dict(SPARSE_WORKLOAD, nframes=T, frame_shape=[H, W], workload=SPARSE_WORKLOAD["workload"].replace(
+            "sparse", "sparse_csr" if kind == "sparse" else "event_lists"),
+            parallelism="replicas" if world > 1 else "single", n_elements=n_elem,
+            binned_pixels=P_b, binned_events=n_binned_events, pair_ops=pairs)
+        line = {
+            "metric": "g2_frames_per_s", "value": world * T / (ms / 1e3), "unit": "frames/s", "n_gpus": world,
+            "steps": steps, "warmup": max(warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg,
+            "hbm_GB_per_s_step": step_bytes / (ms / 1e3) / 1e9,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": profile_traffic("event_pairsum_2162x2068_T20000.md",
+                                                    "traffic_bytes_per_launch" if kind == "event"
+                                                    else "traffic_bytes_per_launch_packed"),
+                         "kernel": "g2_event_pairsum",
+                         "peak_source": "%s hbm_gbs" % peak_kind, "algorithmic_bytes_per_launch": pair_bytes,
+                         "launch_ms": pair_ms,
+                         "note": "bound by shared-memory atomics (one per event pair), not by HBM"},
+            "stages": stage_report, "clocks": clocks, "gpu_launches": launches * steps, "plan": info,
+        }
+        if e2e:
+            host = [x.cpu().pin_memory() for x in inputs]
+            corr.correlate(*host)
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                corr.correlate(*host)
+            barrier()
+            e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / steps)
+            line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
+                           "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in host)),
+                           "d2h_bytes_per_step": int(n_bins * T * 4 + 4), "ms_per_step": e2e_ms}
+            del host
+        if cpu_line is not None:
+            line["cpu_baseline"] = dict(cpu_line)
+        out[kind] = line
+        del corr
+    return out
+
+
+def run_sparse(args):
+    import torch
+    from dynamix_gb300 import build as b
+    rank, world, local = dist_info()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    b.build(force=False)
+    lines = measure_sparse(args, dev, args.frames, args.steps, args.warmup, which=(args.workload,),
+                           shape=sparse_shape(args), dist=dist, world=world, rank=rank, cpu=not args.no_cpu,
+                           e2e=not args.no_e2e)
     if rank == 0:
-        print(json.dumps(line))
+        print(json.dumps(lines[args.workload]))
     if dist is not None:
         dist.destroy_process_group()
     return 0
 
 
 def run_sparse_reference(args):
-    import numpy as np
+    """The CPU reference of the event pair sums (the reference's own
+    evtcorrelator.cl compiled as C, else the C restatement), each step a
+    sample of rows scaled by pair operations to the whole stack."""
     import torch
     rank, world, local = dist_info()
     if rank != 0:
@@ -693,31 +761,20 @@ def run_sparse_reference(args):
     (data, indices, indptr, offsets), qmask = make_sparse_workload(dev, T, (H, W))
     offsets = offsets.to(torch.int32)
     sc = SparseCorrelator((H, W), T, qmask=qmask)
-    t_h, d_h, o_h = (x.cpu().numpy() for x in sc.engine.to_events(data, indices, indptr, offsets, 4,
-                                                                   int(data.numel())))
-    o_h = o_h.view(np.uint32)
+    ev = [x.clone() for x in sc.engine.to_events(data, indices, indptr, offsets, 4, int(data.numel()))]
     del data, indices, indptr, offsets, sc
-    ev_off = torch.from_numpy(o_h.view(np.int32))
-    _, pairs = event_stats(ev_off, qmask)
+    _, pairs = event_stats(ev[2], qmask)
     for _ in range(args.warmup):
-        cpu_event_sample(t_h, d_h, o_h, qmask, (H, W), T, CPU_SAMPLE_PIXEL_STRIDE * 4)
-    ts = []
-    for _ in range(args.steps):
-        secs, sp = cpu_event_sample(t_h, d_h, o_h, qmask, (H, W), T, CPU_SAMPLE_PIXEL_STRIDE * 4)
-        ts.append(secs * pairs / max(sp, 1))
-    t = sum(ts) / len(ts)
-    v = T / t
-    ncores = os.cpu_count()
+        cpu_event_baseline(*ev, qmask, (H, W), T, pairs)
+    vals = [cpu_event_baseline(*ev, qmask, (H, W), T, pairs) for _ in range(args.steps)]
+    v = sum(x["value"] for x in vals) / len(vals)
     line = {
         "metric": "g2_frames_per_s", "value": v, "unit": "frames/s", "impl": "reference", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": T / v * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": dict(SPARSE_WORKLOAD, nframes=T, workload=SPARSE_WORKLOAD["workload"].replace(
             "sparse", "event_lists")),
-        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": ncores, "kind": "port",
-                         "sample": "each step: event pair sums (C restatement, %d threads) over every %dth binned "
-                                   "pixel, scaled by pair ops to all %d pair ops" % (
-                                       ncores, CPU_SAMPLE_PIXEL_STRIDE * 4, pairs)},
+        "cpu_baseline": dict(vals[-1], value=v),
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -890,77 +947,120 @@ U16_WORKLOAD = {
 U16_ORACLE_FRAMES = 1024
 
 
-def run_u16(args):
+def measure_u16(args, dev, T, steps, warmup, cpu=True, e2e=True):
+    """The precision-stress line: 256 x 256 u16 counts <= 4095 (mean 50), 12
+    bins, through MatMulCorrelator (the operand the counts allow: fp16 counts
+    <= 2048 here), plus the same stack forced onto the hi/lo byte planes
+    (4 Grams per bin, the split the configuration is meant to exercise), each
+    with the float32 g2's largest relative error per bin against the FP64
+    oracle on the first frames and N/D bit-exactness there."""
     import numpy as np
     import torch
 
-    from dynamix_gb300 import build as b
+    from dynamix_gb300 import _lib as L
     from dynamix_gb300.correlator import MatMulCorrelator
     from dynamix_gb300.plan import gram_macs
     from dynamix_gb300.speckle import annular_qmask, speckle_torch
+    from oracle.g2_oracle import g2_exact
 
-    rank, world, local = dist_info()
-    dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
-    b.build(force=False)
-    T = args.frames
     H, W = U16_WORKLOAD["frame_shape"]
     qmask = annular_qmask((H, W), U16_WORKLOAD["n_bins"], 8.0, 128.0, center=(128, 128))
     frames = speckle_torch(T, (H, W), U16_WORKLOAD["rho"], U16_WORKLOAD["mean_photons"], seed=U16_WORKLOAD["seed"],
                            dtype="uint16", max_count=U16_WORKLOAD["max_count"], device=dev)
-    corr = MatMulCorrelator((H, W), T, qmask=qmask)
-    eng = corr.engine
-    for _ in range(max(args.warmup, 3)):
-        corr.correlate_device(frames)
-    eng.check_error()
-    stream = torch.cuda.current_stream(dev)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize(dev)
-    e0.record(stream)
-    for _ in range(args.steps):
-        corr.correlate_device(frames)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / args.steps
-    info = dict(eng.last)
-    eng.profile = True
-    corr.correlate_device(frames)
-    st = eng.stage_times(eng.take_events())
-    eng.profile = False
     npix = np.bincount(qmask.ravel(), minlength=U16_WORKLOAD["n_bins"] + 1)[1:]
     macs = gram_macs(T, npix)
-    planes = 4 if info["mode"] == "bytes" else 1
-    peaks, peak_kind = measured_peaks()
-    gram = st.get("gram_tc", float("nan"))
-    executed = 2.0 * macs * planes / (gram / 1e3) / 1e12
-    # per-bin g2 error against the FP64 oracle on the first frames
-    from oracle.g2_oracle import g2_exact
+    stream = torch.cuda.current_stream(dev)
+    peak_f16, _ = tc_rate(dev, L.KIND_FP16)
     Ts = min(U16_ORACLE_FRAMES, T)
     sub = frames[:Ts].cpu().numpy()
-    c2 = MatMulCorrelator((H, W), Ts, qmask=qmask)
-    g32 = c2.correlate(sub)
     ref = g2_exact(sub, qmask)
-    exact = bool(np.array_equal(c2.numerator, ref["numerator"]) and np.array_equal(c2.denominator,
-                                                                                    ref["denominator"]))
-    with np.errstate(divide="ignore", invalid="ignore"):
-        rel = np.abs(g32.astype(np.float64) - ref["g2"]) / np.abs(ref["g2"])
-    per_bin = [float(np.nanmax(r)) if np.isfinite(r).any() else None for r in rel]
-    line = {
-        "metric": "g2_frames_per_s", "value": T / (ms / 1e3), "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u16", "data": "synthetic", "config": dict(U16_WORKLOAD, nframes=T),
-        "plan": info, "stages_ms": st,
-        "tiles": {"block": "128 x 256 (tcgen05 M128 N256)", "k_stage": "64 fp16 columns per TMA stage",
-                  "operand": info["mode"], "grams_per_bin": planes, "k_split_chunks": info.get("n_grams")},
-        "roofline": {"bound": "tensor", "achieved": executed, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
-                     "frac": executed / peaks.get("bf16_tflops"), "kernel": "g2_gram_tc",
-                     "peak_source": "%s bf16_tflops (kind::f16 on byte planes; executed ops = %d x algorithmic)"
-                                    % (peak_kind, planes)},
-        "fp64_check": {"frames": Ts, "numerator_denominator_bit_exact": exact,
-                       "max_rel_err_float32_g2_vs_fp64_per_bin": per_bin},
-    }
-    print(json.dumps(line))
+
+    def one(operand):
+        corr = MatMulCorrelator((H, W), T, qmask=qmask, extra_options={"operand": operand})
+        eng = corr.engine
+        for _ in range(max(warmup, 3)):
+            corr.correlate_device(frames)
+        eng.check_error()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(steps):
+            corr.correlate_device(frames)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        eng.check_error()
+        ms = e0.elapsed_time(e1) / steps
+        info = dict(eng.last)
+        eng.profile = True
+        corr.correlate_device(frames)
+        st = eng.stage_times(eng.take_events())
+        eng.profile = False
+        planes = 4 if info["mode"] == "bytes" else 1
+        gram = st.get("gram_tc", float("nan"))
+        executed = 2.0 * macs * planes / (gram / 1e3) / 1e12
+        c2 = MatMulCorrelator((H, W), Ts, qmask=qmask, extra_options={"operand": operand})
+        g32 = c2.correlate(sub)
+        exact = bool(np.array_equal(c2.numerator, ref["numerator"]) and np.array_equal(c2.denominator,
+                                                                                        ref["denominator"]))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            rel = np.abs(g32.astype(np.float64) - ref["g2"]) / np.abs(ref["g2"])
+        per_bin = [float(np.nanmax(r)) if np.isfinite(r).any() else None for r in rel]
+        out = {
+            "metric": "g2_frames_per_s", "value": T / (ms / 1e3), "unit": "frames/s", "n_gpus": 1, "steps": steps,
+            "warmup": max(warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u16", "data": "synthetic", "config": dict(U16_WORKLOAD, nframes=T),
+            "plan": info, "stages_ms": st,
+            "tiles": {"block": {"pair": "256 x n (tcgen05 cta_group::2 M256)",
+                                "single": "128 x 256 (tcgen05 M128 N256)"}[info.get("tile", "single")],
+                      "k_stage": "64 fp16 columns per TMA stage",
+                      "operand": info["mode"], "grams_per_bin": planes, "k_split_chunks": info.get("n_grams"),
+                      "autotuner_candidates": "tile, pipeline chunks, operand (dynamix_gb300.tune)"},
+            "roofline": {"bound": "tensor", "achieved": executed, "peak": peak_f16, "unit": "TFLOP/s",
+                         "frac": executed / peak_f16, "kernel": "g2_gram_tc_pair" if info.get("tile") == "pair"
+                         else "g2_gram_tc", "launch_ms": gram,
+                         "peak_source": "tcgen05 kind::f16 rate measured in this run (g2_tc_rate_probe); executed "
+                                        "ops = %d x the algorithmic %.3e" % (planes, 2.0 * macs)},
+            "fp64_check": {"frames": Ts, "numerator_denominator_bit_exact": exact,
+                           "max_rel_err_float32_g2_vs_fp64_per_bin": per_bin},
+            "gpu_launches": 4 * steps,
+        }
+        return corr, out
+
+    corr, line = one("auto")
+    if e2e:
+        host = frames.cpu().pin_memory()
+        corr.correlate(host)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            corr.correlate(host)
+        torch.cuda.synchronize(dev)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
+        line["e2e"] = {"value": T / (e2e_ms / 1e3), "unit": "frames/s", "ms_per_step": e2e_ms,
+                       "h2d_bytes_per_step": int(host.numel() * host.element_size()),
+                       "d2h_bytes_per_step": int(U16_WORKLOAD["n_bins"] * T * 12 + 4)}
+        del host
+    del corr
+    _, line["byte_planes"] = one("bytes")
+    if cpu:
+        ts, kind, label = cpu_port_time(frames.cpu().numpy(), qmask)
+        ncores = host_cores()
+        line["cpu_baseline"] = {"value": T / ts[0], "unit": "frames/s", "cores": ncores, "kind": kind,
+                                "sample": "the whole stack (all %d frames, 12 bins): %s, %d threads, %.2f s"
+                                          % (T, label, ncores, ts[0])}
+    return line
+
+
+def run_u16(args):
+    import torch
+    from dynamix_gb300 import build as b
+    rank, world, local = dist_info()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    b.build(force=False)
+    print(json.dumps(measure_u16(args, dev, args.frames, args.steps, args.warmup, cpu=not args.no_cpu,
+                                 e2e=not args.no_e2e)))
     return 0
 
 
