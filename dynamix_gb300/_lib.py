@@ -63,6 +63,8 @@ SIGNATURES = {
     "g2_tc_rate_probe": (C.c_int, [_i32, _i64, _i32, _p, _p]),
     "g2_gram_std": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p, _p, _p, _i64, _p, _i32, _p]),
     "g2_std_finalize": (C.c_int, [_p, _p, _p, _i32, _i64, _p, _p, _p]),
+    "g2_gram_matrix": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _i64, _i32, _p, _i32, _p]),
+    "g2_matrix_deviation": (C.c_int, [_p, _i64, _i64, _p, C.c_double, _p, _p, _p, _p, _p]),
     "g2_gram_ttcf": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _i64, _i32, _p, _i32, _p]),
     "g2_ttcf_finish": (C.c_int, [_p, _i64, _i64, _p, _i32, _p]),
     "g2_event_pairsum": (C.c_int, [_p, _p, _i32, _i64, _p, _i64, _p, _p, _p, _i32, _p, _i32, _i32, _i32, _i32, _p,

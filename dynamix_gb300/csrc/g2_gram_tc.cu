@@ -79,6 +79,7 @@ struct StdOut {
 constexpr int MODE_NUMER = 0;  // lag sums of G (the numerator)
 constexpr int MODE_STD = 1;    // deviation of the per-pair ratio (calc_std)
 constexpr int MODE_TTCF = 2;   // per-pair ratio written as the two-time matrix
+constexpr int MODE_MATRIX = 3; // 2^shift G(t,t') for t' >= t written (or added) to a matrix
 
 struct MapsParam {
   CUtensorMap a[G2_MAX_JOBS];
@@ -110,12 +111,13 @@ __device__ __forceinline__ bool named_bar_any(uint32_t id, uint32_t n, bool v) {
 template <int MODE>
 __device__ __forceinline__ bool item_ok(const g2_gram_item& w, const MapsParam& maps, int n_jobs,
                                         int64_t numer_len, int64_t sums_len, int64_t max_frames) {
-  constexpr bool STD = MODE != MODE_NUMER;
-  if (MODE == MODE_TTCF && w.nframes > max_frames) return false;
+  constexpr bool STD = MODE == MODE_STD || MODE == MODE_TTCF;
+  if ((MODE == MODE_TTCF || MODE == MODE_MATRIX) && w.nframes > max_frames) return false;
   if (w.job < 0 || w.job >= n_jobs) return false;
   const int bk = stage_elems(maps.kind[w.job]);
   const bool shape = w.k_len > 0 && (w.k_len % bk) == 0 && (w.a_k0 % bk) == 0 && (w.b_k0 % bk) == 0 &&
                      w.nframes > 0 && w.out_off >= 0 && w.out_off + w.nframes <= numer_len;
+  if (MODE == MODE_MATRIX) return shape && w.shift >= 0 && w.shift <= 30;
   if (STD) return shape && w.shift > 0 && w.s_off >= 0 && w.s_off + w.nframes <= sums_len;
   return shape && w.shift >= 0 && w.shift <= 32 &&
          (w.s_off < 0 || (maps.ones[w.job] && w.shift == 0 && w.s_off + w.nframes <= sums_len));
@@ -288,6 +290,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const bool row_live = w.i0 + row < w.nframes;
       const int col_end = min(BN, w.nframes - w.j0);                // columns < col_end are frames
       const int lag0 = w.j0 - w.i0 - (BM - 1);
+      if (MODE == MODE_MATRIX) {
+        // ---------------------------------------- Gram matrix mode epilogue
+        // this item's plane combination of the bin, weighted by 2^shift, for
+        // every pair t' >= t; `mirror` set: added to what earlier launches wrote
+        const float wgt = unscale * static_cast<float>(1u << w.shift);
+        const int64_t t = static_cast<int64_t>(w.i0) + row;
+#pragma unroll 1
+        for (int cc = 0; cc < BN / 32; ++cc) {
+          uint32_t v[32];
+          __syncwarp();
+          tmem_ld_32x32b_x32(tbase + static_cast<uint32_t>(cc * 32), v);
+          tmem_wait_ld();
+          if (!row_live) continue;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int c = cc * 32 + j;
+            const int64_t t2 = static_cast<int64_t>(w.j0) + c;
+            if (c >= col_end || t2 < t) continue;  // t' >= T, or below the diagonal
+            float* o = so.ttcf + t * so.ld + t2;
+            const float g = __uint_as_float(v[j]) * wgt;
+            *o = so.mirror ? *o + g : g;
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&acce[buf]);
+        continue;
+      }
       if (MODE == MODE_TTCF) {
         // ---------------------------------------- two-time mode epilogue
         const float P = static_cast<float>(w.shift);
@@ -576,6 +605,21 @@ extern "C" int g2_gram_ttcf(const g2_job* jobs, int32_t n_jobs, const g2_gram_it
   return launch_gram<tc::MODE_TTCF>(jobs, n_jobs, items_dev, n_items, nullptr, sums_len,
                                     reinterpret_cast<uint64_t*>(const_cast<int64_t*>(sums_dev)), sums_len, err_dev,
                                     grid, stream, so);
+}
+
+extern "C" int g2_gram_matrix(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                              float* matrix_dev, int64_t nframes, int64_t ld, int32_t accumulate, int32_t* err_dev,
+                              int32_t grid, void* stream) {
+  using namespace g2;
+  if (!jobs || n_jobs < 1 || n_jobs > G2_MAX_JOBS || n_items < 0 || !matrix_dev || nframes <= 0 || ld < nframes ||
+      !err_dev)
+    return G2_ERR_ARG;
+  if (n_items > 0 && !items_dev) return G2_ERR_ARG;
+  const tc::StdOut so = {nullptr, nullptr, nullptr, nullptr, nullptr, matrix_dev, ld, nframes, accumulate ? 1 : 0};
+  // items may not have more frames than the matrix (out_off + nframes bounded by nframes);
+  // numer and sums are not written in this mode
+  return launch_gram<tc::MODE_MATRIX>(jobs, n_jobs, items_dev, n_items, nullptr, nframes, nullptr, 0, err_dev, grid,
+                                      stream, so);
 }
 
 extern "C" int g2_ttcf_finish(float* ttcf_dev, int64_t nframes, int64_t ld, const int64_t* bin_sums_dev,

@@ -181,8 +181,61 @@ __global__ void std_finalize_kernel(const double* __restrict__ sum_d, const doub
   }
 }
 
+// Deviation statistics of one bin from its Gram matrix G[t][t'] (t' >= t,
+// row stride ld): for every pair, r = P G / (S(t) S(t')) and d = r - centre(tau)
+// (0 when the centre is not finite), summed per lag in double into sum_d and
+// sum_d2; pairs with S(t) S(t') = 0 are counted in zeros.  A block owns 256
+// consecutive lags (a thread each, so that the loads of a row are
+// coalesced) and a range of rows; one double atomic per lag per block.
+__global__ void __launch_bounds__(256)
+    matrix_deviation_kernel(const float* __restrict__ G, int64_t T, int64_t ld, const long long* __restrict__ S,
+                            double P, const float* __restrict__ centre, double* __restrict__ sum_d,
+                            double* __restrict__ sum_d2, unsigned int* __restrict__ zeros, int64_t rows_per_block) {
+  const int64_t tau = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (tau >= T) return;
+  const float cf = centre[tau];
+  const double c = isfinite(cf) ? static_cast<double>(cf) : 0.0;
+  const int64_t t0 = static_cast<int64_t>(blockIdx.y) * rows_per_block;
+  int64_t t1 = t0 + rows_per_block;
+  if (t1 > T - tau) t1 = T - tau;
+  double sd = 0.0, sd2 = 0.0;
+  unsigned int nz = 0;
+  for (int64_t t = t0; t < t1; ++t) {
+    const double den = static_cast<double>(S[t]) * static_cast<double>(S[t + tau]);
+    if (den == 0.0) {
+      ++nz;
+    } else {
+      const double d = P * static_cast<double>(G[t * ld + t + tau]) / den - c;
+      sd += d;
+      sd2 += d * d;
+    }
+  }
+  if (t1 > t0) {
+    if (sd != 0.0) atomicAdd(&sum_d[tau], sd);
+    if (sd2 != 0.0) atomicAdd(&sum_d2[tau], sd2);
+    if (nz) atomicAdd(&zeros[tau], nz);
+  }
+}
+
 }  // namespace norm
 }  // namespace g2
+
+extern "C" int g2_matrix_deviation(const float* matrix_dev, int64_t nframes, int64_t ld, const int64_t* bin_sums_dev,
+                                   double npix, const float* centre_dev, double* sum_d_dev, double* sum_d2_dev,
+                                   uint32_t* zeros_dev, void* stream) {
+  using namespace g2;
+  if (!matrix_dev || !bin_sums_dev || !centre_dev || !sum_d_dev || !sum_d2_dev || !zeros_dev || nframes <= 0 ||
+      ld < nframes || !(npix > 0.0))
+    return G2_ERR_ARG;
+  const int64_t rows_per_block = 256;
+  const int64_t gx = (nframes + 255) / 256, gy = (nframes + rows_per_block - 1) / rows_per_block;
+  if (gx > 0x7fffffff || gy > 65535) return G2_ERR_TOO_LARGE;
+  norm::matrix_deviation_kernel<<<dim3(static_cast<unsigned>(gx), static_cast<unsigned>(gy)), 256, 0,
+                                  as_stream(stream)>>>(matrix_dev, nframes, ld,
+                                                       reinterpret_cast<const long long*>(bin_sums_dev), npix,
+                                                       centre_dev, sum_d_dev, sum_d2_dev, zeros_dev, rows_per_block);
+  return launch_status();
+}
 
 extern "C" int g2_std_finalize(const double* sum_d_dev, const double* sum_d2_dev, const uint32_t* zeros_dev,
                                int32_t n_rows, int64_t nframes, float* dev_f32, double* dev_f64, void* stream) {

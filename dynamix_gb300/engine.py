@@ -658,7 +658,7 @@ class DenseEngine:
         if L is None or self.packed is None:
             raise RuntimeError("deviation() needs a preceding run()")
         if L.split:
-            raise NotImplementedError("calc_std needs counts <= 2048 (this stack uses byte planes)")
+            return self._deviation_planes(L)
         key = ("std", L.mode, self.T)
         if key not in self._items_cache:
             from .plan import std_items
@@ -682,6 +682,50 @@ class DenseEngine:
                                             ptr(self.err), self.grid, st), "g2_gram_std")
         _lib.check(self.lib.g2_std_finalize(ptr(sd), ptr(sd2), ptr(zeros), self.n_bins, self.T, ptr(d32), ptr(d64),
                                             st), "g2_std_finalize")
+        self.dev_f64 = d64
+        return d32[: self.n_bins]
+
+    def _deviation_planes(self, L):
+        """calc_std of a byte-plane stack (counts above 2048): the per-pair
+        ratio needs the four plane Grams of a pair together, so each bin's
+        Gram G = 2^16 G_hh + 2^8 (G_hl + G_lh) + G_ll is assembled in a T x T
+        float32 matrix (one tensor-core pass per plane combination, whole K)
+        and each lag's deviation statistics are reduced from it."""
+        torch = _torch()
+        from .plan import _tiles
+        T = self.T
+        rows = max(self.n_bins, 1)
+        z = lambda dt: torch.zeros((rows, T), dtype=dt, device=self.dev)
+        sd, sd2, zeros, d32, d64 = z(torch.float64), z(torch.float64), z(torch.int32), z(torch.float32), \
+            z(torch.float64)
+        mat = getattr(self, "_gram_matrix", None)
+        if mat is None or mat.numel() < T * T:
+            self._gram_matrix = None
+            mat = self._gram_matrix = torch.empty((T, T), dtype=torch.float32, device=self.dev)
+        npix = np.bincount(self.qmask.ravel()[self.qmask.ravel() > 0], minlength=self.n_bins + 1)[1:]
+        i0, j0 = _tiles(T, TILE_SHAPES["tc"][0], TILE_SHAPES["tc"][1])
+        st = stream_handle(self.dev)
+        jobs = _lib.jobs_array([(self.packed.data_ptr(), T, L.packed_cols, L.kind, 0)])
+        by_bin = {}
+        for (b, a_off, b_off, kp, shift) in L.grams():
+            by_bin.setdefault(b, []).append((a_off, b_off, kp, shift))
+        for b, combos in by_bin.items():
+            if int(npix[b]) == 0:
+                continue
+            for n, (a_off, b_off, kp, shift) in enumerate(combos):
+                it = np.zeros(i0.size, dtype=_lib.ITEM_DTYPE)
+                it["i0"], it["j0"] = i0, j0
+                it["a_k0"], it["b_k0"], it["k_len"], it["shift"] = a_off, b_off, kp, shift
+                it["nframes"], it["out_off"], it["s_off"] = T, 0, -1
+                dev_items = torch.from_numpy(it.view(np.uint8).copy()).to(self.dev)
+                _lib.check(self.lib.g2_gram_matrix(jobs, 1, ptr(dev_items), it.size, ptr(mat), T, T, 1 if n else 0,
+                                                   ptr(self.err), self.grid, st), "g2_gram_matrix")
+            S = self.sums[b * T:(b + 1) * T] if self.sums.dim() == 1 else self.sums[b]
+            _lib.check(self.lib.g2_matrix_deviation(ptr(mat), T, T, ptr(S), float(npix[b]), ptr(self.g2_f32[b]),
+                                                    ptr(sd[b]), ptr(sd2[b]), ptr(zeros[b]), st),
+                       "g2_matrix_deviation")
+        _lib.check(self.lib.g2_std_finalize(ptr(sd), ptr(sd2), ptr(zeros), self.n_bins, T, ptr(d32), ptr(d64), st),
+                   "g2_std_finalize")
         self.dev_f64 = d64
         return d32[: self.n_bins]
 

@@ -428,6 +428,23 @@ int g2_gram_std(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_de
 int g2_std_finalize(const double* sum_d_dev, const double* sum_d2_dev, const uint32_t* zeros_dev, int32_t n_rows,
                     int64_t nframes, float* dev_f32, double* dev_f64, void* stream);
 
+/* calc_std for stacks whose counts need byte planes (above 2048), where the
+ * per-pair ratio needs the four plane Grams of a pair together:
+ * g2_gram_matrix runs one bin's items of ONE plane combination (whole K;
+ * item.shift = the combination's weight exponent 0, 8 or 16) and writes
+ * 2^shift * G(t,t') for every pair t' >= t into matrix_dev[t * ld + t']
+ * (float32), or adds it with accumulate != 0 -- one launch per combination,
+ * so no element is written twice in a launch.  g2_matrix_deviation then
+ * reduces the bin's matrix as g2_gram_std does (r = npix * G / (S(t) S(t')),
+ * d = r - centre[tau]; sums of d and d^2 in double, zero denominators counted)
+ * into sum_d / sum_d2 / zeros (caller zeroes them); g2_std_finalize follows. */
+int g2_gram_matrix(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                   float* matrix_dev, int64_t nframes, int64_t ld, int32_t accumulate, int32_t* err_dev,
+                   int32_t grid, void* stream);
+int g2_matrix_deviation(const float* matrix_dev, int64_t nframes, int64_t ld, const int64_t* bin_sums_dev,
+                        double npix, const float* centre_dev, double* sum_d_dev, double* sum_d2_dev,
+                        uint32_t* zeros_dev, void* stream);
+
 /* ---- two-time correlation (the TTCF of event_y.py:141-157) ---------------
  * g2_gram_ttcf runs the Gram tiles of one bin's items (built as for
  * g2_gram_std: whole K, shift = the bin's pixel count P, s_off = the offset of

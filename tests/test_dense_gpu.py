@@ -264,12 +264,39 @@ def test_calc_std(built_lib, cuda_device, name):
     assert np.allclose(d1, got[0], rtol=1e-9, equal_nan=True)
 
 
-def test_calc_std_byte_planes_not_supported(built_lib, cuda_device):
+@pytest.mark.parametrize("case", ["golden_u16_forced_planes", "bright_u16"])
+def test_calc_std_byte_planes(built_lib, cuda_device, case):
+    """calc_std on byte-plane operands (counts above 2048, or the planes
+    forced): each bin's Gram is assembled from its four plane combinations in
+    float32 and the deviation reduced in float64 -- within 1e-4 relative of the
+    float64 oracle, within 1e-3 of the reference's own float32 result where
+    the golden vectors have it, NaN exactly where the reference divides by
+    zero."""
     from dynamix_gb300.correlator import MatMulCorrelator
-    fr = np.full((40, 6, 6), 3000, np.uint16)
-    c = MatMulCorrelator((6, 6), 40)
-    with pytest.raises(NotImplementedError):
-        c.correlate(fr, calc_std=True)
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    if case == "golden_u16_forced_planes":
+        z = golden("dense_u16")
+        fr, qm, rs = z["frames"], z["qmask"], z["g2_ref_std"].astype(np.float64)
+        opts = {"operand": "bytes"}
+    else:
+        fr = speckle_numpy(300, (24, 30), 0.99, 900.0, seed=19, dtype=np.uint16, max_count=4095)
+        assert fr.max() > 2048
+        qm = annular_qmask((24, 30), 3, 0.0, 15.0)
+        rs, opts = None, {}
+        fr[100:110] = 0                                # dark frames: zero denominators (NaN deviations)
+    c = MatMulCorrelator(fr.shape[1:], fr.shape[0], qmask=qm, extra_options=opts)
+    res, dev = c.correlate(fr, calc_std=True)
+    assert c.engine.last["split"] == 1
+    assert np.array_equal(c.numerator, o.g2_exact(fr, qm)["numerator"])
+    want = o.dense_std_exact(fr, qm)
+    got = c.engine.dev_f64[: c.n_bins].cpu().numpy()
+    assert np.array_equal(np.isfinite(got), np.isfinite(want))
+    ok = np.isfinite(want)
+    assert np.all(np.abs(got[ok] - want[ok]) <= 1e-4 * np.abs(want[ok]) + 1e-9)
+    assert np.allclose(dev, got.astype(np.float32), rtol=1e-6, equal_nan=True)
+    if rs is not None:
+        okr = np.isfinite(rs) & (np.abs(rs) > 1e-6)
+        assert np.max(np.abs(got[okr] - rs[okr]) / np.abs(rs[okr])) < 1e-3
 
 
 def test_autotuner_keeps_results_exact(built_lib, cuda_device):
