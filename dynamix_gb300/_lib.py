@@ -57,6 +57,7 @@ SIGNATURES = {
     "g2_pack_e4m3_units": (C.c_int, [_p, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p]),
     "g2_gram_tc": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_gram_tc_pair": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
+    "g2_gram_tc_wide": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _i32, _p]),
     "g2_gram_workers": (C.c_int, [_i32, _p]),
     "g2_plain_direct": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _p]),
     "g2_plain_dp4a": (C.c_int, [_p, _i32, _p, _i64, _p, _i64, _p, _i64, _p, _p]),

@@ -144,8 +144,9 @@ class DenseEngine:
     ``"bytes"``.  The plain comparator always uses fp16.
 
     ``tile`` selects the tensor-core kernel: ``"pair"`` (256 x 256 blocks on
-    CTA pairs, g2_gram_tc_pair) or ``"single"`` (128 x 256 blocks, one CTA
-    each, g2_gram_tc)."""
+    CTA pairs, g2_gram_tc_pair), ``"wide"`` (256 x 512 blocks on CTA pairs,
+    g2_gram_tc_wide: fewer bytes per MMA, epilogue not overlapped) or
+    ``"single"`` (128 x 256 blocks, one CTA each, g2_gram_tc)."""
 
     MODES = {"fp16": MODE_FP16, "bytes": MODE_BYTES, "e4m3": MODE_E4M3}
 
@@ -171,8 +172,8 @@ class DenseEngine:
         self.method = method
         self.operand = operand
         tile = self.TILE if tile is None else tile
-        if tile not in ("pair", "single"):
-            raise ValueError("tile must be 'pair' or 'single'")
+        if tile not in ("pair", "single", "wide"):
+            raise ValueError("tile must be 'pair', 'wide' or 'single'")
         self.tile = tile
         self.exact_limit = int(exact_limit)
         self.grid = int(grid)
@@ -332,19 +333,19 @@ class DenseEngine:
     def item_kind(self):
         """The planner's block kind of this engine's numerator kernel."""
         if self.method == "tc":
-            return "pair" if self.tile == "pair" else "tc"
+            return {"pair": "pair", "wide": "wide"}.get(self.tile, "tc")
         return self.method
 
     def workers(self):
         """Persistent workers of a tensor-core Gram launch (CTAs, or CTA pairs
         for the pair tile), as the kernel will use them."""
-        pair = self.tile == "pair"
+        pair = {"pair": 1, "wide": 2}.get(self.tile, 0)
         if self.grid > 0:
             return (self.grid + 1) // 2 if pair else self.grid
         key = (str(self.dev), pair)
         if key not in _WORKERS:
             n = C.c_int32(0)
-            _lib.check(self.lib.g2_gram_workers(1 if pair else 0, C.byref(n)), "g2_gram_workers")
+            _lib.check(self.lib.g2_gram_workers(pair, C.byref(n)), "g2_gram_workers")
             _WORKERS[key] = int(n.value)
         return _WORKERS[key]
 
@@ -414,8 +415,9 @@ class DenseEngine:
 
     def gram_launch(self, jobs, items_ptr, n_items, stream):
         """One launch of the tensor-core Gram kernel this engine's tile selects."""
-        fn, name = ((self.lib.g2_gram_tc_pair, "g2_gram_tc_pair") if self.tile == "pair"
-                    else (self.lib.g2_gram_tc, "g2_gram_tc"))
+        fn, name = {"pair": (self.lib.g2_gram_tc_pair, "g2_gram_tc_pair"),
+                    "wide": (self.lib.g2_gram_tc_wide, "g2_gram_tc_wide")}.get(
+                        self.tile, (self.lib.g2_gram_tc, "g2_gram_tc"))
         _lib.check(fn(jobs, 1, C.c_void_p(items_ptr), n_items, ptr(self.numer), self.numer.numel(), ptr(self.sums),
                       self.sums.numel(), ptr(self.err), self.grid,
                       stream if isinstance(stream, C.c_void_p) else C.c_void_p(stream)), name)

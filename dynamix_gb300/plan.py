@@ -33,11 +33,11 @@ MODE_FP16, MODE_BYTES, MODE_E4M3 = 0, 1, 2
 UNIT_NONE, UNIT_VEC, UNIT_WORD, UNIT_GATHER, UNIT_BYTE = 0, 1, 2, 3, 4   # classes of the e4m3 pack's units
 
 # (rows, columns) of one Gram item per kernel: the single-CTA tensor-core
-# block (g2_gram_tc), the CTA-pair block (g2_gram_tc_pair: 256 rows over two
-# SMs), and the CUDA-core comparators' blocks
+# block (g2_gram_tc), the CTA-pair blocks (g2_gram_tc_pair: 256 rows over two
+# SMs; g2_gram_tc_wide: 256 x 512), and the CUDA-core comparators' blocks
 PAIR_BM, PAIR_BN = 256, 256
-TILE_SHAPES = {"tc": (TC_BM, TC_BN), "pair": (PAIR_BM, PAIR_BN), "plain": (PLAIN_BM, PLAIN_BN),
-               "dp4a": (PLAIN_BM, PLAIN_BN)}
+TILE_SHAPES = {"tc": (TC_BM, TC_BN), "pair": (PAIR_BM, PAIR_BN), "wide": (PAIR_BM, 2 * PAIR_BN),
+               "plain": (PLAIN_BM, PLAIN_BN), "dp4a": (PLAIN_BM, PLAIN_BN)}
 
 
 def _roundup(x, m):
@@ -354,14 +354,23 @@ def item_costs(items, stage_elems, kind, ones=True):
     """Relative tensor-core time of each item: its K stages times the share
     of a full-width MMA its columns take, plus a fixed per-item cost.  Pair
     items use n = min(256, frames (+ row of ones) left from j0, rounded up to
-    32) columns (g2_gram_tc_pair); single-CTA items always 256."""
+    32) columns (g2_gram_tc_pair), wide items two such halves, the left one
+    skipped below the diagonal, and an epilogue that is not overlapped
+    (g2_gram_tc_wide); single-CTA items always 256."""
     bn = TILE_SHAPES[kind][1]
     stages = items["k_len"].astype(np.float64) / float(stage_elems)
-    if kind == "pair":
+    if kind in ("pair", "wide"):
         live = items["nframes"].astype(np.int64) - items["j0"].astype(np.int64)
         if ones:
             live = live + (items["s_off"] >= 0)
-        n = np.clip((live + 31) // 32 * 32, 32, bn)
+        r = (live + 31) // 32 * 32
+        if kind == "pair":
+            n = np.clip(r, 32, bn)
+        else:
+            n0 = np.where(items["j0"].astype(np.int64) + PAIR_BN <= items["i0"], 0, np.clip(r, 32, PAIR_BN))
+            n1 = np.clip(r - PAIR_BN, 0, PAIR_BN)
+            n = n0 + n1
+            return stages * (n / float(bn)) + ITEM_OVERHEAD_STAGES + n / 64.0
         stages = stages * (n / float(bn))
     return stages + ITEM_OVERHEAD_STAGES
 

@@ -12,7 +12,8 @@ free parameters that change speed but never results:
   slabs keep the rows the concurrent tiles read inside L2 at the price of
   more epilogues;
 * ``tile`` -- the tensor-core block: ``"pair"`` (256 x 256 on CTA pairs,
-  tcgen05 cta_group::2) or ``"single"`` (128 x 256 on one CTA);
+  tcgen05 cta_group::2), ``"wide"`` (256 x 512 on CTA pairs, single-buffered
+  accumulator: long K) or ``"single"`` (128 x 256 on one CTA);
 * ``operand`` -- the packed operand kind tried first: ``"e4m3"`` (kind::f8f6f4,
   counts <= 16), ``"fp16"`` (kind::f16, counts <= 2048) or ``"bytes"``
   (kind::f16 on byte planes); a stack whose counts do not fit falls back to a
@@ -33,7 +34,7 @@ import threading
 
 import numpy as np
 
-DEFAULT_CANDIDATES = [(2048, pc, 0, tile, op) for tile in ("pair", "single") for pc in (6, 8, 12)
+DEFAULT_CANDIDATES = [(2048, pc, 0, tile, op) for tile in ("pair", "wide", "single") for pc in (6, 8, 12)
                       for op in ("e4m3", "fp16")]
 FIELDS = ("super_rows", "pipe_chunks", "kslab", "tile", "operand")
 
@@ -98,7 +99,7 @@ def complete(cand, engine):
 def set_choice(engine, v):
     engine.super_rows, engine.pipe_chunks = int(v[0]), int(v[1])
     engine.kslab = int(v[2]) if len(v) > 2 else 0
-    if len(v) > 3 and v[3] in ("pair", "single"):
+    if len(v) > 3 and v[3] in ("pair", "wide", "single"):
         engine.tile = v[3]
     if len(v) > 4 and hasattr(engine, "set_operand_hint"):
         engine.set_operand_hint(v[4])

@@ -212,9 +212,21 @@ int g2_gram_tc_pair(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* item
                     uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
                     int32_t* err_dev, int32_t grid, void* stream);
 
+/* The same Gram on CTA pairs with wide items: rows [i0, i0+256) against
+ * rows [j0, j0+512) as two pair MMAs (N <= 256 each) that share each stage's
+ * A rows, so each SM streams 48 instead of 64 bytes per MMA cycle.  The left
+ * half is skipped when it lies below the diagonal (j0 + 256 <= i0); each
+ * half's width is the frames (and row of ones) it holds, rounded up to 32.
+ * The accumulator fills the whole TMEM, so an item's epilogue does not
+ * overlap the next item's MMAs: meant for long K.  Same item fields,
+ * exactness contract and outputs as g2_gram_tc. */
+int g2_gram_tc_wide(const g2_job* jobs, int32_t n_jobs, const g2_gram_item* items_dev, int64_t n_items,
+                    uint64_t* numer_dev, int64_t numer_len, uint64_t* sums_dev, int64_t sums_len,
+                    int32_t* err_dev, int32_t grid, void* stream);
+
 /* Number of persistent workers W a Gram launch with grid <= 0 uses on the
  * current device: CTAs for g2_gram_tc (pair = 0), CTA pairs resident at once
- * for g2_gram_tc_pair (pair = 1).  No reference counterpart (the reference's
+ * for g2_gram_tc_pair (pair = 1) or g2_gram_tc_wide (pair = 2).  No reference counterpart (the reference's
  * work-group shapes are fixed, dense.py:184-188). */
 int g2_gram_workers(int32_t pair, int32_t* workers);
 
