@@ -10,10 +10,12 @@ and length) arrive while others run.  The server
 * copies the frames in (when they come from host memory) and packs them on a
   side stream, while the tensor cores work on the jobs admitted earlier;
 * runs the Gram work of all active jobs as a sequence of grouped persistent
-  launches (``g2_gram_tc`` takes up to ``G2_MAX_JOBS`` jobs per launch): each
-  launch takes a slice of every active job's tiles, shortest remaining job
-  first, so a short job that arrives behind a long one finishes in a few
-  launches instead of waiting for it;
+  launches (``g2_gram_tc_pair`` takes up to ``G2_MAX_JOBS`` jobs per launch): each
+  launch takes a slice of the active jobs' tiles -- oldest job first while
+  few jobs are in the server, so that below saturation each finishes about
+  as soon as it would alone; shortest remaining first, with a share for
+  every job, once the backlog grows, so a short job that arrives behind long
+  ones finishes in a few launches instead of waiting for them;
 * finishes a job whose last tiles were launched (denominator and g2 on the
   compute stream, results copied to pinned host memory) and hands the result
   to the caller.
@@ -40,9 +42,8 @@ import numpy as np
 from . import _lib
 from .engine import (DenseEngine, DeviceError, _torch, device_layout, frames_to_device, ptr, require_cuda,
                      stream_handle)
-from .plan import MODE_BYTES, MODE_E4M3, MODE_FP16, gram_items
+from .plan import MODE_BYTES, MODE_E4M3, MODE_FP16, TILE_SHAPES, gram_items
 
-TC_OPS_PER_ITEM_COL = 2 * 128 * 256       # int ops of one 128 x 256 tile per unit of k_len
 
 
 class ArenaFull(Exception):
@@ -83,31 +84,63 @@ class Arena:
         return self.n - sum(ln for _, ln in self.free)
 
 
-def plan_slice(remaining, item_ops, next_items, slice_ops):
+def plan_slice(remaining, item_ops, next_items, slice_ops, policy="srpt", age=None):
     """Items each active job contributes to one grouped launch.
 
     ``remaining[j]``: int ops job j still needs; ``item_ops[j]``: ops of each of
     its items (launch order); ``next_items[j]``: its first item not launched.
-    Jobs are served shortest remaining first; a job gets what is left of
-    ``slice_ops`` but at least ``slice_ops / (2 n)`` and at least one item, so
-    every job advances in every launch.  Returns ``(job, n_items, ops)`` in
-    that order, jobs with nothing left omitted."""
+
+    ``policy="srpt"``: jobs are served shortest remaining first; a job gets
+    what is left of ``slice_ops`` but at least ``slice_ops / (2 n)`` and at
+    least one item, so every job advances in every launch.
+    ``policy="fifo"``: jobs are served oldest first (ascending ``age``, e.g.
+    submission times); the oldest takes up to the whole slice and what it
+    leaves goes to the next, so a launch holds more than one job only where a
+    job ends inside the slice (at least one item of the oldest job), and jobs
+    finish in age order.
+
+    Returns ``(job, n_items, ops)`` in service order, jobs with nothing left
+    omitted."""
     n = len(remaining)
     if n == 0:
         return []
-    floor = float(slice_ops) / (2 * n)
+    if policy == "fifo":
+        key = (lambda j: (age[j], j)) if age is not None else (lambda j: j)
+        floor = 0.0
+    elif policy == "srpt":
+        key = lambda j: (remaining[j], j)   # noqa: E731
+        floor = float(slice_ops) / (2 * n)
+    else:
+        raise ValueError("unknown slice policy %r" % (policy,))
     left = float(slice_ops)
     out = []
-    for j in sorted(range(n), key=lambda j: (remaining[j], j)):
+    for j in sorted(range(n), key=key):
         k0 = int(next_items[j])
         ops = np.asarray(item_ops[j], dtype=np.float64)[k0:]
         if ops.size == 0:
             continue
         cum = np.cumsum(ops)
-        k = min(max(1, int(np.searchsorted(cum, max(left, floor), side="right"))), ops.size)
+        k = int(np.searchsorted(cum, max(left, floor), side="right"))
+        if policy == "fifo" and out:
+            if k == 0:                      # the rest of the slice holds no item of the next job
+                break
+        else:
+            k = min(max(1, k), ops.size)    # the first job (fifo) and every job (srpt) advance
         out.append((j, k, float(cum[k - 1])))
         left -= float(cum[k - 1])
+        if policy == "fifo" and k < ops.size:
+            break                           # the next job waits for this one's remaining items
     return out
+
+
+def slice_policy(n_backlog, fifo_max):
+    """The slice policy for ``n_backlog`` jobs in the server (queued, packing
+    or running): oldest first while the backlog is short -- below saturation
+    every job then finishes about as soon as it would alone, and the longest
+    job is not pushed back again and again by shorter arrivals -- and
+    shortest remaining first once it grows past ``fifo_max``, when short jobs
+    would otherwise wait behind long ones."""
+    return "fifo" if n_backlog <= fifo_max else "srpt"
 
 
 def admit_order(needs, used, budget, free_slots):
@@ -202,10 +235,12 @@ class G2Server:
     server may hold for admitted jobs (frames in flight + packed operands);
     ``arena_elems``: int64 elements of each of the N and S arenas (the sum of
     ``n_bins * T`` over the active jobs must fit); ``slice_ops``: tensor-core
-    int ops per grouped launch."""
+    int ops per grouped launch; ``policy``: ``"auto"`` (oldest first while at
+    most ``fifo_max`` jobs are queued, packing or running, shortest remaining
+    first beyond; :func:`slice_policy`), ``"fifo"`` or ``"srpt"``."""
 
     def __init__(self, hbm_budget=150e9, max_active=_lib.MAX_JOBS, arena_elems=1 << 25, slice_ops=2e13,
-                 device=None, method="tc"):
+                 device=None, method="tc", policy="auto", fifo_max=4):
         torch = _torch()
         self.lib = _lib.load()
         self.dev = require_cuda(device)
@@ -213,6 +248,14 @@ class G2Server:
         self.max_active = min(int(max_active), _lib.MAX_JOBS)
         self.slice_ops = float(slice_ops)
         self.method = method
+        # tensor-core launches run 256 x 256 blocks on CTA pairs (g2_gram_tc_pair)
+        self.kind = "pair" if method == "tc" else method
+        bm, bn = TILE_SHAPES[self.kind]
+        self.ops_per_col = 2.0 * bm * bn           # int ops of one block per unit of k_len
+        if policy not in ("auto", "fifo", "srpt"):
+            raise ValueError("unknown slice policy %r" % (policy,))
+        self.policy = policy
+        self.fifo_max = int(fifo_max)
         self.arena = Arena(arena_elems)
         self.numer_arena = torch.zeros(int(arena_elems), dtype=torch.int64, device=self.dev)
         self.sums_arena = torch.zeros(int(arena_elems), dtype=torch.int64, device=self.dev)
@@ -229,7 +272,7 @@ class G2Server:
         self._digest_cache = {}    # (id(qmask), H, W) -> (qmask, digest)
         self.packing = []          # jobs whose copy-in / packing is in flight
         self.stats = {"launches": 0, "items": 0, "admitted": 0, "finished": 0, "max_active": 0,
-                      "max_used_bytes": 0}
+                      "max_used_bytes": 0, "fifo_launches": 0, "srpt_launches": 0}
         self._thread = None
         self._stop = False
 
@@ -475,7 +518,7 @@ class G2Server:
                     self.packing.append(job)
                     continue
                 off = job.arena_off
-                items = gram_items(job.T, grams, job=0, out_base=off, kind=self.method,
+                items = gram_items(job.T, grams, job=0, out_base=off, kind=self.kind,
                                    s_base=off if (eng.ones(L) and self.method == "tc") else None)
             except Exception as e:
                 self._release(job)
@@ -496,7 +539,7 @@ class G2Server:
         job.reserved = packed_bytes
         self.used += packed_bytes
         job.items = items
-        job.item_ops = items["k_len"].astype(np.float64) * TC_OPS_PER_ITEM_COL
+        job.item_ops = items["k_len"].astype(np.float64) * self.ops_per_col
         job.remaining_ops = float(job.item_ops.sum())
         job.next_item = 0
         job.req.info.update(mode=None if job.layout is None else ["fp16", "bytes", "e4m3"][job.layout.mode],
@@ -517,8 +560,13 @@ class G2Server:
         if not self.active or len(self._inflight) >= 2:
             return False
         act = self.active
+        policy = self.policy
+        if policy == "auto":
+            with self.lock:
+                queued = len(self.queue)
+            policy = slice_policy(queued + len(self.packing) + len(act), self.fifo_max)
         plan = plan_slice([j.remaining_ops for j in act], [j.item_ops for j in act], [j.next_item for j in act],
-                          self.slice_ops)
+                          self.slice_ops, policy=policy, age=[(j.req.t_submit, j.req.id) for j in act])
         parts, jobs, taken = [], [], []
         for idx, k, ops in plan:
             job = act[idx]
@@ -539,9 +587,10 @@ class G2Server:
             jarr = _lib.jobs_array(jobs)
             st = stream_handle(self.dev)
             if self.method == "tc":
-                _lib.check(self.lib.g2_gram_tc(jarr, len(jobs), ptr(dev_items), items.size, ptr(self.numer_arena),
-                                               self.numer_arena.numel(), ptr(self.sums_arena),
-                                               self.sums_arena.numel(), ptr(self.err), 0, st), "g2_gram_tc")
+                _lib.check(self.lib.g2_gram_tc_pair(jarr, len(jobs), ptr(dev_items), items.size,
+                                                    ptr(self.numer_arena), self.numer_arena.numel(),
+                                                    ptr(self.sums_arena), self.sums_arena.numel(), ptr(self.err), 0,
+                                                    st), "g2_gram_tc_pair")
             else:                                   # the CUDA-core comparator, same items and sums
                 _lib.check(self.lib.g2_plain_direct(jarr, len(jobs), ptr(dev_items), items.size,
                                                     ptr(self.numer_arena), self.numer_arena.numel(), ptr(self.err),
@@ -555,6 +604,7 @@ class G2Server:
             members.append(job)
         self._inflight.append((ev, host, dev_items, members))
         self.stats["launches"] += 1
+        self.stats[policy + "_launches"] += 1
         self.stats["items"] += int(items.size)
         for job in [j for j in self.active if j.next_item >= j.items.size]:
             self._finish(job)

@@ -64,6 +64,20 @@ def test_mix_matches_oracle_and_alone(built_lib, cuda_device):
             assert np.array_equal(getattr(q, k), getattr(r, k), equal_nan=True), k
 
 
+@pytest.mark.parametrize("policy", ["fifo", "srpt"])
+def test_mix_each_policy(built_lib, cuda_device, policy):
+    """Oldest-first and shortest-first slices give the same exact results."""
+    from dynamix_gb300.serving import G2Server
+    jobs = _mix()
+    srv = G2Server(hbm_budget=2e9, slice_ops=2e8, policy=policy)
+    reqs = [srv.submit(fr, qm) for fr, qm in jobs]
+    srv.run_until_idle()
+    assert srv.stats[policy + "_launches"] == srv.stats["launches"] >= 3
+    for r, (fr, qm) in zip(reqs, jobs):
+        r.wait()
+        _check(r, fr, qm)
+
+
 def test_background_thread_and_budget(built_lib, cuda_device):
     from dynamix_gb300.serving import G2Server
     jobs = _mix()[:3]
