@@ -436,25 +436,117 @@ __global__ void __launch_bounds__(THREADS, 4)
 // chunk or bin padding) -- and groups them in blocks of 32 units of one
 // class; warp w of a block takes blocks w, w + 8, ... of its chunk and runs
 // each over the step's F frames.  Units are uint4 {destination (in units of
-// the class's size), source(s), source(s), class}, read from L1 each step.
+// the class's size), source(s), source(s), class}; a warp's first UNIT_REGS
+// blocks stay in registers for the whole launch (a 2048-pixel chunk rarely
+// has more than 8 blocks), later ones are read from L1 each step.
+// The frames stream through a ring of UNIT_STAGES steps of staged rows
+// (cp.async), so the next steps' copies are in flight while one is moved; the
+// ring (16.6 KB with two steps) leaves room for a pack CTA beside a Gram
+// CTA on one SM.
 // The range check ORs every moved byte into one word per thread: with counts
 // <= 15 every byte of it stays <= 15, and only a count of 16 or more can make
 // one exceed 16, in which case G2_DEVERR_RANGE_CHECK asks the caller for the
 // exact maximum (g2_binned_max) -- one instruction per word instead of four.
-constexpr uint32_t UNIT_NONE = 0, UNIT_VEC = 1, UNIT_WORD = 2, UNIT_GATHER = 3, UNIT_BYTE = 4;
+constexpr uint32_t UNIT_VEC = 1, UNIT_WORD = 2, UNIT_GATHER = 3, UNIT_BYTE = 4;
+constexpr int UNIT_THREADS = 512;  // 16 warps: a chunk's blocks (9 on average, rarely above 13) in one round
+constexpr int UNIT_STAGES = 2;
+constexpr int UNIT_REGS = 1;
 
-__global__ void __launch_bounds__(THREADS, 4)
+// One unit over the step's nf frames: source rows at base + delta[f], packed
+// rows at row[f].
+template <int F>
+__device__ __forceinline__ void move_unit(const uint4& u, const uint8_t* base, const uint32_t (&delta)[F],
+                                          uint8_t* const (&row)[F], int nf, int64_t n_vec, int64_t n_word,
+                                          int64_t packed_cols, uint32_t& seen, bool& bad) {
+  if (u.w == UNIT_VEC) {
+    if (u.x >= n_vec || u.y > CH - 16) {
+      bad = true;
+      return;
+    }
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      if (f >= nf) break;
+      // the 16 bytes at o from the two aligned 16-byte words around them:
+      // two 16-byte shared loads (a warp's consecutive units read one
+      // contiguous span, 4 wavefronts each) instead of five 4-byte loads
+      // that a 16-byte lane stride puts four lanes on one bank
+      const uint32_t o = delta[f] + u.y;
+      const uint4 q0 = *reinterpret_cast<const uint4*>(base + (o & ~15u));
+      const uint4 q1 = *reinterpret_cast<const uint4*>(base + (o & ~15u) + 16);
+      const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+      const uint32_t k = (o >> 2) & 3u, sh = 8 * (o & 3u);
+      uint32_t x[5];
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        const uint32_t lo = (k & 1u) ? w[i + 1] : w[i];
+        const uint32_t hi = (k & 1u) ? w[i + 3] : w[i + 2];
+        x[i] = (k & 2u) ? hi : lo;
+      }
+      uint4 v;
+      v.x = __funnelshift_r(x[0], x[1], sh);
+      v.y = __funnelshift_r(x[1], x[2], sh);
+      v.z = __funnelshift_r(x[2], x[3], sh);
+      v.w = __funnelshift_r(x[3], x[4], sh);
+      seen |= v.x | v.y | v.z | v.w;
+      *reinterpret_cast<uint4*>(row[f] + 16 * static_cast<int64_t>(u.x)) = v;
+    }
+  } else if (u.w == UNIT_WORD) {
+    if (u.x >= n_word || u.y > CH - 4) {
+      bad = true;
+      return;
+    }
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      if (f >= nf) break;
+      const uint32_t o = delta[f] + u.y;
+      const uint32_t* p = reinterpret_cast<const uint32_t*>(base + (o & ~3u));
+      const uint32_t v = __funnelshift_r(p[0], p[1], 8 * (o & 3u));
+      seen |= v;
+      *reinterpret_cast<uint32_t*>(row[f] + 4 * static_cast<int64_t>(u.x)) = v;
+    }
+  } else if (u.w == UNIT_GATHER) {
+    const uint32_t s0 = u.y & 0xFFFFu, s1 = u.y >> 16, s2 = u.z & 0xFFFFu, s3 = u.z >> 16;
+    if (u.x >= n_word || s0 >= CH || s1 >= CH || s2 >= CH || s3 >= CH) {
+      bad = true;
+      return;
+    }
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      if (f >= nf) break;
+      const uint8_t* q = base + delta[f];
+      const uint32_t v = static_cast<uint32_t>(q[s0]) | (static_cast<uint32_t>(q[s1]) << 8) |
+                         (static_cast<uint32_t>(q[s2]) << 16) | (static_cast<uint32_t>(q[s3]) << 24);
+      seen |= v;
+      *reinterpret_cast<uint32_t*>(row[f] + 4 * static_cast<int64_t>(u.x)) = v;
+    }
+  } else if (u.w == UNIT_BYTE) {
+    if (u.x >= packed_cols || u.y >= CH) {
+      bad = true;
+      return;
+    }
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      if (f >= nf) break;
+      const uint8_t v = base[delta[f] + u.y];
+      seen |= v;
+      row[f][u.x] = v;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(UNIT_THREADS, 2)
     pack_e4m3_units_kernel(const uint8_t* __restrict__ frames, int64_t T, int64_t npix,
                            const int32_t* __restrict__ block_off, const uint4* __restrict__ units,
                            uint8_t* __restrict__ packed, int64_t packed_cols, int32_t* __restrict__ err) {
   using C = Cfg<uint8_t>;
   constexpr int F = C::F;
   constexpr int ROW = C::BUF + 16;  // staging row: the chunk, its unaligned start, spare words
-  __shared__ __align__(16) uint8_t s_buf[2][F][ROW];
+  __shared__ __align__(16) uint8_t s_buf[UNIT_STAGES][F][ROW];
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
+  constexpr int WARPS = UNIT_THREADS / 32;
   const int64_t c = blockIdx.x;
   const int64_t p0 = c * CH;
   const int b0 = block_off[c];
@@ -464,33 +556,42 @@ __global__ void __launch_bounds__(THREADS, 4)
   uint32_t seen = 0;  // OR of every moved byte
   bool bad = false;
 
+  // this warp's first blocks, for the whole launch
+  uint4 ureg[UNIT_REGS];
+#pragma unroll
+  for (int k = 0; k < UNIT_REGS; ++k) {
+    const int blk = warp + k * WARPS;
+    ureg[k] = blk < nb ? units[static_cast<int64_t>(b0 + blk) * 32 + lane] : make_uint4(0, 0, 0, 0);
+  }
+
   auto issue = [&](int64_t t0, int buf) {
-    for (int w = tid; w < F * C::WORDS; w += THREADS) {
-      const int f = w / C::WORDS;
-      const int wi = w - f * C::WORDS;
-      const int64_t t = t0 + f;
-      const int64_t a = ((t * npix + p0) & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
-      const int64_t avail = t < T ? total_bytes - a : 0;
-      const int nbytes = avail <= 0 ? 0 : (avail >= 16 ? 16 : static_cast<int>(avail));
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(&s_buf[buf][f][wi * 16])),
-                   "l"(nbytes ? frames + a : frames), "r"(nbytes)
-                   : "memory");
+    if (t0 < T) {
+      for (int w = tid; w < F * C::WORDS; w += UNIT_THREADS) {
+        const int f = w / C::WORDS;
+        const int wi = w - f * C::WORDS;
+        const int64_t t = t0 + f;
+        const int64_t a = ((t * npix + p0) & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
+        const int64_t avail = t < T ? total_bytes - a : 0;
+        const int nbytes = avail <= 0 ? 0 : (avail >= 16 ? 16 : static_cast<int>(avail));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(&s_buf[buf][f][wi * 16])),
+                     "l"(nbytes ? frames + a : frames), "r"(nbytes)
+                     : "memory");
+      }
     }
-    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");  // an empty group past the end keeps the count
   };
 
   const int64_t stride = static_cast<int64_t>(gridDim.y) * F;
-  int64_t t0 = static_cast<int64_t>(blockIdx.y) * F;
-  if (t0 < T) issue(t0, 0);
-  for (int step = 0; t0 < T; ++step, t0 += stride) {
-    const int buf = step & 1;
-    if (t0 + stride < T) {
-      issue(t0 + stride, buf ^ 1);
-    } else {
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    }
-    asm volatile("cp.async.wait_group 1;" ::: "memory");
+  const int64_t first = static_cast<int64_t>(blockIdx.y) * F;
+#pragma unroll
+  for (int s = 0; s < UNIT_STAGES - 1; ++s) issue(first + s * stride, s);
+  int buf = 0;
+  for (int64_t t0 = first; t0 < T; t0 += stride) {
+    asm volatile("cp.async.wait_group %0;" ::"n"(UNIT_STAGES - 2) : "memory");
+    // this step's rows have landed (every thread's copies), and every thread
+    // is done with the buffer refilled next (moved at the previous step)
     __syncthreads();
+    issue(t0 + (UNIT_STAGES - 1) * stride, buf == 0 ? UNIT_STAGES - 1 : buf - 1);
     const int nf = static_cast<int>(T - t0 < F ? T - t0 : F);
     uint32_t delta[F];
     uint8_t* row[F];
@@ -500,72 +601,14 @@ __global__ void __launch_bounds__(THREADS, 4)
       row[f] = packed + (t0 + f) * packed_cols;
     }
     const uint8_t* base = &s_buf[buf][0][0];
-    for (int blk = warp; blk < nb; blk += THREADS / 32) {
+#pragma unroll
+    for (int k = 0; k < UNIT_REGS; ++k)
+      if (warp + k * WARPS < nb) move_unit<F>(ureg[k], base, delta, row, nf, n_vec, n_word, packed_cols, seen, bad);
+    for (int blk = warp + UNIT_REGS * WARPS; blk < nb; blk += WARPS) {
       const uint4 u = units[static_cast<int64_t>(b0 + blk) * 32 + lane];
-      if (u.w == UNIT_VEC) {
-        if (u.x >= n_vec || u.y > CH - 16) {
-          bad = true;
-          continue;
-        }
-#pragma unroll
-        for (int f = 0; f < F; ++f) {
-          if (f >= nf) break;
-          const uint32_t o = delta[f] + u.y;
-          const uint32_t* p = reinterpret_cast<const uint32_t*>(base + (o & ~3u));
-          const uint32_t sh = 8 * (o & 3u);
-          uint4 v;
-          v.x = __funnelshift_r(p[0], p[1], sh);
-          v.y = __funnelshift_r(p[1], p[2], sh);
-          v.z = __funnelshift_r(p[2], p[3], sh);
-          v.w = __funnelshift_r(p[3], p[4], sh);
-          seen |= v.x | v.y | v.z | v.w;
-          *reinterpret_cast<uint4*>(row[f] + 16 * static_cast<int64_t>(u.x)) = v;
-        }
-      } else if (u.w == UNIT_WORD) {
-        if (u.x >= n_word || u.y > CH - 4) {
-          bad = true;
-          continue;
-        }
-#pragma unroll
-        for (int f = 0; f < F; ++f) {
-          if (f >= nf) break;
-          const uint32_t o = delta[f] + u.y;
-          const uint32_t* p = reinterpret_cast<const uint32_t*>(base + (o & ~3u));
-          const uint32_t v = __funnelshift_r(p[0], p[1], 8 * (o & 3u));
-          seen |= v;
-          *reinterpret_cast<uint32_t*>(row[f] + 4 * static_cast<int64_t>(u.x)) = v;
-        }
-      } else if (u.w == UNIT_GATHER) {
-        const uint32_t s0 = u.y & 0xFFFFu, s1 = u.y >> 16, s2 = u.z & 0xFFFFu, s3 = u.z >> 16;
-        if (u.x >= n_word || s0 >= CH || s1 >= CH || s2 >= CH || s3 >= CH) {
-          bad = true;
-          continue;
-        }
-#pragma unroll
-        for (int f = 0; f < F; ++f) {
-          if (f >= nf) break;
-          const uint8_t* q = base + delta[f];
-          const uint32_t v = static_cast<uint32_t>(q[s0]) | (static_cast<uint32_t>(q[s1]) << 8) |
-                             (static_cast<uint32_t>(q[s2]) << 16) | (static_cast<uint32_t>(q[s3]) << 24);
-          seen |= v;
-          *reinterpret_cast<uint32_t*>(row[f] + 4 * static_cast<int64_t>(u.x)) = v;
-        }
-      } else if (u.w == UNIT_BYTE) {
-        if (u.x >= packed_cols || u.y >= CH) {
-          bad = true;
-          continue;
-        }
-#pragma unroll
-        for (int f = 0; f < F; ++f) {
-          if (f >= nf) break;
-          const uint8_t v = base[delta[f] + u.y];
-          seen |= v;
-          row[f][u.x] = v;
-        }
-      }
+      move_unit<F>(u, base, delta, row, nf, n_vec, n_word, packed_cols, seen, bad);
     }
-    // the buffer just read is refilled by the copies issued at the next step
-    __syncthreads();
+    buf = buf == UNIT_STAGES - 1 ? 0 : buf + 1;
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
@@ -705,7 +748,7 @@ extern "C" int g2_pack_e4m3_units(const void* frames_dev, int64_t nframes, int64
   if (gy > 65535) gy = 65535;
   if (gy < 1) gy = 1;
   dim3 grid(static_cast<unsigned>(n_chunks), static_cast<unsigned>(gy));
-  pack::pack_e4m3_units_kernel<<<grid, pack::THREADS, 0, as_stream(stream)>>>(
+  pack::pack_e4m3_units_kernel<<<grid, pack::UNIT_THREADS, 0, as_stream(stream)>>>(
       reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, unit_block_off_dev,
       reinterpret_cast<const uint4*>(units_dev), reinterpret_cast<uint8_t*>(packed_dev), packed_cols, err_dev);
   return launch_status();
