@@ -62,7 +62,7 @@ def parse():
                    help="dense line only: skip the u16 / sparse / event sub-lines (configurations 3 and 4)")
     p.add_argument("--frames", type=int, default=None, help="override T (testing only)")
     p.add_argument("--shape", default=None, help="H,W of the sparse/event frames (profiling only)")
-    p.add_argument("--tile", default=None, choices=["pair", "single"],
+    p.add_argument("--tile", default=None, choices=["pair", "wide", "single"],
                    help="tensor-core block of the dense Gram (default: the engine's)")
     p.add_argument("--workload", default="dense", choices=["dense", "u16", "sparse", "event", "serving", "compress"],
                    help="dense: 514x1030x10k u8 Gram path (default); sparse / event: 2162x2068x20k CSR or "
@@ -348,7 +348,7 @@ def run_ours(args):
     n_attr = max(3, min(args.steps, 10))
     tile0 = eng.tile
     by_tile = {}
-    for tile in (tile0, "single" if tile0 == "pair" else "pair"):
+    for tile in [tile0] + [t for t in ("pair", "wide", "single") if t != tile0]:
         eng.tile = tile
         g_ms, p_ms = [], []
         corr.correlate_device(frames)
@@ -382,7 +382,8 @@ def run_ours(args):
                    probe["launch_ms"]))
     pack_bytes = T * H * W + T * info["packed_cols"] * (1 if info.get("mode") == "e4m3" else 2)
     pack_avg = sum(pack_ms) / len(pack_ms)
-    traffic = profile_traffic("gram_tc_dense_514x1030_%s.md" % info.get("mode"))
+    # DRAM bytes of one Gram launch from the committed ncu summary of the tile measured there
+    traffic = profile_traffic("gram_pair_dense_514x1030_%s.md" % info.get("mode")) if tile0 == "pair" else None
 
     line = {
         "metric": "g2_frames_per_s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
@@ -395,7 +396,8 @@ def run_ours(args):
                                          "2^24)",
                                  "bytes": "tcgen05 kind::f16 on hi/lo byte planes (4 Grams)"}[info["mode"]]),
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": "g2_gram_tc",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": {"pair": "g2_gram_tc_pair", "wide": "g2_gram_tc_wide"}.get(tile0, "g2_gram_tc"),
                      "peak_source": peak_src,
                      "algorithmic_ops_per_launch": 2 * macs, "launch_ms": gram_avg,
                      "other_peaks": {"tcgen05_f16_probe": peak_f16, "bf16_cublas_" + peak_kind: peaks.get(
@@ -789,7 +791,11 @@ SERVING_WORKLOAD = {
     "qmask": "n_bins equal annuli r 0 to 0.4 min(H, W) around the frame centre", "seed": 5, "jobs": 24,
     "hbm_budget_gb": 150,
     "inputs": "device-resident frame pools (one per shape and dtype, 20,000 frames); a job's frames are the "
-              "first T frames of its pool, used in place (the server copies nothing in)",
+              "first T frames of its pool, used in place (the server copies nothing in); the host_submission "
+              "point submits the same frames from page-locked host pools, so each job's copy to the device is "
+              "inside its latency, at 0.8 x the one-at-a-time capacity of host submission",
+    "policies": "batched = oldest job first while at most 4 jobs are queued, packing or running, shortest "
+                "remaining first beyond (G2Server policy 'auto'); batched_srpt = shortest remaining first always",
 }
 
 
@@ -863,6 +869,81 @@ def latency_summary(reqs, wall, jobs):
             "jobs_per_s": len(reqs) / wall, "frames_per_s": frames / wall, "gram_tops": ops / wall / 1e12}
 
 
+def host_pools(pools, jobs):
+    """Page-locked host copies of the frame pools, each as long as its longest
+    job: numpy arrays registered with the CUDA runtime (torch's pinned
+    allocator would round every pool up to a power of two).  None when they
+    would take more than half of the host's available memory."""
+    import numpy as np
+    import torch
+    need = {}
+    for j in jobs:
+        key = (tuple(j["shape"]), j["dtype"] == "uint16")
+        need[key] = max(need.get(key, 0), j["T"])
+    total = sum(pools[k][:T].numel() * pools[k].element_size() for k, T in need.items())
+    avail = None
+    try:
+        with open("/proc/meminfo") as f:
+            for ln in f:
+                if ln.startswith("MemAvailable:"):
+                    avail = int(ln.split()[1]) * 1024
+    except OSError:
+        pass
+    if avail is None or total > avail // 2:
+        return None, total, avail
+    cudart = torch.cuda.cudart()
+    out = {}
+    for k, T in need.items():
+        src = pools[k][:T]
+        host = np.empty(tuple(src.shape), dtype=np.uint16 if k[1] else np.uint8)
+        t = torch.from_numpy(host.view(np.int16) if k[1] else host)
+        rc = cudart.cudaHostRegister(t.data_ptr(), host.nbytes, 0)
+        if int(rc) != 0:
+            for h, _ in out.values():
+                cudart.cudaHostUnregister(h.ctypes.data)
+            return None, total, avail
+        t.copy_(src.view(torch.int16) if k[1] else src)
+        out[k] = (host, t.view(torch.uint16) if k[1] else t)
+    return out, total, avail
+
+
+def serving_host_point(jobs, pools, gaps, server, ref, load=0.8):
+    """One sweep point with every job submitted from page-locked host memory
+    (its copy to the device inside its latency): the one-at-a-time capacity
+    of host submission first (all jobs queued at once), then Poisson
+    arrivals at ``load`` x that capacity for both servers."""
+    import numpy as np
+    import torch
+    hp, total, avail = host_pools(pools, jobs)
+    if hp is None:
+        return {"skipped": "host pools of %.1f GB do not fit half of the %s available" % (
+            total / 1e9, "unknown" if avail is None else "%.1f GB" % (avail / 1e9))}
+    try:
+        torch.cuda.synchronize()
+        hjobs = [dict(j, frames=hp[(tuple(j["shape"]), j["dtype"] == "uint16")][1][:j["T"]]) for j in jobs]
+        q_reqs, q_wall = drive(server("one_at_a_time"), hjobs, [0.0] * len(hjobs))
+        capacity = len(hjobs) / q_wall
+        rate = load * capacity
+        arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
+        row = {"one_at_a_time_capacity_jobs_per_s": capacity, "load_vs_one_at_a_time_capacity": load,
+               "rate_jobs_per_s": rate,
+               "h2d_bytes": int(sum(j["frames"].numel() * j["frames"].element_size() for j in hjobs))}
+        identical = all(np.array_equal(r.numerator, q.numerator) for r, q in zip(q_reqs, ref))
+        for kind in ("batched", "one_at_a_time"):
+            reqs, wall = drive(server(kind), hjobs, arrivals)
+            row[kind] = latency_summary(reqs, wall, hjobs)
+            identical &= all(np.array_equal(r.numerator, q.numerator) and np.array_equal(r.denominator, q.denominator)
+                             for r, q in zip(reqs, ref))
+        row["p99_speedup"] = row["one_at_a_time"]["p99_ms"] / row["batched"]["p99_ms"]
+        row["identical"] = identical
+        return row
+    finally:
+        torch.cuda.synchronize()
+        cudart = torch.cuda.cudart()
+        for host, _ in hp.values():
+            cudart.cudaHostUnregister(host.ctypes.data)
+
+
 def run_serving(args):
     import numpy as np
     import torch
@@ -889,6 +970,8 @@ def run_serving(args):
     def server(kind):
         if kind == "batched":
             return G2Server(hbm_budget=budget)
+        if kind == "batched_srpt":
+            return G2Server(hbm_budget=budget, policy="srpt")
         if kind == "one_at_a_time":
             return G2Server(hbm_budget=budget, max_active=1, slice_ops=1e30)
         return G2Server(hbm_budget=budget, max_active=1, slice_ops=1e30, method="plain")
@@ -908,13 +991,16 @@ def run_serving(args):
         rate = load * capacity
         arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
         row = {"load_vs_one_at_a_time_capacity": load, "rate_jobs_per_s": rate}
-        for kind in ("batched", "one_at_a_time"):
+        for kind in ("batched", "batched_srpt", "one_at_a_time"):
             reqs, wall = drive(server(kind), jobs, arrivals)
             row[kind] = latency_summary(reqs, wall, jobs)
             identical &= all(np.array_equal(r.numerator, q.numerator) and np.array_equal(r.denominator, q.denominator)
                              for r, q in zip(reqs, ref))
         row["p99_speedup"] = row["one_at_a_time"]["p99_ms"] / row["batched"]["p99_ms"]
         sweep.append(row)
+    host_point = serving_host_point(jobs, pools, gaps, server, ref)
+    if host_point is not None:
+        identical &= host_point.pop("identical")
     clocks = sampler.stop()
     plain = None
     if not args.no_plain:
@@ -929,7 +1015,7 @@ def run_serving(args):
         "config": dict(SERVING_WORKLOAD, pool_generation_s=t_gen),
         "jobs": [{k: (list(v) if k == "shape" else v) for k, v in j.items() if k not in ("frames", "qmask")}
                  for j in jobs],
-        "one_at_a_time_capacity_jobs_per_s": capacity, "sweep": sweep,
+        "one_at_a_time_capacity_jobs_per_s": capacity, "sweep": sweep, "host_submission": host_point,
         "plain_one_at_a_time_all_queued": plain, "results_identical_across_runs": bool(identical),
         "clocks": clocks,
     }
@@ -1012,13 +1098,16 @@ def measure_u16(args, dev, T, steps, warmup, cpu=True, e2e=True):
             "vs_baseline": None, "dtype": "u16", "data": "synthetic", "config": dict(U16_WORKLOAD, nframes=T),
             "plan": info, "stages_ms": st,
             "tiles": {"block": {"pair": "256 x n (tcgen05 cta_group::2 M256)",
+                                "wide": "256 x 512 (two tcgen05 cta_group::2 M256 N256)",
                                 "single": "128 x 256 (tcgen05 M128 N256)"}[info.get("tile", "single")],
                       "k_stage": "64 fp16 columns per TMA stage",
                       "operand": info["mode"], "grams_per_bin": planes, "k_split_chunks": info.get("n_grams"),
                       "autotuner_candidates": "tile, pipeline chunks, operand (dynamix_gb300.tune)"},
             "roofline": {"bound": "tensor", "achieved": executed, "peak": peak_f16, "unit": "TFLOP/s",
-                         "frac": executed / peak_f16, "kernel": "g2_gram_tc_pair" if info.get("tile") == "pair"
-                         else "g2_gram_tc", "launch_ms": gram,
+                         "frac": executed / peak_f16,
+                         "kernel": {"pair": "g2_gram_tc_pair", "wide": "g2_gram_tc_wide"}.get(info.get("tile"),
+                                                                                             "g2_gram_tc"),
+                         "launch_ms": gram,
                          "peak_source": "tcgen05 kind::f16 rate measured in this run (g2_tc_rate_probe); executed "
                                         "ops = %d x the algorithmic %.3e" % (planes, 2.0 * macs)},
             "fp64_check": {"frames": Ts, "numerator_denominator_bit_exact": exact,
