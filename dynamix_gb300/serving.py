@@ -216,6 +216,7 @@ class _Job:
         self.next_item = 0
         self.remaining_ops = 0
         self.arena_off = None
+        self.staging_off = None    # 256-byte units into the staging arena (pinned host frames)
         self.reserved = 0          # bytes of the HBM budget held
         self.frames_dev = None
         self.mode = None
@@ -237,10 +238,13 @@ class G2Server:
     ``n_bins * T`` over the active jobs must fit); ``slice_ops``: tensor-core
     int ops per grouped launch; ``policy``: ``"auto"`` (oldest first while at
     most ``fifo_max`` jobs are queued, packing or running, shortest remaining
-    first beyond; :func:`slice_policy`), ``"fifo"`` or ``"srpt"``."""
+    first beyond; :func:`slice_policy`), ``"fifo"`` or ``"srpt"``;
+    ``staging_bytes``: device bytes of the staging arena that frames copied
+    from page-locked host memory land in until they are packed (allocated at
+    the first such job; a job larger than it gets its own buffer)."""
 
     def __init__(self, hbm_budget=150e9, max_active=_lib.MAX_JOBS, arena_elems=1 << 25, slice_ops=2e13,
-                 device=None, method="tc", policy="auto", fifo_max=4):
+                 device=None, method="tc", policy="auto", fifo_max=4, staging_bytes=48e9):
         torch = _torch()
         self.lib = _lib.load()
         self.dev = require_cuda(device)
@@ -257,6 +261,13 @@ class G2Server:
         self.policy = policy
         self.fifo_max = int(fifo_max)
         self.arena = Arena(arena_elems)
+        # frames copied in from page-locked host memory live in one staging
+        # arena (first-fit ranges, 256-byte aligned) until packed, so that jobs
+        # of every size reuse the same device memory instead of allocating and
+        # freeing tens of GB each
+        self.staging_bytes = int(staging_bytes) // 256 * 256
+        self.staging = None
+        self.staging_arena = Arena(self.staging_bytes // 256)
         self.numer_arena = torch.zeros(int(arena_elems), dtype=torch.int64, device=self.dev)
         self.sums_arena = torch.zeros(int(arena_elems), dtype=torch.int64, device=self.dev)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
@@ -419,6 +430,15 @@ class G2Server:
                 job.arena_off = self.arena.alloc(job.rows * job.T)
             except ArenaFull:
                 continue                           # stays queued until sums space frees up
+            if self._stageable(req):
+                units = -(-self._frame_bytes(job) // 256)
+                if units <= self.staging_arena.n:
+                    try:
+                        job.staging_off = self.staging_arena.alloc(units)
+                    except ArenaFull:              # stays queued until staging space frees up
+                        self.arena.release(job.arena_off, job.rows * job.T)
+                        job.arena_off = None
+                        continue
             self._dequeue(req)
             job.reserved = need
             self.used += need
@@ -430,6 +450,35 @@ class G2Server:
                 continue
             admitted = True
         return admitted
+
+    @staticmethod
+    def _stageable(req):
+        """Frames in page-locked host memory, copied asynchronously."""
+        torch = _torch()
+        fr = req.frames
+        return (isinstance(fr, torch.Tensor) and not fr.is_cuda and fr.dtype in (torch.uint8, torch.uint16)
+                and fr.is_pinned() and fr.is_contiguous())
+
+    @staticmethod
+    def _frame_bytes(job):
+        return job.T * job.shape[0] * job.shape[1] * job.elem_bytes
+
+    def _staged_frames(self, job, fr):
+        """The device tensor a pinned host stack is copied into: its range of
+        the staging arena, or a buffer of its own."""
+        torch = _torch()
+        if job.staging_off is None:
+            return torch.empty(fr.shape, dtype=fr.dtype, device=self.dev)
+        if self.staging is None:
+            self.staging = torch.empty(self.staging_bytes, dtype=torch.uint8, device=self.dev)
+        off = job.staging_off * 256
+        raw = self.staging[off:off + self._frame_bytes(job)]
+        return raw.view(fr.dtype).view(fr.shape)
+
+    def _release_staging(self, job):
+        if job.staging_off is not None:
+            self.staging_arena.release(job.staging_off, -(-self._frame_bytes(job) // 256))
+            job.staging_off = None
 
     def _dequeue(self, req):
         with self.lock:
@@ -450,9 +499,8 @@ class G2Server:
         with torch.cuda.stream(self.side):
             numer.zero_()                           # the pack zeroes the sums
             fr = req.frames
-            if (isinstance(fr, torch.Tensor) and not fr.is_cuda and fr.dtype in (torch.uint8, torch.uint16)
-                    and fr.is_pinned() and fr.is_contiguous()):
-                frames_dev = torch.empty(fr.shape, dtype=fr.dtype, device=self.dev)
+            if self._stageable(req):
+                frames_dev = self._staged_frames(job, fr)
                 frames_dev.copy_(fr, non_blocking=True)         # asynchronous on the side stream
             else:
                 frames_dev = frames_to_device(fr, self.dev)      # validates, converts, or uses in place
@@ -532,6 +580,7 @@ class G2Server:
         """A packed job joins the grouped launches."""
         eng = job.engine
         job.frames_dev = None                      # packed: the frames are no longer needed
+        self._release_staging(job)                 # the pack that read them has completed
         if eng.packed is not None:
             eng.packed.record_stream(self.compute)
         packed_bytes = 0 if eng.packed is None else eng.packed.numel()
@@ -673,6 +722,8 @@ class G2Server:
         return bool(done)
 
     def _release(self, job):
+        job.frames_dev = None
+        self._release_staging(job)
         if job.arena_off is not None:
             self.arena.release(job.arena_off, job.rows * job.T)
             job.arena_off = None

@@ -236,3 +236,18 @@ def test_kslab_caps_item_k_and_keeps_the_sums():
     items = plan.gram_items(T, grams, kind="tc")
     N = run_items(packed, items, nb, T, TC_BM, TC_BN)
     assert np.array_equal(N, o.g2_exact(fr, qm)["numerator"])
+
+
+@pytest.mark.parametrize("T,n,growth", [(10000, 8, 1.5), (10000, 8, 0.0), (1000, 3, 1.5), (300, 1, 1.5),
+                                        (2100, 8, 2.0), (257, 2, 1.5)])
+def test_pipeline_chunk_bounds(T, n, growth):
+    """Frame chunks of the e4m3 pipeline: cut at multiples of 128 frames,
+    strictly increasing, covering [0, T); with growth > 0 they do not shrink
+    (apart from rounding and the last one)."""
+    from dynamix_gb300.engine import DenseEngine
+    b = DenseEngine.pipe_bounds(T, n, growth)
+    assert b[0] == 0 and b[-1] == T and np.all(np.diff(b) > 0)
+    assert np.all(b[1:-1] % 128 == 0) and b.size - 1 <= n
+    if growth > 0 and b.size > 3:
+        d = np.diff(b)[:-1]
+        assert np.all(d[1:] >= d[:-1] - 128)
