@@ -265,7 +265,7 @@ def run_reference(args):
         "steps": 1, "warmup": 1, "steps_requested": args.steps, "warmup_requested": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(WORKLOAD, nframes=T_full, parallelism="single"),
+        "config": dict(WORKLOAD, nframes=T_full, parallelism="replicas" if world > 1 else "single"),
         "note": "one full-size call (all %d frames, all 16 bins) timed; a warm-up call on the first %d frames "
                 "before it; more steps would take minutes each" % (T_full, Tw),
         "cpu_baseline": {"value": v, "unit": "frames/s", "cores": ncores, "kind": kind,
@@ -389,12 +389,10 @@ def run_ours(args):
         "metric": "g2_frames_per_s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": dict(WORKLOAD, nframes=T, parallelism="replicas" if world > 1 else "single",
-                       mma_kind={"e4m3": "tcgen05 kind::f8f6f4 (e4m3 counts <= 16, fp32 accumulate, exact "
-                                         "below 2^24)",
-                                 "fp16": "tcgen05 kind::f16 (fp16 counts <= 2048, fp32 accumulate, exact below "
-                                         "2^24)",
-                                 "bytes": "tcgen05 kind::f16 on hi/lo byte planes (4 Grams)"}[info["mode"]]),
+        "config": dict(WORKLOAD, nframes=T, parallelism="replicas" if world > 1 else "single"),
+        "mma_kind": {"e4m3": "tcgen05 kind::f8f6f4 (e4m3 counts <= 16, fp32 accumulate, exact below 2^24)",
+                     "fp16": "tcgen05 kind::f16 (fp16 counts <= 2048, fp32 accumulate, exact below 2^24)",
+                     "bytes": "tcgen05 kind::f16 on hi/lo byte planes (4 Grams)"}[info["mode"]],
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": {"pair": "g2_gram_tc_pair", "wide": "g2_gram_tc_wide"}.get(tile0, "g2_gram_tc"),
@@ -912,6 +910,8 @@ def serving_host_point(jobs, pools, gaps, server, ref, load=0.8):
     (its copy to the device inside its latency): the one-at-a-time capacity
     of host submission first (all jobs queued at once), then Poisson
     arrivals at ``load`` x that capacity for both servers."""
+    import gc
+
     import numpy as np
     import torch
     hp, total, avail = host_pools(pools, jobs)
@@ -921,7 +921,18 @@ def serving_host_point(jobs, pools, gaps, server, ref, load=0.8):
     try:
         torch.cuda.synchronize()
         hjobs = [dict(j, frames=hp[(tuple(j["shape"]), j["dtype"] == "uint16")][1][:j["T"]]) for j in jobs]
-        q_reqs, q_wall = drive(server("one_at_a_time"), hjobs, [0.0] * len(hjobs))
+
+        def fresh(kind):
+            # each run's server starts from a released allocator cache: the
+            # servers of the device sweep and earlier runs (staging arenas,
+            # packed operands) leave it close to the whole device
+            gc.collect()
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            return server(kind)
+
+        drive(fresh("batched"), hjobs, [0.0] * len(hjobs))      # warm-up
+        q_reqs, q_wall = drive(fresh("one_at_a_time"), hjobs, [0.0] * len(hjobs))
         capacity = len(hjobs) / q_wall
         rate = load * capacity
         arrivals = np.cumsum(gaps / rate) - gaps[0] / rate
@@ -930,7 +941,7 @@ def serving_host_point(jobs, pools, gaps, server, ref, load=0.8):
                "h2d_bytes": int(sum(j["frames"].numel() * j["frames"].element_size() for j in hjobs))}
         identical = all(np.array_equal(r.numerator, q.numerator) for r, q in zip(q_reqs, ref))
         for kind in ("batched", "one_at_a_time"):
-            reqs, wall = drive(server(kind), hjobs, arrivals)
+            reqs, wall = drive(fresh(kind), hjobs, arrivals)
             row[kind] = latency_summary(reqs, wall, hjobs)
             identical &= all(np.array_equal(r.numerator, q.numerator) and np.array_equal(r.denominator, q.denominator)
                              for r, q in zip(reqs, ref))
