@@ -1,6 +1,12 @@
 // Host utilities of the C ABI: status strings, device queries, tensor maps.
+#include <algorithm>
 #include <cstring>
+#include <functional>
 #include <mutex>
+#include <numeric>
+#include <queue>
+#include <utility>
+#include <vector>
 #include <cudaTypedefs.h>
 #include "g2_host.h"
 
@@ -71,5 +77,41 @@ extern "C" int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, 
   *sm_count = n;
   *cc_major = ma;
   *cc_minor = mi;
+  return G2_OK;
+}
+
+// Longest-processing-time list schedule of a launch's items over the
+// persistent workers (host code: no device is touched).  Items in descending
+// cost (ties in index order) go one by one to the least-loaded worker (ties
+// to the lower worker index); each worker then keeps its items in index
+// order, and worker w's k-th item lands in slot w + k * workers -- the slots
+// the kernels read.  slot_out[i] is item i's slot; *n_slots the length of the
+// slot list (workers times the longest worker list).
+extern "C" int g2_balance_lpt(const double* cost, int64_t n, int32_t workers, int64_t* slot_out,
+                              int64_t* n_slots) {
+  if (!cost || !slot_out || !n_slots || n < 0 || workers <= 0) return G2_ERR_ARG;
+  for (int64_t i = 0; i < n; ++i)
+    if (!(cost[i] >= 0.0)) return G2_ERR_ARG;  // also rejects NaN
+  std::vector<int64_t> order(static_cast<size_t>(n));
+  std::iota(order.begin(), order.end(), int64_t(0));
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cost[a] > cost[b]; });
+  using Slot = std::pair<double, int32_t>;
+  std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> heap;
+  for (int32_t w = 0; w < workers; ++w) heap.push(Slot(0.0, w));
+  std::vector<int32_t> owner(static_cast<size_t>(n));
+  for (int64_t i : order) {
+    Slot s = heap.top();
+    heap.pop();
+    owner[static_cast<size_t>(i)] = s.second;
+    heap.push(Slot(s.first + cost[i], s.second));
+  }
+  std::vector<int64_t> next(static_cast<size_t>(workers), 0);
+  int64_t longest = 0;
+  for (int64_t i = 0; i < n; ++i) {  // index order within each worker
+    const int32_t w = owner[static_cast<size_t>(i)];
+    slot_out[i] = w + next[static_cast<size_t>(w)] * workers;
+    longest = std::max(longest, ++next[static_cast<size_t>(w)]);
+  }
+  *n_slots = longest * workers;
   return G2_OK;
 }

@@ -383,25 +383,56 @@ def balance_items(items, workers, stage_elems, kind, ones=True):
     kernels' pattern), unused slots holding ``job = G2_ITEM_EMPTY``.  Items
     keep their relative order within a worker (bins and super-tiles stay
     together in time)."""
-    import heapq
     n = items.size
     if workers <= 1 or n <= workers:
         return items
-    cost = item_costs(items, stage_elems, kind, ones)
+    cost = np.ascontiguousarray(item_costs(items, stage_elems, kind, ones), dtype=np.float64)
+    slots, n_slots = lpt_slots(cost, workers)
+    out = np.zeros(n_slots, dtype=ITEM_DTYPE)
+    out["job"] = ITEM_EMPTY
+    out[slots] = items
+    return out
+
+
+def lpt_slots(cost, workers):
+    """Slot of every item in the longest-first schedule of
+    :func:`balance_items`, and the slot count: the library's
+    ``g2_balance_lpt`` (microseconds for ten thousand items), or the same
+    schedule in Python where the library is not built (planning on a host
+    without the toolkit)."""
+    import ctypes as C
+    n = int(cost.size)
+    try:
+        from . import _lib
+        lib = _lib.load()
+    except ImportError:
+        lib = None
+    if lib is not None:
+        slots = np.empty(n, dtype=np.int64)
+        n_slots = C.c_int64(0)
+        _lib.check(lib.g2_balance_lpt(cost.ctypes.data_as(C.c_void_p), n, int(workers),
+                                      slots.ctypes.data_as(C.c_void_p), C.byref(n_slots)), "g2_balance_lpt")
+        return slots, int(n_slots.value)
+    return lpt_slots_py(cost, workers)
+
+
+def lpt_slots_py(cost, workers):
+    """:func:`lpt_slots` in Python (a heap of worker loads)."""
+    import heapq
     order = np.argsort(-cost, kind="stable")
     heap = [(0.0, w) for w in range(workers)]
-    lists = [[] for _ in range(workers)]
+    owner = np.empty(cost.size, dtype=np.int64)
     for i in order:
         load, w = heapq.heappop(heap)
-        lists[w].append(i)
-        heapq.heappush(heap, (load + cost[i], w))
-    m = max(len(lst) for lst in lists)
-    out = np.zeros(m * workers, dtype=ITEM_DTYPE)
-    out["job"] = ITEM_EMPTY
-    for w, lst in enumerate(lists):
-        if lst:
-            out[w + workers * np.arange(len(lst))] = items[np.sort(np.asarray(lst))]
-    return out
+        owner[i] = w
+        heapq.heappush(heap, (load + float(cost[i]), w))
+    slots = np.empty(cost.size, dtype=np.int64)
+    nxt = np.zeros(workers, dtype=np.int64)
+    for i in range(cost.size):
+        w = owner[i]
+        slots[i] = w + nxt[w] * workers
+        nxt[w] += 1
+    return slots, int(nxt.max()) * workers
 
 
 def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT, kslab=0):

@@ -106,6 +106,12 @@ int         g2_abi_version(void);
 const char* g2_status_string(int status);
 /* SM count and compute capability of a device. */
 int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+/* Host-only: longest-processing-time schedule of n items (cost[i] >= 0) over
+ * `workers` persistent workers of a Gram launch.  Item i goes to slot
+ * slot_out[i] of a list of *n_slots slots read by worker w at w, w + workers,
+ * ...; slots left over hold G2_ITEM_EMPTY items (the caller fills them).  No
+ * reference counterpart (the reference launches one thread per output). */
+int g2_balance_lpt(const double* cost, int64_t n, int32_t workers, int64_t* slot_out, int64_t* n_slots);
 
 /* ---- G1: pack + bin sums ------------------------------------------------
  * Replaces compute_sums_dense (dynamix/resources/opencl/densecorrelator.cl:65-150)

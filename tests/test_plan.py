@@ -251,3 +251,30 @@ def test_pipeline_chunk_bounds(T, n, growth):
     if growth > 0 and b.size > 3:
         d = np.diff(b)[:-1]
         assert np.all(d[1:] >= d[:-1] - 128)
+
+
+@pytest.mark.parametrize("n,workers", [(2520, 76), (301, 76), (77, 76), (1000, 1), (5, 8), (0, 4)])
+def test_native_lpt_schedule_matches_python(built_lib, n, workers):
+    """g2_balance_lpt (the library's host scheduler) places every item in the
+    same slot as the Python schedule, each worker's items in index order."""
+    rng = np.random.default_rng(n)
+    cost = np.round(rng.random(n) * 8, 1) + 0.5      # many equal costs: ties must break alike
+    a, na = plan.lpt_slots(cost, workers)
+    b, nb = plan.lpt_slots_py(cost, workers)
+    assert na == nb and np.array_equal(a, b)
+    assert np.unique(a).size == n and (n == 0 or a.max() < na)
+    w = a % workers
+    for k in range(workers):
+        assert np.all(np.diff(a[w == k]) > 0)          # index order within a worker
+
+
+def test_native_lpt_rejects_bad_arguments(built_lib):
+    import ctypes as C
+    slots = np.empty(3, dtype=np.int64)
+    n_slots = C.c_int64(0)
+    bad = np.array([1.0, np.nan, 2.0])
+    assert built_lib.g2_balance_lpt(bad.ctypes.data_as(C.c_void_p), 3, 2, slots.ctypes.data_as(C.c_void_p),
+                                    C.byref(n_slots)) != 0
+    ok = np.array([1.0, 2.0, 3.0])
+    assert built_lib.g2_balance_lpt(ok.ctypes.data_as(C.c_void_p), 3, 0, slots.ctypes.data_as(C.c_void_p),
+                                    C.byref(n_slots)) != 0
