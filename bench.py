@@ -362,9 +362,12 @@ def run_ours(args):
         by_tile[tile] = (g_ms, p_ms)
     eng.tile = tile0
     gram_ms, pack_ms = by_tile[tile0]
-    eng.profile = False
+    # one pipelined step with events at every pack and Gram launch of it
     eng.pipeline = True
-    serial_info = dict(eng.last)
+    corr.correlate_device(frames)
+    eng.take_events()
+    timeline = eng.take_timeline()
+    eng.profile = False
 
     peaks, peak_kind = measured_peaks()
     gram_avg = sum(gram_ms) / len(gram_ms)
@@ -401,6 +404,7 @@ def run_ours(args):
                      "other_peaks": {"tcgen05_f16_probe": peak_f16, "bf16_cublas_" + peak_kind: peaks.get(
                          "bf16_tflops")}},
         "gram_ms_by_tile": {t: sum(v[0]) / len(v[0]) for t, v in by_tile.items()},
+        "pipeline_timeline_ms": {k: round(v, 4) for k, v in timeline.items()},
         "stages_ms": {"pack": pack_avg, "gram_tc": gram_avg, "tile": tile0,
                       "note": "stage times from %d steps run unpipelined (one pack, one Gram launch); the timed "
                               "steps overlap the pack of frame chunk c+1 with the Gram tiles chunk c completes "

@@ -235,6 +235,26 @@ class DenseEngine:
         ev, self._events = self._events, []
         return ev
 
+    def _tmark(self, name, stream):
+        """A CUDA event on ``stream`` for the pipeline timeline (profile mode)."""
+        if self.profile:
+            torch = _torch()
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(stream)
+            self._timeline.append((name, ev))
+
+    def take_timeline(self):
+        """Milliseconds from the start of the last pipelined run (profile mode)
+        to each recorded point: ``pack<c>``/``pack<c>_end`` on the pack stream,
+        ``gram<c>``/``gram<c>_end`` on the chunk's Gram stream (the first when
+        the launch may begin), ``normalise``, ``end``.  Synchronises."""
+        tl, self._timeline = getattr(self, "_timeline", []), []
+        if not tl:
+            return {}
+        tl[-1][1].synchronize()
+        t0 = tl[0][1]
+        return {name: t0.elapsed_time(ev) for name, ev in tl}
+
     @staticmethod
     def stage_times(events):
         """Milliseconds per stage from a list of (name, event); synchronises."""
@@ -588,6 +608,8 @@ class DenseEngine:
         copy_s.wait_event(start)
         pack_s.wait_event(start)
         gram_s.wait_event(start)
+        self._timeline = []
+        self._tmark("start", cur)
         npix, pc = self.npix, L.packed_cols
         jobs = _lib.jobs_array([(packed.data_ptr(), self.T, pc, L.kind, self.ones(L))])
         item_bytes = _lib.ITEM_DTYPE.itemsize
@@ -599,22 +621,28 @@ class DenseEngine:
                     e = torch.cuda.Event()
                     e.record(copy_s)
                 pack_s.wait_event(e)
+            self._tmark("pack%d" % c, pack_s)
             self.pack_e4m3(frames_dev.data_ptr() + t0 * npix, 1, t1 - t0, L, packed.data_ptr() + t0 * pc,
                            pack_s.cuda_stream)
+            self._tmark("pack%d_end" % c, pack_s)
             e = torch.cuda.Event()
             e.record(pack_s)
             k0, k1 = int(starts[c]), int(starts[c + 1])
             if k1 > k0:
                 gs = gram_streams[c % len(gram_streams)]
                 gs.wait_event(e)
+                self._tmark("gram%d" % c, gs)
                 self.gram_launch(jobs, dev_items.data_ptr() + k0 * item_bytes, k1 - k0, gs.cuda_stream)
+                self._tmark("gram%d_end" % c, gs)
         if len(gram_streams) > 1:
             done = torch.cuda.Event()
             done.record(gram_s)
             cur.wait_event(done)
         self._mark("normalise")
+        self._tmark("normalise", cur)
         self.normalise()
         self._mark("end")
+        self._tmark("end", cur)
         if host:
             self._frames_host_ref = frames            # alive until the copies are done
         code = self.resolve_range_check(int(self.err.item()), frames_dev)
