@@ -513,11 +513,20 @@ class DenseEngine:
     # +0.05 ms, 1.5: +0.2 ms, 2.0: +0.3 ms per step), so chunks are equal
     PIPE_GROWTH = 0.0
     PIPE_GRAM_STREAMS = 2     # consecutive chunks' Gram launches alternate streams (-0.11 ms per step)
+    # Frames copied from the host: the copies set the pace, and the Gram tiles
+    # of the last chunk (a column strip of the whole triangle) can only run
+    # after the last copy.  The last chunk is therefore cut into pieces of
+    # 1/2, 1/4, ... of it (PIPE_TAPER_HOST halvings), so that the work left
+    # after the last copy is a thin strip (pinned 514x1030x10k u8 stack:
+    # 28.8 ms per call untapered, 27.6-28.2 ms with 2 to 4 cuts).
+    PIPE_TAPER_HOST = 2
 
     @staticmethod
-    def pipe_bounds(T, n, growth):
+    def pipe_bounds(T, n, growth, taper=0):
         """Frame bounds of ``n`` pipeline chunks (multiples of 128 frames, the
-        last ending at T); chunk c's length grows as (c + 1) ** growth."""
+        last ending at T); chunk c's length grows as (c + 1) ** growth; with
+        ``taper`` > 0 the last chunk is cut into pieces of half, a quarter,
+        ... of it (``taper`` cuts, pieces of at least 128 frames)."""
         w = np.arange(1, n + 1, dtype=np.float64) ** float(growth)
         cum = np.cumsum(w)[:-1] / w.sum() * T
         b = [0]
@@ -525,15 +534,22 @@ class DenseEngine:
             v = int(round(x / 128.0)) * 128
             if b[-1] < v < T:
                 b.append(v)
+        rest = int(T) - b[-1]
+        for _ in range(int(taper)):
+            v = b[-1] + int(round(rest / 2.0 / 128.0)) * 128
+            if not b[-1] < v < T or T - v < 128:
+                break
+            b.append(v)
+            rest = int(T) - v
         b.append(int(T))
         return np.array(b, dtype=np.int64)
 
-    def _pipe_plan(self, L):
+    def _pipe_plan(self, L, taper=0):
         """Items of the e4m3 Gram grouped by the frame chunk whose packing
         makes them ready (a tile needs frames up to its last column), LPT order
         inside a group; cached per layout."""
         key = ("pipe", L.mode, self.T, self.exact_limit, self.grid, self.pipe_chunks, self.super_rows, self.kslab,
-               self.item_kind, self.pipe_growth)
+               self.item_kind, self.pipe_growth, int(taper))
         if key not in self._items_cache:
             torch = _torch()
             grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit, self.kslab)
@@ -541,7 +557,7 @@ class DenseEngine:
                                s_base=0 if self.ones(L) else None, super_rows=self.super_rows)
             T = self.T
             n = max(1, min(self.pipe_chunks, T // 256))
-            bounds = self.pipe_bounds(T, n, self.pipe_growth)
+            bounds = self.pipe_bounds(T, n, self.pipe_growth, taper)
             need = np.minimum(items["j0"].astype(np.int64) + TILE_SHAPES[self.item_kind][1], T)
             grp = np.searchsorted(bounds[1:], need, side="left")
             # each chunk's launch balanced over the kernel's workers
@@ -586,8 +602,8 @@ class DenseEngine:
         torch = _torch()
         L = self._layout(MODE_E4M3)
         packed = self._packed_buffer(L)
-        items, dev_items, bounds, starts, n_grams = self._pipe_plan(L)
         host = not frames.is_cuda
+        items, dev_items, bounds, starts, n_grams = self._pipe_plan(L, self.PIPE_TAPER_HOST if host else 0)
         frames_dev = self._frames_buffer(frames) if host else frames
         if not host and frames_dev.data_ptr() % 16:
             frames_dev = frames_dev.clone()

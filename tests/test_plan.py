@@ -278,3 +278,18 @@ def test_native_lpt_rejects_bad_arguments(built_lib):
     ok = np.array([1.0, 2.0, 3.0])
     assert built_lib.g2_balance_lpt(ok.ctypes.data_as(C.c_void_p), 3, 0, slots.ctypes.data_as(C.c_void_p),
                                     C.byref(n_slots)) != 0
+
+
+@pytest.mark.parametrize("T,n", [(10000, 8), (2100, 8), (1000, 3), (300, 1), (5000, 4)])
+def test_pipeline_chunk_bounds_tapered(T, n):
+    """Host-input pipelines cut the last chunk into halving pieces: the
+    untapered bounds stay, the pieces are multiples of 128 frames (the last
+    one ends at T) and no piece grows towards the end."""
+    from dynamix_gb300.engine import DenseEngine
+    plain = DenseEngine.pipe_bounds(T, n, 0.0)
+    b = DenseEngine.pipe_bounds(T, n, 0.0, taper=3)
+    assert b[0] == 0 and b[-1] == T and np.all(np.diff(b) > 0)
+    assert set(plain[:-1].tolist()) <= set(b.tolist())
+    assert np.all(b[1:-1] % 128 == 0) and b.size - plain.size <= 3
+    tail = np.diff(b[plain.size - 2:])
+    assert np.all(tail[1:-1] <= tail[:-2])
