@@ -235,6 +235,22 @@ class EventEngine:
         return self.run_device(times, counts, offs, n_ev, mx)
 
     HOST_CHUNKS = 8
+    # the last pixel chunk is cut into halving pieces (HOST_TAPER cuts): the
+    # pair sums left after the last copy cover a thin slice of the pixels
+    HOST_TAPER = 2
+
+    @staticmethod
+    def host_chunk_bounds(npix, chunks, taper):
+        """Pixel bounds of the host pipeline's chunks: ``chunks`` equal ones,
+        the last cut ``taper`` times in half."""
+        b = [npix * c // chunks for c in range(chunks)]
+        for _ in range(int(taper)):
+            mid = (b[-1] + npix) // 2
+            if not b[-1] < mid < npix:
+                break
+            b.append(mid)
+        b.append(npix)
+        return b
 
     def host_pipeline_ok(self, vol_times, vol_data, offsets):
         """Pinned host tensors (times int32, counts uint8/uint16, offsets
@@ -249,16 +265,15 @@ class EventEngine:
                 and vol_times.numel() == vol_data.numel() and self.n_bins > 0)
 
     def _chunk_plans(self):
-        """Per pixel chunk (raster order, equal pixel counts): its binned
-        pixels bin by bin and their CTA ranges, for both pair kernels."""
+        """Per pixel chunk (raster order, :meth:`host_chunk_bounds`): its
+        binned pixels bin by bin and their CTA ranges, for both pair kernels."""
         plans = getattr(self, "_host_plans", None)
         if plans is None:
             torch = _torch()
             sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
-            K = self.HOST_CHUNKS
-            bounds = [self.npix * c // K for c in range(K + 1)]
+            bounds = self.host_chunk_bounds(self.npix, self.HOST_CHUNKS, self.HOST_TAPER)
             plans = []
-            for c in range(K):
+            for c in range(len(bounds) - 1):
                 keep = (self.binned >= bounds[c]) & (self.binned < bounds[c + 1])
                 pix, bins = self.binned[keep], self.binned_bin[keep]
                 d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.dev)
@@ -332,7 +347,7 @@ class EventEngine:
         self._mark("normalize")
         self._host_refs = (vol_times, offsets)            # alive until the copies have run
         self._times_checked = True
-        self.last = {"n_events": n_ev, "max_count": mx, "kernel": kind, "host_chunks": self.HOST_CHUNKS}
+        self.last = {"n_events": n_ev, "max_count": mx, "kernel": kind, "host_chunks": len(self._host_plans)}
         return self.g2_f32[: self.n_bins]
 
     def run_device(self, times, counts, offs, n_ev, mx, reset_error=True):

@@ -55,3 +55,16 @@ def test_cta_ranges_empty():
     from dynamix_gb300.engine_sparse import cta_ranges
     ro, rb, cro = cta_ranges(np.zeros(0, np.int32), 152)
     assert ro.tolist() == [0] and rb.size == 0 and cro.tolist() == [0, 0]
+
+
+@pytest.mark.parametrize("npix,chunks,taper", [(2162 * 2068, 8, 2), (1000, 8, 0), (10, 8, 2), (3, 8, 2)])
+def test_host_chunk_bounds_cover_pixels(npix, chunks, taper):
+    """Pixel chunks of the pinned-host event pipeline: they tile [0, npix),
+    and the tapered tail never grows."""
+    from dynamix_gb300.engine_sparse import EventEngine
+    b = np.asarray(EventEngine.host_chunk_bounds(npix, chunks, taper))
+    assert b[0] == 0 and b[-1] == npix and np.all(np.diff(b) >= 0)
+    assert b.size - 1 <= chunks + taper
+    if npix >= 64 * chunks:
+        d = np.diff(b)
+        assert np.all(d[chunks - 1:-1] <= d[chunks - 2:-2] + 1)
