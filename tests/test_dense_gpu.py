@@ -401,3 +401,26 @@ def test_matches_reference_dense_kernel(built_lib, cuda_device, name, tile):
     ok = np.isfinite(ref)
     assert np.array_equal(np.isfinite(g), ok)
     assert np.all(np.abs(g[ok] - ref[ok]) <= 2e-6 * np.abs(ref[ok]))
+
+
+@pytest.mark.parametrize("operand", ["fp16", "bytes"])
+def test_k_split_reuse_across_stacks(built_lib, cuda_device, operand):
+    """One correlator, several fp16 / byte-plane stacks: a stack whose energy
+    bounds lie within those planned for before reuses the K split without a
+    host round trip; a brighter one is detected on the device and run again
+    through the planned path.  Every result is exact."""
+    from dynamix_gb300.correlator import MatMulCorrelator
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    T, shape = 400, (24, 40)
+    qm = annular_qmask(shape, 4, 1.0, 20.0)
+    mus = {"fp16": (20.0, 60.0, 5.0, 20.0), "bytes": (700.0, 2000.0, 300.0, 700.0)}[operand]
+    c = MatMulCorrelator(shape, T, qmask=qm, extra_options={"operand": operand})
+    plans = []
+    for i, mu in enumerate(mus):
+        fr = speckle_numpy(T, shape, 0.97, mu, seed=40 + i, dtype=np.uint16, max_count=65535)
+        g = c.correlate(fr)
+        assert c.engine.last["mode"] == operand
+        assert_exact(c, o.g2_exact(fr, qm), g)
+        plans.append(c.engine.last["plan"])
+    assert plans[0] == "planned" and plans[1] == "planned"   # the first stack, then a brighter one
+    assert plans[2] == "reused" and plans[3] == "reused"     # dimmer, and the first again
