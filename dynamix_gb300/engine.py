@@ -333,6 +333,16 @@ class DenseEngine:
         # the pack kernels flag counts that do not fit and the step reruns wider
         return self._u8_hint if frames_dev.element_size() == 1 else self._u16_hint
 
+    def pack_fp16_frames(self, frames_ptr, elem_bytes, nframes, L, packed_ptr, emax, stream):
+        """One launch of the fp16 pack (with the row of ones: no bin sums)
+        over ``nframes`` frames at ``frames_ptr`` into the packed rows at
+        ``packed_ptr``; the energy maxima are combined into ``emax``."""
+        _lib.check(self.lib.g2_pack_frames(
+            C.c_void_p(frames_ptr), elem_bytes, nframes, self.npix, ptr(L.d_chunk_entry_off), ptr(L.d_entry_dst),
+            ptr(L.d_entry_meta), ptr(L.d_chunk_slot_bin), ptr(L.d_chunk_piece_off), ptr(L.d_bin_kpad), L.n_chunks,
+            MODE_FP16, C.c_void_p(packed_ptr), L.packed_cols, None, self.n_bins, ptr(emax), L.n_pieces,
+            ptr(self.err), stream if isinstance(stream, C.c_void_p) else C.c_void_p(stream)), "g2_pack_frames")
+
     def pack(self, frames_dev, mode):
         L = self._layout(mode)
         packed = self._packed_buffer(L)
@@ -544,15 +554,17 @@ class DenseEngine:
         b.append(int(T))
         return np.array(b, dtype=np.int64)
 
-    def _pipe_plan(self, L, taper=0):
-        """Items of the e4m3 Gram grouped by the frame chunk whose packing
-        makes them ready (a tile needs frames up to its last column), LPT order
-        inside a group; cached per layout."""
+    def _pipe_plan(self, L, taper=0, grams=None):
+        """Items of the Gram grouped by the frame chunk whose packing makes
+        them ready (a tile needs frames up to its last column), LPT order
+        inside a group; cached per layout and K split (``grams``; default the
+        e4m3 split, which needs no energies)."""
         key = ("pipe", L.mode, self.T, self.exact_limit, self.grid, self.pipe_chunks, self.super_rows, self.kslab,
-               self.item_kind, self.pipe_growth, int(taper))
+               self.item_kind, self.pipe_growth, int(taper), None if grams is None else tuple(grams))
         if key not in self._items_cache:
             torch = _torch()
-            grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit, self.kslab)
+            if grams is None:
+                grams = chunk_grams(L, e4m3_segment_bound(L), self.exact_limit, self.kslab)
             items = gram_items(self.T, grams, job=0, out_base=0, kind=self.item_kind,
                                s_base=0 if self.ones(L) else None, super_rows=self.super_rows)
             T = self.T
@@ -586,13 +598,31 @@ class DenseEngine:
         return self._frames_buf
 
     def pipelined_ok(self, frames):
-        """The chunked pipeline applies to u8 stacks on the tensor-core path
-        while their counts are known (or expected) to be <= 16."""
+        """The chunked pipeline applies on the tensor-core path to u8 stacks
+        while their counts are known (or expected) to be <= 16 (e4m3), and to
+        u8 / u16 stacks in pinned host memory on fp16 operands once a K split
+        can be reused (see :meth:`_speculative_ok`): fp16 packs keep no
+        per-frame state except energy maxima, which chunks combine."""
+        return self._pipeline_mode(frames) is not None
+
+    def _pipeline_mode(self, frames):
         torch = _torch()
-        return (self.method == "tc" and self.operand in ("auto", "e4m3") and self.pipeline
-                and isinstance(frames, torch.Tensor) and frames.dtype == torch.uint8
-                and (self.operand == "e4m3" or self._u8_hint == MODE_E4M3) and self.n_bins > 0
-                and (frames.is_cuda or (frames.is_pinned() and frames.is_contiguous())))
+        if not (self.method == "tc" and self.pipeline and isinstance(frames, torch.Tensor) and self.n_bins > 0
+                and frames.dtype in (torch.uint8, torch.uint16)
+                and (frames.is_cuda or (frames.is_pinned() and frames.is_contiguous()))):
+            return None
+        if (frames.dtype == torch.uint8 and self.operand in ("auto", "e4m3")
+                and (self.operand == "e4m3" or self._u8_hint == MODE_E4M3)):
+            return MODE_E4M3
+        # fp16 from pinned host memory only: there the copies set the pace and
+        # hide the pack and most of the Gram (256x256x5k u16: 4.99 -> 3.94 ms per
+        # call); a device-resident stack runs faster unchunked (1.80 against
+        # 2.00 ms: the chunk launches of so short a Gram cost more than the
+        # 0.47 ms pack they would hide)
+        mode = self.choose_mode(frames)
+        if mode == MODE_FP16 and not frames.is_cuda and self._speculative_ok(mode):
+            return MODE_FP16
+        return None
 
     def run_pipelined(self, frames):
         """G1 + G2 chunk by chunk of frames: copy (host input) -> pack -> the
@@ -600,10 +630,15 @@ class DenseEngine:
         and tensor-core work overlap; then G3 + G4.  One synchronisation at the
         end reads the error word; counts above 16 rerun on fp16 operands."""
         torch = _torch()
-        L = self._layout(MODE_E4M3)
+        mode = self._pipeline_mode(frames)
+        L = self._layout(mode)
         packed = self._packed_buffer(L)
         host = not frames.is_cuda
-        items, dev_items, bounds, starts, n_grams = self._pipe_plan(L, self.PIPE_TAPER_HOST if host else 0)
+        if mode == MODE_E4M3:
+            grams, bound = None, None
+        else:                                 # fp16: the reused K split and the bounds it covers
+            _, bound, grams = self._plans[mode]
+        items, dev_items, bounds, starts, n_grams = self._pipe_plan(L, self.PIPE_TAPER_HOST if host else 0, grams)
         frames_dev = self._frames_buffer(frames) if host else frames
         if not host and frames_dev.data_ptr() % 16:
             frames_dev = frames_dev.clone()
@@ -619,6 +654,10 @@ class DenseEngine:
         self.numer.zero_()
         self.sums.zero_()
         self.err.zero_()
+        emax = None
+        if mode != MODE_E4M3:
+            emax = self._piece_emax(L)
+            emax.zero_()                      # chunks combine their energy maxima (atomicMax)
         start = torch.cuda.Event()
         start.record(cur)                     # the previous call's work and the zeroing are done first
         copy_s.wait_event(start)
@@ -627,6 +666,8 @@ class DenseEngine:
         self._timeline = []
         self._tmark("start", cur)
         npix, pc = self.npix, L.packed_cols
+        eb = frames_dev.element_size()
+        row_bytes = L.packed_bytes_per_frame
         jobs = _lib.jobs_array([(packed.data_ptr(), self.T, pc, L.kind, self.ones(L))])
         item_bytes = _lib.ITEM_DTYPE.itemsize
         for c in range(bounds.size - 1):
@@ -638,8 +679,12 @@ class DenseEngine:
                     e.record(copy_s)
                 pack_s.wait_event(e)
             self._tmark("pack%d" % c, pack_s)
-            self.pack_e4m3(frames_dev.data_ptr() + t0 * npix, 1, t1 - t0, L, packed.data_ptr() + t0 * pc,
-                           pack_s.cuda_stream)
+            if mode == MODE_E4M3:
+                self.pack_e4m3(frames_dev.data_ptr() + t0 * npix, 1, t1 - t0, L, packed.data_ptr() + t0 * pc,
+                               pack_s.cuda_stream)
+            else:
+                self.pack_fp16_frames(frames_dev.data_ptr() + t0 * npix * eb, eb, t1 - t0, L,
+                                      packed.data_ptr() + t0 * row_bytes, emax, pack_s.cuda_stream)
             self._tmark("pack%d_end" % c, pack_s)
             e = torch.cuda.Event()
             e.record(pack_s)
@@ -661,6 +706,18 @@ class DenseEngine:
         self._tmark("end", cur)
         if host:
             self._frames_host_ref = frames            # alive until the copies are done
+        if mode != MODE_E4M3:
+            # one synchronisation: the error word and whether the stack's
+            # energy bounds exceed those the reused split covers
+            m = L.n_pieces
+            above = ((emax[:m].to(torch.int64) & 0xFFFFFFFF) > bound).any().to(torch.int32)
+            code, over = (int(x) for x in torch.stack([self.err[0], above]).cpu())
+            if code or over:                          # out of range, or a brighter stack: planned path
+                return self.run(frames_dev, pipelined=False, reuse_split=False)
+            self.last = {"mode": "fp16", "split": int(L.split), "n_items": int(items.size), "n_grams": n_grams,
+                         "packed_cols": L.packed_cols, "pipeline_chunks": int(bounds.size - 1), "tile": self.tile,
+                         "plan": "reused"}
+            return self.g2_f32[: self.n_bins]
         code = self.resolve_range_check(int(self.err.item()), frames_dev)
         if code & _lib.DEVERR_RANGE and self.operand == "auto":
             self._u8_hint = MODE_FP16                 # counts above 16: rerun on fp16 operands
@@ -670,10 +727,13 @@ class DenseEngine:
         return self.g2_f32[: self.n_bins]
 
     # -- whole pipeline ----------------------------------------------------
-    def run(self, frames_dev, pipelined=True):
+    def run(self, frames_dev, pipelined=True, reuse_split=True):
         """Run G1..G4 on a device stack; returns the float32 g2 device tensor.
 
-        Synchronises once after G1 to read the segment energies (K split)."""
+        Pipelined stacks (see :meth:`pipelined_ok`) and stacks whose K split
+        can be reused synchronise once, at the end; otherwise once after G1
+        to read the segment energies (K split).  ``reuse_split=False`` plans
+        the split from this stack's energies."""
         if tuple(frames_dev.shape) != (self.T,) + self.shape:
             raise ValueError("frames should have shape %s, got %s" % ((self.T,) + self.shape,
                                                                     tuple(frames_dev.shape)))
@@ -689,7 +749,7 @@ class DenseEngine:
             return self._run_dp4a(frames_dev)
         mode = self.choose_mode(frames_dev)
         self._mark("pack")
-        if self._speculative_ok(mode):
+        if reuse_split and self._speculative_ok(mode):
             g2 = self._run_speculative(frames_dev, mode)
             if g2 is not None:
                 return g2

@@ -424,3 +424,32 @@ def test_k_split_reuse_across_stacks(built_lib, cuda_device, operand):
         plans.append(c.engine.last["plan"])
     assert plans[0] == "planned" and plans[1] == "planned"   # the first stack, then a brighter one
     assert plans[2] == "reused" and plans[3] == "reused"     # dimmer, and the first again
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16])
+def test_fp16_pipeline_with_reused_split(built_lib, cuda_device, dtype):
+    """Stacks on fp16 operands reuse a K split once one covers them: from
+    pinned host memory through the chunked copy / pack / Gram pipeline,
+    device-resident ones unchunked; a brighter stack falls back to the
+    planned path; every result equals the oracle."""
+    import torch
+    from dynamix_gb300.correlator import MatMulCorrelator
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    T, shape = 1100, (30, 50)
+    qm = annular_qmask(shape, 5, 2.0, 25.0)
+    c = MatMulCorrelator(shape, T, qmask=qm, extra_options={"operand": "fp16"})
+    seen = []
+    for i, (mu, where) in enumerate(((20.0, "device"), (12.0, "device"), (12.0, "host"), (60.0, "host"),
+                                     (25.0, "device"))):
+        fr = speckle_numpy(T, shape, 0.98, mu, seed=70 + i, dtype=dtype, max_count=255 if dtype == np.uint8 else 2000)
+        inp = torch.from_numpy(fr)
+        inp = inp.to(cuda_device) if where == "device" else inp.pin_memory()
+        g = c.correlate(inp)
+        assert c.engine.last["mode"] == "fp16"
+        assert_exact(c, o.g2_exact(fr, qm), g)
+        seen.append((c.engine.last.get("plan"), "pipeline_chunks" in c.engine.last))
+    assert seen[0] == ("planned", False)
+    assert seen[1] == ("reused", False)                   # device-resident: unchunked, split reused
+    assert seen[2] == ("reused", True)                    # pinned host: the chunked pipeline
+    assert seen[3] == ("planned", False)                  # brighter: detected, run again on a fresh plan
+    assert seen[4] == ("reused", False)
