@@ -523,6 +523,9 @@ class DenseEngine:
     # +0.05 ms, 1.5: +0.2 ms, 2.0: +0.3 ms per step), so chunks are equal
     PIPE_GROWTH = 0.0
     PIPE_GRAM_STREAMS = 2     # consecutive chunks' Gram launches alternate streams (-0.11 ms per step)
+    # the first two chunks' Gram tiles share one launch (the first chunk's
+    # alone leave most SMs idle: 11.81 -> 11.72 ms per step; three: 11.92)
+    PIPE_MERGE_FIRST = 2
     # Frames copied from the host: the copies set the pace, and the Gram tiles
     # of the last chunk (a column strip of the whole triangle) can only run
     # after the last copy.  The last chunk is therefore cut into pieces of
@@ -688,7 +691,12 @@ class DenseEngine:
             self._tmark("pack%d_end" % c, pack_s)
             e = torch.cuda.Event()
             e.record(pack_s)
-            k0, k1 = int(starts[c]), int(starts[c + 1])
+            # the first PIPE_MERGE_FIRST chunks' tiles go in one launch (the
+            # first chunk alone completes too few tiles to fill the GPU)
+            merge = max(1, min(int(self.PIPE_MERGE_FIRST), bounds.size - 1))
+            if c < merge - 1:
+                continue
+            k0, k1 = int(starts[0 if c == merge - 1 else c]), int(starts[c + 1])
             if k1 > k0:
                 gs = gram_streams[c % len(gram_streams)]
                 gs.wait_event(e)
