@@ -338,8 +338,10 @@ def run_ours(args):
     value = whole_job_rate(T, ms, world)
     info = dict(eng.last)
     chunks = int(info.get("pipeline_chunks", 1))
-    # pack + one Gram per frame chunk, denominator, finalize
-    launches_per_step = 2 * chunks + 2 if "pipeline_chunks" in info else 4
+    # a pack per frame chunk, a Gram per chunk (the first chunks' Grams in one
+    # launch), denominator, finalize
+    merged = max(1, min(int(eng.PIPE_MERGE_FIRST), chunks)) - 1
+    launches_per_step = 2 * chunks - merged + 2 if "pipeline_chunks" in info else 4
 
     # stage attribution: the same step run as one pack and one Gram launch,
     # with CUDA events on the launching stream around each stage
