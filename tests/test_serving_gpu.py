@@ -112,3 +112,22 @@ def test_errors_do_not_stop_the_server(built_lib, cuda_device):
         neg.wait()
     ok.wait()
     _check(ok, fr[:50], qm)
+
+
+def test_staging_arena_limits(built_lib, cuda_device):
+    """Pinned host frames go through the staging arena: a job larger than the
+    whole arena gets a buffer of its own, jobs that do not fit beside each
+    other wait for space; the results stay exact and the arena drains."""
+    import torch
+    from dynamix_gb300.serving import G2Server
+    jobs = _mix()
+    sizes = [fr.nbytes for fr, _ in jobs]
+    srv = G2Server(hbm_budget=2e9, slice_ops=2e8, staging_bytes=max(sizes) * 1.5)
+    reqs = [srv.submit(torch.from_numpy(fr).pin_memory(), qm) for fr, qm in jobs]
+    big = np.concatenate([jobs[0][0]] * 2)                     # twice the first job's frames
+    reqs.append(srv.submit(torch.from_numpy(big).pin_memory(), jobs[0][1]))
+    srv.run_until_idle()
+    for r, (fr, qm) in zip(reqs, jobs + [(big, jobs[0][1])]):
+        r.wait()
+        _check(r, fr, qm)
+    assert srv.staging_arena.used == 0 and srv.arena.used == 0 and srv.used == 0
