@@ -28,10 +28,12 @@ namespace ev {
 
 constexpr int THREADS = 768;
 constexpr int WARPS = THREADS / 32;
+constexpr int LANES = 16;                  // lanes per pixel: a warp walks two pixels side by side
+constexpr int HALVES = 32 / LANES;
 constexpr int EV = 128;                    // events of one pixel staged per block of pairs
 constexpr int ROWS = 8;                    // rows of the pair block walked together
 constexpr uint32_t DRAIN = 1u << 31;
-constexpr int SMEM_FIXED = WARPS * 2 * EV * 4;
+constexpr int SMEM_FIXED = WARPS * HALVES * 2 * EV * 4;
 constexpr int SMEM_STATIC = WARPS * 8;    // block-reduction slots
 
 __device__ __forceinline__ void add_counter(uint32_t* c, unsigned long long* g, uint32_t x) {
@@ -66,10 +68,10 @@ template <bool FAST, bool PACKED, typename Tv>
 __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, const Tv* __restrict__ data,
                                             int64_t base, int n, int T, uint32_t maxc, uint32_t* hist,
                                             uint32_t* shist, unsigned long long* gN, unsigned long long* gS,
-                                            uint32_t* bufA, uint32_t* bufB, int lane, bool& bad) {
+                                            uint32_t* bufA, uint32_t* bufB, int lane, uint32_t mask, bool& bad) {
   for (int ib = 0; ib < n; ib += EV) {
     const int na = min(EV, n - ib);
-    for (int e = lane; e < na; e += 32) {
+    for (int e = lane; e < na; e += LANES) {
       bool ok;
       const uint32_t w = load_event<PACKED>(times, data, base + ib + e, T, maxc, ok);
       const int t = static_cast<int>(w >> 16);
@@ -83,17 +85,17 @@ __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, c
           add_counter(&shist[t], &gS[t], v);
       }
     }
-    __syncwarp();
+    __syncwarp(mask);
     for (int jb = ib; jb < n; jb += EV) {
       const int nb = min(EV, n - jb);
       const uint32_t* B = bufA;
       if (jb != ib) {
-        for (int e = lane; e < nb; e += 32) {
+        for (int e = lane; e < nb; e += LANES) {
           bool ok;
           const uint32_t w = load_event<PACKED>(times, data, base + jb + e, T, maxc, ok);
           bufB[e] = ok ? w : 0u;
         }
-        __syncwarp();
+        __syncwarp(mask);
         B = bufB;
       }
       // ROWS rows (i .. i + ROWS - 1) per pass: each partner word read from
@@ -113,7 +115,7 @@ __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, c
           any |= vi[r];
         }
         if (any == 0) continue;  // warp-uniform
-        for (int j = (tri ? i : 0) + lane; j < nb; j += 32) {
+        for (int j = (tri ? i : 0) + lane; j < nb; j += LANES) {
           const uint32_t wj = B[j];
           const int tj = static_cast<int>(wj >> 16);
           const uint32_t vj = wj & 0xFFFFu;
@@ -128,7 +130,7 @@ __device__ __forceinline__ void pixel_pairs(const int32_t* __restrict__ times, c
           }
         }
       }
-      __syncwarp();
+      __syncwarp(mask);
     }
   }
 }
@@ -145,9 +147,11 @@ __global__ void __launch_bounds__(THREADS, 1)
   __shared__ unsigned long long s_red[WARPS];
   uint32_t* hist = sm;              // [T] lag sums of this range's bin
   uint32_t* shist = sm + T;         // [T] frame sums
-  uint32_t* evbuf = sm + 2 * T;     // [WARPS][2][EV] staged events (t << 16 | v)
+  uint32_t* evbuf = sm + 2 * T;     // [WARPS][HALVES][2][EV] staged events (t << 16 | v)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint32_t* bufA = evbuf + warp * 2 * EV;
+  const int half = lane / LANES, hl = lane % LANES;
+  const uint32_t hmask = (LANES == 32 ? 0xffffffffu : ((1u << LANES) - 1u)) << (half * LANES);
+  uint32_t* bufA = evbuf + (warp * HALVES + half) * 2 * EV;
   uint32_t* bufB = bufA + EV;
   bool bad = false;
   for (int i = threadIdx.x; i < 2 * T; i += THREADS) sm[i] = 0;
@@ -180,7 +184,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     const bool fast = max2 == 0 || tot < (1ull << 32) / max2;
     unsigned long long* gN = numer + static_cast<int64_t>(bin) * T;
     unsigned long long* gS = sums + static_cast<int64_t>(bin) * T;
-    for (int li = range_off[r] + warp; li < range_off[r + 1]; li += WARPS) {
+    // each half-warp takes its own pixel (its own staging buffers; it syncs
+    // only its own lanes), so that a pixel's pair rows leave half as many
+    // lanes idle at their ends as 32-lane rows would
+    for (int li = range_off[r] + warp * HALVES + half; li < range_off[r + 1]; li += WARPS * HALVES) {
       const int32_t p = pix_list[li];
       if (p < 0 || p >= npix) {
         bad = true;
@@ -194,9 +201,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       const int n = static_cast<int>(end - base);
       if (fast)
-        pixel_pairs<true, PACKED>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
+        pixel_pairs<true, PACKED>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, hl, hmask, bad);
       else
-        pixel_pairs<false, PACKED>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, lane, bad);
+        pixel_pairs<false, PACKED>(times, data, base, n, T, maxc, hist, shist, gN, gS, bufA, bufB, hl, hmask, bad);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < T; i += THREADS) {

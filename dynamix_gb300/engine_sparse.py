@@ -21,6 +21,11 @@ import numpy as np
 from . import _lib
 from .engine import DeviceError, _torch, ptr, require_cuda, stream_handle
 
+# shared memory of the shared-counter pair kernel besides its 2 x T counters:
+# 24 warps x 2 half-warp pixels x 2 staging buffers x 128 events x 4 bytes
+# (g2_event.cu, ev::SMEM_FIXED)
+PAIRS_SMEM_FIXED = 24 * 2 * 2 * 128 * 4
+
 
 def _is_cuda(a):
     torch = _torch()
@@ -316,7 +321,7 @@ class EventEngine:
         self.numer.zero_()
         self.sums.zero_()
         self.err.zero_()
-        use_smem = self.T * 8 + 24576 + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
+        use_smem = self.T * 8 + PAIRS_SMEM_FIXED + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
         kind = "smem" if use_smem else "global"
         host_off = offsets                                 # pinned host offsets for the chunk bounds
         st = stream_handle(self.dev)
@@ -362,7 +367,7 @@ class EventEngine:
         st = stream_handle(self.dev)
         # the C side makes the same choice (shared counters for 2 x T frames,
         # times below 2^16, products below 2^31)
-        use_smem = self.T * 8 + 24576 + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
+        use_smem = self.T * 8 + PAIRS_SMEM_FIXED + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
         ro, rb, cro, n_ranges, n_ctas = self.plans["smem" if use_smem else "global"]
         self._mark("start_pairs")
         if n_ranges and self.n_bins and n_ev and counts is None:     # packed words (t << 16) | v
