@@ -134,13 +134,16 @@ __global__ void __launch_bounds__(THR)
 
 // Launch G3 with enough blocks to fill the GPU: the frame windows are split
 // over gridDim.z and the partial sums added atomically (mod 2^64, exact).
+// The work of a lag block falls with its lags (fewer frames pair up), so the
+// first blocks set the time: z aims at 32 blocks per SM, not just enough to
+// occupy every SM (2162x2068x20k events, 32 bins: 1.01 -> 0.71 ms).
 inline int launch_denominator(const long long* S, int32_t n_rows, int64_t T, long long* D, cudaStream_t st) {
   const int64_t gx = (T + LAGS - 1) / LAGS;
   if (gx > 0x7fffffff) return G2_ERR_TOO_LARGE;
   const int sms = sm_count_current();
   if (sms <= 0) return G2_ERR_CUDA;
   const int64_t windows = (T + WIN - 1) / WIN;
-  int64_t z = (4ll * sms + gx * n_rows - 1) / (gx * n_rows);
+  int64_t z = (32ll * sms + gx * n_rows - 1) / (gx * n_rows);
   z = z < 1 ? 1 : (z > windows ? windows : (z > 32 ? 32 : z));
   if (z > 1 && cudaMemsetAsync(D, 0, static_cast<size_t>(n_rows) * T * sizeof(long long), st) != cudaSuccess)
     return G2_ERR_CUDA;
