@@ -291,55 +291,92 @@ class EventEngine:
         return plans
 
     def run_host_pipelined(self, vol_times, vol_data, offsets):
-        """Events in pinned host memory: offsets and counts are copied and
-        checked first (one synchronisation: offsets start at 0 and never
-        decrease, counts give the kernel choice), then the frame times in
-        pixel chunks, each chunk's pair sums running while the next chunk is
-        copied; times outside [0, nframes) are found by the pair kernel and
-        raise ValueError after the call."""
+        """Events in pinned host memory: the offsets first, then every pixel
+        chunk's counts and frame times back to back on the copy stream.  As
+        soon as a chunk's counts have arrived its largest count is taken on
+        the device and read by the host (it picks the chunk's pair kernel and
+        whether its counters need drain checks), and the chunk's pair sums
+        run while later chunks are still being copied.  Offsets that do not
+        start at 0 or decrease are found on the device and raise ValueError
+        after the call (the pair kernels bound every access), as do frame
+        times outside [0, nframes)."""
         torch = _torch()
         cur = torch.cuda.current_stream(self.dev)
         copy_s = getattr(self, "_copy_stream", None)
         if copy_s is None:
             copy_s = self._copy_stream = torch.cuda.Stream(self.dev)
-        offs64 = offsets.to(self.dev, non_blocking=True).to(torch.int64)
-        counts = vol_data.to(self.dev, non_blocking=True)
-        n_ev = int(offs64[-1].item())                     # synchronises the two copies
-        bad = bool(offs64[0].item() != 0) or bool(torch.any(offs64[1:] < offs64[:-1]).item())
-        if bad:
-            raise ValueError("offsets must start at 0 and be non-decreasing")
+        max_s = getattr(self, "_max_stream", None)
+        if max_s is None:
+            max_s = self._max_stream = torch.cuda.Stream(self.dev)
+        host_off = offsets                                 # pinned host offsets: chunk bounds, n_ev
+        n_ev = int(host_off[-1])
+        if host_off.dtype == torch.int32:
+            n_ev &= 0xFFFFFFFF                             # uint32 offsets held in int32
         if n_ev >= 2 ** 32:
             raise ValueError("too many events for uint32 offsets")
         if vol_times.numel() < n_ev:
             raise ValueError("offsets reference %d events but only %d are given" % (n_ev, vol_times.numel()))
-        mx = int(counts[:n_ev].to(torch.int32).max().item()) if n_ev else 0
-        offs = offs64.to(torch.int32)                     # uint32 bit pattern (n_ev < 2^32)
+        offs64 = offsets.to(self.dev, non_blocking=True).to(torch.int64)
+        if offsets.dtype == torch.int32:
+            offs64 = offs64 & 0xFFFFFFFF                   # uint32 offsets held in int32
+        self._offsets_bad = ((offs64[0] != 0) | (offs64[1:] < offs64[:-1]).any()).to(torch.int32)
+        offs = offs64.to(torch.int32)                      # uint32 bit pattern (n_ev < 2^32)
         times = getattr(self, "_times_buf", None)
         if times is None or times.numel() < max(n_ev, 1):
             self._times_buf = None
             times = self._times_buf = torch.empty(max(n_ev, 1), dtype=torch.int32, device=self.dev)
+        counts = getattr(self, "_counts_buf", None)
+        if counts is None or counts.numel() < max(n_ev, 1) or counts.dtype != vol_data.dtype:
+            self._counts_buf = None
+            counts = self._counts_buf = torch.empty(max(n_ev, 1), dtype=vol_data.dtype, device=self.dev)
         self.numer.zero_()
         self.sums.zero_()
         self.err.zero_()
-        use_smem = self.T * 8 + PAIRS_SMEM_FIXED + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
-        kind = "smem" if use_smem else "global"
-        host_off = offsets                                 # pinned host offsets for the chunk bounds
         st = stream_handle(self.dev)
         start = torch.cuda.Event()
         start.record(cur)
         copy_s.wait_event(start)
+        max_s.wait_event(start)
+        plans = self._chunk_plans()
+        mx_host = torch.zeros(len(plans), dtype=torch.int32, pin_memory=True)
+        spans, ready, mx_ready = [], [], []
+        for c, (p0, p1, pix, per) in enumerate(plans):    # every copy first, so the link never waits
+            e0 = min(int(host_off[p0]) & 0xFFFFFFFF, n_ev)   # malformed offsets: kept in range here,
+            e1 = min(int(host_off[p1]) & 0xFFFFFFFF, n_ev)   # reported after the call
+            spans.append((e0, e1))
+            if e1 <= e0:
+                ready.append(None)
+                mx_ready.append(None)
+                continue
+            with torch.cuda.stream(copy_s):
+                counts[e0:e1].copy_(vol_data[e0:e1], non_blocking=True)
+                times[e0:e1].copy_(vol_times[e0:e1], non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(copy_s)
+            ready.append(done)
+            with torch.cuda.stream(max_s):
+                max_s.wait_event(done)
+                part = counts[e0:e1]
+                m = torch.amax(part if part.dtype == torch.uint8 else part.to(torch.int32)).to(torch.int32)
+                mx_host[c].copy_(m, non_blocking=True)
+                got = torch.cuda.Event()
+                got.record(max_s)
+            mx_ready.append(got)
         self._mark("start_pairs")
-        for p0, p1, pix, per in self._chunk_plans():
-            e0 = int(host_off[p0]) & 0xFFFFFFFF
-            e1 = int(host_off[p1]) & 0xFFFFFFFF
-            if e1 > e0:
-                with torch.cuda.stream(copy_s):
-                    times[e0:e1].copy_(vol_times[e0:e1], non_blocking=True)
-                    done = torch.cuda.Event()
-                    done.record(copy_s)
-                cur.wait_event(done)
+        mx_all, kinds = 0, set()
+        for c, (p0, p1, pix, per) in enumerate(plans):
+            e0, e1 = spans[c]
+            if ready[c] is None:
+                continue
+            mx_ready[c].synchronize()                      # this chunk's counts are in: its largest
+            mx = int(mx_host[c])
+            mx_all = max(mx_all, mx)
+            use_smem = self.T * 8 + PAIRS_SMEM_FIXED + 192 <= 227 * 1024 and self.T <= 65535 and mx * mx < 2 ** 31
+            kind = "smem" if use_smem else "global"
+            kinds.add(kind)
             ro, rb, cro, n_ranges, n_ctas = per[kind]
-            if n_ranges and e1 > e0:
+            cur.wait_event(ready[c])
+            if n_ranges:
                 _lib.check(self.lib.g2_event_pairsum(
                     ptr(times), ptr(counts), counts.element_size(), n_ev, ptr(offs), self.npix, ptr(pix),
                     ptr(ro), ptr(rb), n_ranges, ptr(cro), n_ctas, self.T, self.n_bins, mx, ptr(self.numer),
@@ -350,9 +387,11 @@ class EventEngine:
         _lib.check(self.lib.g2_finalize(ptr(self.numer), ptr(self.denom), ptr(self.scale), self.n_bins,
                                         self.T, ptr(self.g2_f32), ptr(self.g2_f64), st), "g2_finalize")
         self._mark("normalize")
-        self._host_refs = (vol_times, offsets)            # alive until the copies have run
+        self._host_refs = (vol_times, vol_data, offsets)  # alive until the copies have run
         self._times_checked = True
-        self.last = {"n_events": n_ev, "max_count": mx, "kernel": kind, "host_chunks": len(self._host_plans)}
+        self.last = {"n_events": n_ev, "max_count": mx_all,
+                     "kernel": "smem" if kinds <= {"smem"} else ("global" if kinds == {"global"} else "mixed"),
+                     "host_chunks": len(plans)}
         return self.g2_f32[: self.n_bins]
 
     def run_device(self, times, counts, offs, n_ev, mx, reset_error=True):
@@ -395,6 +434,9 @@ class EventEngine:
         code = int(self.err.item())
         times_checked, csr_checked = getattr(self, "_times_checked", False), getattr(self, "_csr_checked", False)
         self._times_checked = self._csr_checked = False
+        offsets_bad, self._offsets_bad = getattr(self, "_offsets_bad", None), None
+        if offsets_bad is not None and int(offsets_bad.item()):
+            raise ValueError("offsets must start at 0 and be non-decreasing")
         if code == _lib.DEVERR_BOUNDS and times_checked:
             raise ValueError("event times must lie in [0, nframes)")
         if code == _lib.DEVERR_BOUNDS and csr_checked:
