@@ -421,7 +421,8 @@ def run_ours(args):
     # ---- end to end through the public API, frames in pinned host memory
     if not args.no_e2e:
         host = frames.cpu().pin_memory()
-        corr.correlate(host)
+        for _ in range(max(3, args.warmup)):
+            corr.correlate(host)
         barrier()
         t0 = time.perf_counter()
         e0.record(stream)
@@ -710,16 +711,22 @@ def measure_sparse(args, dev, T, steps, warmup, which=("sparse", "event"), shape
         }
         if e2e:
             host = [x.cpu().pin_memory() for x in inputs]
-            corr.correlate(*host)
+            for _ in range(max(3, warmup)):
+                corr.correlate(*host)
             barrier()
             t0 = time.perf_counter()
+            per_call = []
             for _ in range(steps):
-                corr.correlate(*host)
+                t1 = time.perf_counter()
+                corr.correlate(*host)                  # returns host arrays: synchronous
+                per_call.append((time.perf_counter() - t1) * 1e3)
             barrier()
             e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / steps)
             line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
                            "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in host)),
-                           "d2h_bytes_per_step": int(n_bins * T * 4 + 4), "ms_per_step": e2e_ms}
+                           "d2h_bytes_per_step": int(n_bins * T * 4 + 4), "ms_per_step": e2e_ms,
+                           "ms_per_call_min_median_max": [min(per_call), sorted(per_call)[len(per_call) // 2],
+                                                          max(per_call)]}
             del host
         if cpu_line is not None:
             line["cpu_baseline"] = dict(cpu_line)
@@ -1136,16 +1143,22 @@ def measure_u16(args, dev, T, steps, warmup, cpu=True, e2e=True):
     corr, line = one("auto")
     if e2e:
         host = frames.cpu().pin_memory()
-        corr.correlate(host)
+        for _ in range(max(3, warmup)):
+            corr.correlate(host)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
+        per_call = []
         for _ in range(steps):
-            corr.correlate(host)
+            t1 = time.perf_counter()
+            corr.correlate(host)                       # returns host arrays: synchronous
+            per_call.append((time.perf_counter() - t1) * 1e3)
         torch.cuda.synchronize(dev)
         e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
         line["e2e"] = {"value": T / (e2e_ms / 1e3), "unit": "frames/s", "ms_per_step": e2e_ms,
                        "h2d_bytes_per_step": int(host.numel() * host.element_size()),
-                       "d2h_bytes_per_step": int(U16_WORKLOAD["n_bins"] * T * 12 + 4)}
+                       "d2h_bytes_per_step": int(U16_WORKLOAD["n_bins"] * T * 12 + 4),
+                       "ms_per_call_min_median_max": [min(per_call), sorted(per_call)[len(per_call) // 2],
+                                                      max(per_call)]}
         del host
     del corr
     _, line["byte_planes"] = one("bytes")

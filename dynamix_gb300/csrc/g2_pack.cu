@@ -434,23 +434,13 @@ __global__ void __launch_bounds__(THREADS, 4)
 // store), 4 from 4 consecutive (one 32-bit funnel shift), 4 gathered from 4
 // arbitrary source bytes, single bytes (words shared with a neighbouring
 // chunk or bin padding) -- and groups them in blocks of 32 units of one
-// class; warp w of a block takes blocks w, w + 8, ... of its chunk and runs
-// each over the step's F frames.  Units are uint4 {destination (in units of
-// the class's size), source(s), source(s), class}; a warp's first UNIT_REGS
-// blocks stay in registers for the whole launch (a 2048-pixel chunk rarely
-// has more than 8 blocks), later ones are read from L1 each step.
-// The frames stream through a ring of UNIT_STAGES steps of staged rows
-// (cp.async), so the next steps' copies are in flight while one is moved; the
-// ring (16.6 KB with two steps) leaves room for a pack CTA beside a Gram
-// CTA on one SM.
+// class, each run by one warp over a step's F frames.  Units are uint4
+// {destination (in units of the class's size), source(s), source(s), class}.
 // The range check ORs every moved byte into one word per thread: with counts
 // <= 15 every byte of it stays <= 15, and only a count of 16 or more can make
 // one exceed 16, in which case G2_DEVERR_RANGE_CHECK asks the caller for the
 // exact maximum (g2_binned_max) -- one instruction per word instead of four.
 constexpr uint32_t UNIT_VEC = 1, UNIT_WORD = 2, UNIT_GATHER = 3, UNIT_BYTE = 4;
-constexpr int UNIT_THREADS = 512;  // 16 warps: a chunk's blocks (9 on average, rarely above 13) in one round
-constexpr int UNIT_STAGES = 2;
-constexpr int UNIT_REGS = 1;
 
 // One unit over the step's nf frames: source rows at base + delta[f], packed
 // rows at row[f].
@@ -534,64 +524,111 @@ __device__ __forceinline__ void move_unit(const uint4& u, const uint8_t* base, c
   }
 }
 
-__global__ void __launch_bounds__(UNIT_THREADS, 2)
-    pack_e4m3_units_kernel(const uint8_t* __restrict__ frames, int64_t T, int64_t npix,
-                           const int32_t* __restrict__ block_off, const uint4* __restrict__ units,
-                           uint8_t* __restrict__ packed, int64_t packed_cols, int32_t* __restrict__ err) {
+// The kernel: a CTA owns one 2048-pixel chunk over every gridDim.y-th step of
+// F frames.  The frames stream through a ring of RING_STAGES steps of staged
+// rows: warp 0 lane 0 copies each step's F frame rows of the chunk with 1-D
+// bulk copies (one per frame, completing on the stage's full barrier); warps
+// 1..RING_MOVERS each keep one block of units in registers for the whole
+// launch, move it at every step and arrive on the stage's empty barrier.  No
+// block-wide barrier per step, no per-thread copy instructions, and warps
+// without a block leave at once (a chunk of the 514 x 1030 detector holds 9
+// blocks on average, 13 at most): fewer instructions per moved byte than a
+// ring of per-thread cp.async copies and __syncthreads, which counts most
+// when the pack runs beside the Gram on the same SMs.  The ring (16.6 KB)
+// leaves room for a pack CTA beside a Gram CTA on one SM.
+constexpr int RING_THREADS = 512;
+constexpr int RING_MOVERS = RING_THREADS / 32 - 1;  // chunks rarely hold more than 13 blocks
+constexpr int RING_STAGES = 2;
+
+__global__ void __launch_bounds__(RING_THREADS, 2)
+    pack_e4m3_ring_kernel(const uint8_t* __restrict__ frames, int64_t T, int64_t npix,
+                          const int32_t* __restrict__ block_off, const uint4* __restrict__ units,
+                          uint8_t* __restrict__ packed, int64_t packed_cols, int32_t* __restrict__ err) {
   using C = Cfg<uint8_t>;
   constexpr int F = C::F;
-  constexpr int ROW = C::BUF + 16;  // staging row: the chunk, its unaligned start, spare words
-  __shared__ __align__(16) uint8_t s_buf[UNIT_STAGES][F][ROW];
+  constexpr int ROW = C::BUF + 16;                        // staging row: the chunk, its unaligned start, spare words
+  constexpr uint32_t SPAN = C::WORDS * 16;                // bytes per frame: the chunk from its aligned start
+  static_assert(ROW % 16 == 0 && SPAN <= ROW, "bulk copy rows");
+  __shared__ __align__(128) uint8_t s_buf[RING_STAGES][F][ROW];
+  __shared__ __align__(8) uint64_t full[RING_STAGES];
+  __shared__ __align__(8) uint64_t empty[RING_STAGES];
+  __shared__ int s_abort;
 
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5;
-  const int lane = tid & 31;
-  constexpr int WARPS = UNIT_THREADS / 32;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int64_t c = blockIdx.x;
-  const int64_t p0 = c * CH;
+  const int64_t p0 = c * CH;  // < npix: the launch has ceil(npix / CH) chunks
   const int b0 = block_off[c];
   const int nb = block_off[c + 1] - b0;
+  const int movers = nb < RING_MOVERS ? nb : RING_MOVERS;
+  if (movers <= 0) return;  // no packed byte comes from this chunk
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < RING_STAGES; ++s) {
+      mbar_init(&full[s], 1);        // the copier's arrive.expect_tx, then the bytes
+      mbar_init(&empty[s], movers);  // one arrival per mover warp
+    }
+    s_abort = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+  volatile int* abort_flag = &s_abort;
   const int64_t total_bytes = T * npix;
+  const int64_t stride = static_cast<int64_t>(gridDim.y) * F;
+  const int64_t first = static_cast<int64_t>(blockIdx.y) * F;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ copier
+    if (lane == 0) {
+      int64_t k = 0;
+      for (int64_t t0 = first; t0 < T; t0 += stride, ++k) {
+        const int s = static_cast<int>(k % RING_STAGES);
+        const uint32_t ph = static_cast<uint32_t>((k / RING_STAGES) & 1);
+        if (k >= RING_STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag, err)) break;
+        const int nf = static_cast<int>(T - t0 < F ? T - t0 : F);
+        uint32_t bytes = 0;
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          if (f >= nf) break;
+          const int64_t a = ((t0 + f) * npix + p0) & ~int64_t(15);
+          const int64_t avail = total_bytes - a;  // > 0
+          const uint32_t n = avail >= SPAN ? SPAN : static_cast<uint32_t>(avail);
+          // the stack's last bytes short of a multiple of 16: plain copies,
+          // made visible by the arrive below (only the last frame has them)
+          for (uint32_t i = n & ~15u; i < n; ++i) s_buf[s][f][i] = frames[a + i];
+          bytes += n & ~15u;
+        }
+        mbar_arrive_expect_tx(&full[s], bytes);
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          if (f >= nf) break;
+          const int64_t a = ((t0 + f) * npix + p0) & ~int64_t(15);
+          const int64_t avail = total_bytes - a;
+          const uint32_t n = (avail >= SPAN ? SPAN : static_cast<uint32_t>(avail)) & ~15u;
+          if (n) bulk_load_1d(&s_buf[s][f][0], frames + a, n, &full[s]);
+        }
+      }
+      // after a timed-out wait a copy of this CTA may still be landing
+      if (*abort_flag) {
+        const uint64_t w0 = global_timer_ns();
+        while (global_timer_ns() - w0 < 100000ull) {
+        }
+      }
+    }
+    return;
+  }
+
+  // -------------------------------------------------------------- movers
+  const int mw = warp - 1;
+  if (mw >= movers) return;
+  const uint4 u0 = units[static_cast<int64_t>(b0 + mw) * 32 + lane];
   const int64_t n_vec = packed_cols / 16, n_word = packed_cols / 4;
   uint32_t seen = 0;  // OR of every moved byte
   bool bad = false;
-
-  // this warp's first blocks, for the whole launch
-  uint4 ureg[UNIT_REGS];
-#pragma unroll
-  for (int k = 0; k < UNIT_REGS; ++k) {
-    const int blk = warp + k * WARPS;
-    ureg[k] = blk < nb ? units[static_cast<int64_t>(b0 + blk) * 32 + lane] : make_uint4(0, 0, 0, 0);
-  }
-
-  auto issue = [&](int64_t t0, int buf) {
-    if (t0 < T) {
-      for (int w = tid; w < F * C::WORDS; w += UNIT_THREADS) {
-        const int f = w / C::WORDS;
-        const int wi = w - f * C::WORDS;
-        const int64_t t = t0 + f;
-        const int64_t a = ((t * npix + p0) & ~int64_t(15)) + static_cast<int64_t>(wi) * 16;
-        const int64_t avail = t < T ? total_bytes - a : 0;
-        const int nbytes = avail <= 0 ? 0 : (avail >= 16 ? 16 : static_cast<int>(avail));
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(&s_buf[buf][f][wi * 16])),
-                     "l"(nbytes ? frames + a : frames), "r"(nbytes)
-                     : "memory");
-      }
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");  // an empty group past the end keeps the count
-  };
-
-  const int64_t stride = static_cast<int64_t>(gridDim.y) * F;
-  const int64_t first = static_cast<int64_t>(blockIdx.y) * F;
-#pragma unroll
-  for (int s = 0; s < UNIT_STAGES - 1; ++s) issue(first + s * stride, s);
-  int buf = 0;
-  for (int64_t t0 = first; t0 < T; t0 += stride) {
-    asm volatile("cp.async.wait_group %0;" ::"n"(UNIT_STAGES - 2) : "memory");
-    // this step's rows have landed (every thread's copies), and every thread
-    // is done with the buffer refilled next (moved at the previous step)
-    __syncthreads();
-    issue(t0 + (UNIT_STAGES - 1) * stride, buf == 0 ? UNIT_STAGES - 1 : buf - 1);
+  int64_t k = 0;
+  for (int64_t t0 = first; t0 < T; t0 += stride, ++k) {
+    const int s = static_cast<int>(k % RING_STAGES);
+    const uint32_t ph = static_cast<uint32_t>((k / RING_STAGES) & 1);
+    if (!mbar_wait(&full[s], ph, abort_flag, err)) break;
     const int nf = static_cast<int>(T - t0 < F ? T - t0 : F);
     uint32_t delta[F];
     uint8_t* row[F];
@@ -600,19 +637,16 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2)
       delta[f] = static_cast<uint32_t>(((t0 + f) * npix + p0) & 15) + f * ROW;
       row[f] = packed + (t0 + f) * packed_cols;
     }
-    const uint8_t* base = &s_buf[buf][0][0];
-#pragma unroll
-    for (int k = 0; k < UNIT_REGS; ++k)
-      if (warp + k * WARPS < nb) move_unit<F>(ureg[k], base, delta, row, nf, n_vec, n_word, packed_cols, seen, bad);
-    for (int blk = warp + UNIT_REGS * WARPS; blk < nb; blk += WARPS) {
+    const uint8_t* base = &s_buf[s][0][0];
+    move_unit<F>(u0, base, delta, row, nf, n_vec, n_word, packed_cols, seen, bad);
+    for (int blk = mw + RING_MOVERS; blk < nb; blk += RING_MOVERS) {
       const uint4 u = units[static_cast<int64_t>(b0 + blk) * 32 + lane];
       move_unit<F>(u, base, delta, row, nf, n_vec, n_word, packed_cols, seen, bad);
     }
-    buf = buf == UNIT_STAGES - 1 ? 0 : buf + 1;
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
   if (bad) atomicOr(err, G2_DEVERR_BOUNDS);
-  // a byte of the OR above 16 means some count may exceed 16
   if (((seen & 0x7F7F7F7Fu) + 0x6F6F6F6Fu | seen) & 0x80808080u) atomicOr(err, G2_DEVERR_RANGE_CHECK);
 }
 
@@ -748,7 +782,7 @@ extern "C" int g2_pack_e4m3_units(const void* frames_dev, int64_t nframes, int64
   if (gy > 65535) gy = 65535;
   if (gy < 1) gy = 1;
   dim3 grid(static_cast<unsigned>(n_chunks), static_cast<unsigned>(gy));
-  pack::pack_e4m3_units_kernel<<<grid, pack::UNIT_THREADS, 0, as_stream(stream)>>>(
+  pack::pack_e4m3_ring_kernel<<<grid, pack::RING_THREADS, 0, as_stream(stream)>>>(
       reinterpret_cast<const uint8_t*>(frames_dev), nframes, npix, unit_block_off_dev,
       reinterpret_cast<const uint4*>(units_dev), reinterpret_cast<uint8_t*>(packed_dev), packed_cols, err_dev);
   return launch_status();

@@ -66,6 +66,35 @@ def test_units_pack_equals_word_pack(built_lib, cuda_device, mask):
     assert ea == _lib.DEVERR_RANGE_CHECK and eb == _lib.DEVERR_RANGE
 
 
+@pytest.mark.parametrize("kind", ["interleaved", "empty_chunks"])
+def test_units_pack_unusual_chunks(built_lib, cuda_device, kind):
+    # interleaved: two bins alternating pixel by pixel, so every destination
+    # word is a gather and a 2048-pixel chunk holds 16 blocks of units (more
+    # than one per mover warp); empty_chunks: the first 5,000 pixels unbinned,
+    # so whole chunks move nothing
+    import torch
+    from dynamix_gb300.engine import device_layout
+    from dynamix_gb300.plan import MODE_E4M3
+    shape = (64, 130)
+    qm = np.zeros(shape, np.int32)
+    if kind == "interleaved":
+        qm.ravel()[:] = 1 + np.arange(qm.size) % 2
+        nb = 2
+    else:
+        qm.ravel()[5000:] = 1 + (np.arange(qm.size - 5000) // 700) % 3
+        nb = 3
+    L = device_layout(qm, nb, MODE_E4M3, cuda_device)
+    blocks = np.diff(L.unit_block_off)
+    assert blocks.max() > 15 if kind == "interleaved" else (blocks == 0).any()
+    rng = np.random.default_rng(7)
+    for T in (1, 6, 41):
+        fr = torch.from_numpy(rng.integers(0, 16, (T,) + shape).astype(np.uint8)).to(cuda_device)
+        a, ea = _packed(built_lib, torch, cuda_device, fr, L, units=True)
+        b, eb = _packed(built_lib, torch, cuda_device, fr, L, units=False)
+        assert np.array_equal(a, b)
+        assert ea == 0 and eb == 0
+
+
 @pytest.mark.parametrize("pipelined", [True, False])
 @pytest.mark.parametrize("top", [16, 17])
 def test_range_check_resolution(built_lib, cuda_device, top, pipelined):
