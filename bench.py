@@ -436,9 +436,13 @@ def run_ours(args):
         d2h = eng.n_bins * T * 4 + 4 + eng.n_bins * T * 8
         if "pipeline_chunks" not in eng.last:
             d2h += info["packed_cols"] // 64 * 4
+        # the bytes that crossed the host link: the frames cropped to the
+        # q-mask's column window (u8 stacks with a narrower binned region)
+        h2d = int(eng.last.get("h2d_bytes") or host.numel() * host.element_size())
         line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
-                       "h2d_bytes_per_step": int(host.numel() * host.element_size()),
-                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                       "input": "the whole (T, H, W) u8 stack in pinned host memory, correlate(host_tensor); "
+                                "copied in cropped to the q-mask's columns %s" % (eng.last.get("crop"),)}
         del host
 
     # ---- same-GPU plain (CUDA-core) comparators: the u8 __dp4a kernel (four

@@ -51,6 +51,7 @@ SIGNATURES = {
     "g2_status_string": (C.c_char_p, [C.c_int]),
     "g2_device_info": (C.c_int, [C.c_int, _p, _p, _p]),
     "g2_balance_lpt": (C.c_int, [_p, _i64, _i32, _p, _p]),
+    "g2_copy_cols_h2d": (C.c_int, [_p, _p, _i64, _i64, _i64, _i64, _p]),
     "g2_pack_frames": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _p, _p, _p, _i64, _i32, _p, _i64, _p, _i32, _p,
                                  _i64, _p, _p]),
     "g2_pack_e4m3": (C.c_int, [_p, _i32, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _p, _p]),

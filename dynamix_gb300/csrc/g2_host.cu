@@ -115,3 +115,18 @@ extern "C" int g2_balance_lpt(const double* cost, int64_t n, int32_t workers, in
   *n_slots = longest * workers;
   return G2_OK;
 }
+
+// Host-to-device copy of a column window of many rows: the frames of a stack
+// cropped to the q-mask's bounding columns, so that only those bytes cross
+// the host link.  One cudaMemcpy2DAsync (the copy engines walk the rows).
+extern "C" int g2_copy_cols_h2d(void* dst_dev, const void* src_host, int64_t src_pitch, int64_t col0, int64_t width,
+                                int64_t rows, void* stream) {
+  if (!dst_dev || !src_host || src_pitch <= 0 || col0 < 0 || width <= 0 || col0 + width > src_pitch || rows < 0)
+    return G2_ERR_ARG;
+  if (rows == 0) return G2_OK;
+  const cudaError_t e = cudaMemcpy2DAsync(dst_dev, static_cast<size_t>(width),
+                                          static_cast<const char*>(src_host) + col0, static_cast<size_t>(src_pitch),
+                                          static_cast<size_t>(width), static_cast<size_t>(rows),
+                                          cudaMemcpyHostToDevice, g2::as_stream(stream));
+  return e == cudaSuccess ? G2_OK : G2_ERR_CUDA;
+}

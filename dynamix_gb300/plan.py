@@ -457,6 +457,27 @@ def chunk_grams(layout, seg_emax, limit=EXACT_LIMIT, kslab=0):
     return out
 
 
+def column_window(qmask2d, n_bins, min_saving, min_gap=192):
+    """(first column, width) of the smallest column window holding every
+    binned pixel of a (H, W) q-mask, widened to 16-byte multiples of a u8 row
+    (16-byte aligned host reads), or None when nothing is binned or the window
+    leaves less than ``min_saving`` of the row, or less than ``min_gap``
+    bytes, out.  (Row-by-row host-to-device copies whose rows skip only a
+    short gap ran far below the link rate: 27-81 GB/s at 928 to 1024 of 1030
+    bytes and at 2048 of 2068, against 198-206 GB/s for windows of at most
+    896 of 1030 and 1856 of 2068.)"""
+    q = np.asarray(qmask2d)
+    W = q.shape[1]
+    cols = np.flatnonzero(((q >= 1) & (q <= n_bins)).any(axis=0))
+    if cols.size == 0:
+        return None
+    c0 = int(cols[0]) // 16 * 16
+    c1 = min(W, -(-(int(cols[-1]) + 1) // 16) * 16)
+    if c1 - c0 > (1.0 - float(min_saving)) * W or W - (c1 - c0) < int(min_gap):
+        return None
+    return c0, c1 - c0
+
+
 def e4m3_segment_bound(layout):
     """Energy bound per 64-column segment for e4m3 operands without looking at
     the data: every count is <= 16, so a segment's sum of squares is <= 64 * 256

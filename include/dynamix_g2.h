@@ -112,6 +112,14 @@ int g2_device_info(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc
  * ...; slots left over hold G2_ITEM_EMPTY items (the caller fills them).  No
  * reference counterpart (the reference launches one thread per output). */
 int g2_balance_lpt(const double* cost, int64_t n, int32_t workers, int64_t* slot_out, int64_t* n_slots);
+/* Host-to-device copy of the byte columns [col0, col0 + width) of `rows`
+ * rows of pitch src_pitch (a stack of frames seen as T*H rows) into rows of
+ * pitch `width` at dst_dev, on `stream` (one cudaMemcpy2DAsync): frames in
+ * host memory cropped to the q-mask's bounding columns on their way in, so
+ * that only the bytes the pack reads cross the host link.  The reference
+ * reads whole frames from host memory (dense.py:49, `frames[:, ind]`). */
+int g2_copy_cols_h2d(void* dst_dev, const void* src_host, int64_t src_pitch, int64_t col0, int64_t width,
+                     int64_t rows, void* stream);
 
 /* ---- G1: pack + bin sums ------------------------------------------------
  * Replaces compute_sums_dense (dynamix/resources/opencl/densecorrelator.cl:65-150)

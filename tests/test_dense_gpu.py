@@ -236,6 +236,41 @@ def test_chunked_pipeline_matches_single_pass(built_lib, cuda_device, T):
     assert np.array_equal(g, gb, equal_nan=True)
 
 
+@pytest.mark.parametrize("top", [None, 16, 17])
+def test_host_frames_cropped_to_qmask_columns(built_lib, cuda_device, top):
+    """u8 frames in pinned host memory cross the link cropped to the q-mask's
+    column window; the results equal the oracle's, also when a count of 16
+    needs the exact maximum of the cropped frames and when a count of 17 moves
+    the stack to fp16 operands (rerun from the whole host frames)."""
+    import torch
+    from dynamix_gb300.correlator import MatMulCorrelator
+    from dynamix_gb300.speckle import annular_qmask, speckle_numpy
+    T, shape = 700, (48, 400)
+    fr = speckle_numpy(T, shape, 0.99, 0.4, seed=5, dtype=np.uint8, max_count=15)
+    qm = annular_qmask(shape, 6, 3.0, 30.0, center=(24, 200))    # binned columns 171..229
+    fr[T // 3, 5, 2] = 200                                      # unbinned, outside the window
+    if top is not None:
+        fr[T // 2, 24, 210] = top                               # binned
+        fr[T // 2, 24, 211] = 1
+    ref = o.g2_exact(fr, qm)
+    c = MatMulCorrelator(shape, T, qmask=qm)
+    eng = c.engine
+    c0, wc = eng.crop
+    assert c0 % 16 == 0 and wc % 16 == 0 and c0 <= 171 and c0 + wc > 229 and wc < shape[1]
+    host = torch.from_numpy(fr).pin_memory()
+    g = c.correlate(host)
+    assert_exact(c, ref, g)
+    if top == 17:
+        assert eng.last["mode"] == "fp16"
+    else:
+        assert eng.last["mode"] == "e4m3" and eng.last["crop"] == [c0, wc]
+        assert eng.last["h2d_bytes"] == T * shape[0] * wc
+    g = c.correlate(host)                 # after a rerun on fp16 the next call starts there
+    assert_exact(c, ref, g)
+    g = c.correlate(host.to(cuda_device))  # device input: whole frames
+    assert_exact(c, ref, g)
+
+
 @pytest.mark.parametrize("name", ["dense_small_u8", "dense_bright_u8", "dense_128x128_u8", "dense_u16"])
 def test_calc_std(built_lib, cuda_device, name):
     """calc_std (dense.py:58-66): against the float64 oracle to 1e-4 relative

@@ -293,3 +293,32 @@ def test_pipeline_chunk_bounds_tapered(T, n):
     assert np.all(b[1:-1] % 128 == 0) and b.size - plain.size <= 3
     tail = np.diff(b[plain.size - 2:])
     assert np.all(tail[1:-1] <= tail[:-2])
+
+
+def test_column_window_and_cropped_layout():
+    # host frames are copied cropped to the q-mask's column window: the window
+    # is 16-byte aligned, and the cropped frame's layout packs the same pixels
+    # into the same columns
+    from dynamix_gb300.plan import MODE_E4M3, MODE_FP16, PackLayout, column_window
+    from dynamix_gb300.speckle import annular_qmask
+    q = annular_qmask((514, 1030), 16, 20.0, 400.0, center=(257, 515))
+    assert column_window(q, 16, 0.1) == (112, 816)
+    assert column_window(annular_qmask((256, 256), 12, 8.0, 128.0, center=(128, 128)), 12, 0.1) is None
+    assert column_window(np.zeros((4, 64), np.int32), 1, 0.1) is None
+    z = np.zeros((4, 400), np.int32)
+    z[:, 395] = 1
+    z[:, 3] = 2                                   # above n_bins: not binned
+    assert column_window(z, 1, 0.1) == (384, 16)
+    assert column_window(z[:, 210:], 1, 0.1) is None   # 176 of 190 columns skipped: under the 192-byte gap
+    z[0, 3] = 1
+    assert column_window(z, 1, 0.1) is None       # columns 0..395 of 400
+    for qm, nb in ((q, 16), (annular_qmask((61, 300), 5, 0.0, 30.0, center=(30, 140)), 5)):
+        c0, wc = column_window(qm, nb, 0.1)
+        W = qm.shape[1]
+        for mode in (MODE_E4M3, MODE_FP16):
+            full = PackLayout(qm, nb, mode)
+            crop = PackLayout(np.ascontiguousarray(qm[:, c0:c0 + wc]), nb, mode)
+            assert crop.packed_cols == full.packed_cols
+            cs = crop.col_src.astype(np.int64)
+            mapped = np.where(cs >= 0, cs // wc * W + c0 + cs % wc, -1)
+            assert np.array_equal(mapped, full.col_src)
