@@ -21,6 +21,8 @@ Multi-GPU (torchrun): independent replicas, one stack per GPU ("weak" scaling).
 from __future__ import annotations
 
 import argparse
+import contextlib
+import gc
 import json
 import math
 import os
@@ -48,6 +50,22 @@ SPARSE_WORKLOAD = {
 }
 CPU_SAMPLE_PIXEL_STRIDE = 16
 
+
+
+@contextlib.contextmanager
+def no_gc():
+    """A timed region runs with Python's cyclic garbage collector paused (as
+    timeit does): single calls of the end-to-end loops run after the dense
+    line otherwise showed stalls of 7-33 ms (collections of the bench
+    process's heap, not work of the call)."""
+    gc.collect()
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
 
 def parse():
     p = argparse.ArgumentParser()
@@ -326,11 +344,12 @@ def run_ours(args):
     sampler.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        corr.correlate_device(frames)
-    e1.record(stream)
-    barrier()
+    with no_gc():
+        e0.record(stream)
+        for _ in range(args.steps):
+            corr.correlate_device(frames)
+        e1.record(stream)
+        barrier()
     clocks = sampler.stop()
     eng.check_error()
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
@@ -424,13 +443,14 @@ def run_ours(args):
         for _ in range(max(3, args.warmup)):
             corr.correlate(host)
         barrier()
-        t0 = time.perf_counter()
-        e0.record(stream)
-        for _ in range(args.steps):
-            corr.correlate(host)
-        e1.record(stream)
-        barrier()
-        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+        with no_gc():
+            t0 = time.perf_counter()
+            e0.record(stream)
+            for _ in range(args.steps):
+                corr.correlate(host)
+            e1.record(stream)
+            barrier()
+            e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
         # g2, the error word, S for the int64 range check (and the segment
         # energies when the step is not pipelined)
         d2h = eng.n_bins * T * 4 + 4 + eng.n_bins * T * 8
@@ -664,13 +684,14 @@ def measure_sparse(args, dev, T, steps, warmup, which=("sparse", "event"), shape
         sampler.start()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step_events = []
-        for _ in range(steps):
-            corr.correlate_device(*inputs)
-            step_events.append(events_engine.take_events())
-        e1.record(stream)
-        barrier()
+        with no_gc():
+            e0.record(stream)
+            step_events = []
+            for _ in range(steps):
+                corr.correlate_device(*inputs)
+                step_events.append(events_engine.take_events())
+            e1.record(stream)
+            barrier()
         clocks = sampler.stop()
         events_engine.profile = False
         corr.engine.check_error()
@@ -718,13 +739,14 @@ def measure_sparse(args, dev, T, steps, warmup, which=("sparse", "event"), shape
             for _ in range(max(3, warmup)):
                 corr.correlate(*host)
             barrier()
-            t0 = time.perf_counter()
-            per_call = []
-            for _ in range(steps):
-                t1 = time.perf_counter()
-                corr.correlate(*host)                  # returns host arrays: synchronous
-                per_call.append((time.perf_counter() - t1) * 1e3)
-            barrier()
+            with no_gc():
+                t0 = time.perf_counter()
+                per_call = []
+                for _ in range(steps):
+                    t1 = time.perf_counter()
+                    corr.correlate(*host)              # returns host arrays: synchronous
+                    per_call.append((time.perf_counter() - t1) * 1e3)
+                barrier()
             e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / steps)
             line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
                            "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in host)),
@@ -1098,11 +1120,12 @@ def measure_u16(args, dev, T, steps, warmup, cpu=True, e2e=True):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(dev)
-        e0.record(stream)
-        for _ in range(steps):
-            corr.correlate_device(frames)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
+        with no_gc():
+            e0.record(stream)
+            for _ in range(steps):
+                corr.correlate_device(frames)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
         eng.check_error()
         ms = e0.elapsed_time(e1) / steps
         info = dict(eng.last)
@@ -1150,13 +1173,14 @@ def measure_u16(args, dev, T, steps, warmup, cpu=True, e2e=True):
         for _ in range(max(3, warmup)):
             corr.correlate(host)
         torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        per_call = []
-        for _ in range(steps):
-            t1 = time.perf_counter()
-            corr.correlate(host)                       # returns host arrays: synchronous
-            per_call.append((time.perf_counter() - t1) * 1e3)
-        torch.cuda.synchronize(dev)
+        with no_gc():
+            t0 = time.perf_counter()
+            per_call = []
+            for _ in range(steps):
+                t1 = time.perf_counter()
+                corr.correlate(host)                   # returns host arrays: synchronous
+                per_call.append((time.perf_counter() - t1) * 1e3)
+            torch.cuda.synchronize(dev)
         e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
         line["e2e"] = {"value": T / (e2e_ms / 1e3), "unit": "frames/s", "ms_per_step": e2e_ms,
                        "h2d_bytes_per_step": int(host.numel() * host.element_size()),
@@ -1255,11 +1279,12 @@ def run_compress(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     comp.profile = True  # CUDA events between the passes of every timed call
-    e0.record(stream)
-    for _ in range(args.steps):
-        comp.run(frames)
-    e1.record(stream)
-    barrier()
+    with no_gc():
+        e0.record(stream)
+        for _ in range(args.steps):
+            comp.run(frames)
+        e1.record(stream)
+        barrier()
     clocks = sampler.stop()
     comp.profile = False
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
@@ -1309,11 +1334,12 @@ def run_compress(args):
 
         for _ in range(2):
             e2e_step()
-        t0 = time.perf_counter()
-        d2h = 0
-        for _ in range(args.steps):
-            d2h = e2e_step()
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        with no_gc():
+            t0 = time.perf_counter()
+            d2h = 0
+            for _ in range(args.steps):
+                d2h = e2e_step()
+            e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
         line["e2e"] = {"value": T / (e2e_ms / 1e3), "unit": "frames/s", "ms_per_step": e2e_ms,
                        "h2d_bytes_per_step": stack_bytes, "d2h_bytes_per_step": d2h,
                        "path": "pinned host stack -> device -> StackCompressor.run -> pinned host events"}
