@@ -446,8 +446,11 @@ def run_ours(args):
         with no_gc():
             t0 = time.perf_counter()
             e0.record(stream)
+            per_call = []
             for _ in range(args.steps):
-                corr.correlate(host)
+                t1 = time.perf_counter()
+                corr.correlate(host)                   # returns host arrays: synchronous
+                per_call.append((time.perf_counter() - t1) * 1e3)
             e1.record(stream)
             barrier()
             e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
@@ -461,6 +464,8 @@ def run_ours(args):
         h2d = int(eng.last.get("h2d_bytes") or host.numel() * host.element_size())
         line["e2e"] = {"value": world * T / (e2e_ms / 1e3), "unit": "frames/s",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                       "ms_per_call_min_median_max": [min(per_call), sorted(per_call)[len(per_call) // 2],
+                                                      max(per_call)],
                        "input": "the whole (T, H, W) u8 stack in pinned host memory, correlate(host_tensor); "
                                 "copied in cropped to the q-mask's columns %s" % (eng.last.get("crop"),)}
         del host
